@@ -1,0 +1,374 @@
+#!/usr/bin/env python3
+"""Benchmark: FIRE minimisation of the 200^3 multi-constant lattice with
+homeotropic z-walls and a centred homeotropic colloid (L1, L2, L3 =
+2.32, 1.0, 0.5), FP64, on GB300.
+
+A step is one FIRE iteration (velocity Verlet + force + FIRE update) over the
+whole 8,000,000-site lattice.  `value` is site-steps/s with the state resident
+in HBM; `e2e` times the same run through the C ABI from pinned host buffers
+(upload of Q0 and site types, K iterations, download of the final Q).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+
+With N > 1 (torchrun) every rank minimises its own replica of the lattice
+(independent solves, no collective on the data path); timing is the max over
+ranks.  `--impl reference` times the CPU restatement of the reference's CPU
+path (the oracle) on this host's cores.
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "time to max|F|<1e-6 & site-steps/s, warm-start+FP32 vs plain FIRE, 1 GB300"
+WORKLOAD = dict(L=(200, 200, 200), seed=13371, Ls=(2.32, 1.0, 0.5), W=5.3, walls=(0, 199), sphere=((100.0, 100.0, 100.0), 30.0),
+                dt=5e-4)
+# algorithmic bytes per site for one launch of each FIRE-iteration kernel (FP64 / FP32 state):
+#  predictor: read Q,V,F  write Q,V           = 25 values
+#  derivative planes: read Q, types, write 15 = 20 values + 1 B
+#  force + kick: read Q, V, types, write F, V = 20 values + 1 B
+#  control: scalars only
+KERNEL_BYTES = {8: [200, 161, 161, 0], 4: [100, 81, 81, 0]}
+KERNEL_NAMES = ["fire_predictor", "first_derivatives", "force_kick_reduce", "fire_control"]
+
+
+def measured_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return d["hbm_gbs"], "measured"
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi sampling of SM clocks and throttle reasons during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.FIELDS,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx = float(parts[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower() in ("active", "1", "0x1"):
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def build_workload_host(q, precision=None):
+    """Host set-up of the workload through the package's own host helpers."""
+    a, b, c, S0 = q.cli_phase_constants()
+    w = WORKLOAD
+    Q = q.host_random_nematic(w["L"], w["seed"], S0)
+    g = q.Geometry(w["L"], Q)
+    for plane in w["walls"]:
+        g.add_wall(2, plane, q.HOMEOTROPIC, w["W"], S0)
+    g.add_sphere(w["sphere"][0], w["sphere"][1], q.HOMEOTROPIC, w["W"], S0)
+    return (a, b, c, S0), g
+
+
+def make_lattice(q, consts, g, precision):
+    a, b, c, S0 = consts
+    lat = q.Lattice(WORKLOAD["L"], precision)
+    lat.set_params(a, b, c, *WORKLOAD["Ls"])
+    lat.set_objects(g.objects())
+    return lat
+
+
+def traffic_from_profiles(kernel, precision_tag):
+    """DRAM bytes per launch recorded in profiles/ by the ncu capture, if present."""
+    p = os.path.join(ROOT, "profiles", "dram_traffic.md")
+    if not os.path.exists(p):
+        return None
+    for line in open(p):
+        parts = [x.strip() for x in line.strip().strip("|").split("|")]
+        if len(parts) >= 4 and parts[0] == kernel and parts[1] == precision_tag:
+            try:
+                return float(parts[3])
+            except ValueError:
+                return None
+    return None
+
+
+def run_ours(args, rank, world):
+    import torch
+    import __graft_entry__ as ge
+    q = ge.load_package()
+    dev = int(os.environ.get("LOCAL_RANK", 0))
+    torch.cuda.set_device(dev)
+    consts, g = build_workload_host(q)
+    N = g.Q.shape[0]
+    K, W = args.steps, args.warmup
+    dist = world > 1
+
+    def barrier():
+        if dist:
+            torch.distributed.barrier()
+
+    def timed_fire(precision):
+        lat = make_lattice(q, consts, g, precision)
+        stream = torch.cuda.Stream()
+        lat_stream = stream.cuda_stream
+        q._check(q.lib().qmin_set_stream(lat._h, lat_stream))
+        lat.set_state(g.Q, g.types)
+        lat.fire_init(dt=WORKLOAD["dt"])
+        lat.fire_run(W)
+        torch.cuda.synchronize()
+        barrier()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        l0 = lat.launches()
+        with ClockSampler(dev) as clk:
+            torch.cuda.synchronize()
+            e0.record(stream)
+            r = lat.fire_run(W + K)
+            e1.record(stream)
+            torch.cuda.synchronize()
+        barrier()
+        ms = e0.elapsed_time(e1)
+        return lat, r, ms, lat.launches() - l0, clk.summary()
+
+    # ---- device-resident FP64 run (the headline)
+    lat, r, ms, launches, clocks = timed_fire(q.FP64)
+    ms_all = [ms]
+    if dist:
+        t = torch.tensor([ms], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+    value = world * N * K / (ms / 1e3)
+
+    # ---- roofline of the dominant kernel (direct launches, CUDA events per kernel)
+    kms = np.zeros(4)
+    import ctypes as C
+    arr = (C.c_double * 4)()
+    q._check(q.lib().qmin_fire_profile(lat._h, 20, arr))
+    kms[:] = list(arr)
+    dom = int(np.argmax(kms))
+    peak, peak_kind = measured_peaks()
+    achieved = KERNEL_BYTES[8][dom] * N / (kms[dom] / 1e3) / 1e9
+    roofline = {"bound": "hbm", "kernel": KERNEL_NAMES[dom], "achieved": achieved, "peak": peak, "unit": "GB/s",
+                "frac": achieved / peak, "peak_source": peak_kind,
+                "traffic": traffic_from_profiles(KERNEL_NAMES[dom], "f64"),
+                "kernel_ms": dict(zip(KERNEL_NAMES, [float(x) for x in kms])),
+                "algorithmic_bytes_per_site": KERNEL_BYTES[8][dom]}
+    # whole-iteration view: 241 B/site for the fused ideal (read Q,V,F,types; write Q,V,F)
+    it_ms = ms / (K)
+    roofline["iteration_achieved_gbs_at_241B"] = 241 * N / (it_ms / 1e3) / 1e9
+    fire_state = {"forceMax": r["forceMax"], "iterations": r["iterations"]}
+    lat.close()
+
+    # ---- end to end through the C ABI from pinned host memory
+    import torch as _t
+    Qh = _t.from_numpy(g.Q).pin_memory()
+    Th = _t.from_numpy(g.types).pin_memory()
+    Qout = _t.empty_like(Qh).pin_memory()
+    lat = make_lattice(q, consts, g, q.FP64)
+    stream = torch.cuda.Stream()
+    q._check(q.lib().qmin_set_stream(lat._h, stream.cuda_stream))
+    lat.set_state_ptr(Qh.data_ptr(), Th.data_ptr())
+    lat.fire_init(dt=WORKLOAD["dt"])
+    lat.fire_run(W)
+    torch.cuda.synchronize()
+    barrier()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    t0 = time.perf_counter()
+    e0.record(stream)
+    lat.set_state_ptr(Qh.data_ptr(), Th.data_ptr())
+    lat.fire_init(dt=WORKLOAD["dt"])
+    lat.fire_run(K)
+    lat.get_state_ptr(Qout.data_ptr(), None, None)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    wall_e2e = time.perf_counter() - t0
+    barrier()
+    ms_e2e = max(e0.elapsed_time(e1), wall_e2e * 1e3)
+    if dist:
+        t = torch.tensor([ms_e2e], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms_e2e = float(t.item())
+    h2d = N * 5 * 8 + N * 4
+    d2h = N * 5 * 8
+    e2e = {"value": world * N * K / (ms_e2e / 1e3), "unit": "site-steps/s", "h2d_bytes_per_step": h2d / K,
+           "d2h_bytes_per_step": d2h / K,
+           "note": "per job: upload Q0 (AoS f64) + int32 types, K FIRE iterations, download final Q; bytes amortised over K"}
+    lat.close()
+
+    # ---- FP32 form (FP32 state/stencils, FP64 reductions) on the same input
+    lat32, r32, ms32, _, _ = timed_fire(q.FP32)
+    fp32 = {"value": N * K / (ms32 / 1e3), "unit": "site-steps/s", "ms_per_step": ms32 / K,
+            "forceMax": r32["forceMax"], "forceMax_rel_err_vs_fp64": abs(r32["forceMax"] - r["forceMax"]) / r["forceMax"]}
+    arr = (C.c_double * 4)()
+    q._check(q.lib().qmin_fire_profile(lat32._h, 20, arr))
+    k32 = np.array(list(arr))
+    d32 = int(np.argmax(k32))
+    a32 = KERNEL_BYTES[4][d32] * N / (k32[d32] / 1e3) / 1e9
+    fp32["roofline"] = {"bound": "hbm", "kernel": KERNEL_NAMES[d32], "achieved": a32, "peak": peak, "unit": "GB/s",
+                        "frac": a32 / peak, "kernel_ms": dict(zip(KERNEL_NAMES, [float(x) for x in k32]))}
+    lat32.close()
+
+    out = None
+    if rank == 0:
+        out = {"metric": METRIC, "value": value, "unit": "site-steps/s", "n_gpus": world, "steps": K, "warmup": W,
+               "ms_per_step": ms / K, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+               "dtype": "f64", "data": "synthetic (seeded random-director Q0, reference geometry builders)",
+               "config": {"workload": "200^3 lattice, homeotropic z-walls (planes 0 and 199) + centred homeotropic "
+                                      "sphere r=30, W=5.3, L1-L3 = 2.32/1.0/0.5, FIRE dt=5e-4, CLI FIRE params",
+                          "sites": N, "fire_steps_per_run": K, "precision": "fp64",
+                          "l2": "inputs larger than L2 (Q,V,F state = 960 MB)",
+                          "parallelism": "replicas" if world > 1 else "single GPU"},
+               "clocks": clocks, "e2e": e2e, "gpu_launches": launches, "roofline": roofline,
+               "fire_state_after_run": fire_state, "fp32_form": fp32}
+    return out
+
+
+def cpu_baseline(sample_iters=2, threads=1):
+    """The oracle (CPU restatement of the reference's CPU path) on a bounded
+    sample of the same workload: `sample_iters` FIRE iterations of the 200^3
+    lattice, timed with wall clock around the FIRE loop."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import qmin_oracle as qo
+    qo.build()
+    used = qo.set_threads(threads)
+    w = WORKLOAD
+    s = qo.System(w["L"], Ls=w["Ls"] + (0.0,))
+    s.random_nematic(w["seed"])
+    for plane in w["walls"]:
+        s.add_wall(2, plane, 0, w["W"])
+    s.add_sphere(w["sphere"][0], w["sphere"][1], 0, w["W"])
+    t0 = time.perf_counter()
+    r = s.fire(sample_iters, dt=w["dt"])
+    dt = time.perf_counter() - t0
+    # minimize() evaluates the force once on entry: count it as part of the sample's work
+    value = s.N * sample_iters / dt
+    return {"value": value, "unit": "site-steps/s", "cores": used, "kind": "port",
+            "sample": f"{sample_iters} FIRE iterations (+1 entry force evaluation) of the 200^3 workload, "
+                      f"{used} thread(s); oracle = C restatement of the reference CPU path"}, r
+
+
+def run_reference(args):
+    """--impl reference: the reference's CPU path (its C restatement) on all host cores."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import qmin_oracle as qo
+    qo.build()
+    threads = os.cpu_count() or 1
+    used = qo.set_threads(threads)
+    w = WORKLOAD
+    s = qo.System(w["L"], Ls=w["Ls"] + (0.0,))
+    s.random_nematic(w["seed"])
+    for plane in w["walls"]:
+        s.add_wall(2, plane, 0, w["W"])
+    s.add_sphere(w["sphere"][0], w["sphere"][1], 0, w["W"])
+    V = np.zeros((s.N, 5))
+    # warm-up: one iteration, then time up to K iterations within a bounded budget
+    fp = qo.FireParams(w["dt"], 0.99, 100 * w["dt"], 1.1, 0.95, 0.9, 0.0, 1e-12, 4)
+    st = qo.FireState()
+    lib = qo.lib()
+    lib.qo_fire_init(qo.C.byref(fp), qo.C.byref(st))
+    F = np.zeros((s.N, 5))
+    import ctypes as C
+    dp = lambda a: a.ctypes.data_as(C.POINTER(C.c_double))
+    ip = lambda a: a.ctypes.data_as(C.POINTER(C.c_int))
+    lib.qo_fire(C.byref(s.p), dp(s.Q), dp(V), dp(F), ip(s.types), s.objs, C.byref(fp), max(args.warmup, 1),
+                C.byref(st), None)
+    budget = 90.0
+    done, t0 = 0, time.perf_counter()
+    while done < args.steps and time.perf_counter() - t0 < budget:
+        target = st.iterations + 1
+        lib.qo_fire(C.byref(s.p), dp(s.Q), dp(V), dp(F), ip(s.types), s.objs, C.byref(fp), target, C.byref(st), None)
+        done += 1
+    el = time.perf_counter() - t0
+    value = s.N * done / el
+    cpu = {"value": value, "unit": "site-steps/s", "cores": used, "kind": "port",
+           "sample": f"{done} FIRE iterations of the 200^3 workload (each with the minimize() entry force "
+                     f"evaluation), {used} OpenMP threads, wall-clock bounded to {budget:.0f} s"}
+    return {"metric": METRIC, "value": value, "unit": "site-steps/s", "n_gpus": 0, "steps": done,
+            "warmup": max(args.warmup, 1), "ms_per_step": el / max(done, 1) * 1e3, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": "200^3 lattice, homeotropic z-walls (planes 0 and 199) + centred homeotropic "
+                                   "sphere r=30, W=5.3, L1-L3 = 2.32/1.0/0.5, FIRE dt=5e-4", "sites": s.N},
+            "impl": "reference", "cpu_baseline": cpu,
+            "e2e": {"value": value, "unit": "site-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=2000)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--cpu-sample-iters", type=int, default=2)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    rank = int(os.environ.get("RANK", 0))
+    world = int(os.environ.get("WORLD_SIZE", 1))
+
+    if args.impl == "reference":
+        if rank != 0:
+            return 0
+        print(json.dumps(run_reference(args)))
+        return 0
+
+    if world > 1:
+        import torch
+        torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", 0)))
+        torch.distributed.init_process_group("nccl")
+    out = run_ours(args, rank, world)
+    if rank == 0:
+        if not args.no_cpu_baseline:
+            out["cpu_baseline"], _ = cpu_baseline(args.cpu_sample_iters)
+        print(json.dumps(out))
+    if world > 1:
+        import torch
+        torch.distributed.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

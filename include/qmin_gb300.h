@@ -1,0 +1,172 @@
+/* qmin_gb300: GB300-native (sm_103a) Landau-de Gennes Q-tensor minimisation
+ * engine with the capabilities of open-Qmin's minimisation hot path.
+ *
+ * C ABI: plain pointers and sizes, int status codes (QMIN_OK = 0), no
+ * exceptions across the boundary.  A handle owns all device memory for one
+ * lattice; callers own every host buffer they pass.  A handle is used from one
+ * host thread at a time.  All work is issued on the handle's CUDA stream
+ * (qmin_set_stream; default: a stream the handle creates).
+ *
+ * Host arrays use the reference's layout unless a layout argument says
+ * otherwise: Q/V/F as AoS double[N][5] with components (Qxx, Qxy, Qxz, Qyy,
+ * Qyz) (open-Qmin inc/qTensorFunctions.h:8-12), site index
+ * i = x + Lx*(y + Ly*z) (inc/indexer.h:71-131), site types int32 with
+ * 0 = bulk LC, -1 = LC next to an object, -2 = LC on a rank face, j > 0 =
+ * site of object j-1 (src/model/multirankQTensorLatticeModel.h:9-15).
+ *
+ * Each entry point names the reference interface it replaces. */
+#ifndef QMIN_GB300_H
+#define QMIN_GB300_H
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* status codes */
+#define QMIN_OK 0
+#define QMIN_EINVAL 1      /* bad argument (null pointer, size, enum) */
+#define QMIN_ECUDA 2       /* CUDA runtime error (message in qmin_last_error_string) */
+#define QMIN_ENOMEM 3      /* device allocation failed */
+#define QMIN_ESTATE 4      /* call out of order (e.g. force before set_state) */
+#define QMIN_ENONFINITE 5  /* a reduction produced NaN/Inf (state left as computed) */
+#define QMIN_ENODEVICE 6   /* no CUDA device / extension not usable */
+
+/* precision of the resident state and stencil arithmetic */
+#define QMIN_FP64 0        /* every operation in FP64 (oracle-parity form) */
+#define QMIN_FP32 1        /* FP32 state and stencils, FP64 reductions */
+
+/* metric correction semantics (landauDeGennesLC::correctForceFromMetric) */
+#define QMIN_METRIC_CPU 0    /* reference CPU path: M^2 on bulk sites, M on boundary sites */
+#define QMIN_METRIC_SINGLE 1 /* reference GPU path: M once on every site */
+
+/* host array layouts */
+#define QMIN_LAYOUT_AOS 0  /* double[N][5] */
+#define QMIN_LAYOUT_SOA 1  /* double[5][N] */
+
+/* object (boundary) kinds, open-Qmin src/model/latticeBoundaries.h:8 */
+#define QMIN_HOMEOTROPIC 0
+#define QMIN_DEGENERATE_PLANAR 1
+
+typedef struct qmin_ctx *qmin_handle;
+
+typedef struct {
+    int Lx, Ly, Lz;
+    int precision;   /* QMIN_FP64 or QMIN_FP32 */
+    int metric_mode; /* QMIN_METRIC_CPU or QMIN_METRIC_SINGLE */
+} qmin_lattice_desc;
+
+/* landauDeGennesLC parameters (landauDeGennesLC.h:34-36, 76-91).  A, B, C are
+ * the phase constants exactly as the force class stores them (the CLI passes
+ * a = -1, b = -B/A, c = -C/A, openQmin.cpp:173-175). */
+typedef struct {
+    double A, B, C;
+    double L1, L2, L3, L4;
+    int multi_constant;  /* 0: one-constant (L1 only) path; 1: multi-constant forms */
+    int efield;          /* uniform E field on */
+    double E[3], eps, eps0, deps;
+    int hfield;          /* uniform H field on */
+    double H[3], chi, mu0, dchi;
+} qmin_ldg_params;
+
+/* boundaryObject{boundary, P1 = W, P2 = S0} (latticeBoundaries.h:20-39) */
+typedef struct {
+    int kind;
+    double W;
+    double S0;
+} qmin_object;
+
+/* energyMinimizerFIRE::setFIREParameters (energyMinimizerFIRE.h:33) */
+typedef struct {
+    double dt, alpha_start, dt_max, dt_inc, dt_dec, alpha_dec, alpha_min, force_cutoff;
+    int n_min;
+} qmin_fire_params;
+
+typedef struct {
+    int iterations;   /* updater::iterations (cumulative across runs) */
+    double force_max; /* sqrt(sum F._QT F) / nTotal (energyMinimizerFIRE.cpp:110) */
+    double alpha, dt, power;
+    int n_since;
+} qmin_fire_result;
+
+/* ---- lifetime (replaces constructing multirankQTensorLatticeModel +
+ *      landauDeGennesLC + GPUArray storage, openQmin.cpp:194-197) ---- */
+int qmin_create(const qmin_lattice_desc *desc, qmin_handle *out);
+int qmin_destroy(qmin_handle h);
+/* cudaStream_t passed as void* so the header needs no CUDA includes */
+int qmin_set_stream(qmin_handle h, void *stream);
+const char *qmin_last_error_string(void);
+/* count of this library's kernel launches issued through the handle */
+int qmin_kernel_launches(qmin_handle h, long long *count);
+
+/* ---- configuration ---- */
+/* landauDeGennesLC::setPhaseConstants / setElasticConstants / setEField / setHField */
+int qmin_set_params(qmin_handle h, const qmin_ldg_params *p);
+/* cubicLattice::boundaries (the GPUArray<boundaryObject> that createBoundaryObject grows) */
+int qmin_set_objects(qmin_handle h, const qmin_object *objs, int n);
+/* model positions + types (simpleModel::returnPositions/returnTypes, simpleModel.h:65-77);
+ * velocities are zeroed (simpleModel::initializeSimpleModel, simpleModel.cpp:39) */
+int qmin_set_state(qmin_handle h, const double *Q, const int32_t *types, int layout);
+/* read back positions/velocities/forces; any pointer may be NULL */
+int qmin_get_state(qmin_handle h, double *Q, double *V, double *F, int layout);
+/* number of non-object sites (updater::getNTotal, baseUpdater.cpp:10-28) */
+int qmin_n_active(qmin_handle h, long long *n);
+
+/* ---- force and energy ---- */
+/* multirankSimulation::computeForces -> landauDeGennesLC::computeForces
+ * (multirankSimulation.cpp:452-473, landauDeGennesLC.cpp:125-202).  The
+ * forces stay resident; F_out (host, AoS) may be NULL. */
+int qmin_force(qmin_handle h, double *F_out);
+/* multirankSimulation::computePotentialEnergy (multirankSimulation.cpp:475-490):
+ * e_per_active = E / NActive; comps = phase, distortion, anchoring, E-field,
+ * H-field totals (landauDeGennesLC::energyComponents). */
+int qmin_energy(qmin_handle h, double *e_per_active, double comps[5]);
+
+/* ---- minimisers (updater::Update -> performUpdate -> minimize) ---- */
+/* energyMinimizerFIRE constructor + setFIREParameters: resets alpha, dt,
+ * counters (energyMinimizerFIRE.cpp:24-43) */
+int qmin_fire_init(qmin_handle h, const qmin_fire_params *p);
+/* energyMinimizerFIRE::minimize (energyMinimizerFIRE.cpp:151-170) with
+ * setMaximumIterations(max_iterations); velocity Verlet + FIRE on the GPU,
+ * graph-captured, no host synchronisation inside a chunk of iterations. */
+int qmin_fire_run(qmin_handle h, int max_iterations, qmin_fire_result *res);
+/* energyMinimizerAdam::setAdamParameters + minimize (energyMinimizerAdam.h:20-31,
+ * energyMinimizerAdam.cpp:56-76); moments reset when reset != 0 */
+int qmin_adam_run(qmin_handle h, double beta1, double beta2, double eps, double dt, double force_cutoff,
+                  int max_iterations, int reset, int *iterations, double *force_max);
+/* energyMinimizerNesterovAG::setNesterovAGParameters + minimize
+ * (energyMinimizerNesterovAG.h:24-29, .cpp:94-120); the alternate sequence is
+ * re-seeded from Q when reset != 0 */
+int qmin_nesterov_run(qmin_handle h, double dt, double mu, double force_cutoff, int max_iterations, int reset,
+                      int *iterations, double *force_max);
+/* energyMinimizerLoLBFGS::setLoLBFGSParameters + minimize
+ * (energyMinimizerLoLBFGS.h:29-44, .cpp:195-226); history reset when reset != 0 */
+int qmin_lbfgs_run(qmin_handle h, int m, double eta, double force_cutoff, int max_iterations, int reset,
+                   int *iterations, double *force_max);
+
+/* ---- diagnostics ---- */
+/* Run `iterations` FIRE iterations with direct (non-graph) launches and CUDA
+ * events around every kernel; kernel_ms receives the average device time per
+ * launch of [0] predictor, [1] first-derivative planes (0 for one-constant),
+ * [2] force + half kick + reductions, [3] FIRE scalar control.  The FIRE state
+ * advances exactly as in qmin_fire_run.  No reference counterpart (profiling). */
+int qmin_fire_profile(qmin_handle h, int iterations, double kernel_ms[4]);
+
+/* ---- host-side set-up helpers (the reference runs these on the host even
+ *      in GPU runs, openQmin.cpp:261-268) ---- */
+/* qTensorLatticeModel::setNematicQTensorRandomly (qTensorLatticeModel.cpp:134-162)
+ * with noiseSource::setReproducibleSeed(seed): Q is AoS double[N][5] */
+int qmin_host_random_nematic(int Lx, int Ly, int Lz, int seed, double S0, double *Q);
+/* multirankSimulation::createWall (multirankSimulationBoundaries.cpp:101-167);
+ * *nobj is the number of objects so far and is incremented; objs has room
+ * for at least *nobj + 1 entries */
+int qmin_host_add_wall(int Lx, int Ly, int Lz, int xyz, int plane, int kind, double W, double S0, double *Q,
+                       int32_t *types, qmin_object *objs, int *nobj);
+/* multirankSimulation::createSphericalColloid (multirankSimulationBoundaries.cpp:169-215) */
+int qmin_host_add_sphere(int Lx, int Ly, int Lz, const double center[3], double radius, int kind, double W,
+                         double S0, double *Q, int32_t *types, qmin_object *objs, int *nobj);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

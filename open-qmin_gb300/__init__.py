@@ -1,0 +1,278 @@
+"""qmin_gb300: GB300-native (sm_103a) Landau-de Gennes Q-tensor minimisation.
+
+Python host layer over the C ABI in ``include/qmin_gb300.h``.  Two levels:
+
+* ``Lattice``: a thin, 1:1 wrapper of the C handle (state resident in HBM);
+* reference-shaped classes mirroring open-Qmin's model / force / updater /
+  simulation interfaces (``qTensorLatticeModel``, ``landauDeGennesLC``,
+  ``energyMinimizerFIRE``, ``energyMinimizerAdam``,
+  ``energyMinimizerNesterovAG``, ``energyMinimizerLoLBFGS``,
+  ``multirankSimulation``) so code written against the reference reads the
+  same here.
+
+All hot-path arithmetic runs in the CUDA library; there is no CPU fallback:
+without the built library or a CUDA device every compute call raises.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "libqmin_gb300.so")
+
+QMIN_OK, QMIN_EINVAL, QMIN_ECUDA, QMIN_ENOMEM, QMIN_ESTATE, QMIN_ENONFINITE, QMIN_ENODEVICE = range(7)
+FP64, FP32 = 0, 1
+METRIC_CPU, METRIC_SINGLE = 0, 1
+LAYOUT_AOS, LAYOUT_SOA = 0, 1
+HOMEOTROPIC, DEGENERATE_PLANAR = 0, 1
+
+EXPORTED_SYMBOLS = [
+    "qmin_create", "qmin_destroy", "qmin_set_stream", "qmin_last_error_string", "qmin_kernel_launches",
+    "qmin_set_params", "qmin_set_objects", "qmin_set_state", "qmin_get_state", "qmin_n_active", "qmin_force",
+    "qmin_energy", "qmin_fire_init", "qmin_fire_run", "qmin_adam_run", "qmin_nesterov_run", "qmin_lbfgs_run",
+    "qmin_host_random_nematic", "qmin_host_add_wall", "qmin_host_add_sphere",
+]
+
+
+class QminError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"qmin error {code}: {msg}")
+        self.code = code
+
+
+class LatticeDesc(C.Structure):
+    _fields_ = [("Lx", C.c_int), ("Ly", C.c_int), ("Lz", C.c_int), ("precision", C.c_int), ("metric_mode", C.c_int)]
+
+
+class LdgParams(C.Structure):
+    _fields_ = [("A", C.c_double), ("B", C.c_double), ("C", C.c_double),
+                ("L1", C.c_double), ("L2", C.c_double), ("L3", C.c_double), ("L4", C.c_double),
+                ("multi_constant", C.c_int), ("efield", C.c_int),
+                ("E", C.c_double * 3), ("eps", C.c_double), ("eps0", C.c_double), ("deps", C.c_double),
+                ("hfield", C.c_int),
+                ("H", C.c_double * 3), ("chi", C.c_double), ("mu0", C.c_double), ("dchi", C.c_double)]
+
+
+class Object(C.Structure):
+    _fields_ = [("kind", C.c_int), ("W", C.c_double), ("S0", C.c_double)]
+
+
+class FireParams(C.Structure):
+    _fields_ = [("dt", C.c_double), ("alpha_start", C.c_double), ("dt_max", C.c_double), ("dt_inc", C.c_double),
+                ("dt_dec", C.c_double), ("alpha_dec", C.c_double), ("alpha_min", C.c_double),
+                ("force_cutoff", C.c_double), ("n_min", C.c_int)]
+
+
+class FireResult(C.Structure):
+    _fields_ = [("iterations", C.c_int), ("force_max", C.c_double), ("alpha", C.c_double), ("dt", C.c_double),
+                ("power", C.c_double), ("n_since", C.c_int)]
+
+
+_lib = None
+
+
+def lib():
+    """Load the native library; raises if it has not been built."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise RuntimeError(f"qmin_gb300 native library missing ({LIB_PATH}); run __graft_entry__.build()")
+        L = C.CDLL(LIB_PATH)
+        h, dp, ip, vp = C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_int), C.c_void_p
+        sig = {
+            "qmin_create": [C.POINTER(LatticeDesc), C.POINTER(C.c_void_p)],
+            "qmin_destroy": [h], "qmin_set_stream": [h, vp],
+            "qmin_kernel_launches": [h, C.POINTER(C.c_longlong)],
+            "qmin_set_params": [h, C.POINTER(LdgParams)], "qmin_set_objects": [h, C.POINTER(Object), C.c_int],
+            "qmin_set_state": [h, vp, vp, C.c_int], "qmin_get_state": [h, vp, vp, vp, C.c_int],
+            "qmin_n_active": [h, C.POINTER(C.c_longlong)], "qmin_force": [h, vp],
+            "qmin_energy": [h, dp, dp], "qmin_fire_init": [h, C.POINTER(FireParams)],
+            "qmin_fire_run": [h, C.c_int, C.POINTER(FireResult)],
+            "qmin_adam_run": [h, C.c_double, C.c_double, C.c_double, C.c_double, C.c_double, C.c_int, C.c_int, ip, dp],
+            "qmin_nesterov_run": [h, C.c_double, C.c_double, C.c_double, C.c_int, C.c_int, ip, dp],
+            "qmin_lbfgs_run": [h, C.c_int, C.c_double, C.c_double, C.c_int, C.c_int, ip, dp],
+            "qmin_host_random_nematic": [C.c_int, C.c_int, C.c_int, C.c_int, C.c_double, dp],
+            "qmin_host_add_wall": [C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_double, C.c_double, dp,
+                                   ip, C.POINTER(Object), ip],
+            "qmin_host_add_sphere": [C.c_int, C.c_int, C.c_int, dp, C.c_double, C.c_int, C.c_double, C.c_double, dp,
+                                     ip, C.POINTER(Object), ip],
+        }
+        for name, args in sig.items():
+            fn = getattr(L, name)
+            fn.argtypes = args
+            fn.restype = C.c_int
+        L.qmin_last_error_string.restype = C.c_char_p
+        L.qmin_last_error_string.argtypes = []
+        _lib = L
+    return _lib
+
+
+def _check(code):
+    if code != QMIN_OK:
+        raise QminError(code, lib().qmin_last_error_string().decode())
+
+
+def _dp(a):
+    return a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+def _ip(a):
+    return a.ctypes.data_as(C.POINTER(C.c_int))
+
+
+def cli_phase_constants(A=-0.172, B=-2.12, Cc=1.73):
+    """openQmin.cpp:173-175 rescaling and the S0 of openQmin.cpp:266."""
+    a, b, c = -1.0, -B / A, -Cc / A
+    S0 = (-b + np.sqrt(b * b - 24 * a * c)) / (6 * c)
+    return a, b, c, float(S0)
+
+
+# ---------------------------------------------------------------- host set-up
+def host_random_nematic(L, seed, S0):
+    """qTensorLatticeModel::setNematicQTensorRandomly with seed (host)."""
+    N = L[0] * L[1] * L[2]
+    Q = np.zeros((N, 5))
+    _check(lib().qmin_host_random_nematic(L[0], L[1], L[2], int(seed), float(S0), _dp(Q)))
+    return Q
+
+
+class Geometry:
+    """Q field, site types and object table under construction on the host."""
+
+    def __init__(self, L, Q):
+        self.L = tuple(int(x) for x in L)
+        self.Q = np.ascontiguousarray(Q, dtype=np.float64)
+        self.types = np.zeros(self.L[0] * self.L[1] * self.L[2], dtype=np.int32)
+        self.objs = (Object * 127)()
+        self.nobj = C.c_int(0)
+
+    def add_wall(self, xyz, plane, kind, W, S0):
+        _check(lib().qmin_host_add_wall(*self.L, int(xyz), int(plane), int(kind), float(W), float(S0), _dp(self.Q),
+                                        _ip(self.types), self.objs, C.byref(self.nobj)))
+
+    def add_sphere(self, center, radius, kind, W, S0):
+        c = (C.c_double * 3)(*[float(x) for x in center])
+        _check(lib().qmin_host_add_sphere(*self.L, c, float(radius), int(kind), float(W), float(S0), _dp(self.Q),
+                                          _ip(self.types), self.objs, C.byref(self.nobj)))
+
+    def objects(self):
+        return [(self.objs[k].kind, self.objs[k].W, self.objs[k].S0) for k in range(self.nobj.value)]
+
+
+# -------------------------------------------------------------- C handle
+class Lattice:
+    """One lattice resident on the GPU (a qmin_handle)."""
+
+    def __init__(self, L, precision=FP64, metric_mode=METRIC_CPU):
+        self.L = tuple(int(x) for x in L)
+        self.N = self.L[0] * self.L[1] * self.L[2]
+        self.precision = precision
+        d = LatticeDesc(self.L[0], self.L[1], self.L[2], precision, metric_mode)
+        self._h = C.c_void_p()
+        _check(lib().qmin_create(C.byref(d), C.byref(self._h)))
+
+    def close(self):
+        if self._h:
+            lib().qmin_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_params(self, A, B, Cc, L1=0.0, L2=0.0, L3=0.0, L4=0.0, multi_constant=None, E=None, H=None):
+        p = LdgParams()
+        p.A, p.B, p.C = A, B, Cc
+        p.L1, p.L2, p.L3, p.L4 = L1, L2, L3, L4
+        p.multi_constant = int(any(x != 0 for x in (L2, L3, L4))) if multi_constant is None else int(multi_constant)
+        if E is not None:
+            p.efield = 1
+            p.E[0], p.E[1], p.E[2], p.eps, p.eps0, p.deps = E
+        if H is not None:
+            p.hfield = 1
+            p.H[0], p.H[1], p.H[2], p.chi, p.mu0, p.dchi = H
+        _check(lib().qmin_set_params(self._h, C.byref(p)))
+
+    def set_objects(self, objs):
+        arr = (Object * max(len(objs), 1))()
+        for k, (kind, W, S0) in enumerate(objs):
+            arr[k].kind, arr[k].W, arr[k].S0 = kind, W, S0
+        _check(lib().qmin_set_objects(self._h, arr, len(objs)))
+
+    def set_state(self, Q, types, layout=LAYOUT_AOS):
+        Q = np.ascontiguousarray(Q, dtype=np.float64)
+        types = np.ascontiguousarray(types, dtype=np.int32)
+        _check(lib().qmin_set_state(self._h, Q.ctypes.data, types.ctypes.data, layout))
+
+    def set_state_ptr(self, q_ptr, t_ptr, layout=LAYOUT_AOS):
+        _check(lib().qmin_set_state(self._h, q_ptr, t_ptr, layout))
+
+    def get_state(self, Q=True, V=False, F=False, layout=LAYOUT_AOS):
+        shape = (self.N, 5) if layout == LAYOUT_AOS else (5, self.N)
+        out = [np.zeros(shape) if want else None for want in (Q, V, F)]
+        ptrs = [o.ctypes.data if o is not None else None for o in out]
+        _check(lib().qmin_get_state(self._h, *ptrs, layout))
+        return out
+
+    def get_state_ptr(self, q_ptr, v_ptr, f_ptr, layout=LAYOUT_AOS):
+        _check(lib().qmin_get_state(self._h, q_ptr, v_ptr, f_ptr, layout))
+
+    def n_active(self):
+        n = C.c_longlong()
+        _check(lib().qmin_n_active(self._h, C.byref(n)))
+        return n.value
+
+    def force(self, copy=True):
+        F = np.zeros((self.N, 5)) if copy else None
+        _check(lib().qmin_force(self._h, F.ctypes.data if copy else None))
+        return F
+
+    def energy(self):
+        e = C.c_double()
+        comps = np.zeros(5)
+        _check(lib().qmin_energy(self._h, C.byref(e), _dp(comps)))
+        return e.value, comps
+
+    def fire_init(self, dt=5e-4, alpha_start=0.99, dt_max=None, dt_inc=1.1, dt_dec=0.95, alpha_dec=0.9,
+                  n_min=4, force_cutoff=1e-12, alpha_min=0.0):
+        """Defaults: the reference CLI's FIRE parameters (openQmin.cpp:256-258)."""
+        p = FireParams(dt, alpha_start, 100 * dt if dt_max is None else dt_max, dt_inc, dt_dec, alpha_dec,
+                       alpha_min, force_cutoff, n_min)
+        _check(lib().qmin_fire_init(self._h, C.byref(p)))
+
+    def fire_run(self, max_iterations):
+        r = FireResult()
+        _check(lib().qmin_fire_run(self._h, int(max_iterations), C.byref(r)))
+        return dict(iterations=r.iterations, forceMax=r.force_max, alpha=r.alpha, dt=r.dt, power=r.power,
+                    nsince=r.n_since)
+
+    def adam_run(self, max_iterations, dt=1e-4, beta1=0.9, beta2=0.99, eps=1e-8, force_cutoff=1e-12, reset=True):
+        it, fm = C.c_int(), C.c_double()
+        _check(lib().qmin_adam_run(self._h, beta1, beta2, eps, dt, force_cutoff, int(max_iterations), int(reset),
+                                   C.byref(it), C.byref(fm)))
+        return dict(iterations=it.value, forceMax=fm.value)
+
+    def nesterov_run(self, max_iterations, dt=1e-4, mu=0.01, force_cutoff=1e-12, reset=True):
+        it, fm = C.c_int(), C.c_double()
+        _check(lib().qmin_nesterov_run(self._h, dt, mu, force_cutoff, int(max_iterations), int(reset), C.byref(it),
+                                       C.byref(fm)))
+        return dict(iterations=it.value, forceMax=fm.value)
+
+    def lbfgs_run(self, max_iterations, eta=1e-4, m=5, force_cutoff=1e-12, reset=True):
+        it, fm = C.c_int(), C.c_double()
+        _check(lib().qmin_lbfgs_run(self._h, int(m), eta, force_cutoff, int(max_iterations), int(reset), C.byref(it),
+                                    C.byref(fm)))
+        return dict(iterations=it.value, forceMax=fm.value)
+
+    def launches(self):
+        n = C.c_longlong()
+        _check(lib().qmin_kernel_launches(self._h, C.byref(n)))
+        return n.value
+
+
+from .reference_api import (energyMinimizerAdam, energyMinimizerFIRE, energyMinimizerLoLBFGS,  # noqa: E402,F401
+                            energyMinimizerNesterovAG, landauDeGennesLC, multirankSimulation,
+                            qTensorLatticeModel, boundaryObject, boundaryType)

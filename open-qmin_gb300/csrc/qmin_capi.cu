@@ -1,0 +1,746 @@
+// qmin_gb300 C ABI: handle lifetime, state transfer, force/energy and the
+// minimiser drivers.  Minimiser loops run as captured CUDA graphs of a fixed
+// chunk of iterations; the loop condition lives on the device (every kernel of
+// an iteration returns at once when the minimiser is no longer active), and
+// the host reads it back once per chunk.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/qmin_gb300.h"
+#include "qmin_bulk_forms.h"
+#include "qmin_internal.h"
+
+using namespace qmin;
+
+static thread_local std::string g_err;
+
+static int fail(int code, const std::string &msg)
+{
+    g_err = msg;
+    return code;
+}
+
+#define CK(call)                                                                              \
+    do {                                                                                      \
+        cudaError_t e_ = (call);                                                              \
+        if (e_ != cudaSuccess)                                                                \
+            return fail(QMIN_ECUDA, std::string(#call) + ": " + cudaGetErrorString(e_));      \
+    } while (0)
+
+struct qmin_ctx {
+    int Lx = 0, Ly = 0, Lz = 0, N = 0;
+    long long P = 0;
+    int prec = QMIN_FP64, metric_mode = QMIN_METRIC_CPU;
+    size_t esz = 8;
+    cudaStream_t stream = nullptr;
+    bool own_stream = false;
+    void *Q = nullptr, *V = nullptr, *F = nullptr, *D = nullptr;
+    int8_t *types = nullptr;
+    void *objs = nullptr;
+    int nobj = 0;
+    std::vector<qmin_object> objs_host;
+    double *partials = nullptr;
+    int grid = 1;
+    double *stage = nullptr;
+    int32_t *stage_t = nullptr;
+    FireDev *fire = nullptr;
+    FireDev *fire_h = nullptr;  // pinned mirror
+    IterDev *iter = nullptr;
+    IterDev *iter_h = nullptr;  // pinned mirror
+    double *out5 = nullptr;
+    double *out5_h = nullptr;
+    void *M = nullptr, *S = nullptr, *alt = nullptr, *lbp = nullptr, *lbs = nullptr, *lby = nullptr;
+    int lb_m = 0;
+    qmin_ldg_params params{};
+    bool have_params = false, have_state = false, fire_ready = false;
+    int max_type = 0;
+    long long nTotal = 0;
+    long long launches = 0;
+    // cached chunk graphs: 0 FIRE, 1 Adam, 2 Nesterov, 3 L-BFGS
+    cudaGraphExec_t graph[4] = {nullptr, nullptr, nullptr, nullptr};
+    int graph_per_iter[4] = {0, 0, 0, 0};
+    int graph_key[4] = {0, 0, 0, 0};
+    double graph_args[4][4] = {};  // scalar kernel arguments baked into each graph
+    int version = 1;  // bumped whenever kernel arguments change
+};
+
+static const int kChunk = 32;  // iterations per captured graph
+
+template <class T> static Lat<T> make_lat(qmin_ctx *h)
+{
+    Lat<T> L;
+    memset(&L, 0, sizeof L);
+    L.Lx = h->Lx;
+    L.Ly = h->Ly;
+    L.Lz = h->Lz;
+    L.N = h->N;
+    L.P = h->P;
+    L.Q = (T *)h->Q;
+    L.V = (T *)h->V;
+    L.F = (T *)h->F;
+    L.types = h->types;
+    L.D = (T *)h->D;
+    L.objs = (const ObjDev<T> *)h->objs;
+    const qmin_ldg_params &p = h->params;
+    L.a = T(0.5 * p.A);
+    L.b = T(p.B / 3.0);
+    L.c = T(0.25 * p.C);
+    L.L1 = T(p.L1);
+    L.L2 = T(p.L2);
+    L.L3 = T(p.L3);
+    L.L4 = T(p.L4);
+    // uniform-field force vectors (landauDeGennesLCOtherForces.cpp:297-303)
+    auto field = [](const double *fld, double aniso, double perm, T *out) {
+        double pr = aniso * perm;
+        out[0] = T(-0.5 * pr * (fld[0] * fld[0] - fld[2] * fld[2]));
+        out[1] = T(-pr * fld[0] * fld[1]);
+        out[2] = T(-pr * fld[0] * fld[2]);
+        out[3] = T(-0.5 * pr * (fld[1] * fld[1] - fld[2] * fld[2]));
+        out[4] = T(-pr * fld[1] * fld[2]);
+    };
+    if (p.efield) field(p.E, p.deps, p.eps0, L.fE);
+    if (p.hfield) field(p.H, p.dchi, p.mu0, L.fH);
+    L.metric_mode = h->metric_mode;
+    L.multi = p.multi_constant;
+    L.efield = p.efield;
+    L.hfield = p.hfield;
+    const double Lt[3] = {p.L2, p.L3, p.L4};
+    for (int k = 0; k < 5; ++k)
+        for (int n = 0; n < QMIN_BULK_W; ++n) {
+            double c = 0.0;
+            if (n < qmin_bulk_n[k])
+                for (int t = 0; t < 3; ++t) c += Lt[t] * (double)qmin_bulk_k[t][k][n] * 0.25;
+            L.cb[k * QMIN_BULK_W + n] = T(c);
+        }
+    return L;
+}
+
+static void free_ctx(qmin_ctx *h)
+{
+    for (int g = 0; g < 4; ++g)
+        if (h->graph[g]) cudaGraphExecDestroy(h->graph[g]);
+    void *bufs[] = {h->Q, h->V, h->F, h->D, h->types, h->objs, h->partials, h->stage, h->stage_t, h->fire, h->iter,
+                    h->out5, h->M, h->S, h->alt, h->lbp, h->lbs, h->lby};
+    for (void *b : bufs)
+        if (b) cudaFree(b);
+    if (h->fire_h) cudaFreeHost(h->fire_h);
+    if (h->iter_h) cudaFreeHost(h->iter_h);
+    if (h->out5_h) cudaFreeHost(h->out5_h);
+    if (h->own_stream && h->stream) cudaStreamDestroy(h->stream);
+    delete h;
+}
+
+static void invalidate_graphs(qmin_ctx *h)
+{
+    h->version++;
+    for (int g = 0; g < 4; ++g)
+        if (h->graph[g]) {
+            cudaGraphExecDestroy(h->graph[g]);
+            h->graph[g] = nullptr;
+        }
+}
+
+// The API functions below take C linkage from their declarations in
+// qmin_gb300.h (included above).
+
+const char *qmin_last_error_string(void) { return g_err.c_str(); }
+
+int qmin_create(const qmin_lattice_desc *desc, qmin_handle *out)
+{
+    if (!desc || !out) return fail(QMIN_EINVAL, "qmin_create: null argument");
+    *out = nullptr;
+    if (desc->Lx < 3 || desc->Ly < 3 || desc->Lz < 3)
+        return fail(QMIN_EINVAL, "qmin_create: every lattice side must be >= 3");
+    long long N = (long long)desc->Lx * desc->Ly * desc->Lz;
+    if (N > 1500000000LL) return fail(QMIN_EINVAL, "qmin_create: lattice too large (N > 1.5e9 sites)");
+    if (desc->precision != QMIN_FP64 && desc->precision != QMIN_FP32)
+        return fail(QMIN_EINVAL, "qmin_create: precision must be QMIN_FP64 or QMIN_FP32");
+    if (desc->metric_mode != QMIN_METRIC_CPU && desc->metric_mode != QMIN_METRIC_SINGLE)
+        return fail(QMIN_EINVAL, "qmin_create: bad metric_mode");
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+        cudaGetLastError();
+        return fail(QMIN_ENODEVICE, "qmin_create: no CUDA device available");
+    }
+    qmin_ctx *h = new qmin_ctx();
+    h->Lx = desc->Lx;
+    h->Ly = desc->Ly;
+    h->Lz = desc->Lz;
+    h->N = (int)N;
+    h->P = (N + 31) / 32 * 32;
+    h->prec = desc->precision;
+    h->metric_mode = desc->metric_mode;
+    h->esz = h->prec == QMIN_FP64 ? 8 : 4;
+    h->grid = reduction_grid(h->N);
+    cudaError_t e = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking);
+    if (e != cudaSuccess) {
+        delete h;
+        return fail(QMIN_ECUDA, std::string("cudaStreamCreate: ") + cudaGetErrorString(e));
+    }
+    h->own_stream = true;
+    size_t plane = (size_t)h->P * h->esz;
+    bool ok = cudaMalloc(&h->Q, 5 * plane) == cudaSuccess && cudaMalloc(&h->V, 5 * plane) == cudaSuccess &&
+              cudaMalloc(&h->F, 5 * plane) == cudaSuccess && cudaMalloc(&h->types, (size_t)h->P) == cudaSuccess &&
+              cudaMalloc(&h->partials, sizeof(double) * 8 * (size_t)h->grid) == cudaSuccess &&
+              cudaMalloc(&h->fire, sizeof(FireDev)) == cudaSuccess &&
+              cudaMalloc(&h->iter, sizeof(IterDev)) == cudaSuccess &&
+              cudaMalloc(&h->out5, sizeof(double) * 8) == cudaSuccess &&
+              cudaMallocHost(&h->fire_h, sizeof(FireDev)) == cudaSuccess &&
+              cudaMallocHost(&h->iter_h, sizeof(IterDev)) == cudaSuccess &&
+              cudaMallocHost(&h->out5_h, sizeof(double) * 8) == cudaSuccess;
+    if (!ok) {
+        cudaGetLastError();
+        free_ctx(h);
+        return fail(QMIN_ENOMEM, "qmin_create: device allocation failed");
+    }
+    cudaMemsetAsync(h->Q, 0, 5 * plane, h->stream);
+    cudaMemsetAsync(h->V, 0, 5 * plane, h->stream);
+    cudaMemsetAsync(h->F, 0, 5 * plane, h->stream);
+    cudaMemsetAsync(h->types, 0, (size_t)h->P, h->stream);
+    memset(h->fire_h, 0, sizeof(FireDev));
+    memset(h->iter_h, 0, sizeof(IterDev));
+    *out = h;
+    return QMIN_OK;
+}
+
+int qmin_destroy(qmin_handle h)
+{
+    if (!h) return fail(QMIN_EINVAL, "qmin_destroy: null handle");
+    cudaStreamSynchronize(h->stream);
+    free_ctx(h);
+    return QMIN_OK;
+}
+
+int qmin_set_stream(qmin_handle h, void *stream)
+{
+    if (!h) return fail(QMIN_EINVAL, "qmin_set_stream: null handle");
+    CK(cudaStreamSynchronize(h->stream));
+    if (h->own_stream) cudaStreamDestroy(h->stream);
+    h->stream = (cudaStream_t)stream;
+    h->own_stream = false;
+    invalidate_graphs(h);
+    return QMIN_OK;
+}
+
+int qmin_kernel_launches(qmin_handle h, long long *count)
+{
+    if (!h || !count) return fail(QMIN_EINVAL, "qmin_kernel_launches: null argument");
+    *count = h->launches;
+    return QMIN_OK;
+}
+
+int qmin_set_params(qmin_handle h, const qmin_ldg_params *p)
+{
+    if (!h || !p) return fail(QMIN_EINVAL, "qmin_set_params: null argument");
+    h->params = *p;
+    if (p->multi_constant && !h->D) {
+        if (cudaMalloc(&h->D, 15 * (size_t)h->P * h->esz) != cudaSuccess) {
+            cudaGetLastError();
+            return fail(QMIN_ENOMEM, "qmin_set_params: derivative planes allocation failed");
+        }
+        CK(cudaMemsetAsync(h->D, 0, 15 * (size_t)h->P * h->esz, h->stream));
+    }
+    h->have_params = true;
+    invalidate_graphs(h);
+    return QMIN_OK;
+}
+
+int qmin_set_objects(qmin_handle h, const qmin_object *objs, int n)
+{
+    if (!h || (n > 0 && !objs) || n < 0) return fail(QMIN_EINVAL, "qmin_set_objects: bad argument");
+    if (n > 127) return fail(QMIN_EINVAL, "qmin_set_objects: at most 127 objects (int8 site types)");
+    for (int k = 0; k < n; ++k)
+        if (objs[k].kind != QMIN_HOMEOTROPIC && objs[k].kind != QMIN_DEGENERATE_PLANAR)
+            return fail(QMIN_EINVAL, "qmin_set_objects: unknown object kind");
+    h->objs_host.assign(objs, objs + n);
+    h->nobj = n;
+    if (h->objs) cudaFree(h->objs);
+    h->objs = nullptr;
+    size_t bytes = (size_t)std::max(n, 1) * (h->prec == QMIN_FP64 ? sizeof(ObjDev<double>) : sizeof(ObjDev<float>));
+    CK(cudaMalloc(&h->objs, bytes));
+    if (h->prec == QMIN_FP64) {
+        std::vector<ObjDev<double>> o(std::max(n, 1));
+        for (int k = 0; k < n; ++k) o[k] = {objs[k].kind, objs[k].W, objs[k].S0};
+        CK(cudaMemcpy(h->objs, o.data(), bytes, cudaMemcpyHostToDevice));
+    } else {
+        std::vector<ObjDev<float>> o(std::max(n, 1));
+        for (int k = 0; k < n; ++k) o[k] = {objs[k].kind, (float)objs[k].W, (float)objs[k].S0};
+        CK(cudaMemcpy(h->objs, o.data(), bytes, cudaMemcpyHostToDevice));
+    }
+    invalidate_graphs(h);
+    return QMIN_OK;
+}
+
+static int ensure_stage(qmin_ctx *h)
+{
+    if (!h->stage) {
+        if (cudaMalloc(&h->stage, sizeof(double) * 5 * (size_t)h->N) != cudaSuccess ||
+            cudaMalloc(&h->stage_t, sizeof(int32_t) * (size_t)h->N) != cudaSuccess) {
+            cudaGetLastError();
+            return fail(QMIN_ENOMEM, "staging buffer allocation failed");
+        }
+    }
+    return QMIN_OK;
+}
+
+int qmin_set_state(qmin_handle h, const double *Q, const int32_t *types, int layout)
+{
+    if (!h || !Q || !types) return fail(QMIN_EINVAL, "qmin_set_state: null argument");
+    if (layout != QMIN_LAYOUT_AOS && layout != QMIN_LAYOUT_SOA) return fail(QMIN_EINVAL, "qmin_set_state: bad layout");
+    int r = ensure_stage(h);
+    if (r) return r;
+    long long nT = 0;
+    int mx = 0;
+    for (int i = 0; i < h->N; ++i) {
+        int t = types[i];
+        if (t < -2 || t > 127) return fail(QMIN_EINVAL, "qmin_set_state: site type out of range [-2, 127]");
+        if (t <= 0) ++nT;
+        mx = std::max(mx, t);
+    }
+    h->nTotal = nT;
+    h->max_type = mx;
+    CK(cudaMemcpyAsync(h->stage, Q, sizeof(double) * 5 * (size_t)h->N, cudaMemcpyHostToDevice, h->stream));
+    CK(cudaMemcpyAsync(h->stage_t, types, sizeof(int32_t) * (size_t)h->N, cudaMemcpyHostToDevice, h->stream));
+    if (h->prec == QMIN_FP64)
+        h->launches += launch_aos_to_soa<double>(h->stage, (double *)h->Q, h->N, h->P, layout, h->stream);
+    else
+        h->launches += launch_aos_to_soa<float>(h->stage, (float *)h->Q, h->N, h->P, layout, h->stream);
+    h->launches += launch_types_to_i8(h->stage_t, h->types, h->N, h->stream);
+    CK(cudaMemsetAsync(h->V, 0, 5 * (size_t)h->P * h->esz, h->stream));
+    CK(cudaMemsetAsync(h->F, 0, 5 * (size_t)h->P * h->esz, h->stream));
+    CK(cudaGetLastError());
+    h->have_state = true;
+    return QMIN_OK;
+}
+
+int qmin_get_state(qmin_handle h, double *Q, double *V, double *F, int layout)
+{
+    if (!h) return fail(QMIN_EINVAL, "qmin_get_state: null handle");
+    if (layout != QMIN_LAYOUT_AOS && layout != QMIN_LAYOUT_SOA) return fail(QMIN_EINVAL, "qmin_get_state: bad layout");
+    int r = ensure_stage(h);
+    if (r) return r;
+    void *src[3] = {h->Q, h->V, h->F};
+    double *dst[3] = {Q, V, F};
+    for (int a = 0; a < 3; ++a) {
+        if (!dst[a]) continue;
+        if (h->prec == QMIN_FP64)
+            h->launches += launch_soa_to_aos<double>((const double *)src[a], h->stage, h->N, h->P, layout, h->stream);
+        else
+            h->launches += launch_soa_to_aos<float>((const float *)src[a], h->stage, h->N, h->P, layout, h->stream);
+        CK(cudaMemcpyAsync(dst[a], h->stage, sizeof(double) * 5 * (size_t)h->N, cudaMemcpyDeviceToHost, h->stream));
+    }
+    CK(cudaStreamSynchronize(h->stream));
+    return QMIN_OK;
+}
+
+int qmin_n_active(qmin_handle h, long long *n)
+{
+    if (!h || !n) return fail(QMIN_EINVAL, "qmin_n_active: null argument");
+    if (!h->have_state) return fail(QMIN_ESTATE, "qmin_n_active: no state set");
+    *n = h->nTotal;
+    return QMIN_OK;
+}
+
+static int ready(qmin_ctx *h, const char *who)
+{
+    if (!h) return fail(QMIN_EINVAL, std::string(who) + ": null handle");
+    if (!h->have_state) return fail(QMIN_ESTATE, std::string(who) + ": qmin_set_state has not been called");
+    if (!h->have_params) return fail(QMIN_ESTATE, std::string(who) + ": qmin_set_params has not been called");
+    if (h->max_type > h->nobj)
+        return fail(QMIN_ESTATE, std::string(who) + ": a site type names an object that qmin_set_objects did not define");
+    if (h->nobj > 0 && !h->objs) return fail(QMIN_ESTATE, std::string(who) + ": objects missing");
+    if (!h->objs) {
+        // a one-entry dummy table keeps the kernel argument valid
+        if (cudaMalloc(&h->objs, sizeof(ObjDev<double>)) != cudaSuccess) return fail(QMIN_ENOMEM, "object table");
+    }
+    return QMIN_OK;
+}
+
+template <class T> static int force_impl(qmin_ctx *h)
+{
+    Lat<T> L = make_lat<T>(h);
+    h->launches += launch_force<T>(L, h->grid, h->stream);
+    CK(cudaGetLastError());
+    return QMIN_OK;
+}
+
+int qmin_force(qmin_handle h, double *F_out)
+{
+    int r = ready(h, "qmin_force");
+    if (r) return r;
+    r = h->prec == QMIN_FP64 ? force_impl<double>(h) : force_impl<float>(h);
+    if (r) return r;
+    if (F_out) return qmin_get_state(h, nullptr, nullptr, F_out, QMIN_LAYOUT_AOS);
+    CK(cudaStreamSynchronize(h->stream));
+    return QMIN_OK;
+}
+
+int qmin_energy(qmin_handle h, double *e_per_active, double comps[5])
+{
+    int r = ready(h, "qmin_energy");
+    if (r) return r;
+    const qmin_ldg_params &p = h->params;
+    double E0[3] = {0, 0, 0}, H0[3] = {0, 0, 0};
+    const double *E = p.efield ? p.E : E0, *H = p.hfield ? p.H : H0;
+    if (h->prec == QMIN_FP64)
+        h->launches += launch_energy_full<double>(make_lat<double>(h), h->partials, h->grid, h->out5, E, p.eps, p.eps0,
+                                                  p.deps, H, p.chi, p.mu0, p.dchi, h->stream);
+    else
+        h->launches += launch_energy_full<float>(make_lat<float>(h), h->partials, h->grid, h->out5, E, p.eps, p.eps0,
+                                                 p.deps, H, p.chi, p.mu0, p.dchi, h->stream);
+    CK(cudaGetLastError());
+    CK(cudaMemcpyAsync(h->out5_h, h->out5, sizeof(double) * 5, cudaMemcpyDeviceToHost, h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+    const double *c = h->out5_h;
+    double total = c[0] + c[1] + c[2] + c[3] + c[4];
+    if (comps)
+        for (int k = 0; k < 5; ++k) comps[k] = c[k];
+    if (e_per_active) *e_per_active = h->nTotal != 0 ? total / (1.0 * (double)h->nTotal) : total;
+    if (!std::isfinite(total)) return fail(QMIN_ENONFINITE, "qmin_energy: non-finite energy");
+    return QMIN_OK;
+}
+
+// ------------------------------------------------------------- graphs
+// Record `per_iter` launches of one iteration kChunk times into a graph.
+template <class F> static int capture_chunk(qmin_ctx *h, int slot, const double (&args)[4], F &&one_iteration)
+{
+    if (h->graph[slot] && h->graph_key[slot] == h->version &&
+        memcmp(h->graph_args[slot], args, sizeof(args)) == 0)
+        return QMIN_OK;
+    if (h->graph[slot]) {
+        cudaGraphExecDestroy(h->graph[slot]);
+        h->graph[slot] = nullptr;
+    }
+    cudaGraph_t g = nullptr;
+    CK(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
+    int per = 0;
+    for (int k = 0; k < kChunk; ++k) per = one_iteration();
+    cudaError_t e = cudaStreamEndCapture(h->stream, &g);
+    if (e != cudaSuccess) return fail(QMIN_ECUDA, std::string("graph capture: ") + cudaGetErrorString(e));
+    e = cudaGraphInstantiate(&h->graph[slot], g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) return fail(QMIN_ECUDA, std::string("graph instantiate: ") + cudaGetErrorString(e));
+    h->graph_per_iter[slot] = per;
+    h->graph_key[slot] = h->version;
+    memcpy(h->graph_args[slot], args, sizeof(args));
+    return QMIN_OK;
+}
+
+// Launch chunks until the device-side `active` flag (at byte offset `flag_off`
+// of the pinned mirror) drops; returns after the final state has been copied.
+template <class S> static int run_chunks(qmin_ctx *h, int slot, S *dev, S *host, int max_chunks)
+{
+    for (int c = 0; c < max_chunks; ++c) {
+        CK(cudaGraphLaunch(h->graph[slot], h->stream));
+        h->launches += (long long)kChunk * h->graph_per_iter[slot];
+        CK(cudaMemcpyAsync(host, dev, sizeof(S), cudaMemcpyDeviceToHost, h->stream));
+        CK(cudaStreamSynchronize(h->stream));
+        if (!host->active) break;
+    }
+    return QMIN_OK;
+}
+
+int qmin_fire_init(qmin_handle h, const qmin_fire_params *p)
+{
+    if (!h || !p) return fail(QMIN_EINVAL, "qmin_fire_init: null argument");
+    if (!(p->dt > 0)) return fail(QMIN_EINVAL, "qmin_fire_init: dt must be > 0");
+    FireDev *f = h->fire_h;
+    memset(f, 0, sizeof(FireDev));
+    // energyMinimizerFIRE::initializeParameters + setFIREParameters (energyMinimizerFIRE.cpp:24-43, 172-183)
+    f->dt = p->dt;
+    f->dtmin = p->dt * .01;
+    f->alpha = p->alpha_start;
+    f->alpha0 = p->alpha_start;
+    f->dtmax = p->dt_max;
+    f->dtinc = p->dt_inc;
+    f->dtdec = p->dt_dec;
+    f->alphadec = p->alpha_dec;
+    f->alphamin = p->alpha_min;
+    f->fcut = p->force_cutoff;
+    f->nmin = p->n_min;
+    f->forceMax = 100.;
+    CK(cudaMemcpyAsync(h->fire, f, sizeof(FireDev), cudaMemcpyHostToDevice, h->stream));
+    if (h->have_state) CK(cudaMemsetAsync(h->V, 0, 5 * (size_t)h->P * h->esz, h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+    h->fire_ready = true;
+    return QMIN_OK;
+}
+
+template <class T> static int fire_impl(qmin_ctx *h, int max_iterations)
+{
+    Lat<T> L = make_lat<T>(h);
+    // minimize(): forces at the current Q first (energyMinimizerFIRE.cpp:157)
+    h->launches += launch_force<T>(L, h->grid, h->stream);
+    const double args[4] = {0, 0, 0, 0};
+    int r = capture_chunk(h, 0, args, [&]() {
+        int n = launch_fire_pred<T>(L, h->fire, h->stream);
+        n += launch_force_kick<T>(L, h->fire, h->partials, h->grid, h->stream);
+        n += launch_fire_control(h->fire, h->partials, h->grid, h->stream);
+        return n;
+    });
+    if (r) return r;
+    int remaining = std::max(max_iterations - h->fire_h->iterations, 1);
+    r = run_chunks(h, 0, h->fire, h->fire_h, (remaining + kChunk - 1) / kChunk + 1);
+    if (r) return r;
+    h->launches += launch_fire_finish<T>(L, h->fire, h->stream);
+    CK(cudaGetLastError());
+    CK(cudaMemcpyAsync(h->fire_h, h->fire, sizeof(FireDev), cudaMemcpyDeviceToHost, h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+    return QMIN_OK;
+}
+
+int qmin_fire_run(qmin_handle h, int max_iterations, qmin_fire_result *res)
+{
+    int r = ready(h, "qmin_fire_run");
+    if (r) return r;
+    if (!h->fire_ready) return fail(QMIN_ESTATE, "qmin_fire_run: qmin_fire_init has not been called");
+    FireDev *f = h->fire_h;
+    CK(cudaMemcpyAsync(f, h->fire, sizeof(FireDev), cudaMemcpyDeviceToHost, h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+    f->max_iters = max_iterations;
+    f->active = 1;  // minimize() always iterates at least once (energyMinimizerFIRE.cpp:158-160)
+    f->status = 0;
+    f->nTotal = h->nTotal;
+    CK(cudaMemcpyAsync(h->fire, f, sizeof(FireDev), cudaMemcpyHostToDevice, h->stream));
+    r = h->prec == QMIN_FP64 ? fire_impl<double>(h, max_iterations) : fire_impl<float>(h, max_iterations);
+    if (r) return r;
+    if (res) {
+        res->iterations = f->iterations;
+        res->force_max = f->forceMax;
+        res->alpha = f->alpha;
+        res->dt = f->dt;
+        res->power = f->power;
+        res->n_since = f->nsince;
+    }
+    if (f->status) return fail(QMIN_ENONFINITE, "qmin_fire_run: non-finite force norm");
+    return QMIN_OK;
+}
+
+// ---------------------------------------------------- Adam / Nesterov
+static int alloc_planes(qmin_ctx *h, void **p, int count)
+{
+    if (*p) return QMIN_OK;
+    if (cudaMalloc(p, (size_t)count * 5 * (size_t)h->P * h->esz) != cudaSuccess) {
+        cudaGetLastError();
+        return fail(QMIN_ENOMEM, "minimiser state allocation failed");
+    }
+    return QMIN_OK;
+}
+
+static int iter_begin(qmin_ctx *h, int reset, double fm0, double fcut, int max_iterations, bool at_least_once)
+{
+    IterDev *it = h->iter_h;
+    CK(cudaMemcpyAsync(it, h->iter, sizeof(IterDev), cudaMemcpyDeviceToHost, h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+    if (reset) {
+        memset(it, 0, sizeof(IterDev));
+        it->forceMax = fm0;
+    }
+    if (fm0 > 0 && !at_least_once) it->forceMax = fm0;
+    it->fcut = fcut;
+    it->max_iters = max_iterations;
+    it->ndof = h->N;
+    it->status = 0;
+    it->active = at_least_once ? 1 : ((it->iterations < max_iterations && it->forceMax > fcut) ? 1 : 0);
+    CK(cudaMemcpyAsync(h->iter, it, sizeof(IterDev), cudaMemcpyHostToDevice, h->stream));
+    return QMIN_OK;
+}
+
+template <class T>
+static int adam_impl(qmin_ctx *h, double b1, double b2, double eps, double dt, int max_iterations)
+{
+    Lat<T> L = make_lat<T>(h);
+    const double args[4] = {b1, b2, eps, dt};
+    int r = capture_chunk(h, 1, args, [&]() {
+        int n = launch_force<T>(L, h->grid, h->stream);
+        n += launch_adam_step<T>(L, (T *)h->M, (T *)h->S, h->iter, b1, b2, eps, dt, h->partials, h->grid, h->stream);
+        n += launch_norm_control(h->iter, h->partials, h->grid, 1, b1, b2, h->stream);
+        return n;
+    });
+    if (r) return r;
+    return run_chunks(h, 1, h->iter, h->iter_h, max_iterations / kChunk + 2);
+}
+
+int qmin_adam_run(qmin_handle h, double beta1, double beta2, double eps, double dt, double force_cutoff,
+                  int max_iterations, int reset, int *iterations, double *force_max)
+{
+    int r = ready(h, "qmin_adam_run");
+    if (r) return r;
+    if ((r = alloc_planes(h, &h->M, 1)) || (r = alloc_planes(h, &h->S, 1))) return r;
+    if (reset) {
+        CK(cudaMemsetAsync(h->M, 0, 5 * (size_t)h->P * h->esz, h->stream));
+        CK(cudaMemsetAsync(h->S, 0, 5 * (size_t)h->P * h->esz, h->stream));
+        invalidate_graphs(h);
+    }
+    // minimize() resets forceMax to 110 (energyMinimizerAdam.cpp:60)
+    r = iter_begin(h, reset, 110.0, force_cutoff, max_iterations, false);
+    if (r) return r;
+    if (reset) {
+        h->iter_h->b1t = beta1;  // setAdamParameters (energyMinimizerAdam.h:20-29)
+        h->iter_h->b2t = beta2;
+        CK(cudaMemcpyAsync(h->iter, h->iter_h, sizeof(IterDev), cudaMemcpyHostToDevice, h->stream));
+    }
+    if (h->iter_h->active) {
+        r = h->prec == QMIN_FP64 ? adam_impl<double>(h, beta1, beta2, eps, dt, max_iterations)
+                                 : adam_impl<float>(h, beta1, beta2, eps, dt, max_iterations);
+        if (r) return r;
+    }
+    CK(cudaMemcpyAsync(h->iter_h, h->iter, sizeof(IterDev), cudaMemcpyDeviceToHost, h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+    if (iterations) *iterations = h->iter_h->iterations;
+    if (force_max) *force_max = h->iter_h->forceMax;
+    if (h->iter_h->status) return fail(QMIN_ENONFINITE, "qmin_adam_run: non-finite force norm");
+    return QMIN_OK;
+}
+
+template <class T> static int nesterov_impl(qmin_ctx *h, double dt, double mu, int max_iterations)
+{
+    Lat<T> L = make_lat<T>(h);
+    const double args[4] = {dt, mu, 0, 0};
+    int r = capture_chunk(h, 2, args, [&]() {
+        int n = launch_force<T>(L, h->grid, h->stream);
+        n += launch_nesterov_step<T>(L, (T *)h->alt, h->iter, dt, mu, h->partials, h->grid, h->stream);
+        n += launch_norm_control(h->iter, h->partials, h->grid, 0, 0.0, 0.0, h->stream);
+        return n;
+    });
+    if (r) return r;
+    return run_chunks(h, 2, h->iter, h->iter_h, max_iterations / kChunk + 2);
+}
+
+int qmin_nesterov_run(qmin_handle h, double dt, double mu, double force_cutoff, int max_iterations, int reset,
+                      int *iterations, double *force_max)
+{
+    int r = ready(h, "qmin_nesterov_run");
+    if (r) return r;
+    if ((r = alloc_planes(h, &h->alt, 1))) return r;
+    if (reset) {
+        // energyMinimizerNesterovAG::initializeFromModel: alternateSequence = positions
+        CK(cudaMemcpyAsync(h->alt, h->Q, 5 * (size_t)h->P * h->esz, cudaMemcpyDeviceToDevice, h->stream));
+        invalidate_graphs(h);
+    }
+    r = iter_begin(h, reset, 110.0, force_cutoff, max_iterations, false);
+    if (r) return r;
+    if (h->iter_h->active) {
+        r = h->prec == QMIN_FP64 ? nesterov_impl<double>(h, dt, mu, max_iterations)
+                                 : nesterov_impl<float>(h, dt, mu, max_iterations);
+        if (r) return r;
+    }
+    CK(cudaMemcpyAsync(h->iter_h, h->iter, sizeof(IterDev), cudaMemcpyDeviceToHost, h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+    if (iterations) *iterations = h->iter_h->iterations;
+    if (force_max) *force_max = h->iter_h->forceMax;
+    if (h->iter_h->status) return fail(QMIN_ENONFINITE, "qmin_nesterov_run: non-finite force norm");
+    return QMIN_OK;
+}
+
+template <class T> static int lbfgs_impl(qmin_ctx *h, int m, double eta, int max_iterations)
+{
+    Lat<T> L = make_lat<T>(h);
+    if (h->iter_h->iterations == 0) {
+        // LoLBFGSStepCPU step 1 (energyMinimizerLoLBFGS.cpp:110-116)
+        h->launches += launch_force<T>(L, h->grid, h->stream);
+        h->launches += launch_lbfgs_first<T>(L, (T *)h->lbp, h->iter, h->stream);
+    }
+    const double args[4] = {(double)m, eta, 0, 0};
+    int r = capture_chunk(h, 3, args, [&]() {
+        return launch_lbfgs_iteration<T>(L, (T *)h->lbp, (T *)h->lbs, (T *)h->lby, h->iter, m, eta, h->partials,
+                                         h->grid, h->stream);
+    });
+    if (r) return r;
+    return run_chunks(h, 3, h->iter, h->iter_h, max_iterations / kChunk + 2);
+}
+
+int qmin_lbfgs_run(qmin_handle h, int m, double eta, double force_cutoff, int max_iterations, int reset,
+                   int *iterations, double *force_max)
+{
+    int r = ready(h, "qmin_lbfgs_run");
+    if (r) return r;
+    if (m < 1 || m > 16) return fail(QMIN_EINVAL, "qmin_lbfgs_run: m must be in [1, 16]");
+    if (h->lb_m != m) {
+        if (h->lbs) cudaFree(h->lbs);
+        if (h->lby) cudaFree(h->lby);
+        h->lbs = h->lby = nullptr;
+        h->lb_m = m;
+        reset = 1;
+    }
+    if ((r = alloc_planes(h, &h->lbp, 1)) || (r = alloc_planes(h, &h->lbs, m)) || (r = alloc_planes(h, &h->lby, m)))
+        return r;
+    if (reset) {
+        CK(cudaMemsetAsync(h->lbs, 0, (size_t)m * 5 * (size_t)h->P * h->esz, h->stream));
+        CK(cudaMemsetAsync(h->lby, 0, (size_t)m * 5 * (size_t)h->P * h->esz, h->stream));
+        CK(cudaMemsetAsync(h->lbp, 0, 5 * (size_t)h->P * h->esz, h->stream));
+        invalidate_graphs(h);
+    }
+    // forceMax starts at 100 (energyMinimizerLoLBFGS.cpp:27); always one iteration (:203)
+    r = iter_begin(h, reset, reset ? 100.0 : -1.0, force_cutoff, max_iterations, true);
+    if (r) return r;
+    r = h->prec == QMIN_FP64 ? lbfgs_impl<double>(h, m, eta, max_iterations)
+                             : lbfgs_impl<float>(h, m, eta, max_iterations);
+    if (r) return r;
+    CK(cudaMemcpyAsync(h->iter_h, h->iter, sizeof(IterDev), cudaMemcpyDeviceToHost, h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+    if (iterations) *iterations = h->iter_h->iterations;
+    if (force_max) *force_max = h->iter_h->forceMax;
+    if (h->iter_h->status) return fail(QMIN_ENONFINITE, "qmin_lbfgs_run: non-finite force norm");
+    return QMIN_OK;
+}
+
+
+// ------------------------------------------------------------ diagnostics
+template <class T> static int fire_profile_impl(qmin_ctx *h, int iterations, double *ms)
+{
+    Lat<T> L = make_lat<T>(h);
+    cudaEvent_t ev[5];
+    for (auto &e : ev) CK(cudaEventCreate(&e));
+    double acc[4] = {0, 0, 0, 0};
+    for (int it = 0; it < iterations; ++it) {
+        CK(cudaEventRecord(ev[0], h->stream));
+        h->launches += launch_fire_pred<T>(L, h->fire, h->stream);
+        CK(cudaEventRecord(ev[1], h->stream));
+        if (L.multi) h->launches += launch_derivs<T>(L, h->stream);
+        CK(cudaEventRecord(ev[2], h->stream));
+        Lat<T> L1 = L;
+        L1.multi = L.multi;
+        // force + kick without re-running the derivative kernel
+        h->launches += launch_force_kick_only<T>(L1, h->fire, h->partials, h->grid, h->stream);
+        CK(cudaEventRecord(ev[3], h->stream));
+        h->launches += launch_fire_control(h->fire, h->partials, h->grid, h->stream);
+        CK(cudaEventRecord(ev[4], h->stream));
+        CK(cudaEventSynchronize(ev[4]));
+        for (int k = 0; k < 4; ++k) {
+            float t = 0;
+            CK(cudaEventElapsedTime(&t, ev[k], ev[k + 1]));
+            acc[k] += t;
+        }
+    }
+    for (int k = 0; k < 4; ++k) ms[k] = iterations > 0 ? acc[k] / iterations : 0.0;
+    h->launches += launch_fire_finish<T>(L, h->fire, h->stream);
+    for (auto &e : ev) cudaEventDestroy(e);
+    CK(cudaMemcpyAsync(h->fire_h, h->fire, sizeof(FireDev), cudaMemcpyDeviceToHost, h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+    return QMIN_OK;
+}
+
+int qmin_fire_profile(qmin_handle h, int iterations, double kernel_ms[4])
+{
+    int r = ready(h, "qmin_fire_profile");
+    if (r) return r;
+    if (!h->fire_ready) return fail(QMIN_ESTATE, "qmin_fire_profile: qmin_fire_init has not been called");
+    if (!kernel_ms || iterations < 1) return fail(QMIN_EINVAL, "qmin_fire_profile: bad argument");
+    FireDev *f = h->fire_h;
+    CK(cudaMemcpyAsync(f, h->fire, sizeof(FireDev), cudaMemcpyDeviceToHost, h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+    f->max_iters = f->iterations + iterations;
+    f->active = 1;
+    f->status = 0;
+    f->nTotal = h->nTotal;
+    CK(cudaMemcpyAsync(h->fire, f, sizeof(FireDev), cudaMemcpyHostToDevice, h->stream));
+    return h->prec == QMIN_FP64 ? fire_profile_impl<double>(h, iterations, kernel_ms)
+                                : fire_profile_impl<float>(h, iterations, kernel_ms);
+}

@@ -1,0 +1,145 @@
+// Device-side Q-tensor algebra shared by the qmin_gb300 kernels.  Every
+// function is templated on the storage/arithmetic type T (double for the FP64
+// form, float for the FP32 form).  Formulas follow open-Qmin's
+// inc/qTensorFunctions.h, src/forces/lcForces.h and
+// src/forces/landauDeGennesLCBoundary.h, written here from the functionals
+// they implement.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace qmin {
+
+template <class T> struct V5 { T c[5]; };
+
+// derivative of tr Q^2, tr Q^3, (tr Q^2)^2 w.r.t. (q0..q4) (qTensorFunctions.h:73-107)
+// and the phase force f = -(a dTrQ2 + b dTrQ3 + c d(TrQ2)^2), a = A/2, b = B/3, c = C/4
+// (landauDeGennesLCDistortionTerms.cpp:23-38)
+template <class T>
+__device__ __forceinline__ void phase_force(T a, T b, T c, const T *q, T *f)
+{
+    const T q0 = q[0], q1 = q[1], q2 = q[2], q3 = q[3], q4 = q[4];
+    T d2[5] = {T(2) * (T(2) * q0 + q3), T(4) * q1, T(4) * q2, T(2) * (q0 + T(2) * q3), T(4) * q4};
+    T d3[5] = {T(-3) * (-q1 * q1 + q3 * q3 + q4 * q4 + T(2) * q0 * q3),
+               T(6) * (q0 * q1 + q1 * q3 + q2 * q4),
+               T(-6) * q2 * q3 + T(6) * q1 * q4,
+               T(-3) * (q0 * q0 - q1 * q1 + q2 * q2 + T(2) * q0 * q3),
+               T(6) * q1 * q2 - T(6) * q0 * q4};
+    const T s = q0 * q0 + q1 * q1 + q2 * q2 + q3 * q3 + q4 * q4 + q0 * q3;
+    T d4[5] = {T(8) * (T(2) * q0 + q3) * s, T(16) * q1 * s, T(16) * q2 * s, T(8) * (q0 + T(2) * q3) * s,
+               T(16) * q4 * s};
+#pragma unroll
+    for (int k = 0; k < 5; ++k) f[k] = ((T(0) - a * d2[k]) - b * d3[k]) - c * d4[k];
+}
+
+// lcForce::bulkL1Force cross terms (lcForces.h:26-37): S0 += S0+S3, S3 += S0+S3, S1,S2,S4 *= 2
+template <class T>
+__device__ __forceinline__ void l1_cross(T *s)
+{
+    const T cross = s[0] + s[3];
+    s[0] += cross;
+    s[1] *= T(2);
+    s[2] *= T(2);
+    s[3] += cross;
+    s[4] *= T(2);
+}
+
+// correctForceFromMetric (landauDeGennesLC.cpp:137-160)
+template <class T>
+__device__ __forceinline__ void metric(T *f)
+{
+    const T f0 = f[0], f3 = f[3];
+    f[0] = (T(2) / T(3)) * (T(2) * f0 - f3);
+    f[3] = (T(2) / T(3)) * (T(2) * f3 - f0);
+}
+
+// QT-metric dot product dotVec (inc/functions.h:140-147)
+template <class T>
+__device__ __forceinline__ T dot_qt(const T *x, const T *y)
+{
+    T s = x[0] * y[0] + x[1] * y[1] + x[2] * y[2] + x[3] * y[3] + x[4] * y[4];
+    return s + x[0] * y[3];
+}
+
+template <class T>
+__device__ __forceinline__ T tr_q2(const T *q)
+{
+    return T(2) * (q[0] * q[0] + q[1] * q[1] + q[2] * q[2] + q[3] * q[3] + q[4] * q[4] + q[0] * q[3]);
+}
+
+template <class T>
+__device__ __forceinline__ T tr_q3(const T *q)
+{
+    return T(-3) * ((-(q[1] * q[1]) + q[3] * q[3] + q[4] * q[4]) * q[0] + q[0] * q[0] * q[3] - q[1] * q[1] * q[3] +
+                    q[2] * q[2] * q[3] - T(2) * q[1] * q[2] * q[4]);
+}
+
+// Fournier-Galatola degenerate planar anchoring (landauDeGennesLCBoundary.h:44-72, W1 = W2 = W):
+// with Qt = Q + S0/2 I, w = Qt nu, s = nu.w, the planar-projected deviation is
+// D = nu w^T + w nu^T - s nu nu^T and E = W tr D^2 + W (tr Q^2 - 3 S0^2 / 2)^2.
+// dE/dQt = 2 W D, mapped to (q0..q4) with Qzz = -q0 - q3.
+template <class T>
+__device__ __forceinline__ void planar_D(const T *q, const T *nu, T S0, T D[6])
+{
+    const T h = T(0.5) * S0;
+    const T Qxx = q[0] + h, Qyy = q[3] + h, Qzz = -q[0] - q[3] + h;
+    const T w0 = Qxx * nu[0] + q[1] * nu[1] + q[2] * nu[2];
+    const T w1 = q[1] * nu[0] + Qyy * nu[1] + q[4] * nu[2];
+    const T w2 = q[2] * nu[0] + q[4] * nu[1] + Qzz * nu[2];
+    const T s = nu[0] * w0 + nu[1] * w1 + nu[2] * w2;
+    D[0] = T(2) * nu[0] * w0 - s * nu[0] * nu[0];                // xx
+    D[1] = nu[0] * w1 + w0 * nu[1] - s * nu[0] * nu[1];          // xy
+    D[2] = nu[0] * w2 + w0 * nu[2] - s * nu[0] * nu[2];          // xz
+    D[3] = T(2) * nu[1] * w1 - s * nu[1] * nu[1];                // yy
+    D[4] = nu[1] * w2 + w1 * nu[2] - s * nu[1] * nu[2];          // yz
+    D[5] = T(2) * nu[2] * w2 - s * nu[2] * nu[2];                // zz
+}
+
+// force on an LC site q from one object neighbour with stored tensor qb
+// (computeBoundaryForce, landauDeGennesLCBoundary.h:26-74), added into f
+template <class T>
+__device__ __forceinline__ void anchoring_force_add(int kind, T W, T S0, const T *q, const T *qb, T *f)
+{
+    if (kind == 0) {
+        T d[5];
+#pragma unroll
+        for (int k = 0; k < 5; ++k) d[k] = T(2) * (q[k] - qb[k]);
+        T ans[5];
+#pragma unroll
+        for (int k = 0; k < 5; ++k) ans[k] = T(2) * d[k];
+        ans[0] += d[3];
+        ans[3] += d[0];
+#pragma unroll
+        for (int k = 0; k < 5; ++k) f[k] += -W * ans[k];
+    } else {
+        T D[6];
+        planar_D(q, qb, S0, D);
+        const T sq = q[0] * q[0] + q[1] * q[1] + q[2] * q[2] + q[3] * q[3] + q[4] * q[4] + q[0] * q[3];
+        const T c2 = T(3) * (S0 * S0) - T(4) * sq;
+        f[0] += T(2) * W * (T(2) * q[0] + q[3]) * c2 - T(2) * W * (D[0] - D[5]);
+        f[1] += T(4) * W * q[1] * c2 - T(4) * W * D[1];
+        f[2] += T(4) * W * q[2] * c2 - T(4) * W * D[2];
+        f[3] += T(2) * W * (q[0] + T(2) * q[3]) * c2 - T(2) * W * (D[3] - D[5]);
+        f[4] += T(4) * W * q[4] * c2 - T(4) * W * D[4];
+    }
+}
+
+// computeBoundaryEnergy (landauDeGennesLCBoundary.h:77-124)
+template <class T>
+__device__ __forceinline__ T anchoring_energy(int kind, T W, T S0, const T *q, const T *qb)
+{
+    if (kind == 0) {
+        T d[5];
+#pragma unroll
+        for (int k = 0; k < 5; ++k) d[k] = q[k] - qb[k];
+        return W * tr_q2(d);
+    }
+    T D[6];
+    planar_D(q, qb, S0, D);
+    const T e1 = D[0] * D[0] + D[3] * D[3] + D[5] * D[5] + T(2) * (D[1] * D[1] + D[2] * D[2] + D[4] * D[4]);
+    const T e2 = T(3) * (S0 * S0) -
+                 T(4) * (q[0] * q[0] + q[1] * q[1] + q[2] * q[2] + q[0] * q[3] + q[3] * q[3] + q[4] * q[4]);
+    return W * e1 + T(0.25) * W * e2 * e2;
+}
+
+}  // namespace qmin

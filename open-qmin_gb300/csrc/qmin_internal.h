@@ -1,0 +1,84 @@
+// Internal declarations shared by the qmin_gb300 translation units.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "qmin_bulk_forms.h"
+
+namespace qmin {
+
+// Object table entry on the device (boundaryObject, latticeBoundaries.h:20-39).
+template <class T> struct ObjDev {
+    int kind;
+    T W, S0;
+};
+
+// Everything a lattice kernel needs, passed by value.  Planes are SoA:
+// component k of site i lives at X[k * P + i]; P = N rounded up to 32.
+template <class T> struct Lat {
+    int Lx, Ly, Lz, N;
+    long long P;
+    T *Q, *V, *F;
+    const int8_t *types;
+    T *D;  // 15 derivative planes (multi-constant only)
+    const ObjDev<T> *objs;
+    T a, b, c;          // A/2, B/3, C/4
+    T L1, L2, L3, L4;
+    T fE[5], fH[5];     // uniform-field force vectors (subtracted, as the reference does)
+    int metric_mode, multi, efield, hfield;
+    T cb[5 * QMIN_BULK_W];  // combined bulk multi-constant coefficients
+};
+
+// FIRE state resident on the device.  The velocity mix that ends one
+// iteration is deferred into the next iteration's first kernel.
+struct FireDev {
+    double alpha, dt, alpha0, dtmax, dtmin, dtinc, dtdec, alphadec, alphamin, fcut;
+    double power, forceMax, scaling, mixA, mixS;
+    int nmin, nsince, iterations, max_iters, active, pending, reset, status;
+    long long nTotal;
+};
+
+// Scalar state for Adam / Nesterov / L-BFGS loops resident on the device.
+struct IterDev {
+    double forceMax, fcut, b1t, b2t;
+    int iterations, max_iters, active, status;
+    long long ndof;
+    double lb[64];  // L-BFGS scalars: sy[0..m), alpha[0..m), scratch
+};
+
+constexpr int kBlock = 256;
+
+// launchers (qmin_kernels.cu); each returns the number of kernels launched
+template <class T> int launch_derivs(const Lat<T> &L, cudaStream_t s);
+template <class T> int launch_force(const Lat<T> &L, int grid, cudaStream_t s);
+template <class T> int launch_fire_pred(const Lat<T> &L, FireDev *fd, cudaStream_t s);
+template <class T> int launch_force_kick(const Lat<T> &L, FireDev *fd, double *partials, int grid, cudaStream_t s);
+template <class T>
+int launch_force_kick_only(const Lat<T> &L, FireDev *fd, double *partials, int grid, cudaStream_t s);
+int launch_fire_control(FireDev *fd, const double *partials, int nparts, cudaStream_t s);
+template <class T> int launch_fire_finish(const Lat<T> &L, FireDev *fd, cudaStream_t s);
+template <class T>
+int launch_energy_full(const Lat<T> &L, double *partials, int grid, double *out5, const double *E, double eps,
+                       double eps0, double deps, const double *H, double chi, double mu0, double dchi, cudaStream_t s);
+template <class T> int launch_aos_to_soa(const double *aos, T *soa, int N, long long P, int layout, cudaStream_t s);
+template <class T> int launch_soa_to_aos(const T *soa, double *aos, int N, long long P, int layout, cudaStream_t s);
+int launch_types_to_i8(const int32_t *t32, int8_t *t8, int N, cudaStream_t s);
+template <class T> int launch_fill(T *x, T v, long long n, cudaStream_t s);
+
+// Adam / Nesterov / L-BFGS
+template <class T>
+int launch_adam_step(const Lat<T> &L, T *M, T *S, IterDev *it, double beta1, double beta2, double eps, double dt,
+                     double *partials, int grid, cudaStream_t s);
+template <class T>
+int launch_nesterov_step(const Lat<T> &L, T *alt, IterDev *it, double dt, double mu, double *partials, int grid,
+                         cudaStream_t s);
+int launch_norm_control(IterDev *it, const double *partials, int nparts, int adam, double beta1, double beta2,
+                        cudaStream_t s);
+template <class T>
+int launch_lbfgs_iteration(const Lat<T> &L, T *p, T *sbase, T *ybase, IterDev *it, int m, double eta,
+                           double *partials, int grid, cudaStream_t s);
+template <class T> int launch_lbfgs_first(const Lat<T> &L, T *p, IterDev *it, cudaStream_t s);
+
+int reduction_grid(int N);
+
+}  // namespace qmin

@@ -1,0 +1,923 @@
+// qmin_gb300 CUDA kernels for sm_103a: Landau-de Gennes force/energy on the
+// cubic Q-tensor lattice and the FIRE / Adam / Nesterov / L-BFGS updates.
+//
+// Layout: SoA planes X[k * P + i] (k = 0..4 for Q/V/F, 0..14 for the
+// derivative planes), int8 site types.  Reductions are deterministic: a fixed
+// grid of blocks writes per-block FP64 partials that one block sums in a
+// fixed order.
+#include <math.h>
+
+#include "qmin_device.cuh"
+#include "qmin_distortion_tables.h"
+#include "qmin_internal.h"
+
+namespace qmin {
+
+// sparse multi-constant forms (term, boundary case, component) -> (input, k)
+__device__ const uint16_t g_dt_offset[3 * 64 * 5 + 1] = QMIN_DT_OFFSET_INIT;
+__device__ const uint8_t g_dt_input[QMIN_DT_NPAIRS] = QMIN_DT_INPUT_INIT;
+__device__ const int8_t g_dt_k[QMIN_DT_NPAIRS] = QMIN_DT_K_INIT;
+
+int reduction_grid(int N)
+{
+    int g = (N + kBlock - 1) / kBlock;
+    const int cap = 152 * 8;  // 8 resident blocks per SM on the 152 SMs of a GB300
+    return g < cap ? (g > 0 ? g : 1) : cap;
+}
+
+// ------------------------------------------------------------------ helpers
+struct Nb {
+    int n[6];  // x-, x+, y-, y+, z-, z+ (cubicLattice::getNeighbors, cubicLattice.cpp:179-244)
+};
+
+template <class T>
+__device__ __forceinline__ Nb neighbours(const Lat<T> &L, int i)
+{
+    const int x = i % L.Lx;
+    const int r = i / L.Lx;
+    const int y = r % L.Ly;
+    const int z = r / L.Ly;
+    const int sx = L.Lx, sy = L.Lx * L.Ly;
+    Nb b;
+    b.n[0] = x == 0 ? i + (L.Lx - 1) : i - 1;
+    b.n[1] = x == L.Lx - 1 ? i - (L.Lx - 1) : i + 1;
+    b.n[2] = y == 0 ? i + (L.Ly - 1) * sx : i - sx;
+    b.n[3] = y == L.Ly - 1 ? i - (L.Ly - 1) * sx : i + sx;
+    b.n[4] = z == 0 ? i + (L.Lz - 1) * sy : i - sy;
+    b.n[5] = z == L.Lz - 1 ? i - (L.Lz - 1) * sy : i + sy;
+    return b;
+}
+
+template <class T>
+__device__ __forceinline__ T ld(const T *p)
+{
+    return __ldg(p);
+}
+
+// block-wide sum of NV doubles; result valid in thread 0
+template <int NV>
+__device__ __forceinline__ void block_sum(double (&v)[NV])
+{
+    __shared__ double sh[NV][kBlock / 32];
+#pragma unroll
+    for (int k = 0; k < NV; ++k)
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v[k] += __shfl_down_sync(0xffffffffu, v[k], o);
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    if (lane == 0)
+#pragma unroll
+        for (int k = 0; k < NV; ++k) sh[k][w] = v[k];
+    __syncthreads();
+    if (w == 0) {
+#pragma unroll
+        for (int k = 0; k < NV; ++k) {
+            v[k] = lane < kBlock / 32 ? sh[k][lane] : 0.0;
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) v[k] += __shfl_down_sync(0xffffffffu, v[k], o);
+        }
+    }
+    __syncthreads();
+}
+
+// deterministic sum of partials[NV * nparts] by one block; result in thread 0
+template <int NV>
+__device__ __forceinline__ void sum_partials(const double *partials, int nparts, double (&v)[NV])
+{
+#pragma unroll
+    for (int k = 0; k < NV; ++k) v[k] = 0.0;
+    for (int b = threadIdx.x; b < nparts; b += kBlock)
+#pragma unroll
+        for (int k = 0; k < NV; ++k) v[k] += partials[NV * b + k];
+    block_sum<NV>(v);
+}
+
+// --------------------------------------------------------- first derivatives
+// landauDeGennesLC::computeFirstDerivatives (landauDeGennesLCOtherForces.cpp:15-145):
+// D[5*axis + k]; central differences, one-sided at type < 0 sites with the
+// "up neighbour is an object" branch first; zero at object sites.
+template <class T>
+__device__ __forceinline__ void site_derivs(const Lat<T> &L, int i, int t, const Nb &b, T *d)
+{
+    const long long P = L.P;
+#pragma unroll
+    for (int ax = 0; ax < 3; ++ax) {
+        const int dn = b.n[2 * ax], up = b.n[2 * ax + 1];
+        int mode = 0;  // 0 central, 1 backward (up is an object), 2 forward
+        if (t < 0) {
+            const int td = L.types[dn], tu = L.types[up];
+            if (!(td <= 0 && tu <= 0)) mode = tu > 0 ? 1 : 2;
+        }
+#pragma unroll
+        for (int k = 0; k < 5; ++k) {
+            const T qd = ld(L.Q + k * P + dn), qu = ld(L.Q + k * P + up);
+            const T q = ld(L.Q + k * P + i);
+            d[5 * ax + k] = mode == 0 ? T(0.5) * (qu - qd) : (mode == 1 ? q - qd : qu - q);
+        }
+    }
+}
+
+template <class T>
+__global__ void __launch_bounds__(kBlock) k_derivs(Lat<T> L)
+{
+    for (int i = blockIdx.x * kBlock + threadIdx.x; i < L.N; i += gridDim.x * kBlock) {
+        const int t = L.types[i];
+        T d[15];
+        if (t > 0) {
+#pragma unroll
+            for (int k = 0; k < 15; ++k) d[k] = T(0);
+        } else {
+            const Nb b = neighbours(L, i);
+            site_derivs(L, i, t, b, d);
+        }
+#pragma unroll
+        for (int k = 0; k < 15; ++k) L.D[k * L.P + i] = d[k];
+    }
+}
+
+// ------------------------------------------------------------------- force
+// One site's force, CPU-path semantics by default (multirankSimulation.cpp:462-466):
+//   type 0:  F = M( M(-phase - distortion) - fields )
+//   type <0: F = M(-phase - distortion + anchoring - fields)
+// metric_mode 1 applies M once everywhere (the reference GPU branch).
+template <class T>
+__device__ __forceinline__ void site_force(const Lat<T> &L, int i, T *f)
+{
+    const int t = L.types[i];
+    if (t > 0) {
+#pragma unroll
+        for (int k = 0; k < 5; ++k) f[k] = T(0);
+        return;
+    }
+    const long long P = L.P;
+    const Nb b = neighbours(L, i);
+    T q[5], nq[6][5];
+#pragma unroll
+    for (int k = 0; k < 5; ++k) q[k] = ld(L.Q + k * P + i);
+#pragma unroll
+    for (int s = 0; s < 6; ++s)
+#pragma unroll
+        for (int k = 0; k < 5; ++k) nq[s][k] = ld(L.Q + k * P + b.n[s]);
+
+    T force[5];
+    phase_force(L.a, L.b, L.c, q, force);
+
+    const bool boundary = (t == -1);  // type -2 uses the bulk forms (DT:241-279)
+    int mask = 0;                     // which neighbours are objects
+    if (t < 0) {
+#pragma unroll
+        for (int s = 0; s < 6; ++s) mask |= (L.types[b.n[s]] > 0) << s;
+    }
+
+    T sp[5] = {T(0), T(0), T(0), T(0), T(0)};
+    if (!L.multi || L.L1 != T(0)) {
+        // lcForce::bulkL1Force / boundaryL1Force (lcForces.h:26-63)
+        T s1[5];
+        if (!boundary) {
+#pragma unroll
+            for (int k = 0; k < 5; ++k)
+                s1[k] = L.L1 * (T(6) * q[k] - nq[0][k] - nq[1][k] - nq[2][k] - nq[3][k] - nq[4][k] - nq[5][k]);
+        } else {
+#pragma unroll
+            for (int k = 0; k < 5; ++k) s1[k] = T(0);
+#pragma unroll
+            for (int ax = 0; ax < 3; ++ax) {
+                if (mask & (1 << (2 * ax)))
+#pragma unroll
+                    for (int k = 0; k < 5; ++k) s1[k] -= (nq[2 * ax + 1][k] - q[k]);
+                if (mask & (1 << (2 * ax + 1)))
+#pragma unroll
+                    for (int k = 0; k < 5; ++k) s1[k] -= (nq[2 * ax][k] - q[k]);
+            }
+#pragma unroll
+            for (int k = 0; k < 5; ++k) s1[k] = s1[k] * L.L1;
+        }
+        l1_cross(s1);
+#pragma unroll
+        for (int k = 0; k < 5; ++k) sp[k] += s1[k];
+    }
+    if (L.multi) {
+        if (!boundary) {
+            // bulk L2/L3/L4 forms, straight-line over their union pattern
+            T s2[5];
+#define QIN(c) q[c]
+#define QN(slot, c) nq[slot][c]
+#define DN(slot, d) ld(L.D + (long long)(d) * P + b.n[slot])
+            QMIN_BULK_FORMS(L.cb, s2);
+#undef QIN
+#undef QN
+#undef DN
+#pragma unroll
+            for (int k = 0; k < 5; ++k) sp[k] += s2[k];
+        } else {
+            // boundary forms: lcForce::getBoundaryCase (lcForces.h:13-25), down wins
+            int xx = 0, yy = 0, zz = 0;
+            if (mask & 2) xx = 1;
+            if (mask & 1) xx = 2;
+            if (mask & 8) yy = 1;
+            if (mask & 4) yy = 2;
+            if (mask & 32) zz = 1;
+            if (mask & 16) zz = 2;
+            const int bcase = xx + 4 * yy + 16 * zz;
+            const T Lt[3] = {L.L2, L.L3, L.L4};
+            for (int term = 0; term < 3; ++term) {
+                if (Lt[term] == T(0)) continue;
+                for (int k = 0; k < 5; ++k) {
+                    const int o0 = g_dt_offset[(term * 64 + bcase) * 5 + k];
+                    const int o1 = g_dt_offset[(term * 64 + bcase) * 5 + k + 1];
+                    T acc = T(0);
+                    for (int e = o0; e < o1; ++e) {
+                        const int j = g_dt_input[e];
+                        T x;
+                        if (j < 5) x = q[j];
+                        else if (j < 35) x = ld(L.Q + (long long)((j - 5) % 5) * P + b.n[(j - 5) / 5]);
+                        else x = ld(L.D + (long long)((j - 35) % 15) * P + b.n[(j - 35) / 15]);
+                        acc += T(g_dt_k[e]) * x;
+                    }
+                    sp[k] += (T(0.5) * Lt[term]) * (acc / T(2));
+                }
+            }
+        }
+    }
+#pragma unroll
+    for (int k = 0; k < 5; ++k) f[k] = force[k] - sp[k];
+
+    if (L.metric_mode == 0 && t == 0) metric(f);
+    if (t < 0 && mask) {
+        // landauDeGennesLC::computeBoundaryForcesCPU (landauDeGennesLCOtherForces.cpp:314-373)
+#pragma unroll
+        for (int s = 0; s < 6; ++s) {
+            if (mask & (1 << s)) {
+                const ObjDev<T> o = L.objs[L.types[b.n[s]] - 1];
+                anchoring_force_add(o.kind, o.W, o.S0, q, nq[s], f);
+            }
+        }
+    }
+    if (L.efield)
+#pragma unroll
+        for (int k = 0; k < 5; ++k) f[k] -= L.fE[k];
+    if (L.hfield)
+#pragma unroll
+        for (int k = 0; k < 5; ++k) f[k] -= L.fH[k];
+    metric(f);
+}
+
+template <class T>
+__global__ void __launch_bounds__(kBlock) k_force(Lat<T> L)
+{
+    for (int i = blockIdx.x * kBlock + threadIdx.x; i < L.N; i += gridDim.x * kBlock) {
+        T f[5];
+        site_force(L, i, f);
+#pragma unroll
+        for (int k = 0; k < 5; ++k) L.F[k * L.P + i] = f[k];
+    }
+}
+
+// ------------------------------------------------------------------- FIRE
+// velocityVerlet::integrateEOMCPU first half (velocityVerlet.cpp:16-25), preceded by
+// the deferred FIRE velocity mix of the previous iteration (energyMinimizerFIRE.cpp:116-120, 143)
+template <class T>
+__global__ void __launch_bounds__(kBlock) k_fire_pred(Lat<T> L, const FireDev *__restrict__ fd)
+{
+    if (!fd->active) return;
+    const T dt = T(fd->dt);
+    const T hdt2 = T(0.5 * fd->dt * fd->dt);
+    const T hdt = T(0.5) * dt;
+    const bool pend = fd->pending, reset = fd->reset;
+    const T ma = T(1.0 - fd->mixA), mb = T(fd->mixA * fd->mixS);
+    const long long n = 5 * L.P;
+    for (long long j = blockIdx.x * (long long)kBlock + threadIdx.x; j < n; j += (long long)gridDim.x * kBlock) {
+        T v = L.V[j];
+        const T f = L.F[j];
+        if (pend) v = reset ? T(0) : ma * v + mb * f;
+        const T disp = dt * v + hdt2 * f;
+        L.V[j] = v + hdt * f;
+        L.Q[j] += disp;
+    }
+}
+
+// force at the moved Q, second half kick (velocityVerlet.cpp:33-37) and the
+// three FIRE reductions F.F, v.v, F.v in the QT metric (energyMinimizerFIRE.cpp:94-103)
+template <class T>
+__global__ void __launch_bounds__(kBlock) k_force_kick(Lat<T> L, const FireDev *__restrict__ fd, double *partials)
+{
+    if (!fd->active) return;
+    const T hdt = T(0.5) * T(fd->dt);
+    double acc[3] = {0.0, 0.0, 0.0};
+    for (int i = blockIdx.x * kBlock + threadIdx.x; i < L.N; i += gridDim.x * kBlock) {
+        T f[5], v[5];
+        site_force(L, i, f);
+#pragma unroll
+        for (int k = 0; k < 5; ++k) {
+            v[k] = L.V[k * L.P + i] + hdt * f[k];
+            L.F[k * L.P + i] = f[k];
+            L.V[k * L.P + i] = v[k];
+        }
+        acc[0] += (double)dot_qt(f, f);
+        acc[1] += (double)dot_qt(v, v);
+        acc[2] += (double)dot_qt(f, v);
+    }
+    block_sum<3>(acc);
+    if (threadIdx.x == 0) {
+        partials[3 * blockIdx.x + 0] = acc[0];
+        partials[3 * blockIdx.x + 1] = acc[1];
+        partials[3 * blockIdx.x + 2] = acc[2];
+    }
+}
+
+// fireStepCPU scalar logic (energyMinimizerFIRE.cpp:104-144) and the
+// minimize() loop condition (:160)
+__global__ void __launch_bounds__(kBlock) k_fire_control(FireDev *fd, const double *partials, int nparts)
+{
+    if (!fd->active) return;
+    double v[3];
+    sum_partials<3>(partials, nparts, v);
+    if (threadIdx.x != 0) return;
+    const double fn = v[0], vn = v[1], pw = v[2];
+    const int it = fd->iterations + 1;
+    fd->power = pw;
+    fd->forceMax = sqrt(fn) / ((double)fd->nTotal);
+    double scaling = 0.0;
+    if (fn > 0.) scaling = sqrt(vn / fn);
+    fd->scaling = scaling;
+    fd->mixA = fd->alpha;
+    fd->mixS = scaling;
+    fd->pending = 1;
+    fd->reset = 0;
+    if (pw > 0 && it % 500 != 0) {
+        if (fd->nsince > fd->nmin) {
+            fd->dt = fmin(fd->dt * fd->dtinc, fd->dtmax);
+            fd->alpha = fmax(fd->alpha * fd->alphadec, fd->alphamin);
+        }
+        fd->nsince += 1;
+    } else {
+        fd->nsince = 0;
+        fd->dt = fmax(fd->dt * fd->dtdec, fd->dtmin);
+        fd->alpha = fd->alpha0;
+        fd->reset = 1;
+    }
+    fd->iterations = it;
+    if (!isfinite(fn) || !isfinite(vn) || !isfinite(pw)) {
+        fd->status = 1;
+        fd->active = 0;
+        return;
+    }
+    fd->active = (it < fd->max_iters && fd->forceMax > fd->fcut) ? 1 : 0;
+}
+
+// apply the last deferred velocity mix so the resident velocities match the
+// reference's state at the end of minimize()
+template <class T>
+__global__ void __launch_bounds__(kBlock) k_fire_finish(Lat<T> L, FireDev *fd)
+{
+    if (!fd->pending) return;
+    const bool reset = fd->reset;
+    const T ma = T(1.0 - fd->mixA), mb = T(fd->mixA * fd->mixS);
+    const long long n = 5 * L.P;
+    for (long long j = blockIdx.x * (long long)kBlock + threadIdx.x; j < n; j += (long long)gridDim.x * kBlock)
+        L.V[j] = reset ? T(0) : ma * L.V[j] + mb * L.F[j];
+}
+
+__global__ void k_fire_clear_pending(FireDev *fd) { fd->pending = 0; }
+
+// ------------------------------------------------------------------ energy
+// landauDeGennesLC::computeEnergyCPU (landauDeGennesLC.cpp:204-353): per-site
+// phase, distortion, anchoring, E and H densities.  The distortion densities
+// are L1/2 dk Qij dk Qij, L2/2 (dj Qij)^2, L3/2 dk Qij dj Qik and
+// L4/2 eps_lik Qlj dk Qij, with the same derivative rules as the forces.
+template <class T>
+__device__ __forceinline__ void sym3(const T *d, T G[3][3])
+{
+    G[0][0] = d[0]; G[0][1] = d[1]; G[0][2] = d[2];
+    G[1][0] = d[1]; G[1][1] = d[3]; G[1][2] = d[4];
+    G[2][0] = d[2]; G[2][1] = d[4]; G[2][2] = -d[0] - d[3];
+}
+
+template <class T>
+__global__ void __launch_bounds__(kBlock) k_energy(Lat<T> L, double *partials, double Ex, double Ey, double Ez,
+                                                   double eps, double eps0, double deps, double Hx, double Hy,
+                                                   double Hz, double chi, double mu0, double dchi)
+{
+    double acc[5] = {0, 0, 0, 0, 0};
+    const long long P = L.P;
+    for (int i = blockIdx.x * kBlock + threadIdx.x; i < L.N; i += gridDim.x * kBlock) {
+        const int t = L.types[i];
+        if (t > 0) continue;
+        T q[5];
+#pragma unroll
+        for (int k = 0; k < 5; ++k) q[k] = ld(L.Q + k * P + i);
+        const T t2 = tr_q2(q);
+        acc[0] += (double)(L.a * t2 + L.b * tr_q3(q) + L.c * (t2 * t2));
+        if (L.efield) {
+            const T ex = T(Ex), ey = T(Ey), ez = T(Ez), e = T(eps), e0 = T(eps0), de = T(deps);
+            acc[3] += (double)(e0 * (T(-0.5) * ex * ex * (e + de * q[0]) - de * ex * ey * q[1] - de * ex * ez * q[2] -
+                                     T(0.5) * ez * ez * (e - de * q[0] - de * q[3]) -
+                                     T(0.5) * ey * ey * (e + de * q[3]) - de * ey * ez * q[4]));
+        }
+        if (L.hfield) {
+            const T hx = T(Hx), hy = T(Hy), hz = T(Hz), c = T(chi), m0 = T(mu0), dc = T(dchi);
+            acc[4] += (double)(m0 * (T(-0.5) * hx * hx * (c + dc * q[0]) - dc * hx * hy * q[1] - dc * hx * hz * q[2] -
+                                     T(0.5) * hz * hz * (c - dc * q[0] - dc * q[3]) -
+                                     T(0.5) * hy * hy * (c + dc * q[3]) - dc * hy * hz * q[4]));
+        }
+        const Nb b = neighbours(L, i);
+        T d[15];
+        site_derivs(L, i, t, b, d);
+        if (t < 0) {
+            T anch = T(0);
+#pragma unroll
+            for (int s = 0; s < 6; ++s) {
+                const int ts = L.types[b.n[s]];
+                if (ts > 0) {
+                    T qb[5];
+#pragma unroll
+                    for (int k = 0; k < 5; ++k) qb[k] = ld(L.Q + k * P + b.n[s]);
+                    const ObjDev<T> o = L.objs[ts - 1];
+                    anch += anchoring_energy(o.kind, o.W, o.S0, q, qb);
+                }
+            }
+            acc[2] += (double)anch;
+        }
+        T G[3][3][3];
+        sym3(d, G[0]);
+        sym3(d + 5, G[1]);
+        sym3(d + 10, G[2]);
+        T dist = T(0);
+        if (L.L1 != T(0)) {
+            T s = T(0);
+#pragma unroll
+            for (int k = 0; k < 3; ++k)
+#pragma unroll
+                for (int x = 0; x < 3; ++x)
+#pragma unroll
+                    for (int y = 0; y < 3; ++y) s += G[k][x][y] * G[k][x][y];
+            dist += T(0.5) * L.L1 * s;
+        }
+        if (L.L2 != T(0)) {
+            T s = T(0);
+#pragma unroll
+            for (int x = 0; x < 3; ++x) {
+                const T dv = G[0][x][0] + G[1][x][1] + G[2][x][2];
+                s += dv * dv;
+            }
+            dist += T(0.5) * L.L2 * s;
+        }
+        if (L.L3 != T(0)) {
+            T s = T(0);
+#pragma unroll
+            for (int k = 0; k < 3; ++k)
+#pragma unroll
+                for (int x = 0; x < 3; ++x)
+#pragma unroll
+                    for (int y = 0; y < 3; ++y) s += G[k][x][y] * G[y][x][k];
+            dist += T(0.5) * L.L3 * s;
+        }
+        if (L.L4 != T(0)) {
+            T Qm[3][3];
+            sym3(q, Qm);
+            // eps_lik Q_lj dk Q_ij over the six permutations (l, i, k)
+            const int perm[6][3] = {{0, 1, 2}, {1, 2, 0}, {2, 0, 1}, {0, 2, 1}, {2, 1, 0}, {1, 0, 2}};
+            T s = T(0);
+#pragma unroll
+            for (int e = 0; e < 6; ++e) {
+                const T sg = e < 3 ? T(1) : T(-1);
+#pragma unroll
+                for (int y = 0; y < 3; ++y) s += sg * Qm[perm[e][0]][y] * G[perm[e][2]][perm[e][1]][y];
+            }
+            dist += T(0.5) * L.L4 * s;
+        }
+        acc[1] += (double)dist;
+    }
+    block_sum<5>(acc);
+    if (threadIdx.x == 0)
+#pragma unroll
+        for (int k = 0; k < 5; ++k) partials[5 * blockIdx.x + k] = acc[k];
+}
+
+__global__ void __launch_bounds__(kBlock) k_sum5(const double *partials, int nparts, double *out)
+{
+    double v[5];
+    sum_partials<5>(partials, nparts, v);
+    if (threadIdx.x == 0)
+#pragma unroll
+        for (int k = 0; k < 5; ++k) out[k] = v[k];
+}
+
+// ------------------------------------------------------- layout conversion
+template <class T>
+__global__ void k_aos_to_soa(const double *aos, T *soa, int N, long long P, int layout)
+{
+    for (long long j = blockIdx.x * (long long)blockDim.x + threadIdx.x; j < 5LL * N;
+         j += (long long)gridDim.x * blockDim.x) {
+        long long i, k;
+        if (layout == 0) { i = j / 5; k = j % 5; }
+        else { k = j / N; i = j % N; }
+        soa[k * P + i] = T(aos[j]);
+    }
+}
+
+template <class T>
+__global__ void k_soa_to_aos(const T *soa, double *aos, int N, long long P, int layout)
+{
+    for (long long j = blockIdx.x * (long long)blockDim.x + threadIdx.x; j < 5LL * N;
+         j += (long long)gridDim.x * blockDim.x) {
+        long long i, k;
+        if (layout == 0) { i = j / 5; k = j % 5; }
+        else { k = j / N; i = j % N; }
+        aos[j] = (double)soa[k * P + i];
+    }
+}
+
+__global__ void k_types_to_i8(const int32_t *t32, int8_t *t8, int N)
+{
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < N; i += gridDim.x * blockDim.x) t8[i] = (int8_t)t32[i];
+}
+
+template <class T>
+__global__ void k_fill(T *x, T v, long long n)
+{
+    for (long long j = blockIdx.x * (long long)blockDim.x + threadIdx.x; j < n; j += (long long)gridDim.x * blockDim.x)
+        x[j] = v;
+}
+
+// ------------------------------------------------------------------- Adam
+// energyMinimizerAdam::adamStepCPU (energyMinimizerAdam.cpp:25-54), the force
+// already computed at the current Q
+template <class T>
+__global__ void __launch_bounds__(kBlock) k_adam(Lat<T> L, T *M, T *S, const IterDev *__restrict__ it, T beta1,
+                                                 T beta2, T eps, T dt, double *partials)
+{
+    if (!it->active) return;
+    const T c1 = T(1.0 / (1.0 - it->b1t)), c2 = T(1.0 / (1.0 - it->b2t));
+    double acc[1] = {0.0};
+    for (int i = blockIdx.x * kBlock + threadIdx.x; i < L.N; i += gridDim.x * kBlock) {
+        T ff = T(0);
+#pragma unroll
+        for (int k = 0; k < 5; ++k) {
+            const long long j = k * L.P + i;
+            const T f = L.F[j];
+            ff += f * f;
+            const T m = beta1 * M[j] + (beta1 - T(1)) * f;
+            const T s = beta2 * S[j] + (T(1) - beta2) * (f * f);
+            M[j] = m;
+            S[j] = s;
+            const T mc = m * c1, vc = s * c2;
+            T root = sqrt(vc);
+            if (root == T(0)) root = eps;
+            L.Q[j] += -dt * mc / root;
+        }
+        acc[0] += (double)ff;
+    }
+    block_sum<1>(acc);
+    if (threadIdx.x == 0) partials[blockIdx.x] = acc[0];
+}
+
+// energyMinimizerNesterovAG::nesterovStepCPU (energyMinimizerNesterovAG.cpp:75-92)
+template <class T>
+__global__ void __launch_bounds__(kBlock) k_nesterov(Lat<T> L, T *alt, const IterDev *__restrict__ it, T dt, T mu,
+                                                     double *partials)
+{
+    if (!it->active) return;
+    double acc[1] = {0.0};
+    for (int i = blockIdx.x * kBlock + threadIdx.x; i < L.N; i += gridDim.x * kBlock) {
+        T ff = T(0);
+#pragma unroll
+        for (int k = 0; k < 5; ++k) {
+            const long long j = k * L.P + i;
+            const T f = L.F[j];
+            ff += f * f;
+            const T old = alt[j];
+            const T a = L.Q[j] + dt * f;
+            alt[j] = a;
+            L.Q[j] = a + mu * (a - old);
+        }
+        acc[0] += (double)ff;
+    }
+    block_sum<1>(acc);
+    if (threadIdx.x == 0) partials[blockIdx.x] = acc[0];
+}
+
+// forceMax = sqrt(F.F) / Ndof and the while-condition of Adam / Nesterov
+__global__ void __launch_bounds__(kBlock) k_norm_control(IterDev *it, const double *partials, int nparts, int adam,
+                                                         double beta1, double beta2)
+{
+    if (!it->active) return;
+    double v[1];
+    sum_partials<1>(partials, nparts, v);
+    if (threadIdx.x != 0) return;
+    it->forceMax = sqrt(v[0]) / (double)it->ndof;
+    if (adam) {
+        it->b1t *= beta1;
+        it->b2t *= beta2;
+    }
+    it->iterations += 1;
+    if (!isfinite(v[0])) {
+        it->status = 1;
+        it->active = 0;
+        return;
+    }
+    it->active = (it->iterations < it->max_iters && it->forceMax > it->fcut) ? 1 : 0;
+}
+
+// ------------------------------------------------------------------ L-BFGS
+// energyMinimizerLoLBFGS::LoLBFGSStepCPU (energyMinimizerLoLBFGS.cpp:105-193).
+// Pair slot t of the two-loop recursion is computed on the device from the
+// iteration counter, so one captured iteration serves every iteration.
+// lb[0..m) = s.y per ii, lb[16..16+m) = alpha per ii, lb[32] = step-3 factor,
+// lb[33] = step-4 factor.
+__device__ __forceinline__ int lb_slot(const IterDev *it, int m, int ii)
+{
+    const int cur = it->iterations % m;
+    return (cur - ii - 1 + m) % m;
+}
+
+template <class T>
+__global__ void __launch_bounds__(kBlock) k_lb_dot(const IterDev *__restrict__ it, int op, int ii, int m,
+                                                   const T *p, const T *sb, const T *yb, long long n5, double *partials)
+{
+    if (!it->active) return;
+    const int t = lb_slot(it, m, ii);
+    const int last = (it->iterations % m - 1 + m) % m;
+    const T *s = sb + t * n5, *y = yb + t * n5;
+    double acc[2] = {0.0, 0.0};
+    for (long long j = blockIdx.x * (long long)kBlock + threadIdx.x; j < n5; j += (long long)gridDim.x * kBlock) {
+        if (op == 0) {
+            acc[0] += (double)(s[j] * y[j]);
+            acc[1] += (double)(s[j] * p[j]);
+        } else if (op == 1) {
+            const T yl = yb[last * n5 + j];
+            acc[0] += (double)(yl * yl);
+        } else if (op == 2) {
+            acc[0] += (double)(y[j] * p[j]);
+        } else {
+            acc[0] += (double)(p[j] * p[j]);
+        }
+    }
+    block_sum<2>(acc);
+    if (threadIdx.x == 0) {
+        partials[2 * blockIdx.x] = acc[0];
+        partials[2 * blockIdx.x + 1] = acc[1];
+    }
+}
+
+__global__ void __launch_bounds__(kBlock) k_lb_scalar(IterDev *it, int op, int ii, const double *partials,
+                                                      int nparts)
+{
+    if (!it->active) return;
+    double v[2];
+    sum_partials<2>(partials, nparts, v);
+    if (threadIdx.x != 0) return;
+    double *lb = it->lb;
+    if (op == 0) {
+        lb[ii] = v[0];
+        lb[16 + ii] = 0;
+        if (v[0] != 0) lb[16 + ii] = v[1] / v[0];
+    } else if (op == 1) {
+        lb[32] = v[0] != 0 ? lb[0] / v[0] : 0.0;
+        lb[34] = v[0] != 0 ? 1.0 : 0.0;
+    } else if (op == 2) {
+        lb[33] = 0.0;
+        if (lb[ii] != 0) lb[33] = lb[16 + ii] - v[0] / lb[ii];
+    } else {
+        it->forceMax = sqrt(v[0]) / (double)it->ndof;
+        it->iterations += 1;
+        if (!isfinite(v[0])) {
+            it->status = 1;
+            it->active = 0;
+            return;
+        }
+        it->active = (it->iterations < it->max_iters && it->forceMax > it->fcut) ? 1 : 0;
+    }
+}
+
+// op 0: p += -alpha[ii] y_t;  op 1: p += (sy0 / y.y) y_last (if y.y != 0);
+// op 2: p += (alpha[ii] - beta) s_t (if s.y != 0)
+template <class T>
+__global__ void __launch_bounds__(kBlock) k_lb_axpy(const IterDev *__restrict__ it, int op, int ii, int m, T *p,
+                                                    const T *sb, const T *yb, long long n5)
+{
+    if (!it->active) return;
+    const int t = lb_slot(it, m, ii);
+    const int last = (it->iterations % m - 1 + m) % m;
+    const double *lb = it->lb;
+    const T *x;
+    T a;
+    if (op == 0) {
+        x = yb + t * n5;
+        a = T(-lb[16 + ii]);
+    } else if (op == 1) {
+        if (lb[34] == 0.0) return;
+        x = yb + last * n5;
+        a = T(lb[32]);
+    } else {
+        if (lb[ii] == 0) return;
+        x = sb + t * n5;
+        a = T(lb[33]);
+    }
+    for (long long j = blockIdx.x * (long long)kBlock + threadIdx.x; j < n5; j += (long long)gridDim.x * kBlock)
+        p[j] = p[j] + a * x[j];
+}
+
+// s_cur = eta p; y_cur = F (old forces); Q += s_cur
+template <class T>
+__global__ void __launch_bounds__(kBlock) k_lb_update(const IterDev *__restrict__ it, int m, T eta, const T *p,
+                                                      T *sb, T *yb, const T *F, T *Q, long long n5)
+{
+    if (!it->active) return;
+    const int cur = it->iterations % m;
+    T *s = sb + cur * n5, *y = yb + cur * n5;
+    for (long long j = blockIdx.x * (long long)kBlock + threadIdx.x; j < n5; j += (long long)gridDim.x * kBlock) {
+        const T sv = eta * p[j];
+        s[j] = sv;
+        y[j] = F[j];
+        Q[j] += sv;
+    }
+}
+
+// p = F (new forces); y_cur += -1 * p; partial p.p
+template <class T>
+__global__ void __launch_bounds__(kBlock) k_lb_post(const IterDev *__restrict__ it, int m, T *p, T *yb, const T *F,
+                                                    long long n5, double *partials)
+{
+    if (!it->active) return;
+    const int cur = it->iterations % m;
+    T *y = yb + cur * n5;
+    double acc[2] = {0.0, 0.0};
+    for (long long j = blockIdx.x * (long long)kBlock + threadIdx.x; j < n5; j += (long long)gridDim.x * kBlock) {
+        const T f = F[j];
+        p[j] = f;
+        y[j] = y[j] + T(-1.0) * f;
+        acc[0] += (double)(f * f);
+    }
+    block_sum<2>(acc);
+    if (threadIdx.x == 0) {
+        partials[2 * blockIdx.x] = acc[0];
+        partials[2 * blockIdx.x + 1] = 0.0;
+    }
+}
+
+template <class T>
+__global__ void k_copy(T *dst, const T *src, long long n)
+{
+    for (long long j = blockIdx.x * (long long)blockDim.x + threadIdx.x; j < n; j += (long long)gridDim.x * blockDim.x)
+        dst[j] = src[j];
+}
+
+// ---------------------------------------------------------------- launchers
+static int elem_grid(long long n)
+{
+    long long g = (n + kBlock - 1) / kBlock;
+    return (int)(g < 152 * 16 ? (g > 0 ? g : 1) : 152 * 16);
+}
+
+template <class T> int launch_derivs(const Lat<T> &L, cudaStream_t s)
+{
+    k_derivs<T><<<elem_grid(L.N), kBlock, 0, s>>>(L);
+    return 1;
+}
+template <class T> int launch_force(const Lat<T> &L, int grid, cudaStream_t s)
+{
+    int n = 0;
+    if (L.multi) n += launch_derivs(L, s);
+    k_force<T><<<grid, kBlock, 0, s>>>(L);
+    return n + 1;
+}
+template <class T> int launch_fire_pred(const Lat<T> &L, FireDev *fd, cudaStream_t s)
+{
+    k_fire_pred<T><<<elem_grid(5 * L.P), kBlock, 0, s>>>(L, fd);
+    return 1;
+}
+template <class T> int launch_force_kick(const Lat<T> &L, FireDev *fd, double *partials, int grid, cudaStream_t s)
+{
+    int n = 0;
+    if (L.multi) n += launch_derivs(L, s);
+    k_force_kick<T><<<grid, kBlock, 0, s>>>(L, fd, partials);
+    return n + 1;
+}
+template <class T>
+int launch_force_kick_only(const Lat<T> &L, FireDev *fd, double *partials, int grid, cudaStream_t s)
+{
+    k_force_kick<T><<<grid, kBlock, 0, s>>>(L, fd, partials);
+    return 1;
+}
+int launch_fire_control(FireDev *fd, const double *partials, int nparts, cudaStream_t s)
+{
+    k_fire_control<<<1, kBlock, 0, s>>>(fd, partials, nparts);
+    return 1;
+}
+template <class T> int launch_fire_finish(const Lat<T> &L, FireDev *fd, cudaStream_t s)
+{
+    k_fire_finish<T><<<elem_grid(5 * L.P), kBlock, 0, s>>>(L, fd);
+    k_fire_clear_pending<<<1, 1, 0, s>>>(fd);
+    return 2;
+}
+template <class T> int launch_aos_to_soa(const double *aos, T *soa, int N, long long P, int layout, cudaStream_t s)
+{
+    k_aos_to_soa<T><<<elem_grid(5LL * N), kBlock, 0, s>>>(aos, soa, N, P, layout);
+    return 1;
+}
+template <class T> int launch_soa_to_aos(const T *soa, double *aos, int N, long long P, int layout, cudaStream_t s)
+{
+    k_soa_to_aos<T><<<elem_grid(5LL * N), kBlock, 0, s>>>(soa, aos, N, P, layout);
+    return 1;
+}
+int launch_types_to_i8(const int32_t *t32, int8_t *t8, int N, cudaStream_t s)
+{
+    k_types_to_i8<<<elem_grid(N), kBlock, 0, s>>>(t32, t8, N);
+    return 1;
+}
+template <class T> int launch_fill(T *x, T v, long long n, cudaStream_t s)
+{
+    k_fill<T><<<elem_grid(n), kBlock, 0, s>>>(x, v, n);
+    return 1;
+}
+template <class T>
+int launch_adam_step(const Lat<T> &L, T *M, T *S, IterDev *it, double beta1, double beta2, double eps, double dt,
+                     double *partials, int grid, cudaStream_t s)
+{
+    k_adam<T><<<grid, kBlock, 0, s>>>(L, M, S, it, T(beta1), T(beta2), T(eps), T(dt), partials);
+    return 1;
+}
+template <class T>
+int launch_nesterov_step(const Lat<T> &L, T *alt, IterDev *it, double dt, double mu, double *partials, int grid,
+                         cudaStream_t s)
+{
+    k_nesterov<T><<<grid, kBlock, 0, s>>>(L, alt, it, T(dt), T(mu), partials);
+    return 1;
+}
+int launch_norm_control(IterDev *it, const double *partials, int nparts, int adam, double beta1, double beta2,
+                        cudaStream_t s)
+{
+    k_norm_control<<<1, kBlock, 0, s>>>(it, partials, nparts, adam, beta1, beta2);
+    return 1;
+}
+template <class T> int launch_lbfgs_first(const Lat<T> &L, T *p, IterDev *it, cudaStream_t s)
+{
+    (void)it;
+    k_copy<T><<<elem_grid(5 * L.P), kBlock, 0, s>>>(p, L.F, 5 * L.P);
+    return 1;
+}
+template <class T>
+int launch_lbfgs_iteration(const Lat<T> &L, T *p, T *sb, T *yb, IterDev *it, int m, double eta, double *partials,
+                           int grid, cudaStream_t s)
+{
+    const long long n5 = 5 * L.P;
+    int n = 0;
+    for (int ii = 0; ii < m; ++ii) {
+        k_lb_dot<T><<<grid, kBlock, 0, s>>>(it, 0, ii, m, p, sb, yb, n5, partials);
+        k_lb_scalar<<<1, kBlock, 0, s>>>(it, 0, ii, partials, grid);
+        k_lb_axpy<T><<<elem_grid(n5), kBlock, 0, s>>>(it, 0, ii, m, p, sb, yb, n5);
+        n += 3;
+    }
+    k_lb_dot<T><<<grid, kBlock, 0, s>>>(it, 1, 0, m, p, sb, yb, n5, partials);
+    k_lb_scalar<<<1, kBlock, 0, s>>>(it, 1, 0, partials, grid);
+    k_lb_axpy<T><<<elem_grid(n5), kBlock, 0, s>>>(it, 1, 0, m, p, sb, yb, n5);
+    n += 3;
+    for (int ii = m - 1; ii >= 0; --ii) {
+        k_lb_dot<T><<<grid, kBlock, 0, s>>>(it, 2, ii, m, p, sb, yb, n5, partials);
+        k_lb_scalar<<<1, kBlock, 0, s>>>(it, 2, ii, partials, grid);
+        k_lb_axpy<T><<<elem_grid(n5), kBlock, 0, s>>>(it, 2, ii, m, p, sb, yb, n5);
+        n += 3;
+    }
+    k_lb_update<T><<<elem_grid(n5), kBlock, 0, s>>>(it, m, T(eta), p, sb, yb, L.F, L.Q, n5);
+    n += 1;
+    // forces at the moved Q (no FIRE state: a force-only launch)
+    n += launch_force(L, grid, s);
+    k_lb_post<T><<<grid, kBlock, 0, s>>>(it, m, p, yb, L.F, n5, partials);
+    k_lb_scalar<<<1, kBlock, 0, s>>>(it, 3, 0, partials, grid);
+    return n + 2;
+}
+
+template <class T>
+int launch_energy_full(const Lat<T> &L, double *partials, int grid, double *out5, const double *E, double eps,
+                       double eps0, double deps, const double *H, double chi, double mu0, double dchi, cudaStream_t s)
+{
+    k_energy<T><<<grid, kBlock, 0, s>>>(L, partials, E[0], E[1], E[2], eps, eps0, deps, H[0], H[1], H[2], chi, mu0,
+                                         dchi);
+    k_sum5<<<1, kBlock, 0, s>>>(partials, grid, out5);
+    return 2;
+}
+
+#define QMIN_INSTANTIATE(T)                                                                                       \
+    template int launch_derivs<T>(const Lat<T> &, cudaStream_t);                                                   \
+    template int launch_force<T>(const Lat<T> &, int, cudaStream_t);                                               \
+    template int launch_fire_pred<T>(const Lat<T> &, FireDev *, cudaStream_t);                                     \
+    template int launch_force_kick<T>(const Lat<T> &, FireDev *, double *, int, cudaStream_t);                     \
+    template int launch_force_kick_only<T>(const Lat<T> &, FireDev *, double *, int, cudaStream_t);                \
+    template int launch_fire_finish<T>(const Lat<T> &, FireDev *, cudaStream_t);                                   \
+    template int launch_aos_to_soa<T>(const double *, T *, int, long long, int, cudaStream_t);                     \
+    template int launch_soa_to_aos<T>(const T *, double *, int, long long, int, cudaStream_t);                     \
+    template int launch_fill<T>(T *, T, long long, cudaStream_t);                                                  \
+    template int launch_adam_step<T>(const Lat<T> &, T *, T *, IterDev *, double, double, double, double,          \
+                                     double *, int, cudaStream_t);                                                 \
+    template int launch_nesterov_step<T>(const Lat<T> &, T *, IterDev *, double, double, double *, int,            \
+                                         cudaStream_t);                                                            \
+    template int launch_lbfgs_first<T>(const Lat<T> &, T *, IterDev *, cudaStream_t);                              \
+    template int launch_lbfgs_iteration<T>(const Lat<T> &, T *, T *, T *, IterDev *, int, double, double *, int,   \
+                                           cudaStream_t);                                                          \
+    template int launch_energy_full<T>(const Lat<T> &, double *, int, double *, const double *, double, double,    \
+                                       double, const double *, double, double, double, cudaStream_t);
+
+QMIN_INSTANTIATE(double)
+QMIN_INSTANTIATE(float)
+
+}  // namespace qmin

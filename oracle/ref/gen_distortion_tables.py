@@ -85,13 +85,48 @@ def main():
     lines = [header, "#pragma once", "#include <stdint.h>",
              f"#define QMIN_DT_NPAIRS {len(inputs)}",
              "/* offset[(term*64 + case)*5 + component] .. offset[... + 1] */",
-             "static const uint16_t qmin_dt_offset[3 * 64 * 5 + 1] = {" +
-             ",".join(str(x) for x in offsets) + "};",
-             "static const uint8_t qmin_dt_input[QMIN_DT_NPAIRS] = {" + ",".join(str(x) for x in inputs) + "};",
-             "static const int8_t qmin_dt_k[QMIN_DT_NPAIRS] = {" + ",".join(str(x) for x in ks) + "};", ""]
+             "/* initialiser lists, so that host and device copies can be defined from them */",
+             "#define QMIN_DT_OFFSET_INIT {" + ",".join(str(x) for x in offsets) + "}",
+             "#define QMIN_DT_INPUT_INIT {" + ",".join(str(x) for x in inputs) + "}",
+             "#define QMIN_DT_K_INIT {" + ",".join(str(x) for x in ks) + "}", ""]
     with open(os.path.join(ROOT, "open-qmin_gb300", "csrc", "qmin_distortion_tables.h"), "w") as f:
         f.write("\n".join(lines))
-    print(f"wrote tables: {len(inputs)} nonzero coefficients")
+    # straight-line bulk forms: the union of the L2, L3, L4 bulk patterns per
+    # component; the kernels multiply each input by a per-handle coefficient
+    # cb[k][n] = sum_t L_t * k_t / 4 computed on the host.
+    union = [sorted(set().union(*[coef[(t, 0, c)].keys() for t in TERMS])) for c in range(5)]
+    W = max(len(u) for u in union)
+    lines = [header.replace("Do not edit.", "Do not edit.  Bulk (case 0) forms, straight-line."), "#pragma once",
+             f"#define QMIN_BULK_W {W}",
+             "/* inputs of component k: qmin_bulk_in[k][0 .. qmin_bulk_n[k]) (0..4 q, 5..34 neighbour q,",
+             "   35..124 neighbour derivatives); per-term integer coefficients qmin_bulk_k[term][k][n] */",
+             "static const int qmin_bulk_n[5] = {" + ",".join(str(len(u)) for u in union) + "};",
+             "static const int qmin_bulk_in[5][QMIN_BULK_W] = {" +
+             ",".join("{" + ",".join(str(x) for x in u + [0] * (W - len(u))) + "}" for u in union) + "};",
+             "static const int qmin_bulk_k[3][5][QMIN_BULK_W] = {" +
+             ",".join("{" + ",".join("{" + ",".join(str(coef[(t, 0, c)].get(x, 0)) for x in union[c] + [-1] * 0) +
+                                      "," * 0 + ",".join([""] * 0) + ("," if len(union[c]) < W else "") +
+                                      ",".join(["0"] * (W - len(union[c]))) + "}" for c in range(5)) + "}"
+                      for t in TERMS) + "};",
+             "",
+             "/* s[k] = sum_n cb[k*QMIN_BULK_W + n] * input; QIN(c) = own q component,",
+             "   QN(slot, c) = neighbour q, DN(slot, d) = neighbour derivative component */",
+             "#define QMIN_BULK_FORMS(cb, s) \\"]
+
+    def term(j):
+        if j < 5:
+            return f"QIN({j})"
+        if j < 35:
+            return f"QN({(j - 5) // 5},{(j - 5) % 5})"
+        return f"DN({(j - 35) // 15},{(j - 35) % 15})"
+    for c in range(5):
+        body = " + ".join(f"(cb)[{c * W + n}] * {term(j)}" for n, j in enumerate(union[c]))
+        lines.append(f"    (s)[{c}] = {body}; \\")
+    lines.append("    do {} while (0)")
+    lines.append("")
+    with open(os.path.join(ROOT, "open-qmin_gb300", "csrc", "qmin_bulk_forms.h"), "w") as f:
+        f.write("\n".join(lines))
+    print(f"wrote tables: {len(inputs)} nonzero coefficients; bulk union widths {[len(u) for u in union]}")
 
 
 if __name__ == "__main__":

@@ -1,0 +1,88 @@
+#!/usr/bin/env python3
+"""Regenerate the golden fixtures in tests/golden/ from the reference itself.
+
+Runs oracle/_ref/ref_dumper (the reference's own CPU objects, compiled from
+the reference tree by oracle/ref/Makefile) on a set of small seeded cases and
+stores its dumps as compressed .npz files.  Needs the reference tree, so it
+runs only where that tree is mounted:
+
+    make -C oracle/ref REF=/root/reference -j8 && python3 tests/golden/make_golden.py
+
+Each case records: the arguments, the initial Q and site types, the force at
+Q0 (CPU-path semantics), the energy at Q0 (E/NActive and its five
+components), the per-iteration minimiser trace where available, and the final
+Q, velocities, forces, forceMax and energy.
+"""
+import json
+import os
+import subprocess
+import tempfile
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+DUMPER = os.path.join(ROOT, "oracle", "_ref", "ref_dumper")
+
+# name -> (dumper arguments, keep full arrays)
+CASES = {
+    # one-constant, all bulk (the 50^3 CLI configuration at a small size)
+    "l1_bulk_fire": (["L=12,10,9", "seed=13371", "Ls=2.32,0,0,0,0", "minimizer=fire", "iters=40", "trace=1"], True),
+    # multi-constant L1-L3, two homeotropic z-walls and a homeotropic sphere
+    "l123_walls_sphere_fire": (["L=12,11,10", "seed=5", "Ls=2.32,1.0,0.5,0,0", "wall=2,0,h,5.3", "wall=2,9,h,5.3",
+                                "sphere=6,5.5,4.5,2.6,h,5.3", "minimizer=fire", "iters=30", "trace=1"], True),
+    # degenerate planar (Fournier-Galatola) sphere, one-constant
+    "planar_sphere_fire": (["L=11,11,11", "seed=17", "Ls=2.32,0,0,0,0", "sphere=5.3,5.6,4.9,3.1,p,1.3",
+                            "minimizer=fire", "iters=30", "trace=1"], True),
+    # L1-L4, planar sphere + homeotropic x-wall, E and H fields
+    "l1234_planar_fields_fire": (["L=10,9,11", "seed=23", "Ls=2.32,1.0,0.5,0.7,0", "wall=0,0,h,3.0",
+                                  "sphere=5,4.5,5.5,2.3,p,2.0", "E=0.1,0.2,0.5,1,1,0.5", "H=0.3,0,0.2,1.2,0.9,0.4",
+                                  "minimizer=fire", "iters=25", "trace=1"], True),
+    # edge cases: sites squeezed between two objects along one axis (walls at z=0 and z=2),
+    # a sphere wrapping through the periodic boundary, overlapping objects
+    "edges_gaps_wrap": (["L=10,10,10", "seed=99", "Ls=2.32,1.0,0.5,0,0", "wall=2,0,h,5.3", "wall=2,2,p,1.0",
+                         "sphere=0.5,0.5,6,2.4,h,4.0", "sphere=8.3,2.2,3.4,1.8,p,2.5", "minimizer=fire", "iters=20",
+                         "trace=1"], True),
+    # the other minimisers on a multi-constant lattice with objects
+    "adam": (["L=10,9,8", "seed=3", "Ls=2.32,1.0,0.5,0,0", "wall=2,0,h,5.3", "sphere=5,4,4,2.1,p,1.5",
+              "minimizer=adam", "iters=25", "dt=0.0005"], True),
+    "nesterov": (["L=10,9,8", "seed=4", "Ls=2.32,1.0,0.5,0,0", "wall=1,0,h,5.3", "sphere=5,4,4,2.1,h,5.3",
+                  "minimizer=nesterov", "iters=25", "dt=0.0005"], True),
+    "lbfgs": (["L=10,9,8", "seed=6", "Ls=2.32,0,0,0,0", "wall=0,0,p,1.0", "sphere=5,4,4,2.1,h,5.3",
+               "minimizer=lbfgs", "iters=25", "dt=0.0005"], True),
+    # the 50^3 one-constant CLI run (openQmin -i 100 -l 50 --L1 2.32): scalars only
+    "c1_50cube_fire100": (["L=50,50,50", "seed=13371", "Ls=2.32,0,0,0,0", "minimizer=fire", "iters=100",
+                           "trace=1"], False),
+}
+
+
+def run_case(name, args, full):
+    with tempfile.TemporaryDirectory() as d:
+        subprocess.run([DUMPER, d] + args, check=True, capture_output=True)
+        ld = lambda f, dt=np.float64: np.fromfile(os.path.join(d, f), dtype=dt)
+        out = {"args": np.array(json.dumps(args))}
+        e0 = np.array([float(x) for x in open(os.path.join(d, "energy0.txt")).read().split()])
+        fin = np.array([float(x) for x in open(os.path.join(d, "final.txt")).read().split()])
+        out["energy0"] = e0
+        out["final"] = fin
+        if os.path.exists(os.path.join(d, "trace.txt")):
+            out["trace"] = np.loadtxt(os.path.join(d, "trace.txt"), ndmin=2)
+        types = ld("types.i32", np.int32)
+        out["types"] = types.astype(np.int8)
+        if full:
+            out["q0"] = ld("q0.f64").reshape(-1, 5)
+            out["force0"] = ld("force0.f64").reshape(-1, 5)
+            out["qfinal"] = ld("qfinal.f64").reshape(-1, 5)
+            out["vfinal"] = ld("vfinal.f64").reshape(-1, 5)
+            out["ffinal"] = ld("ffinal.f64").reshape(-1, 5)
+        np.savez_compressed(os.path.join(HERE, name + ".npz"), **out)
+
+
+def main():
+    for name, (args, full) in CASES.items():
+        run_case(name, args, full)
+        print("wrote", name)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,80 @@
+"""C-ABI library checks that need no GPU: it loads, exports every entry point
+declared in include/qmin_gb300.h, rejects bad arguments with status codes,
+and its host set-up helpers reproduce the reference's initial state."""
+import ctypes as C
+import os
+import re
+
+import numpy as np
+import pytest
+
+from cases import GOLDEN_CASES, load, oracle_system, parse_args
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def declared_symbols():
+    txt = open(os.path.join(ROOT, "include", "qmin_gb300.h")).read()
+    return sorted(set(re.findall(r"^(?:int|const char \*)\s*(qmin_\w+)\(", txt, re.M)))
+
+
+def test_library_exports_every_declared_symbol(qmin):
+    lib = qmin.lib()
+    syms = declared_symbols()
+    assert len(syms) >= 20
+    for s in syms:
+        assert hasattr(lib, s), s
+    assert set(qmin.EXPORTED_SYMBOLS) <= set(syms)
+
+
+def test_status_codes_without_device(qmin):
+    lib = qmin.lib()
+    h = C.c_void_p()
+    assert lib.qmin_create(None, C.byref(h)) == qmin.QMIN_EINVAL
+    d = qmin.LatticeDesc(2, 8, 8, 0, 0)
+    assert lib.qmin_create(C.byref(d), C.byref(h)) == qmin.QMIN_EINVAL
+    assert b"lattice side" in lib.qmin_last_error_string()
+    d = qmin.LatticeDesc(8, 8, 8, 7, 0)
+    assert lib.qmin_create(C.byref(d), C.byref(h)) == qmin.QMIN_EINVAL
+    assert lib.qmin_force(None, None) == qmin.QMIN_EINVAL
+    assert lib.qmin_fire_run(None, 1, None) == qmin.QMIN_EINVAL
+
+
+def test_no_cpu_fallback(qmin):
+    """On a machine without a GPU the compute path refuses loudly."""
+    import torch
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    with pytest.raises(qmin.QminError):
+        qmin.Lattice((8, 8, 8))
+
+
+@pytest.mark.parametrize("name", GOLDEN_CASES)
+def test_host_setup_matches_reference(qmin, oracle, name):
+    g = load(name)
+    cfg = parse_args(g["args"])
+    _, _, _, S0 = qmin.cli_phase_constants()
+    Q = qmin.host_random_nematic(cfg["L"], cfg["seed"], S0)
+    geo = qmin.Geometry(cfg["L"], Q)
+    for xyz, plane, kind, W in cfg["walls"]:
+        geo.add_wall(xyz, plane, kind, W, S0)
+    for c, r, kind, W in cfg["spheres"]:
+        geo.add_sphere(c, r, kind, W, S0)
+    np.testing.assert_array_equal(geo.types, g["types"].astype(np.int32))
+    m = np.isfinite(g["q0"])
+    np.testing.assert_array_equal(geo.Q[m], g["q0"][m])
+
+
+def test_host_setup_rejects_bad_arguments(qmin):
+    lib = qmin.lib()
+    Q = np.zeros((27, 5))
+    t = np.zeros(27, dtype=np.int32)
+    objs = (qmin.Object * 4)()
+    n = C.c_int(0)
+    dp = Q.ctypes.data_as(C.POINTER(C.c_double))
+    ip = t.ctypes.data_as(C.POINTER(C.c_int))
+    assert lib.qmin_host_add_wall(3, 3, 3, 5, 0, 0, 1.0, 0.5, dp, ip, objs, C.byref(n)) == qmin.QMIN_EINVAL
+    assert lib.qmin_host_add_wall(3, 3, 3, 0, 0, 9, 1.0, 0.5, dp, ip, objs, C.byref(n)) == qmin.QMIN_EINVAL
+    c = (C.c_double * 3)(1, 1, 1)
+    assert lib.qmin_host_add_sphere(3, 3, 3, c, -1.0, 0, 1.0, 0.5, dp, ip, objs, C.byref(n)) == qmin.QMIN_EINVAL
+    assert n.value == 0

@@ -1,0 +1,170 @@
+"""GPU parity: the CUDA path (through the C ABI) against the oracle and the
+reference's golden dumps.
+
+Tolerances (written here, used below):
+  FP64 single force evaluation / energy: <= 1e-12 normwise relative
+  FP64 minimiser traces and final state after N iterations: <= 1e-9 relative
+    (reduction order differs from the reference's sequential sums)
+  FP32 form, single force evaluation: <= 2e-6 normwise relative to FP64
+"""
+import numpy as np
+import pytest
+
+from cases import GOLDEN_CASES, gpu_lattice, load, oracle_system, parse_args, rel_err
+
+pytestmark = pytest.mark.gpu
+
+TOL_F64 = 1e-12
+TOL_TRAJ = 1e-9
+TOL_F32 = 2e-6
+
+
+@pytest.mark.parametrize("name", GOLDEN_CASES)
+@pytest.mark.parametrize("metric_mode", [0, 1])
+def test_force_and_energy_fp64(qmin, oracle, name, metric_mode):
+    g = load(name)
+    cfg = parse_args(g["args"])
+    s = oracle_system(oracle, cfg, metric_mode=metric_mode)
+    lat = gpu_lattice(qmin, s, qmin.FP64, metric_mode)
+    F = lat.force()
+    assert rel_err(F, s.force()) <= TOL_F64
+    if metric_mode == 0:
+        assert rel_err(F, g["force0"]) <= TOL_F64
+    e, comps = lat.energy()
+    e_o, comps_o = s.energy()
+    assert abs(e - e_o) <= TOL_F64 * abs(e_o)
+    np.testing.assert_allclose(comps, comps_o, rtol=TOL_F64, atol=TOL_F64 * np.abs(comps_o).max())
+    assert abs(e - g["energy0"][0]) <= TOL_F64 * abs(g["energy0"][0])
+
+
+@pytest.mark.parametrize("name", GOLDEN_CASES)
+def test_force_fp32(qmin, oracle, name):
+    g = load(name)
+    cfg = parse_args(g["args"])
+    s = oracle_system(oracle, cfg)
+    lat = gpu_lattice(qmin, s, qmin.FP32)
+    F = lat.force()
+    assert rel_err(F, g["force0"]) <= TOL_F32
+    e, _ = lat.energy()
+    assert abs(e - g["energy0"][0]) <= 1e-5 * abs(g["energy0"][0])
+
+
+@pytest.mark.parametrize("name", ["l1_bulk_fire", "l123_walls_sphere_fire", "planar_sphere_fire",
+                                  "l1234_planar_fields_fire", "edges_gaps_wrap"])
+def test_fire_trajectory_fp64(qmin, oracle, name):
+    g = load(name)
+    cfg = parse_args(g["args"])
+    s = oracle_system(oracle, cfg)
+    lat = gpu_lattice(qmin, s, qmin.FP64)
+    lat.fire_init(dt=cfg["dt"])
+    n = cfg["iters"]
+    r = lat.fire_run(n)
+    tr = g["trace"]
+    assert r["iterations"] == int(g["final"][0])
+    assert abs(r["forceMax"] - tr[-1, 1]) <= TOL_TRAJ * tr[-1, 1]
+    assert abs(r["alpha"] - tr[-1, 2]) <= TOL_TRAJ * tr[-1, 2]
+    assert abs(r["dt"] - tr[-1, 3]) <= TOL_TRAJ * tr[-1, 3]
+    assert r["nsince"] == int(tr[-1, 5])
+    Q, V, F = lat.get_state(Q=True, V=True, F=True)
+    assert rel_err(Q, g["qfinal"]) <= TOL_TRAJ
+    assert rel_err(V, g["vfinal"]) <= 1e-7
+    assert rel_err(F, g["ffinal"]) <= 1e-7
+    e, _ = lat.energy()
+    assert abs(e - g["final"][2]) <= TOL_TRAJ * abs(g["final"][2])
+
+
+def test_fire_per_iteration_trace(qmin, oracle):
+    """Run FIRE one iteration per call (as the reference's minimize() with a
+    growing iteration cap) and compare every step's scalars."""
+    g = load("l123_walls_sphere_fire")
+    cfg = parse_args(g["args"])
+    s = oracle_system(oracle, cfg)
+    lat = gpu_lattice(qmin, s, qmin.FP64)
+    lat.fire_init(dt=cfg["dt"])
+    for k, row in enumerate(g["trace"], start=1):
+        r = lat.fire_run(k)
+        assert r["iterations"] == k
+        np.testing.assert_allclose([r["forceMax"], r["alpha"], r["dt"], r["power"]], row[1:5], rtol=TOL_TRAJ)
+        assert r["nsince"] == int(row[5])
+
+
+@pytest.mark.parametrize("name", ["adam", "nesterov", "lbfgs"])
+def test_other_minimisers_fp64(qmin, oracle, name):
+    g = load(name)
+    cfg = parse_args(g["args"])
+    s = oracle_system(oracle, cfg)
+    lat = gpu_lattice(qmin, s, qmin.FP64)
+    n, dt = cfg["iters"], cfg["dt"]
+    if name == "adam":
+        r = lat.adam_run(n, dt=dt)
+    elif name == "nesterov":
+        r = lat.nesterov_run(n, dt=dt)
+    else:
+        r = lat.lbfgs_run(n, eta=dt)
+    assert r["iterations"] == int(g["final"][0])
+    assert abs(r["forceMax"] - g["final"][1]) <= TOL_TRAJ * g["final"][1]
+    Q = lat.get_state(Q=True)[0]
+    assert rel_err(Q, g["qfinal"]) <= TOL_TRAJ
+
+
+def test_c1_50cube_fire100(qmin, oracle):
+    """openQmin -i 100 -l 50 --L1 2.32 end state (reference pin)."""
+    g = load("c1_50cube_fire100")
+    cfg = parse_args(g["args"])
+    s = oracle_system(oracle, cfg)
+    lat = gpu_lattice(qmin, s, qmin.FP64)
+    lat.fire_init()
+    r = lat.fire_run(100)
+    assert r["iterations"] == 100
+    assert abs(r["forceMax"] - g["final"][1]) <= TOL_TRAJ * g["final"][1]
+    e, _ = lat.energy()
+    assert abs(e - g["final"][2]) <= TOL_TRAJ * abs(g["final"][2])
+
+
+def test_fp32_fire_tracks_fp64(qmin, oracle):
+    """FP32 stencils with FP64 reductions: 100 FIRE steps of the 50^3 case stay
+    within 1e-4 relative of the FP64 oracle in energy and forceMax."""
+    g = load("c1_50cube_fire100")
+    cfg = parse_args(g["args"])
+    s = oracle_system(oracle, cfg)
+    lat = gpu_lattice(qmin, s, qmin.FP32)
+    lat.fire_init()
+    r = lat.fire_run(100)
+    e, _ = lat.energy()
+    assert abs(e - g["final"][2]) <= 1e-4 * abs(g["final"][2])
+    assert abs(r["forceMax"] - g["final"][1]) <= 1e-3 * g["final"][1]
+
+
+def test_reference_shaped_api(qmin, oracle):
+    """The reference-shaped classes drive the same computation (openQmin.cpp flow)."""
+    a, b, c, S0 = qmin.cli_phase_constants()
+    model = qmin.qTensorLatticeModel(12, 11, 10)
+    sim = qmin.multirankSimulation(0, 1, 1, 1, False, False)
+    lc = qmin.landauDeGennesLC()
+    sim.setConfiguration(model)
+    lc.setPhaseConstants(a, b, c)
+    lc.setElasticConstants(2.32, 1.0, 0.5)
+    sim.addForce(lc)
+    fire = qmin.energyMinimizerFIRE(model)
+    fire.setMaximumIterations(30)
+    fire.setFIREParameters(5e-4, .99, 100 * 5e-4, 1.1, 0.95, 0.9, 4, 1e-12, 0.0)
+    sim.addUpdater(fire, model)
+    model.setNematicQTensorRandomly(5, S0)
+    hom = qmin.boundaryObject(qmin.boundaryType.homeotropic, 5.3, S0)
+    sim.createWall(2, 0, hom)
+    sim.createWall(2, 9, hom)
+    sim.createSphericalColloid((6, 5.5, 4.5), 2.6, hom)
+    sim.finalizeObjects()
+    sim.performTimestep()
+    g = load("l123_walls_sphere_fire")
+    assert abs(fire.getMaxForce() - g["final"][1]) <= TOL_TRAJ * g["final"][1]
+    assert abs(sim.computePotentialEnergy() - g["final"][2]) <= TOL_TRAJ * abs(g["final"][2])
+
+
+def test_launches_counted(qmin, oracle):
+    cfg = parse_args(["L=8,8,8", "seed=1", "Ls=2.32,0,0,0,0"])
+    s = oracle_system(oracle, cfg)
+    lat = gpu_lattice(qmin, s)
+    before = lat.launches()
+    lat.force(copy=False)
+    assert lat.launches() > before
