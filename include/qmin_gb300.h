@@ -152,6 +152,31 @@ int qmin_lbfgs_run(qmin_handle h, int m, double eta, double force_cutoff, int ma
  * advances exactly as in qmin_fire_run.  No reference counterpart (profiling). */
 int qmin_fire_profile(qmin_handle h, int iterations, double kernel_ms[4]);
 
+/* ---- energy without allocation ---- */
+/* Largest lattice (in sites) qmin_energy_noalloc accepts: the size of its
+ * static reduction scratch (one block of 256 sites per partial sum). */
+#define QMIN_NOALLOC_MAX_SITES 8388608
+
+/* Energy of a Q field held in the caller's own device memory, for callers
+ * that cannot call cudaMalloc (their device memory is owned by a pool
+ * allocator of their own, or is fully committed).  Allocates nothing: its
+ * scratch is a static device array of about 1.6 MB that every GPU loading
+ * this library holds until exit.  FP64 only.
+ *   Q_dev:       device, SoA double planes Q_dev[k * plane_stride + i], k = 0..4
+ *   types_dev:   device, int8 site types (same meaning as qmin_set_state's)
+ *   out_dev:     device, 6 doubles: E / NActive, then the phase, distortion,
+ *                anchoring, E-field and H-field totals (as qmin_energy)
+ *   objs:        host array of nobj objects; stream: cudaStream_t or NULL
+ * Results match qmin_energy on the same state.  Returns QMIN_EINVAL for a
+ * lattice larger than QMIN_NOALLOC_MAX_SITES sites.  The first call on each
+ * device looks up the scratch address; make it before any stream capture.
+ * All calls share the scratch: calls that overlap on the GPU race, so
+ * serialise them.  The result is ready when the stream reaches it.
+ * No counterpart in the reference (an addition for allocation-free callers). */
+int qmin_energy_noalloc(const qmin_lattice_desc *desc, const qmin_ldg_params *p, const qmin_object *objs, int nobj,
+                        const double *Q_dev, long long plane_stride, const int8_t *types_dev, double *out_dev,
+                        void *stream);
+
 /* ---- host-side set-up helpers (the reference runs these on the host even
  *      in GPU runs, openQmin.cpp:261-268) ---- */
 /* qTensorLatticeModel::setNematicQTensorRandomly (qTensorLatticeModel.cpp:134-162)

@@ -18,11 +18,13 @@
 
 using namespace qmin;
 
-static thread_local std::string g_err;
+namespace qmin {
+thread_local std::string g_last_error;
+}
 
 static int fail(int code, const std::string &msg)
 {
-    g_err = msg;
+    qmin::g_last_error = msg;
     return code;
 }
 
@@ -149,7 +151,7 @@ static void invalidate_graphs(qmin_ctx *h)
 // The API functions below take C linkage from their declarations in
 // qmin_gb300.h (included above).
 
-const char *qmin_last_error_string(void) { return g_err.c_str(); }
+const char *qmin_last_error_string(void) { return qmin::g_last_error.c_str(); }
 
 int qmin_create(const qmin_lattice_desc *desc, qmin_handle *out)
 {

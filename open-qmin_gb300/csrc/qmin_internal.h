@@ -3,6 +3,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <string>
+
 #include "qmin_bulk_forms.h"
 
 namespace qmin {
@@ -47,6 +49,9 @@ struct IterDev {
 };
 
 constexpr int kBlock = 256;
+
+// message behind the last non-zero status returned on this host thread
+extern thread_local std::string g_last_error;
 
 // launchers (qmin_kernels.cu); each returns the number of kernels launched
 template <class T> int launch_derivs(const Lat<T> &L, cudaStream_t s);
