@@ -103,6 +103,13 @@ class ClockSampler:
         return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
 
 
+def scale_workload(side):
+    """The same geometry on a side^3 lattice (walls at 0 and side-1, centred sphere r = 0.15 side)."""
+    WORKLOAD["L"] = (side, side, side)
+    WORKLOAD["walls"] = (0, side - 1)
+    WORKLOAD["sphere"] = ((side / 2.0, side / 2.0, side / 2.0), 0.15 * side)
+
+
 def build_workload_host(q, precision=None):
     """Host set-up of the workload through the package's own host helpers."""
     a, b, c, S0 = q.cli_phase_constants()
@@ -175,6 +182,11 @@ def run_ours(args, rank, world):
         ms = e0.elapsed_time(e1)
         return lat, r, ms, lat.launches() - l0, clk.summary()
 
+    if args.forms == "fp32":
+        lat32, r32, ms32, launches32, _ = timed_fire(q.FP32)
+        lat32.close()
+        return {"form": "fp32", "value": N * K / (ms32 / 1e3), "ms_per_step": ms32 / K, "forceMax": r32["forceMax"],
+                "gpu_launches": launches32}
     # ---- device-resident FP64 run (the headline)
     lat, r, ms, launches, clocks = timed_fire(q.FP64)
     ms_all = [ms]
@@ -203,9 +215,21 @@ def run_ours(args, rank, world):
     roofline["iteration_achieved_gbs_at_241B"] = 241 * N / (it_ms / 1e3) / 1e9
     fire_state = {"forceMax": r["forceMax"], "iterations": r["iterations"]}
     lat.close()
+    if args.forms == "fp64":
+        return {"form": "fp64", "value": value, "ms_per_step": ms / K, "roofline": roofline, "gpu_launches": launches}
 
     # ---- end to end through the C ABI from pinned host memory
+    e2e = None
+    if not args.no_e2e:
+        e2e = run_e2e(q, consts, g, K, W, barrier, dist)
+    return finish(q, args, rank, world, consts, g, N, K, W, timed_fire, value, ms, launches, clocks, roofline,
+                  fire_state, r, e2e, peak, C)
+
+
+def run_e2e(q, consts, g, K, W, barrier, dist):
+    import torch
     import torch as _t
+    N = g.Q.shape[0]
     Qh = _t.from_numpy(g.Q).pin_memory()
     Th = _t.from_numpy(g.types).pin_memory()
     Qout = _t.empty_like(Qh).pin_memory()
@@ -235,11 +259,16 @@ def run_ours(args, rank, world):
         ms_e2e = float(t.item())
     h2d = N * 5 * 8 + N * 4
     d2h = N * 5 * 8
+    world = int(os.environ.get("WORLD_SIZE", 1))
     e2e = {"value": world * N * K / (ms_e2e / 1e3), "unit": "site-steps/s", "h2d_bytes_per_step": h2d / K,
            "d2h_bytes_per_step": d2h / K,
            "note": "per job: upload Q0 (AoS f64) + int32 types, K FIRE iterations, download final Q; bytes amortised over K"}
     lat.close()
+    return e2e
 
+
+def finish(q, args, rank, world, consts, g, N, K, W, timed_fire, value, ms, launches, clocks, roofline, fire_state,
+           r, e2e, peak, C):
     # ---- FP32 form (FP32 state/stencils, FP64 reductions) on the same input
     lat32, r32, ms32, _, _ = timed_fire(q.FP32)
     fp32 = {"value": N * K / (ms32 / 1e3), "unit": "site-steps/s", "ms_per_step": ms32 / K,
@@ -345,9 +374,14 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--cpu-sample-iters", type=int, default=2)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--lattice", type=int, default=200, help="cube side (profiling of smaller cases)")
+    ap.add_argument("--forms", default="both", choices=["both", "fp64", "fp32"])
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", 0))
     world = int(os.environ.get("WORLD_SIZE", 1))
+    if args.lattice != 200:
+        scale_workload(args.lattice)
 
     if args.impl == "reference":
         if rank != 0:
@@ -361,7 +395,7 @@ def main():
         torch.distributed.init_process_group("nccl")
     out = run_ours(args, rank, world)
     if rank == 0:
-        if not args.no_cpu_baseline:
+        if not args.no_cpu_baseline and args.forms == "both":
             out["cpu_baseline"], _ = cpu_baseline(args.cpu_sample_iters)
         print(json.dumps(out))
     if world > 1:

@@ -168,3 +168,16 @@ def test_launches_counted(qmin, oracle):
     before = lat.launches()
     lat.force(copy=False)
     assert lat.launches() > before
+
+
+def test_cpp_host_example_reproduces_cli_pin(qmin):
+    """The C++ host layer (open-qmin_gb300/host) runs the reference CLI's default
+    50^3 / 100-iteration FIRE job and prints the reference's end state."""
+    import os
+    import subprocess
+    exe = os.path.join(os.path.dirname(qmin.LIB_PATH), "example_fire")
+    out = subprocess.run([exe], capture_output=True, text=True, check=True).stdout.split()
+    fmax, e = float(out[2]), float(out[3].split("=")[1])
+    g = load("c1_50cube_fire100")
+    assert abs(fmax - g["final"][1]) <= TOL_TRAJ * g["final"][1]
+    assert abs(e - g["final"][2]) <= TOL_TRAJ * abs(g["final"][2])
