@@ -38,6 +38,26 @@ WORKLOAD = dict(L=(200, 200, 200), seed=13371, Ls=(2.32, 1.0, 0.5), W=5.3, walls
 #  control: scalars only
 KERNEL_BYTES = {8: [200, 161, 161, 0], 4: [100, 81, 81, 0]}
 KERNEL_NAMES = ["fire_predictor", "first_derivatives", "force_kick_reduce", "fire_control"]
+# the fused tiled iteration: read Q, V, F, types; write Q, V, F (halo re-reads excluded)
+FUSED_BYTES = {8: 241, 4: 121}
+
+
+def kernel_roofline(lat, esz, N, peak, peak_kind, tag):
+    """Dominant kernel of the FIRE iteration, timed with CUDA events per launch."""
+    kms, fused = lat.fire_profile(20)
+    names = list(KERNEL_NAMES)
+    nbytes = list(KERNEL_BYTES[esz])
+    if fused:
+        names[2] = "fire_fused"
+        nbytes[2] = FUSED_BYTES[esz]
+    dom = int(np.argmax(kms))
+    achieved = nbytes[dom] * N / (kms[dom] / 1e3) / 1e9
+    out = {"bound": "hbm", "kernel": names[dom], "achieved": achieved, "peak": peak, "unit": "GB/s",
+           "frac": achieved / peak, "peak_source": peak_kind, "traffic": traffic_from_profiles(names[dom], tag),
+           "kernel_ms": {n: float(x) for n, x in zip(names, kms) if x > 0},
+           "algorithmic_bytes_per_site": nbytes[dom], "sites_per_launch": N}
+    out["autotuned"] = lat.fire_tuning()
+    return out
 
 
 def measured_peaks():
@@ -197,19 +217,9 @@ def run_ours(args, rank, world):
     value = world * N * K / (ms / 1e3)
 
     # ---- roofline of the dominant kernel (direct launches, CUDA events per kernel)
-    kms = np.zeros(4)
     import ctypes as C
-    arr = (C.c_double * 4)()
-    q._check(q.lib().qmin_fire_profile(lat._h, 20, arr))
-    kms[:] = list(arr)
-    dom = int(np.argmax(kms))
     peak, peak_kind = measured_peaks()
-    achieved = KERNEL_BYTES[8][dom] * N / (kms[dom] / 1e3) / 1e9
-    roofline = {"bound": "hbm", "kernel": KERNEL_NAMES[dom], "achieved": achieved, "peak": peak, "unit": "GB/s",
-                "frac": achieved / peak, "peak_source": peak_kind,
-                "traffic": traffic_from_profiles(KERNEL_NAMES[dom], "f64"),
-                "kernel_ms": dict(zip(KERNEL_NAMES, [float(x) for x in kms])),
-                "algorithmic_bytes_per_site": KERNEL_BYTES[8][dom]}
+    roofline = kernel_roofline(lat, 8, N, peak, peak_kind, "f64")
     # whole-iteration view: 241 B/site for the fused ideal (read Q,V,F,types; write Q,V,F)
     it_ms = ms / (K)
     roofline["iteration_achieved_gbs_at_241B"] = 241 * N / (it_ms / 1e3) / 1e9
@@ -273,13 +283,7 @@ def finish(q, args, rank, world, consts, g, N, K, W, timed_fire, value, ms, laun
     lat32, r32, ms32, _, _ = timed_fire(q.FP32)
     fp32 = {"value": N * K / (ms32 / 1e3), "unit": "site-steps/s", "ms_per_step": ms32 / K,
             "forceMax": r32["forceMax"], "forceMax_rel_err_vs_fp64": abs(r32["forceMax"] - r["forceMax"]) / r["forceMax"]}
-    arr = (C.c_double * 4)()
-    q._check(q.lib().qmin_fire_profile(lat32._h, 20, arr))
-    k32 = np.array(list(arr))
-    d32 = int(np.argmax(k32))
-    a32 = KERNEL_BYTES[4][d32] * N / (k32[d32] / 1e3) / 1e9
-    fp32["roofline"] = {"bound": "hbm", "kernel": KERNEL_NAMES[d32], "achieved": a32, "peak": peak, "unit": "GB/s",
-                        "frac": a32 / peak, "kernel_ms": dict(zip(KERNEL_NAMES, [float(x) for x in k32]))}
+    fp32["roofline"] = kernel_roofline(lat32, 4, N, peak, "measured", "f32")
     lat32.close()
 
     out = None

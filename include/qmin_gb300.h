@@ -144,13 +144,28 @@ int qmin_nesterov_run(qmin_handle h, double dt, double mu, double force_cutoff, 
 int qmin_lbfgs_run(qmin_handle h, int m, double eta, double force_cutoff, int max_iterations, int reset,
                    int *iterations, double *force_max);
 
-/* ---- diagnostics ---- */
+/* ---- FIRE iteration strategy and diagnostics ---- */
+#define QMIN_FIRE_SEPARATE 0 /* predictor, derivative planes, force+kick, control as separate kernels */
+#define QMIN_FIRE_FUSED 1    /* one shared-memory tiled kernel per iteration */
+#define QMIN_FIRE_AUTO 2     /* the autotuner picks the fastest of the above (default) */
+/* Choose how qmin_fire_run executes an iteration; all strategies give the
+ * same results to rounding.  No reference counterpart (execution strategy). */
+int qmin_set_fire_kernel(qmin_handle h, int mode);
 /* Run `iterations` FIRE iterations with direct (non-graph) launches and CUDA
  * events around every kernel; kernel_ms receives the average device time per
- * launch of [0] predictor, [1] first-derivative planes (0 for one-constant),
- * [2] force + half kick + reductions, [3] FIRE scalar control.  The FIRE state
+ * launch of [0] predictor, [1] first-derivative planes, [2] force + half kick
+ * + reductions (for the fused kernel: the whole fused iteration), [3] FIRE
+ * scalar control; *fused (may be NULL) tells which path ran.  The FIRE state
  * advances exactly as in qmin_fire_run.  No reference counterpart (profiling). */
-int qmin_fire_profile(qmin_handle h, int iterations, double kernel_ms[4]);
+int qmin_fire_profile(qmin_handle h, int iterations, double kernel_ms[4], int *fused);
+/* The FIRE strategy the autotuner chose on the first run (path 0 separate
+ * kernels with register cap `variant`, path 1 fused kernel with tile shape
+ * `variant` = tile_x x tile_y and `zc` z planes per block) and the measured
+ * ms per iteration of every candidate: ms[0..1] separate (cap 0, 1),
+ * ms[2 + 2*cfg + v] fused (v = 0/1 for the two z extents tried; -1 = not run).
+ * No reference counterpart (the reference's kernelTuner scans block sizes,
+ * src/utilities/kernelTuner.cpp:5-125). */
+int qmin_fire_tuning(qmin_handle h, int *path, int *variant, int *tile_x, int *tile_y, int *zc, double ms[10]);
 
 /* ---- energy without allocation ---- */
 /* Largest lattice (in sites) qmin_energy_noalloc accepts: the size of its

@@ -31,8 +31,10 @@ EXPORTED_SYMBOLS = [
     "qmin_create", "qmin_destroy", "qmin_set_stream", "qmin_last_error_string", "qmin_kernel_launches",
     "qmin_set_params", "qmin_set_objects", "qmin_set_state", "qmin_get_state", "qmin_n_active", "qmin_force",
     "qmin_energy", "qmin_fire_init", "qmin_fire_run", "qmin_adam_run", "qmin_nesterov_run", "qmin_lbfgs_run",
-    "qmin_host_random_nematic", "qmin_host_add_wall", "qmin_host_add_sphere",
+    "qmin_host_random_nematic", "qmin_host_add_wall", "qmin_host_add_sphere", "qmin_set_fire_kernel",
+    "qmin_fire_profile", "qmin_fire_tuning", "qmin_energy_noalloc",
 ]
+FIRE_SEPARATE, FIRE_FUSED, FIRE_AUTO = 0, 1, 2
 
 
 class QminError(RuntimeError):
@@ -93,6 +95,9 @@ def lib():
             "qmin_nesterov_run": [h, C.c_double, C.c_double, C.c_double, C.c_int, C.c_int, ip, dp],
             "qmin_lbfgs_run": [h, C.c_int, C.c_double, C.c_double, C.c_int, C.c_int, ip, dp],
             "qmin_host_random_nematic": [C.c_int, C.c_int, C.c_int, C.c_int, C.c_double, dp],
+            "qmin_set_fire_kernel": [h, C.c_int],
+            "qmin_fire_profile": [h, C.c_int, dp, ip],
+            "qmin_fire_tuning": [h, ip, ip, ip, ip, ip, dp],
             "qmin_host_add_wall": [C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_double, C.c_double, dp,
                                    ip, C.POINTER(Object), ip],
             "qmin_host_add_sphere": [C.c_int, C.c_int, C.c_int, dp, C.c_double, C.c_int, C.c_double, C.c_double, dp,
@@ -266,6 +271,26 @@ class Lattice:
         _check(lib().qmin_lbfgs_run(self._h, int(m), eta, force_cutoff, int(max_iterations), int(reset), C.byref(it),
                                     C.byref(fm)))
         return dict(iterations=it.value, forceMax=fm.value)
+
+    def set_fire_kernel(self, mode):
+        """FIRE_AUTO (default): autotuned; FIRE_FUSED: one tiled kernel per iteration; FIRE_SEPARATE."""
+        _check(lib().qmin_set_fire_kernel(self._h, int(mode)))
+
+    def fire_profile(self, iterations=20):
+        ms = (C.c_double * 4)()
+        fused = C.c_int()
+        _check(lib().qmin_fire_profile(self._h, int(iterations), ms, C.byref(fused)))
+        return list(ms), bool(fused.value)
+
+    def fire_tuning(self):
+        path, var, tx, ty, zc = C.c_int(), C.c_int(), C.c_int(), C.c_int(), C.c_int()
+        ms = (C.c_double * 10)()
+        _check(lib().qmin_fire_tuning(self._h, C.byref(path), C.byref(var), C.byref(tx), C.byref(ty), C.byref(zc),
+                                      ms))
+        names = ["separate", "separate_regcap"] + [f"fused_{a}x{b}_z{v}" for a, b in
+                                                    ((32, 8), (32, 16), (64, 8), (32, 4)) for v in (0, 1)]
+        return dict(path="fused" if path.value else "separate", variant=var.value, tile=(tx.value, ty.value),
+                    zc=zc.value, candidates_ms={n: m for n, m in zip(names, ms) if m >= 0})
 
     def launches(self):
         n = C.c_longlong()

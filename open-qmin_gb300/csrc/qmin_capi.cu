@@ -70,6 +70,14 @@ struct qmin_ctx {
     int graph_key[4] = {0, 0, 0, 0};
     double graph_args[4][4] = {};  // scalar kernel arguments baked into each graph
     int version = 1;  // bumped whenever kernel arguments change
+    // fused tiled FIRE path: second state buffer set (ping-pong) and the tile
+    // configuration chosen by the autotuner for the current parameters
+    void *Q2 = nullptr, *V2 = nullptr, *F2 = nullptr;
+    int fire_mode = QMIN_FIRE_AUTO;  // strategy requested by the caller
+    // strategy chosen by the autotuner for the current parameters
+    int path = -1;  // 0 separate kernels, 1 fused tiled kernel
+    int sep_cap = 0, fused_cfg = -1, fused_zc = 0, fused_nblocks = 0, tuned_version = 0, tuned_mode = -1;
+    double tune_ms[2 + kFusedConfigs * 2] = {};  // separate (cap 0, 1), fused (cfg, z extent)
 };
 
 static const int kChunk = 32;  // iterations per captured graph
@@ -116,8 +124,12 @@ template <class T> static Lat<T> make_lat(qmin_ctx *h)
     for (int k = 0; k < 5; ++k)
         for (int n = 0; n < QMIN_BULK_W; ++n) {
             double c = 0.0;
-            if (n < qmin_bulk_n[k])
-                for (int t = 0; t < 3; ++t) c += Lt[t] * (double)qmin_bulk_k[t][k][n] * 0.25;
+            if (n < qmin_bulk_n[k]) {
+                // k L / 4 per input; halved for derivative inputs (index >= 35), which
+                // the accessors deliver as twice the derivative
+                const double unit = qmin_bulk_in[k][n] >= 35 ? 0.125 : 0.25;
+                for (int t = 0; t < 3; ++t) c += Lt[t] * (double)qmin_bulk_k[t][k][n] * unit;
+            }
             L.cb[k * QMIN_BULK_W + n] = T(c);
         }
     return L;
@@ -128,7 +140,7 @@ static void free_ctx(qmin_ctx *h)
     for (int g = 0; g < 4; ++g)
         if (h->graph[g]) cudaGraphExecDestroy(h->graph[g]);
     void *bufs[] = {h->Q, h->V, h->F, h->D, h->types, h->objs, h->partials, h->stage, h->stage_t, h->fire, h->iter,
-                    h->out5, h->M, h->S, h->alt, h->lbp, h->lbs, h->lby};
+                    h->out5, h->M, h->S, h->alt, h->lbp, h->lbs, h->lby, h->Q2, h->V2, h->F2};
     for (void *b : bufs)
         if (b) cudaFree(b);
     if (h->fire_h) cudaFreeHost(h->fire_h);
@@ -189,7 +201,7 @@ int qmin_create(const qmin_lattice_desc *desc, qmin_handle *out)
     size_t plane = (size_t)h->P * h->esz;
     bool ok = cudaMalloc(&h->Q, 5 * plane) == cudaSuccess && cudaMalloc(&h->V, 5 * plane) == cudaSuccess &&
               cudaMalloc(&h->F, 5 * plane) == cudaSuccess && cudaMalloc(&h->types, (size_t)h->P) == cudaSuccess &&
-              cudaMalloc(&h->partials, sizeof(double) * 8 * (size_t)h->grid) == cudaSuccess &&
+              cudaMalloc(&h->partials, sizeof(double) * std::max(8 * (size_t)h->grid, (size_t)3 * kMaxFusedBlocks)) == cudaSuccess &&
               cudaMalloc(&h->fire, sizeof(FireDev)) == cudaSuccess &&
               cudaMalloc(&h->iter, sizeof(IterDev)) == cudaSuccess &&
               cudaMalloc(&h->out5, sizeof(double) * 8) == cudaSuccess &&
@@ -474,22 +486,163 @@ int qmin_fire_init(qmin_handle h, const qmin_fire_params *p)
     return QMIN_OK;
 }
 
+static int ensure_pingpong(qmin_ctx *h)
+{
+    if (h->Q2) return QMIN_OK;
+    const size_t bytes = 5 * (size_t)h->P * h->esz;
+    if (cudaMalloc(&h->Q2, bytes) != cudaSuccess || cudaMalloc(&h->V2, bytes) != cudaSuccess ||
+        cudaMalloc(&h->F2, bytes) != cudaSuccess) {
+        cudaGetLastError();
+        return fail(QMIN_ENOMEM, "fused FIRE: second state buffer allocation failed");
+    }
+    CK(cudaMemsetAsync(h->Q2, 0, bytes, h->stream));
+    CK(cudaMemsetAsync(h->V2, 0, bytes, h->stream));
+    CK(cudaMemsetAsync(h->F2, 0, bytes, h->stream));
+    return QMIN_OK;
+}
+
+// after an odd number of fused iterations the newest state sits in the second
+// buffer set: copy it back so the resident state is always the first set
+static int settle_pingpong(qmin_ctx *h, int executed)
+{
+    if (!(executed & 1)) return QMIN_OK;
+    const size_t bytes = 5 * (size_t)h->P * h->esz;
+    CK(cudaMemcpyAsync(h->Q, h->Q2, bytes, cudaMemcpyDeviceToDevice, h->stream));
+    CK(cudaMemcpyAsync(h->V, h->V2, bytes, cudaMemcpyDeviceToDevice, h->stream));
+    CK(cudaMemcpyAsync(h->F, h->F2, bytes, cudaMemcpyDeviceToDevice, h->stream));
+    return QMIN_OK;
+}
+
+// Autotuner for the FIRE iteration: times every candidate strategy on the live
+// lattice with CUDA events and keeps the fastest.  Candidates: the separate
+// kernels (predictor, derivative planes, force + kick) with and without a
+// register cap, and the fused tiled kernel for each tile shape and two z
+// extents.  The timing launches leave the state as it was: the fused kernel
+// writes only the second buffer set and the partials, the predictor is timed on
+// the second buffer set, and the velocities are restored after the force + kick
+// timings (whose forces equal the ones already resident).
+template <class T> static int tune_fire(qmin_ctx *h, const Lat<T> &L)
+{
+    if (h->path >= 0 && h->tuned_version == h->version && h->tuned_mode == h->fire_mode) return QMIN_OK;
+    int r = ensure_pingpong(h);
+    if (r) return r;
+    cudaEvent_t e0, e1;
+    CK(cudaEventCreate(&e0));
+    CK(cudaEventCreate(&e1));
+    auto time3 = [&](auto &&launch) -> float {
+        launch();  // warm-up (also sets kernel attributes)
+        cudaEventRecord(e0, h->stream);
+        for (int k = 0; k < 3; ++k) launch();
+        cudaEventRecord(e1, h->stream);
+        cudaEventSynchronize(e1);
+        float ms = 0;
+        cudaEventElapsedTime(&ms, e0, e1);
+        return ms / 3;
+    };
+    const int H = L.multi ? 2 : 1;
+    float best = 1e30f;
+    for (int k = 0; k < 2 + 2 * kFusedConfigs; ++k) h->tune_ms[k] = -1;
+    Lat<T> LB = L;
+    LB.Q = (T *)h->Q2;
+    LB.V = (T *)h->V2;
+    LB.F = (T *)h->F2;
+    if (h->fire_mode != QMIN_FIRE_SEPARATE) {
+        for (int cfg = 0; cfg < kFusedConfigs; ++cfg) {
+            int tx, ty;
+            fused_tile_shape(cfg, &tx, &ty);
+            const int ntiles = ((h->Lx + tx - 1) / tx) * ((h->Ly + ty - 1) / ty);
+            int zc0 = (int)std::ceil((double)h->Lz * ntiles / (152.0 * 4.0));
+            zc0 = std::max(zc0, 2 * H + 2);
+            for (int v = 0; v < 2; ++v) {
+                const int zc = std::min(h->Lz, zc0 << v);
+                const int nz = (h->Lz + zc - 1) / zc;
+                if ((long long)ntiles * nz > kMaxFusedBlocks) continue;
+                int nb = 0, ok = 1;
+                const float ms = time3([&]() {
+                    if (launch_fire_fused<T>(cfg, L, (T *)h->Q2, (T *)h->V2, (T *)h->F2, h->fire, h->partials, zc,
+                                             h->stream, &nb) < 0)
+                        ok = 0;
+                });
+                h->launches += 4;
+                if (!ok || cudaGetLastError() != cudaSuccess) continue;
+                h->tune_ms[2 + 2 * cfg + v] = ms;
+                if (ms < best) {
+                    best = ms;
+                    h->path = 1;
+                    h->fused_cfg = cfg;
+                    h->fused_zc = zc;
+                    h->fused_nblocks = nb;
+                }
+                if (zc >= h->Lz) break;
+            }
+        }
+    }
+    if (h->fire_mode != QMIN_FIRE_FUSED) {
+        const float t_pred = time3([&]() { launch_fire_pred<T>(LB, h->fire, h->stream); });
+        const float t_der = L.multi ? time3([&]() { launch_derivs<T>(L, h->stream); }) : 0.f;
+        const size_t bytes = 5 * (size_t)h->P * h->esz;
+        CK(cudaMemcpyAsync(h->V2, h->V, bytes, cudaMemcpyDeviceToDevice, h->stream));
+        for (int cap = 0; cap < 2; ++cap) {
+            const float t_fk =
+                time3([&]() { launch_force_kick_only<T>(L, h->fire, h->partials, h->grid, h->stream, cap); });
+            const float ms = t_pred + t_der + t_fk;
+            h->tune_ms[cap] = ms;
+            if (ms < best) {
+                best = ms;
+                h->path = 0;
+                h->sep_cap = cap;
+            }
+        }
+        CK(cudaMemcpyAsync(h->V, h->V2, bytes, cudaMemcpyDeviceToDevice, h->stream));
+        h->launches += 4 * (2 + (L.multi ? 1 : 0) + 2);
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    CK(cudaGetLastError());
+    if (h->path < 0) return fail(QMIN_ECUDA, "FIRE autotuner: no strategy could be launched");
+    h->tuned_version = h->version;
+    h->tuned_mode = h->fire_mode;
+    return QMIN_OK;
+}
+
 template <class T> static int fire_impl(qmin_ctx *h, int max_iterations)
 {
     Lat<T> L = make_lat<T>(h);
+    const int it0 = h->fire_h->iterations;
     // minimize(): forces at the current Q first (energyMinimizerFIRE.cpp:157)
     h->launches += launch_force<T>(L, h->grid, h->stream);
-    const double args[4] = {0, 0, 0, 0};
-    int r = capture_chunk(h, 0, args, [&]() {
-        int n = launch_fire_pred<T>(L, h->fire, h->stream);
-        n += launch_force_kick<T>(L, h->fire, h->partials, h->grid, h->stream);
-        n += launch_fire_control(h->fire, h->partials, h->grid, h->stream);
+    int r = tune_fire<T>(h, L);
+    if (r) return r;
+    Lat<T> LB = L;  // the second buffer set as input
+    LB.Q = (T *)h->Q2;
+    LB.V = (T *)h->V2;
+    LB.F = (T *)h->F2;
+    int parity = 0;
+    const double args[4] = {(double)h->path, (double)(h->path ? h->fused_cfg : h->sep_cap), (double)h->fused_zc, 0};
+    r = capture_chunk(h, 0, args, [&]() {
+        int n;
+        if (h->path == 0) {
+            n = launch_fire_pred<T>(L, h->fire, h->stream);
+            n += launch_force_kick<T>(L, h->fire, h->partials, h->grid, h->stream, h->sep_cap);
+            n += launch_fire_control(h->fire, h->partials, h->grid, h->stream);
+        } else {
+            int nb = 0;
+            if (parity == 0)
+                n = launch_fire_fused<T>(h->fused_cfg, L, (T *)h->Q2, (T *)h->V2, (T *)h->F2, h->fire, h->partials,
+                                         h->fused_zc, h->stream, &nb);
+            else
+                n = launch_fire_fused<T>(h->fused_cfg, LB, (T *)h->Q, (T *)h->V, (T *)h->F, h->fire, h->partials,
+                                         h->fused_zc, h->stream, &nb);
+            parity ^= 1;
+            n += launch_fire_control(h->fire, h->partials, nb, h->stream);
+        }
         return n;
     });
     if (r) return r;
-    int remaining = std::max(max_iterations - h->fire_h->iterations, 1);
+    int remaining = std::max(max_iterations - it0, 1);
     r = run_chunks(h, 0, h->fire, h->fire_h, (remaining + kChunk - 1) / kChunk + 1);
     if (r) return r;
+    if (h->path == 1 && (r = settle_pingpong(h, h->fire_h->iterations - it0))) return r;
     h->launches += launch_fire_finish<T>(L, h->fire, h->stream);
     CK(cudaGetLastError());
     CK(cudaMemcpyAsync(h->fire_h, h->fire, sizeof(FireDev), cudaMemcpyDeviceToHost, h->stream));
@@ -698,21 +851,34 @@ int qmin_lbfgs_run(qmin_handle h, int m, double eta, double force_cutoff, int ma
 template <class T> static int fire_profile_impl(qmin_ctx *h, int iterations, double *ms)
 {
     Lat<T> L = make_lat<T>(h);
+    int r = tune_fire<T>(h, L);
+    if (r) return r;
     cudaEvent_t ev[5];
     for (auto &e : ev) CK(cudaEventCreate(&e));
     double acc[4] = {0, 0, 0, 0};
+    const bool fused = h->path == 1;
+    Lat<T> LB = L;
+    LB.Q = (T *)h->Q2;
+    LB.V = (T *)h->V2;
+    LB.F = (T *)h->F2;
     for (int it = 0; it < iterations; ++it) {
         CK(cudaEventRecord(ev[0], h->stream));
-        h->launches += launch_fire_pred<T>(L, h->fire, h->stream);
+        if (!fused) h->launches += launch_fire_pred<T>(L, h->fire, h->stream);
         CK(cudaEventRecord(ev[1], h->stream));
-        if (L.multi) h->launches += launch_derivs<T>(L, h->stream);
+        if (!fused && L.multi) h->launches += launch_derivs<T>(L, h->stream);
         CK(cudaEventRecord(ev[2], h->stream));
-        Lat<T> L1 = L;
-        L1.multi = L.multi;
-        // force + kick without re-running the derivative kernel
-        h->launches += launch_force_kick_only<T>(L1, h->fire, h->partials, h->grid, h->stream);
+        int nparts = h->grid;
+        if (!fused) {
+            h->launches += launch_force_kick_only<T>(L, h->fire, h->partials, h->grid, h->stream, h->sep_cap);
+        } else if ((it & 1) == 0) {
+            h->launches += launch_fire_fused<T>(h->fused_cfg, L, (T *)h->Q2, (T *)h->V2, (T *)h->F2, h->fire,
+                                                h->partials, h->fused_zc, h->stream, &nparts);
+        } else {
+            h->launches += launch_fire_fused<T>(h->fused_cfg, LB, (T *)h->Q, (T *)h->V, (T *)h->F, h->fire,
+                                                h->partials, h->fused_zc, h->stream, &nparts);
+        }
         CK(cudaEventRecord(ev[3], h->stream));
-        h->launches += launch_fire_control(h->fire, h->partials, h->grid, h->stream);
+        h->launches += launch_fire_control(h->fire, h->partials, nparts, h->stream);
         CK(cudaEventRecord(ev[4], h->stream));
         CK(cudaEventSynchronize(ev[4]));
         for (int k = 0; k < 4; ++k) {
@@ -722,6 +888,7 @@ template <class T> static int fire_profile_impl(qmin_ctx *h, int iterations, dou
         }
     }
     for (int k = 0; k < 4; ++k) ms[k] = iterations > 0 ? acc[k] / iterations : 0.0;
+    if (fused && (r = settle_pingpong(h, iterations))) return r;
     h->launches += launch_fire_finish<T>(L, h->fire, h->stream);
     for (auto &e : ev) cudaEventDestroy(e);
     CK(cudaMemcpyAsync(h->fire_h, h->fire, sizeof(FireDev), cudaMemcpyDeviceToHost, h->stream));
@@ -729,7 +896,7 @@ template <class T> static int fire_profile_impl(qmin_ctx *h, int iterations, dou
     return QMIN_OK;
 }
 
-int qmin_fire_profile(qmin_handle h, int iterations, double kernel_ms[4])
+int qmin_fire_profile(qmin_handle h, int iterations, double kernel_ms[4], int *fused)
 {
     int r = ready(h, "qmin_fire_profile");
     if (r) return r;
@@ -743,6 +910,34 @@ int qmin_fire_profile(qmin_handle h, int iterations, double kernel_ms[4])
     f->status = 0;
     f->nTotal = h->nTotal;
     CK(cudaMemcpyAsync(h->fire, f, sizeof(FireDev), cudaMemcpyHostToDevice, h->stream));
-    return h->prec == QMIN_FP64 ? fire_profile_impl<double>(h, iterations, kernel_ms)
-                                : fire_profile_impl<float>(h, iterations, kernel_ms);
+    r = h->prec == QMIN_FP64 ? fire_profile_impl<double>(h, iterations, kernel_ms)
+                             : fire_profile_impl<float>(h, iterations, kernel_ms);
+    if (fused) *fused = h->path == 1;
+    return r;
+}
+
+int qmin_set_fire_kernel(qmin_handle h, int mode)
+{
+    if (!h) return fail(QMIN_EINVAL, "qmin_set_fire_kernel: null handle");
+    if (mode != QMIN_FIRE_SEPARATE && mode != QMIN_FIRE_FUSED && mode != QMIN_FIRE_AUTO)
+        return fail(QMIN_EINVAL, "qmin_set_fire_kernel: mode must be QMIN_FIRE_SEPARATE, _FUSED or _AUTO");
+    if (h->fire_mode != mode) invalidate_graphs(h);
+    h->fire_mode = mode;
+    return QMIN_OK;
+}
+
+int qmin_fire_tuning(qmin_handle h, int *path, int *variant, int *tile_x, int *tile_y, int *zc, double *ms)
+{
+    if (!h) return fail(QMIN_EINVAL, "qmin_fire_tuning: null handle");
+    if (h->path < 0) return fail(QMIN_ESTATE, "qmin_fire_tuning: no FIRE run has been tuned yet");
+    if (path) *path = h->path;
+    if (variant) *variant = h->path ? h->fused_cfg : h->sep_cap;
+    int tx = 0, ty = 0;
+    if (h->path == 1) fused_tile_shape(h->fused_cfg, &tx, &ty);
+    if (tile_x) *tile_x = tx;
+    if (tile_y) *tile_y = ty;
+    if (zc) *zc = h->path == 1 ? h->fused_zc : 0;
+    if (ms)
+        for (int k = 0; k < 2 + 2 * kFusedConfigs; ++k) ms[k] = h->tune_ms[k];
+    return QMIN_OK;
 }

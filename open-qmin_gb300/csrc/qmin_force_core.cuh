@@ -1,0 +1,269 @@
+// The per-site Landau-de Gennes force, written once against an accessor so
+// that the global-memory kernels and the shared-memory tile kernels share one
+// implementation of the force semantics.
+//
+// An accessor A provides, for the site being updated:
+//   int tn(s)          type of neighbour s (0..5 = x-, x+, y-, y+, z-, z+)
+//   T   q(k)           own Q component k
+//   T   nq(s, k)       neighbour s's Q component k
+//   T   dn(s, d)       TWICE neighbour s's first derivative d = 5*axis + component
+//                      (landauDeGennesLC::computeFirstDerivatives rules).  Central
+//                      differences are then plain differences; the exact factor 1/2
+//                      lives in the coefficients, so results are bit-identical.
+#pragma once
+#include "qmin_device.cuh"
+#include "qmin_distortion_tables.h"
+#include "qmin_internal.h"
+
+namespace qmin {
+
+// sparse multi-constant forms (term, boundary case, component) -> (input, k)
+static __device__ const uint16_t g_dt_offset[3 * 64 * 5 + 1] = QMIN_DT_OFFSET_INIT;
+static __device__ const uint8_t g_dt_input[QMIN_DT_NPAIRS] = QMIN_DT_INPUT_INIT;
+static __device__ const int8_t g_dt_k[QMIN_DT_NPAIRS] = QMIN_DT_K_INIT;
+
+template <class T>
+__device__ __forceinline__ T ld(const T *p)
+{
+    return __ldg(p);
+}
+
+struct Nb {
+    int n[6];  // x-, x+, y-, y+, z-, z+ (cubicLattice::getNeighbors, cubicLattice.cpp:179-244)
+};
+
+template <class T>
+__device__ __forceinline__ Nb neighbours(const Lat<T> &L, int i)
+{
+    const int x = i % L.Lx;
+    const int r = i / L.Lx;
+    const int y = r % L.Ly;
+    const int z = r / L.Ly;
+    const int sx = L.Lx, sy = L.Lx * L.Ly;
+    Nb b;
+    b.n[0] = x == 0 ? i + (L.Lx - 1) : i - 1;
+    b.n[1] = x == L.Lx - 1 ? i - (L.Lx - 1) : i + 1;
+    b.n[2] = y == 0 ? i + (L.Ly - 1) * sx : i - sx;
+    b.n[3] = y == L.Ly - 1 ? i - (L.Ly - 1) * sx : i + sx;
+    b.n[4] = z == 0 ? i + (L.Lz - 1) * sy : i - sy;
+    b.n[5] = z == L.Lz - 1 ? i - (L.Lz - 1) * sy : i + sy;
+    return b;
+}
+
+// block-wide sum of NV doubles over a block of NT threads; result valid in thread 0
+template <int NV, int NT = kBlock>
+__device__ __forceinline__ void block_sum(double (&v)[NV])
+{
+    __shared__ double sh[NV][NT / 32];
+#pragma unroll
+    for (int k = 0; k < NV; ++k)
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v[k] += __shfl_down_sync(0xffffffffu, v[k], o);
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    if (lane == 0)
+#pragma unroll
+        for (int k = 0; k < NV; ++k) sh[k][w] = v[k];
+    __syncthreads();
+    if (w == 0) {
+#pragma unroll
+        for (int k = 0; k < NV; ++k) {
+            v[k] = lane < NT / 32 ? sh[k][lane] : 0.0;
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) v[k] += __shfl_down_sync(0xffffffffu, v[k], o);
+        }
+    }
+    __syncthreads();
+}
+
+// deterministic sum of partials[NV * nparts] by one block; result in thread 0
+template <int NV>
+__device__ __forceinline__ void sum_partials(const double *partials, int nparts, double (&v)[NV])
+{
+#pragma unroll
+    for (int k = 0; k < NV; ++k) v[k] = 0.0;
+    for (int b = threadIdx.x; b < nparts; b += kBlock)
+#pragma unroll
+        for (int k = 0; k < NV; ++k) v[k] += partials[NV * b + k];
+    block_sum<NV>(v);
+}
+
+// first derivative of one component along one axis at a site of type t with
+// down/centre/up values and the down/up neighbour types
+// (landauDeGennesLCOtherForces.cpp:50-141): central differences; at type < 0
+// sites one-sided next to objects, the "up neighbour is an object" branch first
+template <class T>
+__device__ __forceinline__ T deriv_rule(int t, int td, int tu, T qd, T q, T qu)
+{
+    if (t > 0) return T(0);
+    if (t == 0 || (td <= 0 && tu <= 0)) return T(0.5) * (qu - qd);
+    if (tu > 0) return q - qd;
+    return qu - q;
+}
+
+// the same rule returning twice the derivative (exact: scaling by 2 is exact)
+template <class T>
+__device__ __forceinline__ T deriv2_rule(int t, int td, int tu, T qd, T q, T qu)
+{
+    if (t > 0) return T(0);
+    if (t == 0 || (td <= 0 && tu <= 0)) return qu - qd;
+    if (tu > 0) return T(2) * (q - qd);
+    return T(2) * (qu - q);
+}
+
+// One site's force, CPU-path semantics by default (multirankSimulation.cpp:462-466):
+//   type 0:  F = M( M(-phase - distortion) - fields )
+//   type <0: F = M(-phase - distortion + anchoring - fields)
+// metric_mode 1 applies M once everywhere (the reference GPU branch).
+template <class T, class A>
+__device__ __forceinline__ void site_force_core(const Lat<T> &L, const A &acc, int t, T *f)
+{
+    if (t > 0) {
+#pragma unroll
+        for (int k = 0; k < 5; ++k) f[k] = T(0);
+        return;
+    }
+    T q[5], nq[6][5];
+#pragma unroll
+    for (int k = 0; k < 5; ++k) q[k] = acc.q(k);
+#pragma unroll
+    for (int s = 0; s < 6; ++s)
+#pragma unroll
+        for (int k = 0; k < 5; ++k) nq[s][k] = acc.nq(s, k);
+
+    T force[5];
+    phase_force(L.a, L.b, L.c, q, force);
+
+    const bool boundary = (t == -1);  // type -2 uses the bulk forms (DT:241-279)
+    int mask = 0;                     // which neighbours are objects
+    if (t < 0) {
+#pragma unroll
+        for (int s = 0; s < 6; ++s) mask |= (acc.tn(s) > 0) << s;
+    }
+
+    T sp[5] = {T(0), T(0), T(0), T(0), T(0)};
+    if (!L.multi || L.L1 != T(0)) {
+        // lcForce::bulkL1Force / boundaryL1Force (lcForces.h:26-63)
+        T s1[5];
+        if (!boundary) {
+#pragma unroll
+            for (int k = 0; k < 5; ++k)
+                s1[k] = L.L1 * (T(6) * q[k] - nq[0][k] - nq[1][k] - nq[2][k] - nq[3][k] - nq[4][k] - nq[5][k]);
+        } else {
+#pragma unroll
+            for (int k = 0; k < 5; ++k) s1[k] = T(0);
+#pragma unroll
+            for (int ax = 0; ax < 3; ++ax) {
+                if (mask & (1 << (2 * ax)))
+#pragma unroll
+                    for (int k = 0; k < 5; ++k) s1[k] -= (nq[2 * ax + 1][k] - q[k]);
+                if (mask & (1 << (2 * ax + 1)))
+#pragma unroll
+                    for (int k = 0; k < 5; ++k) s1[k] -= (nq[2 * ax][k] - q[k]);
+            }
+#pragma unroll
+            for (int k = 0; k < 5; ++k) s1[k] = s1[k] * L.L1;
+        }
+        l1_cross(s1);
+#pragma unroll
+        for (int k = 0; k < 5; ++k) sp[k] += s1[k];
+    }
+    if (L.multi) {
+        if (!boundary) {
+            // bulk L2/L3/L4 forms, straight-line over their union pattern
+            T s2[5];
+#define QIN(c) q[c]
+#define QN(slot, c) nq[slot][c]
+#define DN(slot, d) acc.dn(slot, d)
+            QMIN_BULK_FORMS(L.cb, s2);
+#undef QIN
+#undef QN
+#undef DN
+#pragma unroll
+            for (int k = 0; k < 5; ++k) sp[k] += s2[k];
+        } else {
+            // boundary forms: lcForce::getBoundaryCase (lcForces.h:13-25), down wins
+            int xx = 0, yy = 0, zz = 0;
+            if (mask & 2) xx = 1;
+            if (mask & 1) xx = 2;
+            if (mask & 8) yy = 1;
+            if (mask & 4) yy = 2;
+            if (mask & 32) zz = 1;
+            if (mask & 16) zz = 2;
+            const int bcase = xx + 4 * yy + 16 * zz;
+            const T Lt[3] = {L.L2, L.L3, L.L4};
+            for (int term = 0; term < 3; ++term) {
+                if (Lt[term] == T(0)) continue;
+                for (int k = 0; k < 5; ++k) {
+                    const int o0 = g_dt_offset[(term * 64 + bcase) * 5 + k];
+                    const int o1 = g_dt_offset[(term * 64 + bcase) * 5 + k + 1];
+                    T acc_k = T(0);
+                    for (int e = o0; e < o1; ++e) {
+                        const int j = g_dt_input[e];
+                        T x;
+                        if (j < 5) x = acc.q(j);
+                        else if (j < 35) x = acc.nq((j - 5) / 5, (j - 5) % 5);
+                        else x = T(0.5) * acc.dn((j - 35) / 15, (j - 35) % 15);
+                        acc_k += T(g_dt_k[e]) * x;
+                    }
+                    sp[k] += (T(0.5) * Lt[term]) * (acc_k / T(2));
+                }
+            }
+        }
+    }
+#pragma unroll
+    for (int k = 0; k < 5; ++k) f[k] = force[k] - sp[k];
+
+    if (L.metric_mode == 0 && t == 0) metric(f);
+    if (t < 0 && mask) {
+        // landauDeGennesLC::computeBoundaryForcesCPU (landauDeGennesLCOtherForces.cpp:314-373)
+#pragma unroll
+        for (int s = 0; s < 6; ++s) {
+            if (mask & (1 << s)) {
+                const ObjDev<T> o = L.objs[acc.tn(s) - 1];
+                anchoring_force_add(o.kind, o.W, o.S0, q, nq[s], f);
+            }
+        }
+    }
+    if (L.efield)
+#pragma unroll
+        for (int k = 0; k < 5; ++k) f[k] -= L.fE[k];
+    if (L.hfield)
+#pragma unroll
+        for (int k = 0; k < 5; ++k) f[k] -= L.fH[k];
+    metric(f);
+}
+
+// accessor over the global SoA planes; neighbour derivatives from the D planes.
+// It copies the few pointers it needs: holding a reference to the kernel's
+// parameter block would force that block into local memory.
+template <class T> struct GlobalAcc {
+    const T *Q;
+    const T *D;
+    const int8_t *types;
+    long long P;
+    int i;
+    Nb b;
+    __device__ __forceinline__ GlobalAcc(const Lat<T> &L, int i_)
+        : Q(L.Q), D(L.D), types(L.types), P(L.P), i(i_), b(neighbours(L, i_))
+    {
+    }
+    __device__ __forceinline__ int tn(int s) const { return types[b.n[s]]; }
+    __device__ __forceinline__ T q(int k) const { return ld(Q + (long long)k * P + i); }
+    __device__ __forceinline__ T nq(int s, int k) const { return ld(Q + (long long)k * P + b.n[s]); }
+    __device__ __forceinline__ T dn(int s, int d) const { return ld(D + (long long)d * P + b.n[s]); }
+};
+
+template <class T>
+__device__ __forceinline__ void site_force(const Lat<T> &L, int i, T *f)
+{
+    const int t = L.types[i];
+    if (t > 0) {
+#pragma unroll
+        for (int k = 0; k < 5; ++k) f[k] = T(0);
+        return;
+    }
+    GlobalAcc<T> acc(L, i);
+    site_force_core(L, acc, t, f);
+}
+
+}  // namespace qmin

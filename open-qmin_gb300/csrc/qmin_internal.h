@@ -57,9 +57,10 @@ extern thread_local std::string g_last_error;
 template <class T> int launch_derivs(const Lat<T> &L, cudaStream_t s);
 template <class T> int launch_force(const Lat<T> &L, int grid, cudaStream_t s);
 template <class T> int launch_fire_pred(const Lat<T> &L, FireDev *fd, cudaStream_t s);
-template <class T> int launch_force_kick(const Lat<T> &L, FireDev *fd, double *partials, int grid, cudaStream_t s);
 template <class T>
-int launch_force_kick_only(const Lat<T> &L, FireDev *fd, double *partials, int grid, cudaStream_t s);
+int launch_force_kick(const Lat<T> &L, FireDev *fd, double *partials, int grid, cudaStream_t s, int cap);
+template <class T>
+int launch_force_kick_only(const Lat<T> &L, FireDev *fd, double *partials, int grid, cudaStream_t s, int cap);
 int launch_fire_control(FireDev *fd, const double *partials, int nparts, cudaStream_t s);
 template <class T> int launch_fire_finish(const Lat<T> &L, FireDev *fd, cudaStream_t s);
 template <class T>
@@ -85,5 +86,14 @@ int launch_lbfgs_iteration(const Lat<T> &L, T *p, T *sbase, T *ybase, IterDev *i
 template <class T> int launch_lbfgs_first(const Lat<T> &L, T *p, IterDev *it, cudaStream_t s);
 
 int reduction_grid(int N);
+
+// fused tiled FIRE iteration (qmin_fused.cu): tile configuration cfg in
+// [0, kFusedConfigs), z planes per block zc; returns launches or -1
+constexpr int kFusedConfigs = 4;
+constexpr int kMaxFusedBlocks = 16384;
+template <class T>
+int launch_fire_fused(int cfg, const Lat<T> &L, T *Qn, T *Vn, T *Fn, FireDev *fd, double *partials, int zc,
+                      cudaStream_t s, int *nblocks);
+int fused_tile_shape(int cfg, int *tx, int *ty);
 
 }  // namespace qmin

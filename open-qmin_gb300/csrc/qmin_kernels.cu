@@ -7,88 +7,15 @@
 // fixed order.
 #include <math.h>
 
-#include "qmin_device.cuh"
-#include "qmin_distortion_tables.h"
-#include "qmin_internal.h"
+#include "qmin_force_core.cuh"
 
 namespace qmin {
-
-// sparse multi-constant forms (term, boundary case, component) -> (input, k)
-__device__ const uint16_t g_dt_offset[3 * 64 * 5 + 1] = QMIN_DT_OFFSET_INIT;
-__device__ const uint8_t g_dt_input[QMIN_DT_NPAIRS] = QMIN_DT_INPUT_INIT;
-__device__ const int8_t g_dt_k[QMIN_DT_NPAIRS] = QMIN_DT_K_INIT;
 
 int reduction_grid(int N)
 {
     int g = (N + kBlock - 1) / kBlock;
     const int cap = 152 * 8;  // 8 resident blocks per SM on the 152 SMs of a GB300
     return g < cap ? (g > 0 ? g : 1) : cap;
-}
-
-// ------------------------------------------------------------------ helpers
-struct Nb {
-    int n[6];  // x-, x+, y-, y+, z-, z+ (cubicLattice::getNeighbors, cubicLattice.cpp:179-244)
-};
-
-template <class T>
-__device__ __forceinline__ Nb neighbours(const Lat<T> &L, int i)
-{
-    const int x = i % L.Lx;
-    const int r = i / L.Lx;
-    const int y = r % L.Ly;
-    const int z = r / L.Ly;
-    const int sx = L.Lx, sy = L.Lx * L.Ly;
-    Nb b;
-    b.n[0] = x == 0 ? i + (L.Lx - 1) : i - 1;
-    b.n[1] = x == L.Lx - 1 ? i - (L.Lx - 1) : i + 1;
-    b.n[2] = y == 0 ? i + (L.Ly - 1) * sx : i - sx;
-    b.n[3] = y == L.Ly - 1 ? i - (L.Ly - 1) * sx : i + sx;
-    b.n[4] = z == 0 ? i + (L.Lz - 1) * sy : i - sy;
-    b.n[5] = z == L.Lz - 1 ? i - (L.Lz - 1) * sy : i + sy;
-    return b;
-}
-
-template <class T>
-__device__ __forceinline__ T ld(const T *p)
-{
-    return __ldg(p);
-}
-
-// block-wide sum of NV doubles; result valid in thread 0
-template <int NV>
-__device__ __forceinline__ void block_sum(double (&v)[NV])
-{
-    __shared__ double sh[NV][kBlock / 32];
-#pragma unroll
-    for (int k = 0; k < NV; ++k)
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) v[k] += __shfl_down_sync(0xffffffffu, v[k], o);
-    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    if (lane == 0)
-#pragma unroll
-        for (int k = 0; k < NV; ++k) sh[k][w] = v[k];
-    __syncthreads();
-    if (w == 0) {
-#pragma unroll
-        for (int k = 0; k < NV; ++k) {
-            v[k] = lane < kBlock / 32 ? sh[k][lane] : 0.0;
-#pragma unroll
-            for (int o = 16; o > 0; o >>= 1) v[k] += __shfl_down_sync(0xffffffffu, v[k], o);
-        }
-    }
-    __syncthreads();
-}
-
-// deterministic sum of partials[NV * nparts] by one block; result in thread 0
-template <int NV>
-__device__ __forceinline__ void sum_partials(const double *partials, int nparts, double (&v)[NV])
-{
-#pragma unroll
-    for (int k = 0; k < NV; ++k) v[k] = 0.0;
-    for (int b = threadIdx.x; b < nparts; b += kBlock)
-#pragma unroll
-        for (int k = 0; k < NV; ++k) v[k] += partials[NV * b + k];
-    block_sum<NV>(v);
 }
 
 // --------------------------------------------------------- first derivatives
@@ -102,23 +29,18 @@ __device__ __forceinline__ void site_derivs(const Lat<T> &L, int i, int t, const
 #pragma unroll
     for (int ax = 0; ax < 3; ++ax) {
         const int dn = b.n[2 * ax], up = b.n[2 * ax + 1];
-        int mode = 0;  // 0 central, 1 backward (up is an object), 2 forward
-        if (t < 0) {
-            const int td = L.types[dn], tu = L.types[up];
-            if (!(td <= 0 && tu <= 0)) mode = tu > 0 ? 1 : 2;
-        }
+        const int td = t < 0 ? L.types[dn] : 0, tu = t < 0 ? L.types[up] : 0;
 #pragma unroll
-        for (int k = 0; k < 5; ++k) {
-            const T qd = ld(L.Q + k * P + dn), qu = ld(L.Q + k * P + up);
-            const T q = ld(L.Q + k * P + i);
-            d[5 * ax + k] = mode == 0 ? T(0.5) * (qu - qd) : (mode == 1 ? q - qd : qu - q);
-        }
+        for (int k = 0; k < 5; ++k)
+            d[5 * ax + k] = deriv_rule(t, td, tu, ld(L.Q + k * P + dn), ld(L.Q + k * P + i), ld(L.Q + k * P + up));
     }
 }
 
+// derivative planes for the force: twice the first derivatives (see qmin_force_core.cuh)
 template <class T>
 __global__ void __launch_bounds__(kBlock) k_derivs(Lat<T> L)
 {
+    const long long P = L.P;
     for (int i = blockIdx.x * kBlock + threadIdx.x; i < L.N; i += gridDim.x * kBlock) {
         const int t = L.types[i];
         T d[15];
@@ -127,7 +49,15 @@ __global__ void __launch_bounds__(kBlock) k_derivs(Lat<T> L)
             for (int k = 0; k < 15; ++k) d[k] = T(0);
         } else {
             const Nb b = neighbours(L, i);
-            site_derivs(L, i, t, b, d);
+#pragma unroll
+            for (int ax = 0; ax < 3; ++ax) {
+                const int dn = b.n[2 * ax], up = b.n[2 * ax + 1];
+                const int td = t < 0 ? L.types[dn] : 0, tu = t < 0 ? L.types[up] : 0;
+#pragma unroll
+                for (int k = 0; k < 5; ++k)
+                    d[5 * ax + k] =
+                        deriv2_rule(t, td, tu, ld(L.Q + k * P + dn), ld(L.Q + k * P + i), ld(L.Q + k * P + up));
+            }
         }
 #pragma unroll
         for (int k = 0; k < 15; ++k) L.D[k * L.P + i] = d[k];
@@ -135,132 +65,6 @@ __global__ void __launch_bounds__(kBlock) k_derivs(Lat<T> L)
 }
 
 // ------------------------------------------------------------------- force
-// One site's force, CPU-path semantics by default (multirankSimulation.cpp:462-466):
-//   type 0:  F = M( M(-phase - distortion) - fields )
-//   type <0: F = M(-phase - distortion + anchoring - fields)
-// metric_mode 1 applies M once everywhere (the reference GPU branch).
-template <class T>
-__device__ __forceinline__ void site_force(const Lat<T> &L, int i, T *f)
-{
-    const int t = L.types[i];
-    if (t > 0) {
-#pragma unroll
-        for (int k = 0; k < 5; ++k) f[k] = T(0);
-        return;
-    }
-    const long long P = L.P;
-    const Nb b = neighbours(L, i);
-    T q[5], nq[6][5];
-#pragma unroll
-    for (int k = 0; k < 5; ++k) q[k] = ld(L.Q + k * P + i);
-#pragma unroll
-    for (int s = 0; s < 6; ++s)
-#pragma unroll
-        for (int k = 0; k < 5; ++k) nq[s][k] = ld(L.Q + k * P + b.n[s]);
-
-    T force[5];
-    phase_force(L.a, L.b, L.c, q, force);
-
-    const bool boundary = (t == -1);  // type -2 uses the bulk forms (DT:241-279)
-    int mask = 0;                     // which neighbours are objects
-    if (t < 0) {
-#pragma unroll
-        for (int s = 0; s < 6; ++s) mask |= (L.types[b.n[s]] > 0) << s;
-    }
-
-    T sp[5] = {T(0), T(0), T(0), T(0), T(0)};
-    if (!L.multi || L.L1 != T(0)) {
-        // lcForce::bulkL1Force / boundaryL1Force (lcForces.h:26-63)
-        T s1[5];
-        if (!boundary) {
-#pragma unroll
-            for (int k = 0; k < 5; ++k)
-                s1[k] = L.L1 * (T(6) * q[k] - nq[0][k] - nq[1][k] - nq[2][k] - nq[3][k] - nq[4][k] - nq[5][k]);
-        } else {
-#pragma unroll
-            for (int k = 0; k < 5; ++k) s1[k] = T(0);
-#pragma unroll
-            for (int ax = 0; ax < 3; ++ax) {
-                if (mask & (1 << (2 * ax)))
-#pragma unroll
-                    for (int k = 0; k < 5; ++k) s1[k] -= (nq[2 * ax + 1][k] - q[k]);
-                if (mask & (1 << (2 * ax + 1)))
-#pragma unroll
-                    for (int k = 0; k < 5; ++k) s1[k] -= (nq[2 * ax][k] - q[k]);
-            }
-#pragma unroll
-            for (int k = 0; k < 5; ++k) s1[k] = s1[k] * L.L1;
-        }
-        l1_cross(s1);
-#pragma unroll
-        for (int k = 0; k < 5; ++k) sp[k] += s1[k];
-    }
-    if (L.multi) {
-        if (!boundary) {
-            // bulk L2/L3/L4 forms, straight-line over their union pattern
-            T s2[5];
-#define QIN(c) q[c]
-#define QN(slot, c) nq[slot][c]
-#define DN(slot, d) ld(L.D + (long long)(d) * P + b.n[slot])
-            QMIN_BULK_FORMS(L.cb, s2);
-#undef QIN
-#undef QN
-#undef DN
-#pragma unroll
-            for (int k = 0; k < 5; ++k) sp[k] += s2[k];
-        } else {
-            // boundary forms: lcForce::getBoundaryCase (lcForces.h:13-25), down wins
-            int xx = 0, yy = 0, zz = 0;
-            if (mask & 2) xx = 1;
-            if (mask & 1) xx = 2;
-            if (mask & 8) yy = 1;
-            if (mask & 4) yy = 2;
-            if (mask & 32) zz = 1;
-            if (mask & 16) zz = 2;
-            const int bcase = xx + 4 * yy + 16 * zz;
-            const T Lt[3] = {L.L2, L.L3, L.L4};
-            for (int term = 0; term < 3; ++term) {
-                if (Lt[term] == T(0)) continue;
-                for (int k = 0; k < 5; ++k) {
-                    const int o0 = g_dt_offset[(term * 64 + bcase) * 5 + k];
-                    const int o1 = g_dt_offset[(term * 64 + bcase) * 5 + k + 1];
-                    T acc = T(0);
-                    for (int e = o0; e < o1; ++e) {
-                        const int j = g_dt_input[e];
-                        T x;
-                        if (j < 5) x = q[j];
-                        else if (j < 35) x = ld(L.Q + (long long)((j - 5) % 5) * P + b.n[(j - 5) / 5]);
-                        else x = ld(L.D + (long long)((j - 35) % 15) * P + b.n[(j - 35) / 15]);
-                        acc += T(g_dt_k[e]) * x;
-                    }
-                    sp[k] += (T(0.5) * Lt[term]) * (acc / T(2));
-                }
-            }
-        }
-    }
-#pragma unroll
-    for (int k = 0; k < 5; ++k) f[k] = force[k] - sp[k];
-
-    if (L.metric_mode == 0 && t == 0) metric(f);
-    if (t < 0 && mask) {
-        // landauDeGennesLC::computeBoundaryForcesCPU (landauDeGennesLCOtherForces.cpp:314-373)
-#pragma unroll
-        for (int s = 0; s < 6; ++s) {
-            if (mask & (1 << s)) {
-                const ObjDev<T> o = L.objs[L.types[b.n[s]] - 1];
-                anchoring_force_add(o.kind, o.W, o.S0, q, nq[s], f);
-            }
-        }
-    }
-    if (L.efield)
-#pragma unroll
-        for (int k = 0; k < 5; ++k) f[k] -= L.fE[k];
-    if (L.hfield)
-#pragma unroll
-        for (int k = 0; k < 5; ++k) f[k] -= L.fH[k];
-    metric(f);
-}
-
 template <class T>
 __global__ void __launch_bounds__(kBlock) k_force(Lat<T> L)
 {
@@ -297,8 +101,10 @@ __global__ void __launch_bounds__(kBlock) k_fire_pred(Lat<T> L, const FireDev *_
 
 // force at the moved Q, second half kick (velocityVerlet.cpp:33-37) and the
 // three FIRE reductions F.F, v.v, F.v in the QT metric (energyMinimizerFIRE.cpp:94-103)
-template <class T>
-__global__ void __launch_bounds__(kBlock) k_force_kick(Lat<T> L, const FireDev *__restrict__ fd, double *partials)
+// CAP = 1 limits registers so that 2 (FP64) or 3 (FP32) blocks fit per SM
+template <class T, int CAP>
+__global__ void __launch_bounds__(kBlock, CAP ? (sizeof(T) == 8 ? 2 : 3) : 1)
+    k_force_kick(Lat<T> L, const FireDev *__restrict__ fd, double *partials)
 {
     if (!fd->active) return;
     const T hdt = T(0.5) * T(fd->dt);
@@ -786,17 +592,18 @@ template <class T> int launch_fire_pred(const Lat<T> &L, FireDev *fd, cudaStream
     k_fire_pred<T><<<elem_grid(5 * L.P), kBlock, 0, s>>>(L, fd);
     return 1;
 }
-template <class T> int launch_force_kick(const Lat<T> &L, FireDev *fd, double *partials, int grid, cudaStream_t s)
+template <class T>
+int launch_force_kick(const Lat<T> &L, FireDev *fd, double *partials, int grid, cudaStream_t s, int cap)
 {
     int n = 0;
     if (L.multi) n += launch_derivs(L, s);
-    k_force_kick<T><<<grid, kBlock, 0, s>>>(L, fd, partials);
-    return n + 1;
+    return n + launch_force_kick_only(L, fd, partials, grid, s, cap);
 }
 template <class T>
-int launch_force_kick_only(const Lat<T> &L, FireDev *fd, double *partials, int grid, cudaStream_t s)
+int launch_force_kick_only(const Lat<T> &L, FireDev *fd, double *partials, int grid, cudaStream_t s, int cap)
 {
-    k_force_kick<T><<<grid, kBlock, 0, s>>>(L, fd, partials);
+    if (cap) k_force_kick<T, 1><<<grid, kBlock, 0, s>>>(L, fd, partials);
+    else k_force_kick<T, 0><<<grid, kBlock, 0, s>>>(L, fd, partials);
     return 1;
 }
 int launch_fire_control(FireDev *fd, const double *partials, int nparts, cudaStream_t s)
@@ -901,8 +708,8 @@ int launch_energy_full(const Lat<T> &L, double *partials, int grid, double *out5
     template int launch_derivs<T>(const Lat<T> &, cudaStream_t);                                                   \
     template int launch_force<T>(const Lat<T> &, int, cudaStream_t);                                               \
     template int launch_fire_pred<T>(const Lat<T> &, FireDev *, cudaStream_t);                                     \
-    template int launch_force_kick<T>(const Lat<T> &, FireDev *, double *, int, cudaStream_t);                     \
-    template int launch_force_kick_only<T>(const Lat<T> &, FireDev *, double *, int, cudaStream_t);                \
+    template int launch_force_kick<T>(const Lat<T> &, FireDev *, double *, int, cudaStream_t, int);                \
+    template int launch_force_kick_only<T>(const Lat<T> &, FireDev *, double *, int, cudaStream_t, int);           \
     template int launch_fire_finish<T>(const Lat<T> &, FireDev *, cudaStream_t);                                   \
     template int launch_aos_to_soa<T>(const double *, T *, int, long long, int, cudaStream_t);                     \
     template int launch_soa_to_aos<T>(const T *, double *, int, long long, int, cudaStream_t);                     \

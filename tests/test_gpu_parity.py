@@ -51,11 +51,14 @@ def test_force_fp32(qmin, oracle, name):
 
 @pytest.mark.parametrize("name", ["l1_bulk_fire", "l123_walls_sphere_fire", "planar_sphere_fire",
                                   "l1234_planar_fields_fire", "edges_gaps_wrap"])
-def test_fire_trajectory_fp64(qmin, oracle, name):
+@pytest.mark.parametrize("mode", [0, 1])
+def test_fire_trajectory_fp64(qmin, oracle, name, mode):
+    """Both FIRE execution paths (separate kernels, fused tiled kernel) against the reference."""
     g = load(name)
     cfg = parse_args(g["args"])
     s = oracle_system(oracle, cfg)
     lat = gpu_lattice(qmin, s, qmin.FP64)
+    lat.set_fire_kernel(mode)
     lat.fire_init(dt=cfg["dt"])
     n = cfg["iters"]
     r = lat.fire_run(n)
@@ -73,13 +76,15 @@ def test_fire_trajectory_fp64(qmin, oracle, name):
     assert abs(e - g["final"][2]) <= TOL_TRAJ * abs(g["final"][2])
 
 
-def test_fire_per_iteration_trace(qmin, oracle):
+@pytest.mark.parametrize("mode", [0, 1])
+def test_fire_per_iteration_trace(qmin, oracle, mode):
     """Run FIRE one iteration per call (as the reference's minimize() with a
     growing iteration cap) and compare every step's scalars."""
     g = load("l123_walls_sphere_fire")
     cfg = parse_args(g["args"])
     s = oracle_system(oracle, cfg)
     lat = gpu_lattice(qmin, s, qmin.FP64)
+    lat.set_fire_kernel(mode)
     lat.fire_init(dt=cfg["dt"])
     for k, row in enumerate(g["trace"], start=1):
         r = lat.fire_run(k)
@@ -181,3 +186,26 @@ def test_cpp_host_example_reproduces_cli_pin(qmin):
     g = load("c1_50cube_fire100")
     assert abs(fmax - g["final"][1]) <= TOL_TRAJ * g["final"][1]
     assert abs(e - g["final"][2]) <= TOL_TRAJ * abs(g["final"][2])
+
+
+@pytest.mark.parametrize("L", [(16, 9, 7), (40, 33, 21), (65, 17, 30)])
+@pytest.mark.parametrize("prec", [0, 1])
+def test_fused_matches_separate_kernels(qmin, oracle, L, prec):
+    """The fused tiled kernel on lattices that do not divide its tiles (partial
+    tiles, lattices narrower than a tile, odd z extents) tracks the separate
+    kernels: FP64 to 1e-12 after 7 iterations, FP32 to 1e-5."""
+    cfg = parse_args([f"L={L[0]},{L[1]},{L[2]}", "seed=11", "Ls=2.32,1.0,0.5,0,0", "wall=2,0,h,5.3",
+                      f"sphere={L[0] / 2},{L[1] / 2},{L[2] / 2},{min(L) / 4},p,2.0"])
+    s = oracle_system(oracle, cfg)
+    res = []
+    for mode in (0, 1):
+        lat = gpu_lattice(qmin, s, prec)
+        lat.set_fire_kernel(mode)
+        lat.fire_init()
+        r = lat.fire_run(7)
+        res.append((r, lat.get_state(Q=True, V=True, F=True)))
+    tol = 1e-12 if prec == 0 else 1e-5
+    assert res[0][0]["iterations"] == res[1][0]["iterations"] == 7
+    assert abs(res[0][0]["forceMax"] - res[1][0]["forceMax"]) <= tol * res[0][0]["forceMax"]
+    for a, b in zip(res[0][1], res[1][1]):
+        assert rel_err(b, a) <= tol
