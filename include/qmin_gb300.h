@@ -159,13 +159,14 @@ int qmin_set_fire_kernel(qmin_handle h, int mode);
  * advances exactly as in qmin_fire_run.  No reference counterpart (profiling). */
 int qmin_fire_profile(qmin_handle h, int iterations, double kernel_ms[4], int *fused);
 /* The FIRE strategy the autotuner chose on the first run (path 0 separate
- * kernels with register cap `variant`, path 1 fused kernel with tile shape
- * `variant` = tile_x x tile_y and `zc` z planes per block) and the measured
- * ms per iteration of every candidate: ms[0..1] separate (cap 0, 1),
- * ms[2 + 2*cfg + v] fused (v = 0/1 for the two z extents tried; -1 = not run).
+ * kernels sized for `variant` + 1 blocks per SM, path 1 fused kernel with tile
+ * shape `variant` = tile_x x tile_y and `zc` z planes per block) and the
+ * measured ms per iteration of every candidate: ms[0..2] separate (1, 2, 3
+ * blocks per SM), ms[3 + 2*cfg + v] fused (v = 0/1 for the two z extents
+ * tried); -1 = not run.
  * No reference counterpart (the reference's kernelTuner scans block sizes,
  * src/utilities/kernelTuner.cpp:5-125). */
-int qmin_fire_tuning(qmin_handle h, int *path, int *variant, int *tile_x, int *tile_y, int *zc, double ms[10]);
+int qmin_fire_tuning(qmin_handle h, int *path, int *variant, int *tile_x, int *tile_y, int *zc, double ms[11]);
 
 /* ---- energy without allocation ---- */
 /* Largest lattice (in sites) qmin_energy_noalloc accepts: the size of its

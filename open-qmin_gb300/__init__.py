@@ -284,10 +284,10 @@ class Lattice:
 
     def fire_tuning(self):
         path, var, tx, ty, zc = C.c_int(), C.c_int(), C.c_int(), C.c_int(), C.c_int()
-        ms = (C.c_double * 10)()
+        ms = (C.c_double * 11)()
         _check(lib().qmin_fire_tuning(self._h, C.byref(path), C.byref(var), C.byref(tx), C.byref(ty), C.byref(zc),
                                       ms))
-        names = ["separate", "separate_regcap"] + [f"fused_{a}x{b}_z{v}" for a, b in
+        names = ["separate_1blk", "separate_2blk", "separate_3blk"] + [f"fused_{a}x{b}_z{v}" for a, b in
                                                     ((32, 8), (32, 16), (64, 8), (32, 4)) for v in (0, 1)]
         return dict(path="fused" if path.value else "separate", variant=var.value, tile=(tx.value, ty.value),
                     zc=zc.value, candidates_ms={n: m for n, m in zip(names, ms) if m >= 0})

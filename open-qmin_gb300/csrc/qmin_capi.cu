@@ -35,6 +35,8 @@ static int fail(int code, const std::string &msg)
             return fail(QMIN_ECUDA, std::string(#call) + ": " + cudaGetErrorString(e_));      \
     } while (0)
 
+static const int kSepVariants = 3;  // separate-kernel force + kick with 1, 2, 3 blocks per SM
+
 struct qmin_ctx {
     int Lx = 0, Ly = 0, Lz = 0, N = 0;
     long long P = 0;
@@ -77,7 +79,7 @@ struct qmin_ctx {
     // strategy chosen by the autotuner for the current parameters
     int path = -1;  // 0 separate kernels, 1 fused tiled kernel
     int sep_cap = 0, fused_cfg = -1, fused_zc = 0, fused_nblocks = 0, tuned_version = 0, tuned_mode = -1;
-    double tune_ms[2 + kFusedConfigs * 2] = {};  // separate (cap 0, 1), fused (cfg, z extent)
+    double tune_ms[kSepVariants + kFusedConfigs * 2] = {};  // separate (register caps), fused (cfg, z extent)
 };
 
 static const int kChunk = 32;  // iterations per captured graph
@@ -120,7 +122,7 @@ template <class T> static Lat<T> make_lat(qmin_ctx *h)
     L.multi = p.multi_constant;
     L.efield = p.efield;
     L.hfield = p.hfield;
-    const double Lt[3] = {p.L2, p.L3, p.L4};
+    const double Lt[4] = {p.L2, p.L3, p.L4, p.L1};
     for (int k = 0; k < 5; ++k)
         for (int n = 0; n < QMIN_BULK_W; ++n) {
             double c = 0.0;
@@ -128,7 +130,7 @@ template <class T> static Lat<T> make_lat(qmin_ctx *h)
                 // k L / 4 per input; halved for derivative inputs (index >= 35), which
                 // the accessors deliver as twice the derivative
                 const double unit = qmin_bulk_in[k][n] >= 35 ? 0.125 : 0.25;
-                for (int t = 0; t < 3; ++t) c += Lt[t] * (double)qmin_bulk_k[t][k][n] * unit;
+                for (int t = 0; t < 4; ++t) c += Lt[t] * (double)qmin_bulk_k[t][k][n] * unit;
             }
             L.cb[k * QMIN_BULK_W + n] = T(c);
         }
@@ -541,7 +543,7 @@ template <class T> static int tune_fire(qmin_ctx *h, const Lat<T> &L)
     };
     const int H = L.multi ? 2 : 1;
     float best = 1e30f;
-    for (int k = 0; k < 2 + 2 * kFusedConfigs; ++k) h->tune_ms[k] = -1;
+    for (int k = 0; k < kSepVariants + 2 * kFusedConfigs; ++k) h->tune_ms[k] = -1;
     Lat<T> LB = L;
     LB.Q = (T *)h->Q2;
     LB.V = (T *)h->V2;
@@ -565,7 +567,7 @@ template <class T> static int tune_fire(qmin_ctx *h, const Lat<T> &L)
                 });
                 h->launches += 4;
                 if (!ok || cudaGetLastError() != cudaSuccess) continue;
-                h->tune_ms[2 + 2 * cfg + v] = ms;
+                h->tune_ms[kSepVariants + 2 * cfg + v] = ms;
                 if (ms < best) {
                     best = ms;
                     h->path = 1;
@@ -582,7 +584,7 @@ template <class T> static int tune_fire(qmin_ctx *h, const Lat<T> &L)
         const float t_der = L.multi ? time3([&]() { launch_derivs<T>(L, h->stream); }) : 0.f;
         const size_t bytes = 5 * (size_t)h->P * h->esz;
         CK(cudaMemcpyAsync(h->V2, h->V, bytes, cudaMemcpyDeviceToDevice, h->stream));
-        for (int cap = 0; cap < 2; ++cap) {
+        for (int cap = 0; cap < kSepVariants; ++cap) {
             const float t_fk =
                 time3([&]() { launch_force_kick_only<T>(L, h->fire, h->partials, h->grid, h->stream, cap); });
             const float ms = t_pred + t_der + t_fk;
@@ -594,7 +596,7 @@ template <class T> static int tune_fire(qmin_ctx *h, const Lat<T> &L)
             }
         }
         CK(cudaMemcpyAsync(h->V, h->V2, bytes, cudaMemcpyDeviceToDevice, h->stream));
-        h->launches += 4 * (2 + (L.multi ? 1 : 0) + 2);
+        h->launches += 4 * (2 + (L.multi ? 1 : 0) + kSepVariants);
     }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
@@ -938,6 +940,6 @@ int qmin_fire_tuning(qmin_handle h, int *path, int *variant, int *tile_x, int *t
     if (tile_y) *tile_y = ty;
     if (zc) *zc = h->path == 1 ? h->fused_zc : 0;
     if (ms)
-        for (int k = 0; k < 2 + 2 * kFusedConfigs; ++k) ms[k] = h->tune_ms[k];
+        for (int k = 0; k < kSepVariants + 2 * kFusedConfigs; ++k) ms[k] = h->tune_ms[k];
     return QMIN_OK;
 }

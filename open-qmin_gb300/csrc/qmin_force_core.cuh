@@ -141,7 +141,8 @@ __device__ __forceinline__ void site_force_core(const Lat<T> &L, const A &acc, i
     }
 
     T sp[5] = {T(0), T(0), T(0), T(0), T(0)};
-    if (!L.multi || L.L1 != T(0)) {
+    // multi-constant bulk sites carry L1 inside the combined linear form below
+    if (!L.multi || (boundary && L.L1 != T(0))) {
         // lcForce::bulkL1Force / boundaryL1Force (lcForces.h:26-63)
         T s1[5];
         if (!boundary) {
@@ -169,12 +170,16 @@ __device__ __forceinline__ void site_force_core(const Lat<T> &L, const A &acc, i
     }
     if (L.multi) {
         if (!boundary) {
-            // bulk L2/L3/L4 forms, straight-line over their union pattern
+            // bulk L1/L2/L3/L4 forms, straight-line over their union pattern
             T s2[5];
 #define QIN(c) q[c]
 #define QN(slot, c) nq[slot][c]
 #define DN(slot, d) acc.dn(slot, d)
-            QMIN_BULK_FORMS(L.cb, s2);
+            if (L.L4 == T(0)) {
+                QMIN_BULK_FORMS_NO_L4(L.cb, s2);
+            } else {
+                QMIN_BULK_FORMS(L.cb, s2);
+            }
 #undef QIN
 #undef QN
 #undef DN

@@ -7,6 +7,8 @@
 // fixed order.
 #include <math.h>
 
+#include <type_traits>
+
 #include "qmin_force_core.cuh"
 
 namespace qmin {
@@ -88,22 +90,35 @@ __global__ void __launch_bounds__(kBlock) k_fire_pred(Lat<T> L, const FireDev *_
     const T hdt = T(0.5) * dt;
     const bool pend = fd->pending, reset = fd->reset;
     const T ma = T(1.0 - fd->mixA), mb = T(fd->mixA * fd->mixS);
-    const long long n = 5 * L.P;
+    // 16-byte vectors: 5 * P is a multiple of 32 elements and the planes are 256-byte aligned
+    using V4 = typename std::conditional<sizeof(T) == 8, double2, float4>::type;
+    constexpr int W = 16 / sizeof(T);
+    const long long n = 5 * L.P / W;
+    V4 *Q4 = reinterpret_cast<V4 *>(L.Q), *Vv4 = reinterpret_cast<V4 *>(L.V);
+    const V4 *F4 = reinterpret_cast<const V4 *>(L.F);
     for (long long j = blockIdx.x * (long long)kBlock + threadIdx.x; j < n; j += (long long)gridDim.x * kBlock) {
-        T v = L.V[j];
-        const T f = L.F[j];
-        if (pend) v = reset ? T(0) : ma * v + mb * f;
-        const T disp = dt * v + hdt2 * f;
-        L.V[j] = v + hdt * f;
-        L.Q[j] += disp;
+        V4 vv = Vv4[j], qq = Q4[j];
+        const V4 ff = F4[j];
+        T *v = reinterpret_cast<T *>(&vv), *q = reinterpret_cast<T *>(&qq);
+        const T *f = reinterpret_cast<const T *>(&ff);
+#pragma unroll
+        for (int e = 0; e < W; ++e) {
+            T ve = v[e];
+            if (pend) ve = reset ? T(0) : ma * ve + mb * f[e];
+            const T disp = dt * ve + hdt2 * f[e];
+            v[e] = ve + hdt * f[e];
+            q[e] += disp;
+        }
+        Vv4[j] = vv;
+        Q4[j] = qq;
     }
 }
 
 // force at the moved Q, second half kick (velocityVerlet.cpp:33-37) and the
 // three FIRE reductions F.F, v.v, F.v in the QT metric (energyMinimizerFIRE.cpp:94-103)
-// CAP = 1 limits registers so that 2 (FP64) or 3 (FP32) blocks fit per SM
+// CAP limits registers so that CAP + 1 blocks of 256 threads fit per SM
 template <class T, int CAP>
-__global__ void __launch_bounds__(kBlock, CAP ? (sizeof(T) == 8 ? 2 : 3) : 1)
+__global__ void __launch_bounds__(kBlock, CAP + 1)
     k_force_kick(Lat<T> L, const FireDev *__restrict__ fd, double *partials)
 {
     if (!fd->active) return;
@@ -589,7 +604,7 @@ template <class T> int launch_force(const Lat<T> &L, int grid, cudaStream_t s)
 }
 template <class T> int launch_fire_pred(const Lat<T> &L, FireDev *fd, cudaStream_t s)
 {
-    k_fire_pred<T><<<elem_grid(5 * L.P), kBlock, 0, s>>>(L, fd);
+    k_fire_pred<T><<<elem_grid(5 * L.P / (16 / sizeof(T))), kBlock, 0, s>>>(L, fd);
     return 1;
 }
 template <class T>
@@ -602,7 +617,8 @@ int launch_force_kick(const Lat<T> &L, FireDev *fd, double *partials, int grid, 
 template <class T>
 int launch_force_kick_only(const Lat<T> &L, FireDev *fd, double *partials, int grid, cudaStream_t s, int cap)
 {
-    if (cap) k_force_kick<T, 1><<<grid, kBlock, 0, s>>>(L, fd, partials);
+    if (cap == 2) k_force_kick<T, 2><<<grid, kBlock, 0, s>>>(L, fd, partials);
+    else if (cap == 1) k_force_kick<T, 1><<<grid, kBlock, 0, s>>>(L, fd, partials);
     else k_force_kick<T, 0><<<grid, kBlock, 0, s>>>(L, fd, partials);
     return 1;
 }

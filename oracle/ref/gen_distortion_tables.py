@@ -91,27 +91,42 @@ def main():
              "#define QMIN_DT_K_INIT {" + ",".join(str(x) for x in ks) + "}", ""]
     with open(os.path.join(ROOT, "open-qmin_gb300", "csrc", "qmin_distortion_tables.h"), "w") as f:
         f.write("\n".join(lines))
-    # straight-line bulk forms: the union of the L2, L3, L4 bulk patterns per
-    # component; the kernels multiply each input by a per-handle coefficient
-    # cb[k][n] = sum_t L_t * k_t / 4 computed on the host.
-    union = [sorted(set().union(*[coef[(t, 0, c)].keys() for t in TERMS])) for c in range(5)]
+    # straight-line bulk forms: one linear form per component over the union of
+    # the L1 (bulk, lcForces.h:26-37), L2, L3 and L4 bulk patterns; the kernels
+    # multiply each input by a per-handle coefficient cb[k][n] = sum_t L_t k_t / 4
+    # computed on the host.  The L1 bulk form written in the same units
+    # (k L1 / 4): S = L1 (6 q - sum of the six neighbours), then S0 += S0 + S3,
+    # S3 += S0 + S3, S1, S2, S4 doubled.
+    l1 = {c: {} for c in range(5)}
+    for c in range(5):
+        partners = {0: {0: 2, 3: 1}, 3: {0: 1, 3: 2}}.get(c, {c: 2})
+        for comp, m in partners.items():
+            l1[c][comp] = l1[c].get(comp, 0) + 4 * 6 * m
+            for slot in range(6):
+                j = 5 + 5 * slot + comp
+                l1[c][j] = l1[c].get(j, 0) - 4 * m
+        coef[("L1", 0, c)] = l1[c]
+    TERMS4 = ["L2", "L3", "L4", "L1"]
+    union = [sorted(set().union(*[coef[(t, 0, c)].keys() for t in TERMS4])) for c in range(5)]
     W = max(len(u) for u in union)
+    l4only = [[n for n, j in enumerate(union[c]) if all(coef[(t, 0, c)].get(j, 0) == 0 for t in ("L2", "L3", "L1"))]
+              for c in range(5)]
     lines = [header.replace("Do not edit.", "Do not edit.  Bulk (case 0) forms, straight-line."), "#pragma once",
              f"#define QMIN_BULK_W {W}",
              "/* inputs of component k: qmin_bulk_in[k][0 .. qmin_bulk_n[k]) (0..4 q, 5..34 neighbour q,",
-             "   35..124 neighbour derivatives); per-term integer coefficients qmin_bulk_k[term][k][n] */",
+             "   35..124 neighbour derivatives); per-term integer coefficients qmin_bulk_k[term][k][n],",
+             "   terms L2, L3, L4, L1 */",
              "static const int qmin_bulk_n[5] = {" + ",".join(str(len(u)) for u in union) + "};",
              "static const int qmin_bulk_in[5][QMIN_BULK_W] = {" +
              ",".join("{" + ",".join(str(x) for x in u + [0] * (W - len(u))) + "}" for u in union) + "};",
-             "static const int qmin_bulk_k[3][5][QMIN_BULK_W] = {" +
-             ",".join("{" + ",".join("{" + ",".join(str(coef[(t, 0, c)].get(x, 0)) for x in union[c] + [-1] * 0) +
-                                      "," * 0 + ",".join([""] * 0) + ("," if len(union[c]) < W else "") +
-                                      ",".join(["0"] * (W - len(union[c]))) + "}" for c in range(5)) + "}"
-                      for t in TERMS) + "};",
+             "static const int qmin_bulk_k[4][5][QMIN_BULK_W] = {" +
+             ",".join("{" + ",".join("{" + ",".join([str(coef[(t, 0, c)].get(x, 0)) for x in union[c]] +
+                                                     ["0"] * (W - len(union[c]))) + "}" for c in range(5)) + "}"
+                      for t in TERMS4) + "};",
              "",
              "/* s[k] = sum_n cb[k*QMIN_BULK_W + n] * input; QIN(c) = own q component,",
-             "   QN(slot, c) = neighbour q, DN(slot, d) = neighbour derivative component */",
-             "#define QMIN_BULK_FORMS(cb, s) \\"]
+             "   QN(slot, c) = neighbour q, DN(slot, d) = neighbour derivative component.",
+             "   QMIN_BULK_FORMS_NO_L4 omits the inputs only the L4 term uses. */"]
 
     def term(j):
         if j < 5:
@@ -119,14 +134,17 @@ def main():
         if j < 35:
             return f"QN({(j - 5) // 5},{(j - 5) % 5})"
         return f"DN({(j - 35) // 15},{(j - 35) % 15})"
-    for c in range(5):
-        body = " + ".join(f"(cb)[{c * W + n}] * {term(j)}" for n, j in enumerate(union[c]))
-        lines.append(f"    (s)[{c}] = {body}; \\")
-    lines.append("    do {} while (0)")
-    lines.append("")
+    for name, skip in (("QMIN_BULK_FORMS", [[] for _ in range(5)]), ("QMIN_BULK_FORMS_NO_L4", l4only)):
+        lines.append(f"#define {name}(cb, s) \\")
+        for c in range(5):
+            body = " + ".join(f"(cb)[{c * W + n}] * {term(j)}" for n, j in enumerate(union[c]) if n not in skip[c])
+            lines.append(f"    (s)[{c}] = {body}; \\")
+        lines.append("    do {} while (0)")
+        lines.append("")
     with open(os.path.join(ROOT, "open-qmin_gb300", "csrc", "qmin_bulk_forms.h"), "w") as f:
         f.write("\n".join(lines))
-    print(f"wrote tables: {len(inputs)} nonzero coefficients; bulk union widths {[len(u) for u in union]}")
+    print(f"wrote tables: {len(inputs)} nonzero coefficients; bulk union widths {[len(u) for u in union]}, "
+          f"L4-only {[len(x) for x in l4only]}")
 
 
 if __name__ == "__main__":
