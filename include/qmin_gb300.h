@@ -193,6 +193,30 @@ int qmin_energy_noalloc(const qmin_lattice_desc *desc, const qmin_ldg_params *p,
                         const double *Q_dev, long long plane_stride, const int8_t *types_dev, double *out_dev,
                         void *stream);
 
+/* ---- batched solves (many independent lattices of uneven sizes) ---- */
+/* A batch packs nsolves independent lattices (dims[3*s .. 3*s+2] = Lx, Ly, Lz)
+ * into one device state and minimises them together: each solve follows
+ * energyMinimizerFIRE::minimize on its own lattice (its own FIRE scalars,
+ * stopping rule and iteration count), one launch per kernel per iteration
+ * covers every still-active solve, converged solves retire.  All solves share
+ * the force parameters; each has up to 16 objects.  No reference counterpart
+ * for the batching itself (the reference minimises one lattice per process). */
+typedef struct qmin_batch_ctx *qmin_batch;
+int qmin_batch_create(int nsolves, const int32_t *dims, int precision, int metric_mode, qmin_batch *out);
+int qmin_batch_destroy(qmin_batch b);
+int qmin_batch_set_params(qmin_batch b, const qmin_ldg_params *p);
+/* state of solve s: AoS Q, int32 types (objects numbered 1..nobj within the solve) */
+int qmin_batch_set_solve(qmin_batch b, int s, const double *Q, const int32_t *types, const qmin_object *objs,
+                         int nobj);
+/* read back solve s's Q and/or forces (AoS, either pointer may be NULL) */
+int qmin_batch_get_solve(qmin_batch b, int s, double *Q, double *F);
+/* FIRE parameters for every solve (energyMinimizerFIRE::setFIREParameters) */
+int qmin_batch_fire_init(qmin_batch b, const qmin_fire_params *p);
+/* minimise every solve; per-solve iteration counts and forceMax (arrays of
+ * nsolves, may be NULL) and the number of solves with forceMax <= cutoff */
+int qmin_batch_fire_run(qmin_batch b, int max_iterations, int *iterations, double *force_max, int *converged);
+int qmin_batch_kernel_launches(qmin_batch b, long long *count);
+
 /* ---- host-side set-up helpers (the reference runs these on the host even
  *      in GPU runs, openQmin.cpp:261-268) ---- */
 /* qTensorLatticeModel::setNematicQTensorRandomly (qTensorLatticeModel.cpp:134-162)

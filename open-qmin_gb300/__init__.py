@@ -32,7 +32,9 @@ EXPORTED_SYMBOLS = [
     "qmin_set_params", "qmin_set_objects", "qmin_set_state", "qmin_get_state", "qmin_n_active", "qmin_force",
     "qmin_energy", "qmin_fire_init", "qmin_fire_run", "qmin_adam_run", "qmin_nesterov_run", "qmin_lbfgs_run",
     "qmin_host_random_nematic", "qmin_host_add_wall", "qmin_host_add_sphere", "qmin_set_fire_kernel",
-    "qmin_fire_profile", "qmin_fire_tuning", "qmin_energy_noalloc",
+    "qmin_fire_profile", "qmin_fire_tuning", "qmin_energy_noalloc", "qmin_batch_create", "qmin_batch_destroy",
+    "qmin_batch_set_params", "qmin_batch_set_solve", "qmin_batch_get_solve", "qmin_batch_fire_init",
+    "qmin_batch_fire_run", "qmin_batch_kernel_launches",
 ]
 FIRE_SEPARATE, FIRE_FUSED, FIRE_AUTO = 0, 1, 2
 
@@ -96,6 +98,13 @@ def lib():
             "qmin_lbfgs_run": [h, C.c_int, C.c_double, C.c_double, C.c_int, C.c_int, ip, dp],
             "qmin_host_random_nematic": [C.c_int, C.c_int, C.c_int, C.c_int, C.c_double, dp],
             "qmin_set_fire_kernel": [h, C.c_int],
+            "qmin_batch_create": [C.c_int, ip, C.c_int, C.c_int, C.POINTER(C.c_void_p)],
+            "qmin_batch_destroy": [h], "qmin_batch_set_params": [h, C.POINTER(LdgParams)],
+            "qmin_batch_set_solve": [h, C.c_int, vp, vp, C.POINTER(Object), C.c_int],
+            "qmin_batch_get_solve": [h, C.c_int, vp, vp],
+            "qmin_batch_fire_init": [h, C.POINTER(FireParams)],
+            "qmin_batch_fire_run": [h, C.c_int, ip, dp, ip],
+            "qmin_batch_kernel_launches": [h, C.POINTER(C.c_longlong)],
             "qmin_fire_profile": [h, C.c_int, dp, ip],
             "qmin_fire_tuning": [h, ip, ip, ip, ip, ip, dp],
             "qmin_host_add_wall": [C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_double, C.c_double, dp,
@@ -295,6 +304,74 @@ class Lattice:
     def launches(self):
         n = C.c_longlong()
         _check(lib().qmin_kernel_launches(self._h, C.byref(n)))
+        return n.value
+
+
+class Batch:
+    """Many independent lattices of uneven sizes minimised together (a qmin_batch)."""
+
+    def __init__(self, dims, precision=FP64, metric_mode=METRIC_CPU):
+        self.dims = [tuple(int(x) for x in d) for d in dims]
+        arr = np.ascontiguousarray(np.array(self.dims, dtype=np.int32).ravel())
+        self._h = C.c_void_p()
+        _check(lib().qmin_batch_create(len(self.dims), _ip(arr), precision, metric_mode, C.byref(self._h)))
+
+    def close(self):
+        if self._h:
+            lib().qmin_batch_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_params(self, A, B, Cc, L1=0.0, L2=0.0, L3=0.0, L4=0.0, multi_constant=None, E=None, H=None):
+        p = LdgParams()
+        p.A, p.B, p.C = A, B, Cc
+        p.L1, p.L2, p.L3, p.L4 = L1, L2, L3, L4
+        p.multi_constant = int(any(x != 0 for x in (L2, L3, L4))) if multi_constant is None else int(multi_constant)
+        if E is not None:
+            p.efield = 1
+            p.E[0], p.E[1], p.E[2], p.eps, p.eps0, p.deps = E
+        if H is not None:
+            p.hfield = 1
+            p.H[0], p.H[1], p.H[2], p.chi, p.mu0, p.dchi = H
+        _check(lib().qmin_batch_set_params(self._h, C.byref(p)))
+
+    def set_solve(self, s, Q, types, objs):
+        Q = np.ascontiguousarray(Q, dtype=np.float64)
+        types = np.ascontiguousarray(types, dtype=np.int32)
+        arr = (Object * max(len(objs), 1))()
+        for k, (kind, W, S0) in enumerate(objs):
+            arr[k].kind, arr[k].W, arr[k].S0 = kind, W, S0
+        _check(lib().qmin_batch_set_solve(self._h, int(s), Q.ctypes.data, types.ctypes.data, arr, len(objs)))
+
+    def get_solve(self, s, F=False):
+        n = int(np.prod(self.dims[s]))
+        Q = np.zeros((n, 5))
+        Fo = np.zeros((n, 5)) if F else None
+        _check(lib().qmin_batch_get_solve(self._h, int(s), Q.ctypes.data, Fo.ctypes.data if F else None))
+        return (Q, Fo) if F else Q
+
+    def fire_init(self, dt=5e-4, alpha_start=0.99, dt_max=None, dt_inc=1.1, dt_dec=0.95, alpha_dec=0.9, n_min=4,
+                  force_cutoff=1e-12, alpha_min=0.0):
+        p = FireParams(dt, alpha_start, 100 * dt if dt_max is None else dt_max, dt_inc, dt_dec, alpha_dec,
+                       alpha_min, force_cutoff, n_min)
+        _check(lib().qmin_batch_fire_init(self._h, C.byref(p)))
+
+    def fire_run(self, max_iterations):
+        n = len(self.dims)
+        its = np.zeros(n, dtype=np.int32)
+        fm = np.zeros(n)
+        conv = C.c_int()
+        _check(lib().qmin_batch_fire_run(self._h, int(max_iterations), _ip(its), _dp(fm), C.byref(conv)))
+        return dict(iterations=its, forceMax=fm, converged=conv.value)
+
+    def launches(self):
+        n = C.c_longlong()
+        _check(lib().qmin_batch_kernel_launches(self._h, C.byref(n)))
         return n.value
 
 

@@ -84,22 +84,12 @@ struct qmin_ctx {
 
 static const int kChunk = 32;  // iterations per captured graph
 
-template <class T> static Lat<T> make_lat(qmin_ctx *h)
+namespace qmin {
+// Force parameters shared by every kernel: phase constants as the force uses
+// them, elastic constants, field force vectors and the combined bulk linear
+// form's coefficients.
+template <class T> void fill_lat_params(Lat<T> &L, const qmin_ldg_params &p, int metric_mode)
 {
-    Lat<T> L;
-    memset(&L, 0, sizeof L);
-    L.Lx = h->Lx;
-    L.Ly = h->Ly;
-    L.Lz = h->Lz;
-    L.N = h->N;
-    L.P = h->P;
-    L.Q = (T *)h->Q;
-    L.V = (T *)h->V;
-    L.F = (T *)h->F;
-    L.types = h->types;
-    L.D = (T *)h->D;
-    L.objs = (const ObjDev<T> *)h->objs;
-    const qmin_ldg_params &p = h->params;
     L.a = T(0.5 * p.A);
     L.b = T(p.B / 3.0);
     L.c = T(0.25 * p.C);
@@ -118,7 +108,7 @@ template <class T> static Lat<T> make_lat(qmin_ctx *h)
     };
     if (p.efield) field(p.E, p.deps, p.eps0, L.fE);
     if (p.hfield) field(p.H, p.dchi, p.mu0, L.fH);
-    L.metric_mode = h->metric_mode;
+    L.metric_mode = metric_mode;
     L.multi = p.multi_constant;
     L.efield = p.efield;
     L.hfield = p.hfield;
@@ -134,6 +124,27 @@ template <class T> static Lat<T> make_lat(qmin_ctx *h)
             }
             L.cb[k * QMIN_BULK_W + n] = T(c);
         }
+}
+template void fill_lat_params<double>(Lat<double> &, const qmin_ldg_params &, int);
+template void fill_lat_params<float>(Lat<float> &, const qmin_ldg_params &, int);
+}  // namespace qmin
+
+template <class T> static Lat<T> make_lat(qmin_ctx *h)
+{
+    Lat<T> L;
+    memset(&L, 0, sizeof L);
+    L.Lx = h->Lx;
+    L.Ly = h->Ly;
+    L.Lz = h->Lz;
+    L.N = h->N;
+    L.P = h->P;
+    L.Q = (T *)h->Q;
+    L.V = (T *)h->V;
+    L.F = (T *)h->F;
+    L.types = h->types;
+    L.D = (T *)h->D;
+    L.objs = (const ObjDev<T> *)h->objs;
+    fill_lat_params(L, h->params, h->metric_mode);
     return L;
 }
 

@@ -6,6 +6,7 @@
 //   int tn(s)          type of neighbour s (0..5 = x-, x+, y-, y+, z-, z+)
 //   T   q(k)           own Q component k
 //   T   nq(s, k)       neighbour s's Q component k
+//   ObjDev<T> obj(t)   the object whose sites carry type t > 0
 //   T   dn(s, d)       TWICE neighbour s's first derivative d = 5*axis + component
 //                      (landauDeGennesLC::computeFirstDerivatives rules).  Central
 //                      differences are then plain differences; the exact factor 1/2
@@ -224,7 +225,7 @@ __device__ __forceinline__ void site_force_core(const Lat<T> &L, const A &acc, i
 #pragma unroll
         for (int s = 0; s < 6; ++s) {
             if (mask & (1 << s)) {
-                const ObjDev<T> o = L.objs[acc.tn(s) - 1];
+                const ObjDev<T> o = acc.obj(acc.tn(s));
                 anchoring_force_add(o.kind, o.W, o.S0, q, nq[s], f);
             }
         }
@@ -245,13 +246,15 @@ template <class T> struct GlobalAcc {
     const T *Q;
     const T *D;
     const int8_t *types;
+    const ObjDev<T> *objs;
     long long P;
     int i;
     Nb b;
     __device__ __forceinline__ GlobalAcc(const Lat<T> &L, int i_)
-        : Q(L.Q), D(L.D), types(L.types), P(L.P), i(i_), b(neighbours(L, i_))
+        : Q(L.Q), D(L.D), types(L.types), objs(L.objs), P(L.P), i(i_), b(neighbours(L, i_))
     {
     }
+    __device__ __forceinline__ ObjDev<T> obj(int t) const { return objs[t - 1]; }
     __device__ __forceinline__ int tn(int s) const { return types[b.n[s]]; }
     __device__ __forceinline__ T q(int k) const { return ld(Q + (long long)k * P + i); }
     __device__ __forceinline__ T nq(int s, int k) const { return ld(Q + (long long)k * P + b.n[s]); }

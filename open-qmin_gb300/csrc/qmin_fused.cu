@@ -22,9 +22,11 @@ template <class T, int H, int TX, int TY> struct TileAcc {
     static constexpr int SX = TX + 2 * H, SY = TY + 2 * H, TS = SX * SY, NP = 2 * H + 1;
     const T *sQ;
     const int8_t *sT;
+    const ObjDev<T> *objs;
     int slot[NP];  // ring slot of plane dz = -H..H (index dz + H)
     int p;         // centre position inside a plane
 
+    __device__ __forceinline__ ObjDev<T> obj(int t) const { return objs[t - 1]; }
     __device__ __forceinline__ static int ndz(int s) { return s == 4 ? -1 : (s == 5 ? 1 : 0); }
     __device__ __forceinline__ static int ndp(int s)
     {
@@ -165,6 +167,7 @@ __global__ void __launch_bounds__(TX *BY) k_fire_fused(Lat<T> L, T *__restrict__
             DeepTileAcc<T, H, TX, TY> a;
             a.sQ = sQ;
             a.sT = sT;
+            a.objs = L.objs;
 #pragma unroll
             for (int j = 0; j < NP; ++j) a.slot[j] = slot_of(z - H + j);
 #pragma unroll

@@ -5,6 +5,7 @@
 
 #include <string>
 
+#include "../../include/qmin_gb300.h"
 #include "qmin_bulk_forms.h"
 
 namespace qmin {
@@ -30,6 +31,9 @@ template <class T> struct Lat {
     int metric_mode, multi, efield, hfield;
     T cb[5 * QMIN_BULK_W];  // combined bulk multi-constant coefficients
 };
+
+// force parameters shared by every kernel (qmin_capi.cu)
+template <class T> void fill_lat_params(Lat<T> &L, const qmin_ldg_params &p, int metric_mode);
 
 // FIRE state resident on the device.  The velocity mix that ends one
 // iteration is deferred into the next iteration's first kernel.

@@ -1,0 +1,98 @@
+"""Batched minimisation of uneven independent lattices against the oracle,
+solve by solve.  Tolerances: FIRE trajectories 1e-9 relative (FP64),
+FP32 batch within 1e-4 of the FP64 batch in forceMax."""
+import numpy as np
+import pytest
+
+from cases import oracle_system, parse_args, rel_err
+
+pytestmark = pytest.mark.gpu
+
+
+def _cfgs():
+    return [
+        ["L=9,10,11", "seed=1", "Ls=2.32,0,0,0,0", "sphere=4.3,5.1,5.7,2.2,p,0.7"],
+        ["L=16,12,8", "seed=2", "Ls=2.32,0,0,0,0", "sphere=8.5,6.2,3.9,2.6,p,3.1"],
+        ["L=20,7,13", "seed=3", "Ls=2.32,0,0,0,0"],
+        ["L=5,19,6", "seed=4", "Ls=2.32,0,0,0,0", "sphere=2.5,9.5,3.1,1.7,h,5.3"],
+        ["L=14,14,14", "seed=5", "Ls=2.32,0,0,0,0", "sphere=0.2,13.1,7.7,3.3,p,9.0"],
+    ]
+
+
+def _batch(qmin, systems, prec=0):
+    b = qmin.Batch([s.L for s in systems], prec)
+    p = systems[0].p
+    b.set_params(p.A, p.B, p.C, p.L1, p.L2, p.L3, p.L4, multi_constant=p.multi_constant)
+    for k, s in enumerate(systems):
+        b.set_solve(k, s.Q, s.types, [(s.objs[j].kind, s.objs[j].W, s.objs[j].S0) for j in range(s.nobj)])
+    return b
+
+
+def test_batch_fire_matches_each_solve(qmin, oracle):
+    systems = [oracle_system(oracle, parse_args(c)) for c in _cfgs()]
+    b = _batch(qmin, systems)
+    b.fire_init()
+    r = b.fire_run(25)
+    for k, s in enumerate(systems):
+        ro = s.fire(25)
+        assert r["iterations"][k] == ro["iterations"] == 25
+        assert abs(r["forceMax"][k] - ro["forceMax"]) <= 1e-9 * ro["forceMax"]
+        assert rel_err(b.get_solve(k), s.Q) <= 1e-9
+
+
+def test_batch_multi_constant_with_walls(qmin, oracle):
+    cfgs = [["L=12,11,10", "seed=5", "Ls=2.32,1.0,0.5,0,0", "wall=2,0,h,5.3", "wall=2,9,h,5.3",
+             "sphere=6,5.5,4.5,2.6,h,5.3"],
+            ["L=10,13,9", "seed=8", "Ls=2.32,1.0,0.5,0,0", "wall=0,0,p,1.0", "sphere=5.2,6.3,4.1,2.4,p,2.0"]]
+    systems = [oracle_system(oracle, parse_args(c)) for c in cfgs]
+    b = _batch(qmin, systems)
+    b.fire_init()
+    r = b.fire_run(20)
+    for k, s in enumerate(systems):
+        ro = s.fire(20)
+        assert abs(r["forceMax"][k] - ro["forceMax"]) <= 1e-9 * ro["forceMax"]
+        assert rel_err(b.get_solve(k), s.Q) <= 1e-9
+
+
+def test_batch_retires_converged_solves(qmin, oracle):
+    """Per-solve stopping: with a loose cutoff each solve stops at its own
+    iteration, exactly where its own minimize() would."""
+    systems = [oracle_system(oracle, parse_args(c)) for c in _cfgs()]
+    fcut = 0.05
+    b = _batch(qmin, systems)
+    b.fire_init(force_cutoff=fcut)
+    r = b.fire_run(400)
+    its = []
+    for k, s in enumerate(systems):
+        ro = s.fire(400, fcut=fcut)
+        its.append(ro["iterations"])
+        assert r["iterations"][k] == ro["iterations"]
+        assert abs(r["forceMax"][k] - ro["forceMax"]) <= 1e-9 * ro["forceMax"]
+    assert len(set(its)) > 1, "the cases should stop at different iterations"
+    assert r["converged"] == sum(1 for k in range(len(systems)) if r["forceMax"][k] <= fcut)
+
+
+def test_batch_fp32_tracks_fp64(qmin, oracle):
+    systems = [oracle_system(oracle, parse_args(c)) for c in _cfgs()]
+    res = []
+    for prec in (0, 1):
+        b = _batch(qmin, systems, prec)
+        b.fire_init()
+        res.append(b.fire_run(40)["forceMax"])
+    np.testing.assert_allclose(res[1], res[0], rtol=1e-4)
+
+
+def test_c3_generator_and_batch_smoke(qmin):
+    """The batched configuration's generator builds solves the batch accepts."""
+    import importlib
+    wl = importlib.import_module("qmin_gb300.workloads")
+    solves = [wl.c3_solve(s) for s in range(6)]
+    b = qmin.Batch([d["L"] for d in solves], qmin.FP32)
+    a, bb, c = solves[0]["consts"]
+    b.set_params(a, bb, c, 2.32)
+    for k, d in enumerate(solves):
+        b.set_solve(k, d["Q"], d["types"], d["objects"])
+    b.fire_init()
+    r = b.fire_run(50)
+    assert (r["iterations"] == 50).all()
+    assert np.isfinite(r["forceMax"]).all()
