@@ -96,3 +96,34 @@ def test_c3_generator_and_batch_smoke(qmin):
     r = b.fire_run(50)
     assert (r["iterations"] == 50).all()
     assert np.isfinite(r["forceMax"]).all()
+
+
+def test_batch_reproduces_reference_divergence(qmin, oracle):
+    """Config-3 solve 51 (planar sphere W~8.8 wrapping the periodic corner)
+    diverges under the reference's FIRE schedule (dt grows to its 0.05 cap):
+    the oracle's forceMax turns non-finite at iteration 63, and so does the
+    batched GPU solve; the other solves in the batch are unaffected."""
+    import importlib
+    wl = importlib.import_module("qmin_gb300.workloads")
+    import ctypes as C
+    ids = [50, 51, 52]
+    solves = [wl.c3_solve(s) for s in ids]
+    s51 = oracle.System(solves[1]["L"], Ls=(2.32, 0, 0, 0))
+    s51.random_nematic(51)
+    c, r, W = solves[1]["sphere"]
+    s51.add_sphere(c, r, 1, W)
+    tr = s51.fire(70, fcut=1e-6, trace=True)["trace"]
+    first_bad = next(k for k in range(len(tr)) if not np.isfinite(tr[k, 0])) + 1
+    b = qmin.Batch([d["L"] for d in solves], qmin.FP64)
+    a, bb, cc = solves[0]["consts"]
+    b.set_params(a, bb, cc, 2.32)
+    for k, d in enumerate(solves):
+        b.set_solve(k, d["Q"], d["types"], d["objects"])
+    b.fire_init(force_cutoff=1e-6)
+    its = np.zeros(3, dtype=np.int32)
+    fm = np.zeros(3)
+    conv = C.c_int()
+    rc = qmin.lib().qmin_batch_fire_run(b._h, 200, qmin._ip(its), qmin._dp(fm), C.byref(conv))
+    assert rc == qmin.QMIN_ENONFINITE
+    assert not np.isfinite(fm[1]) and its[1] == first_bad
+    assert np.isfinite(fm[0]) and np.isfinite(fm[2])
