@@ -469,6 +469,63 @@ def run_reference(args):
             "e2e": {"value": value, "unit": "site-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
 
 
+def run_c5(args):
+    """400^3, 8 random homeotropic spheres, L1-L3, uniform E field along z:
+    plain FP64 FIRE and the FP32 form to forceMax < 1e-6, then Adam and L-BFGS
+    (the reference's default parameters, FP32 form) on the same input."""
+    import importlib
+    import torch
+    import __graft_entry__ as ge
+    q = ge.load_package()
+    wl = importlib.import_module("qmin_gb300.workloads")
+    d = wl.c5_lattice(args.lattice if args.lattice != 200 else 400)
+    N = d["Q"].shape[0]
+    a, b, c = d["consts"]
+    out = {"workload": f"{d['L'][0]}^3, {len(d['spheres'])} random homeotropic spheres r U[10,25] W=5.3, "
+                       "L1-L3 = 2.32/1.0/0.5, uniform E = (0, 0, 0.5), eps = eps0 = 1, deps = 0.5, seed 13371",
+           "sites": N, "spheres": d["spheres"]}
+
+    def lattice(prec):
+        lat = q.Lattice(d["L"], prec)
+        lat.set_params(a, b, c, *d["Ls"], E=d["E"])
+        lat.set_objects(d["objects"])
+        lat.set_state(d["Q"], d["types"])
+        return lat
+
+    for prec, tag in ((q.FP64, "fire_fp64"), (q.FP32, "fire_fp32")):
+        lat = lattice(prec)
+        lat.fire_init(force_cutoff=1e-6)
+        lat.fire_run(1)
+        lat.set_state(d["Q"], d["types"])
+        lat.fire_init(force_cutoff=1e-6)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        r = lat.fire_run(args.c5_max_iterations)
+        torch.cuda.synchronize()
+        dt = time.perf_counter() - t0
+        e, comps = lat.energy()
+        out[tag] = {"time_s": dt, "iterations": r["iterations"], "forceMax": r["forceMax"],
+                    "converged": r["forceMax"] < 1e-6, "E_per_site": e, "site_steps_per_s": N * r["iterations"] / dt}
+        lat.close()
+    for name in ("adam", "lbfgs"):
+        lat = lattice(q.FP32)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        if name == "adam":
+            r = lat.adam_run(args.c5_max_iterations, force_cutoff=1e-6)
+        else:
+            r = lat.lbfgs_run(args.c5_max_iterations, force_cutoff=1e-6)
+        torch.cuda.synchronize()
+        dt = time.perf_counter() - t0
+        e, _ = lat.energy()
+        out[name + "_fp32"] = {"time_s": dt, "iterations": r["iterations"], "forceMax": r["forceMax"],
+                               "converged": r["forceMax"] < 1e-6, "E_per_site": e,
+                               "site_steps_per_s": N * r["iterations"] / dt,
+                               "params": "reference defaults (Adam b1 .9 b2 .99 eps 1e-8 dt 1e-4; L-BFGS m 5 eta 1e-4)"}
+        lat.close()
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -481,9 +538,15 @@ def main():
     ap.add_argument("--no-configs", action="store_true", help="skip the c1 and c3 runs")
     ap.add_argument("--lattice", type=int, default=200, help="cube side (profiling of smaller cases)")
     ap.add_argument("--forms", default="both", choices=["both", "fp64", "fp32"])
+    ap.add_argument("--workload", default="c2", choices=["c2", "c5"], help="c5: the 400^3 multi-sphere E-field case")
+    ap.add_argument("--c5-max-iterations", type=int, default=20000)
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", 0))
     world = int(os.environ.get("WORLD_SIZE", 1))
+    if args.workload == "c5":
+        if rank == 0:
+            print(json.dumps(run_c5(args)))
+        return 0
     if args.lattice != 200:
         scale_workload(args.lattice)
 

@@ -33,3 +33,35 @@ def c3_solve(seed, lo=16, hi=64):
     g = Geometry(L, host_random_nematic(L, seed, S0))
     g.add_sphere(centre, r, DEGENERATE_PLANAR, W, S0)
     return dict(L=L, consts=(a, b, c), S0=S0, Q=g.Q, types=g.types, objects=g.objects(), sphere=(centre, r, W))
+
+
+def c5_lattice(side=400, seed=13371, nspheres=8, rmin=10.0, rmax=25.0, gap=2.0):
+    """400^3 box, `nspheres` non-overlapping random homeotropic spheres
+    (r ~ U[rmin, rmax], centres ~ U(box), surfaces at least `gap` sites apart
+    across the periodic box), W = 5.3, L1-L3 = 2.32/1.0/0.5, uniform E field
+    along z (Ez = 0.5, eps = 1, eps0 = 1, deps = 0.5: the reference CLI's
+    dielectric defaults)."""
+    a, b, c, S0 = cli_phase_constants()
+    L = (side, side, side)
+    rng = random.Random(1000003 + seed)
+    spheres = []
+    while len(spheres) < nspheres:
+        r = rng.uniform(rmin, rmax)
+        ctr = tuple(rng.uniform(0.0, L[k]) for k in range(3))
+        ok = True
+        for (c2, r2) in spheres:
+            d2 = 0.0
+            for k in range(3):
+                dk = abs(ctr[k] - c2[k])
+                dk = min(dk, L[k] - dk)
+                d2 += dk * dk
+            if math.sqrt(d2) < r + r2 + gap:
+                ok = False
+                break
+        if ok:
+            spheres.append((ctr, r))
+    g = Geometry(L, host_random_nematic(L, seed, S0))
+    for ctr, r in spheres:
+        g.add_sphere(ctr, r, HOMEOTROPIC, 5.3, S0)
+    return dict(L=L, consts=(a, b, c), S0=S0, Q=g.Q, types=g.types, objects=g.objects(), Ls=(2.32, 1.0, 0.5),
+                E=(0.0, 0.0, 0.5, 1.0, 1.0, 0.5), spheres=spheres)
