@@ -217,6 +217,54 @@ int qmin_batch_fire_init(qmin_batch b, const qmin_fire_params *p);
 int qmin_batch_fire_run(qmin_batch b, int max_iterations, int *iterations, double *force_max, int *converged);
 int qmin_batch_kernel_launches(qmin_batch b, long long *count);
 
+/* ---- learned warm start ----
+ * A 3-D U-Net (4 levels, 32-128 channels, about 0.57M parameters; BF16
+ * weights and activations, FP32 accumulation on the tensor cores) that maps a
+ * lattice's initial Q, object/boundary masks and anchoring kind/strength to a
+ * near-minimal Q, which a minimiser then finishes.  One net object serves
+ * `batch` lattices of Lx x Ly x Lz sites (each side a multiple of 8).  Input
+ * features: [batch][sites][16] BF16; output: [batch][sites][16] FP32 whose
+ * channels 0..4 are the predicted Q (AoS per site).  No reference
+ * counterpart: the reference has no learned component. */
+typedef struct qmin_warmnet_ctx *qmin_warmnet;
+/* train = 0 allocates only what inference needs */
+int qmin_warmnet_create(int batch, int Lx, int Ly, int Lz, int train, qmin_warmnet *out);
+int qmin_warmnet_destroy(qmin_warmnet n);
+/* run on a caller's cudaStream_t (NULL = legacy default stream) */
+int qmin_warmnet_set_stream(qmin_warmnet n, void *stream);
+int qmin_warmnet_param_count(qmin_warmnet n, long long *count);
+int qmin_warmnet_shape(qmin_warmnet n, int *batch, int *Lx, int *Ly, int *Lz);
+/* the net's device buffers: input features, output, training mask */
+int qmin_warmnet_buffers(qmin_warmnet n, void **x, float **y, uint8_t **mask);
+/* FP32 parameters (host, param_count floats); resets the Adam moments */
+int qmin_warmnet_set_params(qmin_warmnet n, const float *host);
+/* FP32 parameters and/or the last backward's gradients (host, may be NULL) */
+int qmin_warmnet_get_params(qmin_warmnet n, float *params, float *grads);
+/* build sample `sample`'s input features from a lattice's device state:
+ * Q_dev SoA planes (QMIN_FP64 or QMIN_FP32, stride plane_stride), int8 types
+ * (qmin_set_state's meaning), host objects (at most 64) */
+int qmin_warmnet_features(qmin_warmnet n, int sample, const void *Q_dev, int precision, long long plane_stride,
+                          const int8_t *types_dev, const qmin_object *objs, int nobj);
+int qmin_warmnet_forward(qmin_warmnet n);
+/* masked mean-squared error of output channels 0..4 against target_dev
+ * ([batch][sites][5] FP32, device) over the sites with type <= 0, and the
+ * gradient of every parameter (overwritten, not accumulated); *loss (host,
+ * may be NULL) waits for the result */
+int qmin_warmnet_backward(qmin_warmnet n, const float *target_dev, double *loss);
+/* one Adam step on the FP32 master parameters (bias-corrected) */
+int qmin_warmnet_adam_step(qmin_warmnet n, double lr, double beta1, double beta2, double eps);
+/* write sample `sample`'s predicted Q into SoA planes on the sites with
+ * type <= 0 (object sites keep their imposed Q) */
+int qmin_warmnet_write_state(qmin_warmnet n, int sample, void *Q_dev, int precision, long long plane_stride,
+                             const int8_t *types_dev);
+int qmin_warmnet_sync(qmin_warmnet n);
+int qmin_warmnet_kernel_launches(qmin_warmnet n, long long *count);
+/* Warm-start a lattice in place: features from its current Q, types and
+ * objects, one forward pass, the prediction written into its Q on the sites
+ * the minimiser moves.  The net must have batch 1 and the lattice's sides.
+ * Call qmin_fire_init (or another minimiser) afterwards. */
+int qmin_warm_start(qmin_handle h, qmin_warmnet n);
+
 /* ---- host-side set-up helpers (the reference runs these on the host even
  *      in GPU runs, openQmin.cpp:261-268) ---- */
 /* qTensorLatticeModel::setNematicQTensorRandomly (qTensorLatticeModel.cpp:134-162)

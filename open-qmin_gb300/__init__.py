@@ -34,7 +34,11 @@ EXPORTED_SYMBOLS = [
     "qmin_host_random_nematic", "qmin_host_add_wall", "qmin_host_add_sphere", "qmin_set_fire_kernel",
     "qmin_fire_profile", "qmin_fire_tuning", "qmin_energy_noalloc", "qmin_batch_create", "qmin_batch_destroy",
     "qmin_batch_set_params", "qmin_batch_set_solve", "qmin_batch_get_solve", "qmin_batch_fire_init",
-    "qmin_batch_fire_run", "qmin_batch_kernel_launches",
+    "qmin_batch_fire_run", "qmin_batch_kernel_launches", "qmin_warmnet_create", "qmin_warmnet_destroy",
+    "qmin_warmnet_set_stream", "qmin_warmnet_param_count", "qmin_warmnet_shape", "qmin_warmnet_buffers",
+    "qmin_warmnet_set_params", "qmin_warmnet_get_params", "qmin_warmnet_features", "qmin_warmnet_forward",
+    "qmin_warmnet_backward", "qmin_warmnet_adam_step", "qmin_warmnet_write_state", "qmin_warmnet_sync",
+    "qmin_warmnet_kernel_launches", "qmin_warm_start",
 ]
 FIRE_SEPARATE, FIRE_FUSED, FIRE_AUTO = 0, 1, 2
 
@@ -107,6 +111,18 @@ def lib():
             "qmin_batch_kernel_launches": [h, C.POINTER(C.c_longlong)],
             "qmin_fire_profile": [h, C.c_int, dp, ip],
             "qmin_fire_tuning": [h, ip, ip, ip, ip, ip, dp],
+            "qmin_warmnet_create": [C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.POINTER(C.c_void_p)],
+            "qmin_warmnet_destroy": [h], "qmin_warmnet_set_stream": [h, vp],
+            "qmin_warmnet_param_count": [h, C.POINTER(C.c_longlong)],
+            "qmin_warmnet_shape": [h, ip, ip, ip, ip],
+            "qmin_warmnet_buffers": [h, C.POINTER(C.c_void_p), C.POINTER(C.c_void_p), C.POINTER(C.c_void_p)],
+            "qmin_warmnet_set_params": [h, vp], "qmin_warmnet_get_params": [h, vp, vp],
+            "qmin_warmnet_features": [h, C.c_int, vp, C.c_int, C.c_longlong, vp, C.POINTER(Object), C.c_int],
+            "qmin_warmnet_forward": [h], "qmin_warmnet_backward": [h, vp, dp],
+            "qmin_warmnet_adam_step": [h, C.c_double, C.c_double, C.c_double, C.c_double],
+            "qmin_warmnet_write_state": [h, C.c_int, vp, C.c_int, C.c_longlong, vp],
+            "qmin_warmnet_sync": [h], "qmin_warmnet_kernel_launches": [h, C.POINTER(C.c_longlong)],
+            "qmin_warm_start": [h, h],
             "qmin_host_add_wall": [C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_double, C.c_double, dp,
                                    ip, C.POINTER(Object), ip],
             "qmin_host_add_sphere": [C.c_int, C.c_int, C.c_int, dp, C.c_double, C.c_int, C.c_double, C.c_double, dp,
@@ -306,6 +322,11 @@ class Lattice:
         _check(lib().qmin_kernel_launches(self._h, C.byref(n)))
         return n.value
 
+    def warm_start(self, net):
+        """Replace Q on the sites the minimiser moves by the net's prediction
+        from the current Q, types and objects (qmin_warm_start)."""
+        _check(lib().qmin_warm_start(self._h, net._h))
+
 
 class Batch:
     """Many independent lattices of uneven sizes minimised together (a qmin_batch)."""
@@ -372,6 +393,136 @@ class Batch:
     def launches(self):
         n = C.c_longlong()
         _check(lib().qmin_batch_kernel_launches(self._h, C.byref(n)))
+        return n.value
+
+
+# Learned warm-start net: (cin, cout, taps, stride, input level, relu) per
+# layer, in the order of its flat parameter vector (weights [cout][tap][cin],
+# then bias [cout]); the table the native library builds.
+WARMNET_LAYERS = [(16, 32, 27, 1, 0, True), (32, 48, 27, 2, 0, True), (48, 64, 27, 2, 1, True),
+                  (64, 128, 27, 2, 2, True), (128, 64, 1, 1, 3, False), (64, 64, 27, 1, 2, True),
+                  (64, 48, 1, 1, 2, False), (48, 48, 27, 1, 1, True), (48, 32, 1, 1, 1, False),
+                  (32, 32, 27, 1, 0, True), (32, 16, 1, 1, 0, False)]
+WARMNET_IN, WARMNET_OUT = 16, 16
+
+
+def warmnet_param_slices():
+    """(weight slice, bias slice, layer spec) of every layer in the flat vector."""
+    out, off = [], 0
+    for spec in WARMNET_LAYERS:
+        cin, cout, taps = spec[0], spec[1], spec[2]
+        w = slice(off, off + cout * taps * cin)
+        off += cout * taps * cin
+        b = slice(off, off + cout)
+        off += cout
+        out.append((w, b, spec))
+    return out
+
+
+def warmnet_init_params(seed=0, head_scale=0.1):
+    """He-normal weights, zero biases; the head starts small."""
+    rng = np.random.default_rng(seed)
+    sl = warmnet_param_slices()
+    p = np.zeros(sl[-1][1].stop, dtype=np.float32)
+    for i, (w, b, (cin, cout, taps, _s, _l, _r)) in enumerate(sl):
+        fan_in = cin * taps
+        if i == 0:
+            fan_in = 10 * taps  # 10 of the 16 input channels carry features
+        std = np.sqrt(2.0 / fan_in) * (head_scale if i == len(sl) - 1 else 1.0)
+        p[w] = rng.normal(0.0, std, w.stop - w.start).astype(np.float32)
+    return p
+
+
+class _DevArray:
+    """A device pointer with __cuda_array_interface__, for zero-copy torch views."""
+
+    def __init__(self, ptr, shape, typestr):
+        self.__cuda_array_interface__ = dict(shape=tuple(shape), typestr=typestr, data=(int(ptr), False), version=2,
+                                             strides=None)
+
+
+class WarmNet:
+    """The learned warm-start net (a qmin_warmnet): `batch` lattices of L sites."""
+
+    def __init__(self, batch, L, train=False):
+        self.batch, self.L = int(batch), tuple(int(x) for x in L)
+        self._h = C.c_void_p()
+        _check(lib().qmin_warmnet_create(self.batch, *self.L, int(bool(train)), C.byref(self._h)))
+        n = C.c_longlong()
+        _check(lib().qmin_warmnet_param_count(self._h, C.byref(n)))
+        self.nparams = n.value
+        self.sites = self.L[0] * self.L[1] * self.L[2]
+
+    def close(self):
+        if self._h:
+            lib().qmin_warmnet_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_stream(self, stream_ptr):
+        _check(lib().qmin_warmnet_set_stream(self._h, C.c_void_p(stream_ptr)))
+
+    def set_params(self, p):
+        p = np.ascontiguousarray(p, dtype=np.float32)
+        assert p.size == self.nparams
+        _check(lib().qmin_warmnet_set_params(self._h, p.ctypes.data))
+
+    def get_params(self, grads=False):
+        p = np.zeros(self.nparams, dtype=np.float32)
+        g = np.zeros(self.nparams, dtype=np.float32) if grads else None
+        _check(lib().qmin_warmnet_get_params(self._h, p.ctypes.data, g.ctypes.data if grads else None))
+        return (p, g) if grads else p
+
+    def buffers(self):
+        """Device pointers of the input features, output and mask."""
+        x, y, m = C.c_void_p(), C.c_void_p(), C.c_void_p()
+        _check(lib().qmin_warmnet_buffers(self._h, C.byref(x), C.byref(y), C.byref(m)))
+        return x.value, y.value, m.value
+
+    def torch_views(self):
+        """Zero-copy torch views (x as bfloat16 [B, sites, 16], y float32
+        [B, sites, 16], mask uint8 [B, sites]) of the net's device buffers."""
+        import torch
+        x, y, m = self.buffers()
+        B, n = self.batch, self.sites
+        xv = torch.as_tensor(_DevArray(x, (B, n, WARMNET_IN), "<i2"), device="cuda").view(torch.bfloat16)
+        yv = torch.as_tensor(_DevArray(y, (B, n, WARMNET_OUT), "<f4"), device="cuda")
+        mv = torch.as_tensor(_DevArray(m, (B, n), "|u1"), device="cuda")
+        return xv, yv, mv
+
+    def features(self, sample, q_ptr, precision, plane_stride, types_ptr, objs):
+        arr = (Object * max(len(objs), 1))()
+        for k, (kind, W, S0) in enumerate(objs):
+            arr[k].kind, arr[k].W, arr[k].S0 = kind, W, S0
+        _check(lib().qmin_warmnet_features(self._h, int(sample), C.c_void_p(q_ptr), int(precision),
+                                           int(plane_stride), C.c_void_p(types_ptr), arr, len(objs)))
+
+    def forward(self):
+        _check(lib().qmin_warmnet_forward(self._h))
+
+    def backward(self, target_ptr, want_loss=True):
+        loss = C.c_double(float("nan"))
+        _check(lib().qmin_warmnet_backward(self._h, C.c_void_p(target_ptr), C.byref(loss) if want_loss else None))
+        return loss.value if want_loss else None
+
+    def adam_step(self, lr, beta1=0.9, beta2=0.999, eps=1e-8):
+        _check(lib().qmin_warmnet_adam_step(self._h, lr, beta1, beta2, eps))
+
+    def write_state(self, sample, q_ptr, precision, plane_stride, types_ptr):
+        _check(lib().qmin_warmnet_write_state(self._h, int(sample), C.c_void_p(q_ptr), int(precision),
+                                              int(plane_stride), C.c_void_p(types_ptr)))
+
+    def sync(self):
+        _check(lib().qmin_warmnet_sync(self._h))
+
+    def launches(self):
+        n = C.c_longlong()
+        _check(lib().qmin_warmnet_kernel_launches(self._h, C.byref(n)))
         return n.value
 
 

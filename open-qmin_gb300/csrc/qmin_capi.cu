@@ -954,3 +954,21 @@ int qmin_fire_tuning(qmin_handle h, int *path, int *variant, int *tile_x, int *t
         for (int k = 0; k < kSepVariants + 2 * kFusedConfigs; ++k) ms[k] = h->tune_ms[k];
     return QMIN_OK;
 }
+
+int qmin_warm_start(qmin_handle h, qmin_warmnet n)
+{
+    int rc = ready(h, "qmin_warm_start");
+    if (rc) return rc;
+    int b = 0, x = 0, y = 0, z = 0;
+    rc = qmin_warmnet_shape(n, &b, &x, &y, &z);
+    if (rc) return rc;
+    if (b != 1 || x != h->Lx || y != h->Ly || z != h->Lz)
+        return fail(QMIN_EINVAL, "qmin_warm_start: the net needs batch 1 and the lattice's sides");
+    CK(cudaStreamSynchronize(h->stream));
+    rc = qmin_warmnet_features(n, 0, h->Q, h->prec, h->P, h->types, h->objs_host.data(), (int)h->objs_host.size());
+    if (!rc) rc = qmin_warmnet_forward(n);
+    if (!rc) rc = qmin_warmnet_write_state(n, 0, h->Q, h->prec, h->P, h->types);
+    if (!rc) rc = qmin_warmnet_sync(n);
+    h->fire_ready = false;
+    return rc;
+}

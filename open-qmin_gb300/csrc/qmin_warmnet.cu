@@ -1,0 +1,889 @@
+// Learned warm start: a small 3-D U-Net that maps (random initial Q, object
+// and boundary masks, anchoring kind and strength) to a near-minimal Q field,
+// which FIRE then finishes.  No reference counterpart: the reference has no
+// learned component.
+//
+// Layout: activations channels-last, [sample][z][y][x][channel]; every
+// tensor-core operand BF16, every accumulator and gradient FP32.  Each
+// convolution (3x3x3 or 1x1x1, stride 1 or 2, zero padding) is an implicit
+// GEMM on the BF16 tensor cores (mma.sync m16n8k16, FP32 accumulate):
+//   forward:      out[v][co]      = sum_{tap,ci} in[src(v,tap)][ci] * W[co][tap][ci]
+//   data grad:    din[u][ci]      = sum_{tap,co} dout[src'(u,tap)][co] * W'[ci][tap][co]
+//   weight grad:  dW[co][tap][ci] = sum_v dout[v][co] * in[src(v,tap)][ci]
+//
+// Network (levels l = 0..3 have grid (Lx, Ly, Lz) >> l):
+//   0 enc0  3^3 s1 16->32 (l0) | 1 enc1 3^3 s2 32->48 (l1) | 2 enc2 3^3 s2 48->64 (l2)
+//   3 enc3  3^3 s2 64->128 (l3)
+//   4 dec2a 1^3 128->64 (l3), x2 nearest up + enc2 -> 5 dec2b 3^3 64->64 (l2)
+//   6 dec1a 1^3 64->48 (l2),  x2 up + enc1        -> 7 dec1b 3^3 48->48 (l1)
+//   8 dec0a 1^3 48->32 (l1),  x2 up + enc0        -> 9 dec0b 3^3 32->32 (l0)
+//  10 head  1^3 32->16 (l0), no ReLU; channels 0..4 are the predicted Q
+// ReLU after every 3^3 convolution; the 1^3 convolutions before an
+// upsampling are linear, so they run on the coarse grid (they commute with
+// nearest upsampling).
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "../../include/qmin_gb300.h"
+#include "qmin_internal.h"
+
+namespace qmin {
+namespace nn {
+
+typedef __nv_bfloat16 bf16;
+
+constexpr int kIn = 16;     // input channels (10 used)
+constexpr int kOut = 16;    // head channels (5 used)
+constexpr int kLayers = 11;
+constexpr int kMaxObj = 64;
+
+struct Geo {
+    int Di, Hi, Wi;  // gathered (input) grid: z, y, x
+    int Do, Ho, Wo;  // GEMM-row (output) grid
+    int cin;         // channels of the gathered tensor (multiple of 16)
+    int cout;        // GEMM columns (multiple of 8)
+    int taps;        // 27 or 1
+    int stride;      // 1 or 2
+    int mode;        // 0 forward gather; 1 the transposed gather of a stride-2 conv
+};
+
+// flat source voxel (sample offset included) of GEMM row r for one tap, or -1
+__device__ __forceinline__ int gather_src(const Geo &g, int r, int tap)
+{
+    const int vo = g.Do * g.Ho * g.Wo;
+    const int b = r / vo;
+    int rem = r - b * vo;
+    const int ox = rem % g.Wo;
+    rem /= g.Wo;
+    const int oy = rem % g.Ho;
+    const int oz = rem / g.Ho;
+    int kx = 0, ky = 0, kz = 0, pad = 0;
+    if (g.taps == 27) {
+        kx = tap % 3;
+        ky = (tap / 3) % 3;
+        kz = tap / 9;
+        pad = 1;
+    }
+    int ix, iy, iz;
+    if (g.mode == 0) {
+        ix = ox * g.stride + kx - pad;
+        iy = oy * g.stride + ky - pad;
+        iz = oz * g.stride + kz - pad;
+    } else {
+        const int tx = ox + pad - kx, ty = oy + pad - ky, tz = oz + pad - kz;
+        if ((tx | ty | tz) & 1) return -1;
+        ix = tx >> 1;
+        iy = ty >> 1;
+        iz = tz >> 1;
+    }
+    if (ix < 0 || iy < 0 || iz < 0 || ix >= g.Wi || iy >= g.Hi || iz >= g.Di) return -1;
+    return ((b * g.Di + iz) * g.Hi + iy) * g.Wi + ix;
+}
+
+__device__ __forceinline__ uint32_t ld32(const bf16 *p) { return *reinterpret_cast<const uint32_t *>(p); }
+
+__device__ __forceinline__ void mma_bf16(float (&d)[4], uint32_t a0, uint32_t a1, uint32_t a2, uint32_t a3,
+                                         uint32_t b0, uint32_t b1)
+{
+    asm volatile(
+        "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+        "{%0,%1,%2,%3};\n"
+        : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
+        : "r"(a0), "r"(a1), "r"(a2), "r"(a3), "r"(b0), "r"(b1));
+}
+
+// C[rows][NT*8] = gather(in)[rows][taps*cin] x W^T with W row-major
+// [NT*8][taps*cin] (BF16).  One warp owns 16 rows and every column; 4 warps a
+// block.  Epilogue: + bias, ReLU, + addend (FP32 outputs), store FP32 or BF16.
+template <int NT, bool OUT_BF16>
+__global__ void __launch_bounds__(128) k_conv_gemm(Geo g, const bf16 *__restrict__ in, const bf16 *__restrict__ w,
+                                                   const float *__restrict__ bias, const float *__restrict__ addend,
+                                                   void *out, int relu, int rows)
+{
+    const int warp = blockIdx.x * 4 + (threadIdx.x >> 5);
+    const int lane = threadIdx.x & 31, gq = lane >> 2, t4 = lane & 3;
+    if (warp * 16 >= rows) return;
+    const int r0 = warp * 16 + gq, r1 = r0 + 8;
+    float acc[NT][4];
+#pragma unroll
+    for (int j = 0; j < NT; ++j) acc[j][0] = acc[j][1] = acc[j][2] = acc[j][3] = 0.f;
+    const int K = g.taps * g.cin;
+    for (int tap = 0; tap < g.taps; ++tap) {
+        const int s0 = r0 < rows ? gather_src(g, r0, tap) : -1;
+        const int s1 = r1 < rows ? gather_src(g, r1, tap) : -1;
+        const bf16 *p0 = in + (size_t)(s0 < 0 ? 0 : s0) * g.cin + 2 * t4;
+        const bf16 *p1 = in + (size_t)(s1 < 0 ? 0 : s1) * g.cin + 2 * t4;
+        const bf16 *wt = w + (size_t)gq * K + tap * g.cin + 2 * t4;
+        for (int c0 = 0; c0 < g.cin; c0 += 16) {
+            const uint32_t a0 = s0 >= 0 ? ld32(p0 + c0) : 0u;
+            const uint32_t a1 = s1 >= 0 ? ld32(p1 + c0) : 0u;
+            const uint32_t a2 = s0 >= 0 ? ld32(p0 + c0 + 8) : 0u;
+            const uint32_t a3 = s1 >= 0 ? ld32(p1 + c0 + 8) : 0u;
+#pragma unroll
+            for (int j = 0; j < NT; ++j) {
+                const bf16 *wr = wt + (size_t)(8 * j) * K + c0;
+                mma_bf16(acc[j], a0, a1, a2, a3, ld32(wr), ld32(wr + 8));
+            }
+        }
+    }
+    constexpr int cout = NT * 8;
+#pragma unroll
+    for (int j = 0; j < NT; ++j) {
+        const int col = 8 * j + 2 * t4;
+        const float bb0 = bias ? bias[col] : 0.f, bb1 = bias ? bias[col + 1] : 0.f;
+        float v[4] = {acc[j][0] + bb0, acc[j][1] + bb1, acc[j][2] + bb0, acc[j][3] + bb1};
+        if (relu)
+#pragma unroll
+            for (int e = 0; e < 4; ++e) v[e] = fmaxf(v[e], 0.f);
+        if (OUT_BF16) {
+            bf16 *o = reinterpret_cast<bf16 *>(out);
+            if (r0 < rows)
+                *reinterpret_cast<__nv_bfloat162 *>(o + (size_t)r0 * cout + col) = __floats2bfloat162_rn(v[0], v[1]);
+            if (r1 < rows)
+                *reinterpret_cast<__nv_bfloat162 *>(o + (size_t)r1 * cout + col) = __floats2bfloat162_rn(v[2], v[3]);
+        } else {
+            float *o = reinterpret_cast<float *>(out);
+            if (addend) {
+                if (r0 < rows) {
+                    const float2 a = *reinterpret_cast<const float2 *>(addend + (size_t)r0 * cout + col);
+                    v[0] += a.x;
+                    v[1] += a.y;
+                }
+                if (r1 < rows) {
+                    const float2 a = *reinterpret_cast<const float2 *>(addend + (size_t)r1 * cout + col);
+                    v[2] += a.x;
+                    v[3] += a.y;
+                }
+            }
+            if (r0 < rows) *reinterpret_cast<float2 *>(o + (size_t)r0 * cout + col) = make_float2(v[0], v[1]);
+            if (r1 < rows) *reinterpret_cast<float2 *>(o + (size_t)r1 * cout + col) = make_float2(v[2], v[3]);
+        }
+    }
+}
+
+// dW[co][tap][ci] += sum_v dout[v][co] * in[src(v,tap)][ci] over rows
+// [blockIdx.x * chunk, +chunk): block tile 64 co x 64 ci for one tap, the
+// row dimension staged through shared memory 16 rows at a time; each block
+// adds its partial tile into dW with FP32 atomics.
+__global__ void __launch_bounds__(128) k_conv_wgrad(Geo g, const bf16 *__restrict__ dout, const bf16 *__restrict__ in,
+                                                    float *__restrict__ dw, int rows, int chunk)
+{
+    __shared__ __align__(16) bf16 sA[16][72];  // dout slab [row][co]
+    __shared__ __align__(16) bf16 sB[16][72];  // gathered input slab [row][ci]
+    const int tap = blockIdx.y;
+    const int ntc = (g.cout + 63) / 64;
+    const int co0 = (blockIdx.z % ntc) * 64, ci0 = (blockIdx.z / ntc) * 64;
+    const int vbeg = blockIdx.x * chunk, vend = min(rows, vbeg + chunk);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, gq = lane >> 2, t4 = lane & 3;
+    float acc[8][4];
+#pragma unroll
+    for (int j = 0; j < 8; ++j) acc[j][0] = acc[j][1] = acc[j][2] = acc[j][3] = 0.f;
+    const int rr = threadIdx.x >> 3, cc = (threadIdx.x & 7) * 8;
+    const bool coin = co0 + cc < g.cout, ciin = ci0 + cc < g.cin;  // channel counts are multiples of 8
+    for (int v0 = vbeg; v0 < vend; v0 += 16) {
+        const int v = v0 + rr;
+        const int src = v < vend ? gather_src(g, v, tap) : -1;
+        uint4 a = make_uint4(0u, 0u, 0u, 0u), b = make_uint4(0u, 0u, 0u, 0u);
+        if (v < vend && coin) a = *reinterpret_cast<const uint4 *>(dout + (size_t)v * g.cout + co0 + cc);
+        if (src >= 0 && ciin) b = *reinterpret_cast<const uint4 *>(in + (size_t)src * g.cin + ci0 + cc);
+        *reinterpret_cast<uint4 *>(&sA[rr][cc]) = a;
+        *reinterpret_cast<uint4 *>(&sB[rr][cc]) = b;
+        __syncthreads();
+        auto pk = [](bf16 lo, bf16 hi) {
+            return (uint32_t)__bfloat16_as_ushort(lo) | ((uint32_t)__bfloat16_as_ushort(hi) << 16);
+        };
+        const int m = 16 * warp;
+        const uint32_t a0 = pk(sA[2 * t4][m + gq], sA[2 * t4 + 1][m + gq]);
+        const uint32_t a1 = pk(sA[2 * t4][m + gq + 8], sA[2 * t4 + 1][m + gq + 8]);
+        const uint32_t a2 = pk(sA[2 * t4 + 8][m + gq], sA[2 * t4 + 9][m + gq]);
+        const uint32_t a3 = pk(sA[2 * t4 + 8][m + gq + 8], sA[2 * t4 + 9][m + gq + 8]);
+#pragma unroll
+        for (int j = 0; j < 8; ++j) {
+            const int n = 8 * j + gq;
+            const uint32_t b0 = pk(sB[2 * t4][n], sB[2 * t4 + 1][n]);
+            const uint32_t b1 = pk(sB[2 * t4 + 8][n], sB[2 * t4 + 9][n]);
+            mma_bf16(acc[j], a0, a1, a2, a3, b0, b1);
+        }
+        __syncthreads();
+    }
+    const int K = g.taps * g.cin;
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+        const int ci = ci0 + 8 * j + 2 * t4;
+        const int coA = co0 + 16 * warp + gq, coB = coA + 8;
+        if (ci < g.cin) {
+            if (coA < g.cout) {
+                atomicAdd(dw + (size_t)coA * K + tap * g.cin + ci, acc[j][0]);
+                atomicAdd(dw + (size_t)coA * K + tap * g.cin + ci + 1, acc[j][1]);
+            }
+            if (coB < g.cout) {
+                atomicAdd(dw + (size_t)coB * K + tap * g.cin + ci, acc[j][2]);
+                atomicAdd(dw + (size_t)coB * K + tap * g.cin + ci + 1, acc[j][3]);
+            }
+        }
+    }
+}
+
+// ------------------------------------------------------------ elementwise
+#define GRID_STRIDE(i, n) \
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < (n); i += (long long)gridDim.x * blockDim.x)
+
+__global__ void k_f32_to_bf16(const float *x, bf16 *y, long long n)
+{
+    GRID_STRIDE(i, n) y[i] = __float2bfloat16(x[i]);
+}
+
+// gradient through the ReLU (mask from the stored BF16 activation), as BF16
+__global__ void k_relu_grad_bf16(const float *g, const bf16 *act, bf16 *y, long long n)
+{
+    GRID_STRIDE(i, n) y[i] = __float2bfloat16(__bfloat162float(act[i]) > 0.f ? g[i] : 0.f);
+}
+
+// data-gradient weights: Wd[ci][tap'][co] = W[co][tap][ci], tap' = 26 - tap
+// for a stride-1 3^3 convolution (flip), tap' = tap otherwise
+__global__ void k_dgrad_weights(const bf16 *w, bf16 *wd, int cout, int cin, int taps, int flip)
+{
+    const long long n = (long long)cout * cin * taps;
+    GRID_STRIDE(i, n)
+    {
+        const int ci = (int)(i % cin), tap = (int)((i / cin) % taps), co = (int)(i / ((long long)cin * taps));
+        const int tp = flip ? taps - 1 - tap : tap;
+        wd[((size_t)ci * taps + tp) * cout + co] = w[i];
+    }
+}
+
+struct Dims {
+    int B, x, y, z;  // coarse grid
+};
+
+// nearest x2 upsampling of h (coarse, FP32) plus a BF16 skip on the fine grid, into BF16
+__global__ void k_up2_add(const float *h, const bf16 *skip, bf16 *out, Dims d, int c)
+{
+    const int X = 2 * d.x, Y = 2 * d.y, Z = 2 * d.z;
+    const long long n = (long long)d.B * X * Y * Z * c;
+    GRID_STRIDE(i, n)
+    {
+        const int ch = (int)(i % c);
+        long long v = i / c;
+        const int x = (int)(v % X);
+        v /= X;
+        const int y = (int)(v % Y);
+        v /= Y;
+        const int z = (int)(v % Z);
+        const int b = (int)(v / Z);
+        const long long src = (((long long)b * d.z + z / 2) * d.y + y / 2) * d.x + x / 2;
+        out[i] = __float2bfloat16(h[src * c + ch] + __bfloat162float(skip[i]));
+    }
+}
+
+// gradient of nearest x2 upsampling: the sum over the 8 children
+__global__ void k_up2_grad(const float *g2, float *g, Dims d, int c)
+{
+    const int X = 2 * d.x, Y = 2 * d.y, Z = 2 * d.z;
+    const long long n = (long long)d.B * d.x * d.y * d.z * c;
+    GRID_STRIDE(i, n)
+    {
+        const int ch = (int)(i % c);
+        long long v = i / c;
+        const int x = (int)(v % d.x);
+        v /= d.x;
+        const int y = (int)(v % d.y);
+        v /= d.y;
+        const int z = (int)(v % d.z);
+        const int b = (int)(v / d.z);
+        float s = 0.f;
+        for (int dz = 0; dz < 2; ++dz)
+            for (int dy = 0; dy < 2; ++dy)
+                for (int dx = 0; dx < 2; ++dx)
+                    s += g2[((((long long)b * Z + 2 * z + dz) * Y + 2 * y + dy) * X + 2 * x + dx) * c + ch];
+        g[i] = s;
+    }
+}
+
+// bias gradient db[c] += sum_v g[v][c] (masked by the ReLU when act != NULL);
+// one block per (row chunk, 32-channel group), a thread per channel and row lane
+__global__ void k_bias_grad(const float *g, const bf16 *act, float *db, long long rows, int c)
+{
+    const int ch = blockIdx.y * 32 + (threadIdx.x & 31);
+    const int lanes = blockDim.x >> 5;
+    float s = 0.f;
+    if (ch < c) {
+        for (long long v = blockIdx.x * (long long)lanes + (threadIdx.x >> 5); v < rows; v += (long long)gridDim.x * lanes) {
+            const float x = g[v * c + ch];
+            s += (act == nullptr || __bfloat162float(act[v * c + ch]) > 0.f) ? x : 0.f;
+        }
+        atomicAdd(db + ch, s);
+    }
+}
+
+__global__ void k_count_mask(const uint8_t *mask, long long n, unsigned long long *count)
+{
+    unsigned long long s = 0;
+    GRID_STRIDE(i, n) s += mask[i] ? 1u : 0u;
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+    if ((threadIdx.x & 31) == 0 && s) atomicAdd(count, s);
+}
+
+// masked mean-squared error over the 5 Q channels of y [rows][16]:
+// loss = sum_{masked v, k<5} (y - t)^2 / count; dy = 2 (y - t) / count (0 elsewhere)
+__global__ void k_mse(const float *y, const float *t, const uint8_t *mask, const unsigned long long *count, float *dy,
+                      double *loss, long long rows)
+{
+    const double inv = 1.0 / (double)max(*count, 1ull);
+    double s = 0.0;
+    GRID_STRIDE(v, rows)
+    {
+        const bool m = mask[v] != 0;
+#pragma unroll
+        for (int k = 0; k < kOut; ++k) {
+            float d = 0.f;
+            if (k < 5 && m) d = y[v * kOut + k] - t[v * 5 + k];
+            dy[v * kOut + k] = (float)(2.0 * d * inv);
+            s += (double)d * d;
+        }
+    }
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+    if ((threadIdx.x & 31) == 0) atomicAdd(loss, s * inv);
+}
+
+// Adam on the FP32 master parameters, refreshing their BF16 copies
+__global__ void k_adam_params(float *p, const float *g, float *m, float *v, bf16 *pb, long long n, float lr, float b1,
+                              float b2, float eps, float c1, float c2)
+{
+    GRID_STRIDE(i, n)
+    {
+        const float gi = g[i];
+        const float mi = b1 * m[i] + (1.f - b1) * gi;
+        const float vi = b2 * v[i] + (1.f - b2) * gi * gi;
+        m[i] = mi;
+        v[i] = vi;
+        const float pi = p[i] - lr * (mi * c1) / (sqrtf(vi * c2) + eps);
+        p[i] = pi;
+        pb[i] = __float2bfloat16(pi);
+    }
+}
+
+struct ObjTab {
+    int n;
+    int kind[kMaxObj];
+    float W[kMaxObj];
+};
+
+// input features of one sample: channels 0..4 Q (the initial field, which on
+// object sites is the imposed anchoring Q), 5 object site, 6 boundary site
+// (type -1), 7 W/10 of the site's object, 8 homeotropic object, 9 degenerate
+// planar object, 10..15 zero; mask = 1 on the sites the minimiser moves (type <= 0)
+template <class T>
+__global__ void k_features(const T *Q, long long P, const int8_t *types, int N, ObjTab objs, bf16 *x, uint8_t *mask)
+{
+    GRID_STRIDE(i, (long long)N)
+    {
+        const int t = types[i];
+        float f[kIn];
+#pragma unroll
+        for (int k = 0; k < kIn; ++k) f[k] = 0.f;
+#pragma unroll
+        for (int k = 0; k < 5; ++k) f[k] = (float)Q[k * P + i];
+        if (t > 0) {
+            f[5] = 1.f;
+            if (t - 1 < objs.n) {
+                f[7] = 0.1f * objs.W[t - 1];
+                f[8] = objs.kind[t - 1] == QMIN_HOMEOTROPIC ? 1.f : 0.f;
+                f[9] = objs.kind[t - 1] == QMIN_DEGENERATE_PLANAR ? 1.f : 0.f;
+            }
+        } else if (t == -1) {
+            f[6] = 1.f;
+        }
+        uint4 pk[2];
+        __nv_bfloat162 *h = reinterpret_cast<__nv_bfloat162 *>(pk);
+#pragma unroll
+        for (int k = 0; k < kIn / 2; ++k) h[k] = __floats2bfloat162_rn(f[2 * k], f[2 * k + 1]);
+        uint4 *dst = reinterpret_cast<uint4 *>(x + (size_t)i * kIn);
+        dst[0] = pk[0];
+        dst[1] = pk[1];
+        if (mask) mask[i] = t <= 0 ? 1 : 0;
+    }
+}
+
+// predicted Q (channels 0..4 of y) into the SoA planes on the sites the
+// minimiser moves; object sites keep their imposed Q
+template <class T>
+__global__ void k_write_state(const float *y, T *Q, long long P, const int8_t *types, int N)
+{
+    GRID_STRIDE(i, (long long)N)
+    {
+        if (types[i] > 0) continue;
+#pragma unroll
+        for (int k = 0; k < 5; ++k) Q[k * P + i] = (T)y[(size_t)i * kOut + k];
+    }
+}
+
+static int grid1(long long n) { return (int)std::max<long long>(1, std::min<long long>((n + 255) / 256, 152 * 16)); }
+
+template <bool OB>
+static void conv_gemm(const Geo &g, const bf16 *in, const bf16 *w, const float *bias, const float *addend, void *out,
+                      int relu, int rows, cudaStream_t s)
+{
+    const int blocks = (rows + 63) / 64;
+    switch (g.cout / 8) {
+    case 2: k_conv_gemm<2, OB><<<blocks, 128, 0, s>>>(g, in, w, bias, addend, out, relu, rows); break;
+    case 4: k_conv_gemm<4, OB><<<blocks, 128, 0, s>>>(g, in, w, bias, addend, out, relu, rows); break;
+    case 6: k_conv_gemm<6, OB><<<blocks, 128, 0, s>>>(g, in, w, bias, addend, out, relu, rows); break;
+    case 8: k_conv_gemm<8, OB><<<blocks, 128, 0, s>>>(g, in, w, bias, addend, out, relu, rows); break;
+    case 16: k_conv_gemm<16, OB><<<blocks, 128, 0, s>>>(g, in, w, bias, addend, out, relu, rows); break;
+    default: break;
+    }
+}
+
+struct Layer {
+    int cin, cout, taps, stride, level;  // level of the input grid
+    bool relu;
+    size_t woff, boff;  // offsets into the flat parameter vector
+};
+
+}  // namespace nn
+}  // namespace qmin
+
+using namespace qmin::nn;
+
+struct qmin_warmnet_ctx {
+    int B = 1, Lx = 0, Ly = 0, Lz = 0;
+    bool train = false;
+    Layer layers[kLayers];
+    size_t nparams = 0;
+    float *p = nullptr, *g = nullptr, *m = nullptr, *v = nullptr;  // FP32 master, gradients, Adam moments
+    bf16 *pb = nullptr;                                           // BF16 weights
+    bf16 *wd = nullptr;                                           // data-gradient weights (scratch)
+    bf16 *x = nullptr;                                            // input features [B][sites][16]
+    uint8_t *mask = nullptr;                                      // [B][sites]
+    float *y = nullptr;                                           // output [B][sites][16]
+    bf16 *act[kLayers] = {};                                      // BF16 layer outputs (0..9)
+    float *pre[kLayers] = {};                                     // FP32 outputs of 4, 6, 8
+    float *sk[3] = {};                                            // skip gradients of levels 0..2
+    float *gA = nullptr, *gB = nullptr;
+    bf16 *gbf = nullptr;
+    double *loss = nullptr;
+    unsigned long long *count = nullptr;
+    cudaStream_t stream = nullptr;
+    bool own_stream = false;
+    long long adam_t = 0;
+    long long launches = 0;
+};
+
+namespace {
+
+int nfail(int code, const std::string &m)
+{
+    qmin::g_last_error = m;
+    return code;
+}
+
+long long sites(const qmin_warmnet_ctx *n, int level)
+{
+    return (long long)(n->Lx >> level) * (n->Ly >> level) * (n->Lz >> level);
+}
+long long rows_at(const qmin_warmnet_ctx *n, int level) { return n->B * sites(n, level); }
+Dims dims_at(const qmin_warmnet_ctx *n, int level) { return Dims{n->B, n->Lx >> level, n->Ly >> level, n->Lz >> level}; }
+
+void build_layers(qmin_warmnet_ctx *n)
+{
+    struct Spec {
+        int cin, cout, taps, stride, level;
+        bool relu;
+    };
+    const Spec s[kLayers] = {{kIn, 32, 27, 1, 0, true}, {32, 48, 27, 2, 0, true},  {48, 64, 27, 2, 1, true},
+                             {64, 128, 27, 2, 2, true}, {128, 64, 1, 1, 3, false}, {64, 64, 27, 1, 2, true},
+                             {64, 48, 1, 1, 2, false},  {48, 48, 27, 1, 1, true},  {48, 32, 1, 1, 1, false},
+                             {32, 32, 27, 1, 0, true},  {32, kOut, 1, 1, 0, false}};
+    size_t off = 0;
+    for (int i = 0; i < kLayers; ++i) {
+        Layer &L = n->layers[i];
+        L.cin = s[i].cin;
+        L.cout = s[i].cout;
+        L.taps = s[i].taps;
+        L.stride = s[i].stride;
+        L.level = s[i].level;
+        L.relu = s[i].relu;
+        L.woff = off;
+        off += (size_t)L.cout * L.taps * L.cin;
+        L.boff = off;
+        off += L.cout;
+    }
+    n->nparams = off;
+}
+
+int out_level(const Layer &L) { return L.level + (L.stride == 2 ? 1 : 0); }
+
+Geo fwd_geo(const qmin_warmnet_ctx *n, const Layer &L)
+{
+    const Dims di = dims_at(n, L.level), dd = dims_at(n, out_level(L));
+    Geo g;
+    g.Di = di.z;
+    g.Hi = di.y;
+    g.Wi = di.x;
+    g.Do = dd.z;
+    g.Ho = dd.y;
+    g.Wo = dd.x;
+    g.cin = L.cin;
+    g.cout = L.cout;
+    g.taps = L.taps;
+    g.stride = L.stride;
+    g.mode = 0;
+    return g;
+}
+
+int check_launch(qmin_warmnet_ctx *n, const char *what, int nk)
+{
+    n->launches += nk;
+    const cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return nfail(QMIN_ECUDA, std::string(what) + ": " + cudaGetErrorString(e));
+    return QMIN_OK;
+}
+
+// forward of layer i: BF16 output into act[i], or FP32 into `f32out`
+void run_layer(qmin_warmnet_ctx *n, int i, const bf16 *in, float *f32out)
+{
+    const Layer &L = n->layers[i];
+    const Geo g = fwd_geo(n, L);
+    const int rows = (int)rows_at(n, out_level(L));
+    if (f32out) conv_gemm<false>(g, in, n->pb + L.woff, n->p + L.boff, nullptr, f32out, L.relu, rows, n->stream);
+    else conv_gemm<true>(g, in, n->pb + L.woff, n->p + L.boff, nullptr, n->act[i], L.relu, rows, n->stream);
+}
+
+// backward of layer i: gout is the FP32 gradient w.r.t. the layer's output
+// (after its ReLU); accumulates the weight and bias gradients and, if gin is
+// given, writes the gradient w.r.t. the layer's input (+ addend) into gin
+void layer_backward(qmin_warmnet_ctx *n, int i, const float *gout, const bf16 *act_in, float *gin, const float *addend)
+{
+    cudaStream_t s = n->stream;
+    const Layer &L = n->layers[i];
+    const long long rows_out = rows_at(n, out_level(L)), rows_in = rows_at(n, L.level);
+    const bf16 *act_out = L.relu ? n->act[i] : nullptr;
+    const long long ne = rows_out * L.cout;
+    if (act_out) k_relu_grad_bf16<<<grid1(ne), 256, 0, s>>>(gout, act_out, n->gbf, ne);
+    else k_f32_to_bf16<<<grid1(ne), 256, 0, s>>>(gout, n->gbf, ne);
+    k_bias_grad<<<dim3((unsigned)std::min<long long>((rows_out + 7) / 8, 1024), (unsigned)((L.cout + 31) / 32)), 256, 0,
+                  s>>>(gout, act_out, n->g + L.boff, rows_out, L.cout);
+    const Geo g = fwd_geo(n, L);
+    {
+        const int tiles = ((L.cout + 63) / 64) * ((L.cin + 63) / 64);
+        const long long want = std::max<long long>(1, 152 * 8 / (L.taps * tiles));
+        long long chunk = (rows_out + want - 1) / want;
+        chunk = std::max<long long>(256, (chunk + 15) / 16 * 16);
+        const dim3 grid((unsigned)((rows_out + chunk - 1) / chunk), (unsigned)L.taps, (unsigned)tiles);
+        k_conv_wgrad<<<grid, 128, 0, s>>>(g, n->gbf, act_in, n->g + L.woff, (int)rows_out, (int)chunk);
+    }
+    n->launches += 3;
+    if (!gin) return;
+    Geo d;
+    d.Di = g.Do;
+    d.Hi = g.Ho;
+    d.Wi = g.Wo;
+    d.Do = g.Di;
+    d.Ho = g.Hi;
+    d.Wo = g.Wi;
+    d.cin = L.cout;
+    d.cout = L.cin;
+    d.taps = L.taps;
+    d.stride = L.stride;
+    d.mode = L.stride == 2 ? 1 : 0;
+    const int flip = (L.stride == 1 && L.taps == 27) ? 1 : 0;
+    k_dgrad_weights<<<grid1((long long)L.cout * L.cin * L.taps), 256, 0, s>>>(n->pb + L.woff, n->wd, L.cout, L.cin,
+                                                                              L.taps, flip);
+    conv_gemm<false>(d, n->gbf, n->wd, nullptr, addend, gin, 0, (int)rows_in, s);
+    n->launches += 2;
+}
+
+template <class T>
+int features_impl(qmin_warmnet_ctx *n, int sample, const T *Q, long long P, const int8_t *types,
+                  const qmin_object *objs, int nobj)
+{
+    ObjTab tab;
+    tab.n = nobj;
+    for (int k = 0; k < nobj; ++k) {
+        tab.kind[k] = objs[k].kind;
+        tab.W[k] = (float)objs[k].W;
+    }
+    const long long N = sites(n, 0);
+    k_features<T><<<grid1(N), 256, 0, n->stream>>>(Q, P, types, (int)N, tab, n->x + (size_t)sample * N * kIn,
+                                                   n->mask ? n->mask + (size_t)sample * N : nullptr);
+    return check_launch(n, "qmin_warmnet_features", 1);
+}
+
+}  // namespace
+
+int qmin_warmnet_create(int batch, int Lx, int Ly, int Lz, int train, qmin_warmnet *out)
+{
+    if (!out) return nfail(QMIN_EINVAL, "qmin_warmnet_create: null output handle");
+    *out = nullptr;
+    if (batch < 1 || Lx < 8 || Ly < 8 || Lz < 8 || (Lx | Ly | Lz) % 8 != 0)
+        return nfail(QMIN_EINVAL, "qmin_warmnet_create: batch >= 1 and every side a positive multiple of 8");
+    if ((long long)batch * Lx * Ly * Lz > (1ll << 30))
+        return nfail(QMIN_EINVAL, "qmin_warmnet_create: batch x sites above 2^30");
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+        cudaGetLastError();
+        return nfail(QMIN_ENODEVICE, "qmin_warmnet_create: no CUDA device available");
+    }
+    auto *n = new qmin_warmnet_ctx();
+    n->B = batch;
+    n->Lx = Lx;
+    n->Ly = Ly;
+    n->Lz = Lz;
+    n->train = train != 0;
+    build_layers(n);
+    bool ok = cudaStreamCreateWithFlags(&n->stream, cudaStreamNonBlocking) == cudaSuccess;
+    n->own_stream = ok;
+    auto al = [&](void **p, size_t bytes) {
+        if (ok && cudaMalloc(p, bytes) != cudaSuccess) ok = false;
+        if (ok) ok = cudaMemsetAsync(*p, 0, bytes, n->stream) == cudaSuccess;
+    };
+    const size_t R0 = (size_t)rows_at(n, 0);
+    al((void **)&n->p, n->nparams * 4);
+    al((void **)&n->pb, n->nparams * 2);
+    al((void **)&n->x, R0 * kIn * 2);
+    al((void **)&n->y, R0 * kOut * 4);
+    al((void **)&n->mask, R0);
+    for (int i = 0; i < kLayers - 1; ++i) {
+        const Layer &L = n->layers[i];
+        const size_t ro = (size_t)rows_at(n, out_level(L));
+        if (i == 4 || i == 6 || i == 8) {
+            // the FP32 output on the coarse grid, and the BF16 upsampled sum on the fine one
+            al((void **)&n->pre[i], ro * L.cout * 4);
+            al((void **)&n->act[i], (size_t)rows_at(n, L.level - 1) * L.cout * 2);
+        } else {
+            al((void **)&n->act[i], ro * L.cout * 2);
+        }
+    }
+    if (n->train) {
+        size_t maxw = 0, maxg = 0;
+        for (const Layer &L : n->layers) {
+            maxw = std::max(maxw, (size_t)L.cout * L.taps * L.cin);
+            maxg = std::max(maxg, (size_t)rows_at(n, L.level) * L.cin);
+            maxg = std::max(maxg, (size_t)rows_at(n, out_level(L)) * L.cout);
+        }
+        al((void **)&n->g, n->nparams * 4);
+        al((void **)&n->m, n->nparams * 4);
+        al((void **)&n->v, n->nparams * 4);
+        al((void **)&n->wd, maxw * 2);
+        al((void **)&n->gA, maxg * 4);
+        al((void **)&n->gB, maxg * 4);
+        al((void **)&n->gbf, maxg * 2);
+        al((void **)&n->sk[0], (size_t)rows_at(n, 0) * 32 * 4);
+        al((void **)&n->sk[1], (size_t)rows_at(n, 1) * 48 * 4);
+        al((void **)&n->sk[2], (size_t)rows_at(n, 2) * 64 * 4);
+        al((void **)&n->loss, sizeof(double));
+        al((void **)&n->count, sizeof(unsigned long long));
+    }
+    if (ok) ok = cudaStreamSynchronize(n->stream) == cudaSuccess;
+    if (!ok) {
+        cudaGetLastError();
+        qmin_warmnet_destroy(n);
+        return nfail(QMIN_ENOMEM, "qmin_warmnet_create: device allocation failed");
+    }
+    *out = n;
+    return QMIN_OK;
+}
+
+int qmin_warmnet_destroy(qmin_warmnet n)
+{
+    if (!n) return nfail(QMIN_EINVAL, "qmin_warmnet_destroy: null handle");
+    if (n->stream) cudaStreamSynchronize(n->stream);
+    void *bufs[] = {n->p, n->g, n->m, n->v, n->pb, n->wd, n->x, n->mask, n->y, n->gA, n->gB, n->gbf, n->loss, n->count,
+                    n->sk[0], n->sk[1], n->sk[2]};
+    for (void *b : bufs)
+        if (b) cudaFree(b);
+    for (int i = 0; i < kLayers; ++i) {
+        if (n->act[i]) cudaFree(n->act[i]);
+        if (n->pre[i]) cudaFree(n->pre[i]);
+    }
+    if (n->own_stream) cudaStreamDestroy(n->stream);
+    delete n;
+    return QMIN_OK;
+}
+
+int qmin_warmnet_set_stream(qmin_warmnet n, void *stream)
+{
+    if (!n) return nfail(QMIN_EINVAL, "qmin_warmnet_set_stream: null handle");
+    cudaStreamSynchronize(n->stream);
+    if (n->own_stream) cudaStreamDestroy(n->stream);
+    n->own_stream = false;
+    n->stream = (cudaStream_t)stream;
+    return QMIN_OK;
+}
+
+int qmin_warmnet_param_count(qmin_warmnet n, long long *count)
+{
+    if (!n || !count) return nfail(QMIN_EINVAL, "qmin_warmnet_param_count: null argument");
+    *count = (long long)n->nparams;
+    return QMIN_OK;
+}
+
+int qmin_warmnet_shape(qmin_warmnet n, int *batch, int *Lx, int *Ly, int *Lz)
+{
+    if (!n) return nfail(QMIN_EINVAL, "qmin_warmnet_shape: null handle");
+    if (batch) *batch = n->B;
+    if (Lx) *Lx = n->Lx;
+    if (Ly) *Ly = n->Ly;
+    if (Lz) *Lz = n->Lz;
+    return QMIN_OK;
+}
+
+int qmin_warmnet_buffers(qmin_warmnet n, void **x, float **y, uint8_t **mask)
+{
+    if (!n) return nfail(QMIN_EINVAL, "qmin_warmnet_buffers: null handle");
+    if (x) *x = n->x;
+    if (y) *y = n->y;
+    if (mask) *mask = n->mask;
+    return QMIN_OK;
+}
+
+int qmin_warmnet_set_params(qmin_warmnet n, const float *host)
+{
+    if (!n || !host) return nfail(QMIN_EINVAL, "qmin_warmnet_set_params: null argument");
+    cudaStream_t s = n->stream;
+    if (cudaMemcpyAsync(n->p, host, n->nparams * 4, cudaMemcpyHostToDevice, s) != cudaSuccess)
+        return nfail(QMIN_ECUDA, "qmin_warmnet_set_params: copy failed");
+    k_f32_to_bf16<<<grid1(n->nparams), 256, 0, s>>>(n->p, n->pb, (long long)n->nparams);
+    if (n->train) {
+        cudaMemsetAsync(n->m, 0, n->nparams * 4, s);
+        cudaMemsetAsync(n->v, 0, n->nparams * 4, s);
+    }
+    n->adam_t = 0;
+    const int rc = check_launch(n, "qmin_warmnet_set_params", 1);
+    if (rc) return rc;
+    return cudaStreamSynchronize(s) == cudaSuccess ? QMIN_OK : nfail(QMIN_ECUDA, "qmin_warmnet_set_params: sync");
+}
+
+int qmin_warmnet_get_params(qmin_warmnet n, float *params, float *grads)
+{
+    if (!n) return nfail(QMIN_EINVAL, "qmin_warmnet_get_params: null handle");
+    if (grads && !n->train) return nfail(QMIN_ESTATE, "qmin_warmnet_get_params: gradients need a training net");
+    if (params) cudaMemcpyAsync(params, n->p, n->nparams * 4, cudaMemcpyDeviceToHost, n->stream);
+    if (grads) cudaMemcpyAsync(grads, n->g, n->nparams * 4, cudaMemcpyDeviceToHost, n->stream);
+    return cudaStreamSynchronize(n->stream) == cudaSuccess ? QMIN_OK : nfail(QMIN_ECUDA, "qmin_warmnet_get_params");
+}
+
+int qmin_warmnet_features(qmin_warmnet n, int sample, const void *Q_dev, int precision, long long plane_stride,
+                          const int8_t *types_dev, const qmin_object *objs, int nobj)
+{
+    if (!n || !Q_dev || !types_dev || (nobj > 0 && !objs)) return nfail(QMIN_EINVAL, "qmin_warmnet_features: null argument");
+    if (sample < 0 || sample >= n->B) return nfail(QMIN_EINVAL, "qmin_warmnet_features: sample out of range");
+    if (nobj < 0 || nobj > kMaxObj) return nfail(QMIN_EINVAL, "qmin_warmnet_features: at most 64 objects");
+    if (plane_stride < sites(n, 0)) return nfail(QMIN_EINVAL, "qmin_warmnet_features: plane stride below the site count");
+    if (precision == QMIN_FP64)
+        return features_impl(n, sample, (const double *)Q_dev, plane_stride, types_dev, objs, nobj);
+    if (precision == QMIN_FP32)
+        return features_impl(n, sample, (const float *)Q_dev, plane_stride, types_dev, objs, nobj);
+    return nfail(QMIN_EINVAL, "qmin_warmnet_features: precision must be QMIN_FP64 or QMIN_FP32");
+}
+
+int qmin_warmnet_forward(qmin_warmnet n)
+{
+    if (!n) return nfail(QMIN_EINVAL, "qmin_warmnet_forward: null handle");
+    cudaStream_t s = n->stream;
+    run_layer(n, 0, n->x, nullptr);
+    run_layer(n, 1, n->act[0], nullptr);
+    run_layer(n, 2, n->act[1], nullptr);
+    run_layer(n, 3, n->act[2], nullptr);
+    run_layer(n, 4, n->act[3], n->pre[4]);
+    k_up2_add<<<grid1(rows_at(n, 2) * 64), 256, 0, s>>>(n->pre[4], n->act[2], n->act[4], dims_at(n, 3), 64);
+    run_layer(n, 5, n->act[4], nullptr);
+    run_layer(n, 6, n->act[5], n->pre[6]);
+    k_up2_add<<<grid1(rows_at(n, 1) * 48), 256, 0, s>>>(n->pre[6], n->act[1], n->act[6], dims_at(n, 2), 48);
+    run_layer(n, 7, n->act[6], nullptr);
+    run_layer(n, 8, n->act[7], n->pre[8]);
+    k_up2_add<<<grid1(rows_at(n, 0) * 32), 256, 0, s>>>(n->pre[8], n->act[0], n->act[8], dims_at(n, 1), 32);
+    run_layer(n, 9, n->act[8], nullptr);
+    run_layer(n, 10, n->act[9], n->y);
+    return check_launch(n, "qmin_warmnet_forward", 14);
+}
+
+int qmin_warmnet_backward(qmin_warmnet n, const float *target_dev, double *loss)
+{
+    if (!n || !target_dev) return nfail(QMIN_EINVAL, "qmin_warmnet_backward: null argument");
+    if (!n->train) return nfail(QMIN_ESTATE, "qmin_warmnet_backward: the net was created without training buffers");
+    cudaStream_t s = n->stream;
+    const long long R = rows_at(n, 0);
+    cudaMemsetAsync(n->g, 0, n->nparams * 4, s);
+    cudaMemsetAsync(n->loss, 0, sizeof(double), s);
+    cudaMemsetAsync(n->count, 0, sizeof(unsigned long long), s);
+    k_count_mask<<<grid1(R), 256, 0, s>>>(n->mask, R, n->count);
+    k_mse<<<grid1(R), 256, 0, s>>>(n->y, target_dev, n->mask, n->count, n->gA, n->loss, R);
+    n->launches += 2;
+    float *gA = n->gA, *gB = n->gB;
+    layer_backward(n, 10, gA, n->act[9], gB, nullptr);        // d act9
+    layer_backward(n, 9, gB, n->act[8], n->sk[0], nullptr);   // d act8 = d skip of enc0
+    k_up2_grad<<<grid1(rows_at(n, 1) * 32), 256, 0, s>>>(n->sk[0], gB, dims_at(n, 1), 32);
+    layer_backward(n, 8, gB, n->act[7], gA, nullptr);         // d act7
+    layer_backward(n, 7, gA, n->act[6], n->sk[1], nullptr);   // d act6 = d skip of enc1
+    k_up2_grad<<<grid1(rows_at(n, 2) * 48), 256, 0, s>>>(n->sk[1], gA, dims_at(n, 2), 48);
+    layer_backward(n, 6, gA, n->act[5], gB, nullptr);         // d act5
+    layer_backward(n, 5, gB, n->act[4], n->sk[2], nullptr);   // d act4 = d skip of enc2
+    k_up2_grad<<<grid1(rows_at(n, 3) * 64), 256, 0, s>>>(n->sk[2], gA, dims_at(n, 3), 64);
+    layer_backward(n, 4, gA, n->act[3], gB, nullptr);         // d act3
+    layer_backward(n, 3, gB, n->act[2], gA, n->sk[2]);        // d act2 (+ skip)
+    layer_backward(n, 2, gA, n->act[1], gB, n->sk[1]);        // d act1 (+ skip)
+    layer_backward(n, 1, gB, n->act[0], gA, n->sk[0]);        // d act0 (+ skip)
+    layer_backward(n, 0, gA, n->x, nullptr, nullptr);
+    n->launches += 3;
+    int rc = check_launch(n, "qmin_warmnet_backward", 0);
+    if (rc) return rc;
+    if (loss) {
+        if (cudaMemcpyAsync(loss, n->loss, sizeof(double), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+            cudaStreamSynchronize(s) != cudaSuccess)
+            return nfail(QMIN_ECUDA, "qmin_warmnet_backward: loss read-back failed");
+        if (!std::isfinite(*loss)) return nfail(QMIN_ENONFINITE, "qmin_warmnet_backward: non-finite loss");
+    }
+    return QMIN_OK;
+}
+
+int qmin_warmnet_adam_step(qmin_warmnet n, double lr, double beta1, double beta2, double eps)
+{
+    if (!n) return nfail(QMIN_EINVAL, "qmin_warmnet_adam_step: null handle");
+    if (!n->train) return nfail(QMIN_ESTATE, "qmin_warmnet_adam_step: the net was created without training buffers");
+    n->adam_t += 1;
+    const double c1 = 1.0 / (1.0 - std::pow(beta1, (double)n->adam_t));
+    const double c2 = 1.0 / (1.0 - std::pow(beta2, (double)n->adam_t));
+    k_adam_params<<<grid1(n->nparams), 256, 0, n->stream>>>(n->p, n->g, n->m, n->v, n->pb, (long long)n->nparams,
+                                                            (float)lr, (float)beta1, (float)beta2, (float)eps,
+                                                            (float)c1, (float)c2);
+    return check_launch(n, "qmin_warmnet_adam_step", 1);
+}
+
+int qmin_warmnet_write_state(qmin_warmnet n, int sample, void *Q_dev, int precision, long long plane_stride,
+                             const int8_t *types_dev)
+{
+    if (!n || !Q_dev || !types_dev) return nfail(QMIN_EINVAL, "qmin_warmnet_write_state: null argument");
+    if (sample < 0 || sample >= n->B) return nfail(QMIN_EINVAL, "qmin_warmnet_write_state: sample out of range");
+    if (plane_stride < sites(n, 0)) return nfail(QMIN_EINVAL, "qmin_warmnet_write_state: plane stride below the site count");
+    const long long N = sites(n, 0);
+    const float *y = n->y + (size_t)sample * N * kOut;
+    if (precision == QMIN_FP64)
+        k_write_state<double><<<grid1(N), 256, 0, n->stream>>>(y, (double *)Q_dev, plane_stride, types_dev, (int)N);
+    else if (precision == QMIN_FP32)
+        k_write_state<float><<<grid1(N), 256, 0, n->stream>>>(y, (float *)Q_dev, plane_stride, types_dev, (int)N);
+    else
+        return nfail(QMIN_EINVAL, "qmin_warmnet_write_state: precision must be QMIN_FP64 or QMIN_FP32");
+    return check_launch(n, "qmin_warmnet_write_state", 1);
+}
+
+int qmin_warmnet_sync(qmin_warmnet n)
+{
+    if (!n) return nfail(QMIN_EINVAL, "qmin_warmnet_sync: null handle");
+    const cudaError_t e = cudaStreamSynchronize(n->stream);
+    return e == cudaSuccess ? QMIN_OK : nfail(QMIN_ECUDA, std::string("qmin_warmnet_sync: ") + cudaGetErrorString(e));
+}
+
+int qmin_warmnet_kernel_launches(qmin_warmnet n, long long *count)
+{
+    if (!n || !count) return nfail(QMIN_EINVAL, "qmin_warmnet_kernel_launches: null argument");
+    *count = n->launches;
+    return QMIN_OK;
+}

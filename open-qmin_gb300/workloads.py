@@ -35,6 +35,27 @@ def c3_solve(seed, lo=16, hi=64):
     return dict(L=L, consts=(a, b, c), S0=S0, Q=g.Q, types=g.types, objects=g.objects(), sphere=(centre, r, W))
 
 
+def c4_solve(seed, side=64, wall_W=5.3, rfrac=(0.1, 0.2), Wrange=(1.0, 10.0), qseed=None):
+    """One sample of the learned-warm-start set: the c2 generator scaled to
+    side^3 (homeotropic z-walls on planes 0 and side-1 with W = 5.3, one
+    homeotropic sphere) with the sphere's radius r ~ U[0.1, 0.2] side, centre
+    x, y ~ U[0, side), z ~ U[r + 3, side - 4 - r] and strength
+    W = exp(U[ln 1, ln 10]) drawn per sample; random-director Q0 from `seed`
+    (or from `qseed`, to pair one geometry with several initial fields)."""
+    a, b, c, S0 = cli_phase_constants()
+    rng = random.Random(1000003 + seed)
+    L = (side, side, side)
+    r = rng.uniform(rfrac[0] * side, rfrac[1] * side)
+    centre = (rng.uniform(0.0, side), rng.uniform(0.0, side), rng.uniform(r + 3.0, side - 4.0 - r))
+    W = math.exp(rng.uniform(math.log(Wrange[0]), math.log(Wrange[1])))
+    g = Geometry(L, host_random_nematic(L, seed if qseed is None else qseed, S0))
+    for plane in (0, side - 1):
+        g.add_wall(2, plane, HOMEOTROPIC, wall_W, S0)
+    g.add_sphere(centre, r, HOMEOTROPIC, W, S0)
+    return dict(L=L, consts=(a, b, c), S0=S0, Q=g.Q, types=g.types, objects=g.objects(), Ls=(2.32, 1.0, 0.5),
+                sphere=(centre, r, W))
+
+
 def c5_lattice(side=400, seed=13371, nspheres=8, rmin=10.0, rmax=25.0, gap=2.0):
     """400^3 box, `nspheres` non-overlapping random homeotropic spheres
     (r ~ U[rmin, rmax], centres ~ U(box), surfaces at least `gap` sites apart

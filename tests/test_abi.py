@@ -38,6 +38,20 @@ def test_status_codes_without_device(qmin):
     assert lib.qmin_create(C.byref(d), C.byref(h)) == qmin.QMIN_EINVAL
     assert lib.qmin_force(None, None) == qmin.QMIN_EINVAL
     assert lib.qmin_fire_run(None, 1, None) == qmin.QMIN_EINVAL
+    # learned warm-start net: sides must be multiples of 8
+    assert lib.qmin_warmnet_create(1, 12, 16, 16, 0, C.byref(h)) == qmin.QMIN_EINVAL
+    assert b"multiple of 8" in lib.qmin_last_error_string()
+    assert lib.qmin_warmnet_create(0, 16, 16, 16, 0, C.byref(h)) == qmin.QMIN_EINVAL
+    assert lib.qmin_warmnet_forward(None) == qmin.QMIN_EINVAL
+    assert lib.qmin_warm_start(None, None) == qmin.QMIN_EINVAL
+
+
+def test_warmnet_parameter_layout(qmin):
+    """The Python layer table matches the native parameter count."""
+    sl = qmin.warmnet_param_slices()
+    assert sl[-1][1].stop == 573760
+    p = qmin.warmnet_init_params(0)
+    assert p.dtype == np.float32 and p.size == 573760 and np.all(p[sl[0][1]] == 0)
 
 
 def test_no_cpu_fallback(qmin):
@@ -47,6 +61,8 @@ def test_no_cpu_fallback(qmin):
         pytest.skip("a GPU is present")
     with pytest.raises(qmin.QminError):
         qmin.Lattice((8, 8, 8))
+    with pytest.raises(qmin.QminError):
+        qmin.WarmNet(1, (16, 16, 16))
 
 
 @pytest.mark.parametrize("name", GOLDEN_CASES)

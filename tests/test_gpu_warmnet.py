@@ -1,0 +1,184 @@
+"""The learned warm-start net's BF16 tensor-core kernels against a plain
+PyTorch float64 restatement of the same net (tests/warmnet_torch.py).
+
+Tolerances: the native path rounds every activation and gradient to BF16
+(8 significant bits) between layers, the reference keeps float64 after
+rounding only the weights and input features to BF16.  Output: normwise
+relative error <= 3e-2.  Loss: relative error <= 3e-2.  Parameter gradients,
+per layer: normwise relative error <= 6e-2 and cosine similarity >= 0.998."""
+import numpy as np
+import pytest
+import torch
+
+import warmnet_torch as wt
+
+pytestmark = pytest.mark.gpu
+
+
+def _lattice(qmin, seed, side):
+    from importlib import import_module
+    w = import_module("qmin_gb300.workloads")
+    return w.c4_solve(seed, side=side)
+
+
+def _dev(sol):
+    n = sol["Q"].shape[0]
+    q = torch.as_tensor(np.ascontiguousarray(sol["Q"].T)).cuda()  # SoA planes, stride n
+    t = torch.as_tensor(sol["types"].astype(np.int8)).cuda()
+    return q, t, n
+
+
+def _features_numpy(sol):
+    Q, types, objs = sol["Q"], sol["types"], sol["objects"]
+    n = Q.shape[0]
+    f = np.zeros((n, 16), dtype=np.float32)
+    f[:, :5] = Q
+    obj = types > 0
+    f[obj, 5] = 1.0
+    f[types == -1, 6] = 1.0
+    for j, (kind, W, _S0) in enumerate(objs):
+        sel = types == j + 1
+        f[sel, 7] = np.float32(0.1) * np.float32(W)
+        f[sel, 8] = 1.0 if kind == 0 else 0.0
+        f[sel, 9] = 1.0 if kind == 1 else 0.0
+    return wt.bf16_round(f).numpy(), (types <= 0).astype(np.uint8)
+
+
+def _net_with_inputs(qmin, sols, train=True, seed=3, head_scale=1.0):
+    L = sols[0]["L"]
+    net = qmin.WarmNet(len(sols), L, train=train)
+    net.set_params(qmin.warmnet_init_params(seed, head_scale=head_scale))
+    keep = []
+    for k, s in enumerate(sols):
+        q, t, n = _dev(s)
+        keep.append((q, t))
+        torch.cuda.synchronize()
+        net.features(k, q.data_ptr(), qmin.FP64, n, t.data_ptr(), s["objects"])
+    net.sync()
+    return net, keep
+
+
+def test_features_match_definition(qmin):
+    sols = [_lattice(qmin, 11, 16), _lattice(qmin, 12, 16)]
+    net, _keep = _net_with_inputs(qmin, sols, train=False)
+    x, _y, m = net.torch_views()
+    xs = x.float().cpu().numpy()
+    ms = m.cpu().numpy()
+    for k, s in enumerate(sols):
+        fx, fm = _features_numpy(s)
+        assert np.array_equal(xs[k], fx)
+        assert np.array_equal(ms[k], fm)
+
+
+@pytest.mark.parametrize("L", [(16, 16, 16), (24, 8, 16)])
+def test_forward_matches_torch_fp64(qmin, L):
+    sols = []
+    for seed in (21, 22):
+        s = _lattice(qmin, seed, max(L))
+        if L != (max(L),) * 3:
+            # a non-cubic lattice: crop the cube's arrays to L (types stay valid labels)
+            side = max(L)
+            idx = np.arange(side ** 3).reshape(side, side, side)[:L[2], :L[1], :L[0]].ravel()
+            s = dict(s, L=L, Q=np.ascontiguousarray(s["Q"][idx]), types=np.ascontiguousarray(s["types"][idx]))
+        sols.append(s)
+    net, _keep = _net_with_inputs(qmin, sols, train=False)
+    net.forward()
+    net.sync()
+    x, y, _m = net.torch_views()
+    yg = y.cpu().numpy().astype(np.float64)
+    xs = x.float().cpu().numpy()
+    p = net.get_params()
+    P = wt.unpack(p, qmin.WARMNET_LAYERS)
+    B, n = len(sols), L[0] * L[1] * L[2]
+    xt = torch.as_tensor(xs.astype(np.float64)).reshape(B, L[2], L[1], L[0], 16).permute(0, 4, 1, 2, 3)
+    with torch.no_grad():
+        yr = wt.forward(P, xt).permute(0, 2, 3, 4, 1).reshape(B, n, 16).numpy()
+    err = np.linalg.norm(yg - yr) / np.linalg.norm(yr)
+    assert err <= 3e-2, err
+
+
+def test_backward_matches_torch_fp64(qmin):
+    L = (16, 16, 16)
+    sols = [_lattice(qmin, s, 16) for s in (31, 32)]
+    net, _keep = _net_with_inputs(qmin, sols, train=True)
+    rng = np.random.default_rng(5)
+    n = 16 ** 3
+    target = (0.3 * rng.standard_normal((2, n, 5))).astype(np.float32)
+    tgt = torch.as_tensor(target).cuda()
+    net.forward()
+    torch.cuda.synchronize()
+    loss = net.backward(tgt.data_ptr())
+    p, g = net.get_params(grads=True)
+    x, _y, m = net.torch_views()
+    xs = x.float().cpu().numpy()
+    ms = m.cpu().numpy()
+    _yr, loss_r, g_r = wt.loss_and_grads(p, qmin.WARMNET_LAYERS, xs, target, ms, L)
+    assert abs(loss - loss_r) <= 3e-2 * loss_r, (loss, loss_r)
+    for i, (ws, bs, spec) in enumerate(qmin.warmnet_param_slices()):
+        for sl, what in ((ws, "w"), (bs, "b")):
+            a, b = g[sl].astype(np.float64), g_r[sl]
+            rel = np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-30)
+            cos = float(a @ b / max(np.linalg.norm(a) * np.linalg.norm(b), 1e-30))
+            assert rel <= 6e-2 and cos >= 0.998, (i, what, spec, rel, cos)
+
+
+def test_adam_steps_reduce_loss(qmin):
+    sols = [_lattice(qmin, s, 16) for s in (41, 42)]
+    net, _keep = _net_with_inputs(qmin, sols, train=True, head_scale=0.1)
+    # target: the initial Q smoothed over the six neighbours
+    tg = []
+    for s in sols:
+        q = s["Q"].reshape(16, 16, 16, 5)
+        sm = sum(np.roll(q, sh, ax) for ax in (0, 1, 2) for sh in (1, -1)) / 6.0
+        tg.append(sm.reshape(-1, 5))
+    tgt = torch.as_tensor(np.array(tg, dtype=np.float32)).cuda()
+    torch.cuda.synchronize()
+    losses = []
+    for it in range(40):
+        net.forward()
+        losses.append(net.backward(tgt.data_ptr()))
+        net.adam_step(2e-3)
+    assert losses[-1] < 0.5 * losses[0], losses[::8]
+
+
+def test_warm_start_writes_only_moved_sites(qmin):
+    s = _lattice(qmin, 51, 16)
+    for prec in (qmin.FP64, qmin.FP32):
+        lat = qmin.Lattice(s["L"], prec)
+        a, b, c = s["consts"]
+        lat.set_params(a, b, c, *s["Ls"])
+        lat.set_objects(s["objects"])
+        lat.set_state(s["Q"], s["types"])
+        net = qmin.WarmNet(1, s["L"])
+        net.set_params(qmin.warmnet_init_params(7, head_scale=1.0))
+        lat.warm_start(net)
+        q = lat.get_state()[0]
+        _x, y, _m = net.torch_views()
+        yp = y[0, :, :5].cpu().numpy().astype(np.float64)
+        obj = s["types"] > 0
+        q0 = s["Q"] if prec == qmin.FP64 else s["Q"].astype(np.float32).astype(np.float64)
+        assert np.array_equal(q[obj], q0[obj])
+        want = yp[~obj] if prec == qmin.FP64 else yp[~obj].astype(np.float32).astype(np.float64)
+        assert np.array_equal(q[~obj], want)
+        assert net.launches() > 0
+        # FIRE runs from the warm-started state
+        lat.fire_init()
+        r = lat.fire_run(5)
+        assert np.isfinite(r["forceMax"])
+
+
+def test_warm_start_rejects_mismatched_net(qmin):
+    s = _lattice(qmin, 61, 16)
+    lat = qmin.Lattice(s["L"])
+    a, b, c = s["consts"]
+    lat.set_params(a, b, c, *s["Ls"])
+    lat.set_objects(s["objects"])
+    lat.set_state(s["Q"], s["types"])
+    net = qmin.WarmNet(1, (16, 16, 8))
+    with pytest.raises(qmin.QminError):
+        lat.warm_start(net)
+    inf = qmin.WarmNet(1, (16, 16, 16), train=False)
+    tgt = torch.zeros((16 ** 3, 5), dtype=torch.float32, device="cuda")
+    with pytest.raises(qmin.QminError) as e:
+        inf.backward(tgt.data_ptr())
+    assert e.value.code == 4
