@@ -34,7 +34,8 @@ WORKLOAD = dict(L=(200, 200, 200), seed=13371, Ls=(2.32, 1.0, 0.5), W=5.3, walls
 # algorithmic bytes per site for one launch of each FIRE-iteration kernel (FP64 / FP32 state):
 #  predictor: read Q,V,F  write Q,V           = 25 values
 #  derivative planes: read Q, types, write 15 = 20 values + 1 B
-#  force + kick: read Q, V, types, write F, V = 20 values + 1 B
+#  force + kick: read Q, V, types, write F, V = 20 values + 1 B (the 15 derivative planes it also
+#                reads are this design's intermediate, 120 / 60 B/site, visible in the measured traffic)
 #  control: scalars only
 KERNEL_BYTES = {8: [200, 161, 161, 0], 4: [100, 81, 81, 0]}
 KERNEL_NAMES = ["fire_predictor", "first_derivatives", "force_kick_reduce", "fire_control"]
@@ -45,18 +46,21 @@ FUSED_BYTES = {8: 241, 4: 121}
 def kernel_roofline(lat, esz, N, peak, peak_kind, tag):
     """Dominant kernel of the FIRE iteration, timed with CUDA events per launch."""
     kms, fused = lat.fire_profile(20)
+    tuning = lat.fire_tuning()
     names = list(KERNEL_NAMES)
     nbytes = list(KERNEL_BYTES[esz])
     if fused:
         names[2] = "fire_fused"
         nbytes[2] = FUSED_BYTES[esz]
+    elif tuning["path"] == "tiled":
+        names[2] = "force_kick_tiled"
     dom = int(np.argmax(kms))
     achieved = nbytes[dom] * N / (kms[dom] / 1e3) / 1e9
     out = {"bound": "hbm", "kernel": names[dom], "achieved": achieved, "peak": peak, "unit": "GB/s",
            "frac": achieved / peak, "peak_source": peak_kind, "traffic": traffic_from_profiles(names[dom], tag),
            "kernel_ms": {n: float(x) for n, x in zip(names, kms) if x > 0},
            "algorithmic_bytes_per_site": nbytes[dom], "sites_per_launch": N}
-    out["autotuned"] = lat.fire_tuning()
+    out["autotuned"] = tuning
     return out
 
 

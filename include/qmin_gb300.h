@@ -147,7 +147,9 @@ int qmin_lbfgs_run(qmin_handle h, int m, double eta, double force_cutoff, int ma
 /* ---- FIRE iteration strategy and diagnostics ---- */
 #define QMIN_FIRE_SEPARATE 0 /* predictor, derivative planes, force+kick, control as separate kernels */
 #define QMIN_FIRE_FUSED 1    /* one shared-memory tiled kernel per iteration */
-#define QMIN_FIRE_AUTO 2     /* the autotuner picks the fastest of the above (default) */
+#define QMIN_FIRE_AUTO 2     /* the autotuner picks the fastest of the others (default) */
+#define QMIN_FIRE_TILED 3    /* separate predictor and derivative planes, force + kick from shared-memory
+                                tiles (FP32 form only) */
 /* Choose how qmin_fire_run executes an iteration; all strategies give the
  * same results to rounding.  No reference counterpart (execution strategy). */
 int qmin_set_fire_kernel(qmin_handle h, int mode);
@@ -158,15 +160,19 @@ int qmin_set_fire_kernel(qmin_handle h, int mode);
  * scalar control; *fused (may be NULL) tells which path ran.  The FIRE state
  * advances exactly as in qmin_fire_run.  No reference counterpart (profiling). */
 int qmin_fire_profile(qmin_handle h, int iterations, double kernel_ms[4], int *fused);
+/* (kernel_ms[2] is the staged force + kick when path 2 runs; *fused is 1 only for path 1) */
 /* The FIRE strategy the autotuner chose on the first run (path 0 separate
- * kernels sized for `variant` + 1 blocks per SM, path 1 fused kernel with tile
- * shape `variant` = tile_x x tile_y and `zc` z planes per block) and the
- * measured ms per iteration of every candidate: ms[0..2] separate (1, 2, 3
- * blocks per SM), ms[3 + 2*cfg + v] fused (v = 0/1 for the two z extents
- * tried); -1 = not run.
+ * kernels sized for `variant` + 1 blocks per SM; path 1 fused kernel and
+ * path 2 staged force + kick, each with tile shape `variant` = tile_x x tile_y
+ * and `zc` z planes per block) and the measured ms per iteration of every
+ * candidate: ms[0..2] separate (1, 2, 3 blocks per SM), ms[3 + 2*cfg + v]
+ * fused (4 shapes, v = 0/1 for the two z extents tried), ms[11 + 2*cfg + v]
+ * staged (3 shapes); -1 = not run.
  * No reference counterpart (the reference's kernelTuner scans block sizes,
  * src/utilities/kernelTuner.cpp:5-125). */
-int qmin_fire_tuning(qmin_handle h, int *path, int *variant, int *tile_x, int *tile_y, int *zc, double ms[11]);
+#define QMIN_TUNE_CANDIDATES 17
+int qmin_fire_tuning(qmin_handle h, int *path, int *variant, int *tile_x, int *tile_y, int *zc,
+                     double ms[QMIN_TUNE_CANDIDATES]);
 
 /* ---- energy without allocation ---- */
 /* Largest lattice (in sites) qmin_energy_noalloc accepts: the size of its

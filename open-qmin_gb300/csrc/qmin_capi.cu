@@ -36,6 +36,8 @@ static int fail(int code, const std::string &msg)
     } while (0)
 
 static const int kSepVariants = 3;  // separate-kernel force + kick with 1, 2, 3 blocks per SM
+static const int kTuneCandidates = kSepVariants + 2 * kFusedConfigs + 2 * kTiledConfigs;
+static_assert(kTuneCandidates == QMIN_TUNE_CANDIDATES, "tuning candidate count");
 
 struct qmin_ctx {
     int Lx = 0, Ly = 0, Lz = 0, N = 0;
@@ -77,9 +79,11 @@ struct qmin_ctx {
     void *Q2 = nullptr, *V2 = nullptr, *F2 = nullptr;
     int fire_mode = QMIN_FIRE_AUTO;  // strategy requested by the caller
     // strategy chosen by the autotuner for the current parameters
-    int path = -1;  // 0 separate kernels, 1 fused tiled kernel
+    int path = -1;  // 0 separate kernels, 1 fused tiled kernel, 2 separate with the staged force + kick
     int sep_cap = 0, fused_cfg = -1, fused_zc = 0, fused_nblocks = 0, tuned_version = 0, tuned_mode = -1;
-    double tune_ms[kSepVariants + kFusedConfigs * 2] = {};  // separate (register caps), fused (cfg, z extent)
+    int tiled_cfg = -1, tiled_zc = 0, tiled_nblocks = 0;
+    // separate (register caps), fused (cfg, z extent), staged force + kick (cfg, z extent)
+    double tune_ms[kTuneCandidates] = {};
 };
 
 static const int kChunk = 32;  // iterations per captured graph
@@ -554,12 +558,12 @@ template <class T> static int tune_fire(qmin_ctx *h, const Lat<T> &L)
     };
     const int H = L.multi ? 2 : 1;
     float best = 1e30f;
-    for (int k = 0; k < kSepVariants + 2 * kFusedConfigs; ++k) h->tune_ms[k] = -1;
+    for (int k = 0; k < kTuneCandidates; ++k) h->tune_ms[k] = -1;
     Lat<T> LB = L;
     LB.Q = (T *)h->Q2;
     LB.V = (T *)h->V2;
     LB.F = (T *)h->F2;
-    if (h->fire_mode != QMIN_FIRE_SEPARATE) {
+    if (h->fire_mode == QMIN_FIRE_AUTO || h->fire_mode == QMIN_FIRE_FUSED) {
         for (int cfg = 0; cfg < kFusedConfigs; ++cfg) {
             int tx, ty;
             fused_tile_shape(cfg, &tx, &ty);
@@ -590,12 +594,41 @@ template <class T> static int tune_fire(qmin_ctx *h, const Lat<T> &L)
             }
         }
     }
-    if (h->fire_mode != QMIN_FIRE_FUSED) {
+    const bool try_sep = h->fire_mode == QMIN_FIRE_AUTO || h->fire_mode == QMIN_FIRE_SEPARATE;
+    const bool try_tiled = (h->fire_mode == QMIN_FIRE_AUTO || h->fire_mode == QMIN_FIRE_TILED) && sizeof(T) == 4;
+    if (try_sep || try_tiled) {
         const float t_pred = time3([&]() { launch_fire_pred<T>(LB, h->fire, h->stream); });
         const float t_der = L.multi ? time3([&]() { launch_derivs<T>(L, h->stream); }) : 0.f;
         const size_t bytes = 5 * (size_t)h->P * h->esz;
         CK(cudaMemcpyAsync(h->V2, h->V, bytes, cudaMemcpyDeviceToDevice, h->stream));
-        for (int cap = 0; cap < kSepVariants; ++cap) {
+        for (int cfg = 0; try_tiled && cfg < kTiledConfigs; ++cfg) {
+            int tx, ty;
+            tiled_tile_shape(cfg, &tx, &ty);
+            const int ntiles = ((h->Lx + tx - 1) / tx) * ((h->Ly + ty - 1) / ty);
+            // short z chunks: many blocks per SM over the launch keep the last wave small
+            int zc0 = 4;
+            while ((long long)ntiles * ((h->Lz + zc0 - 1) / zc0) > kMaxFusedBlocks) ++zc0;
+            for (int v = 0; v < 2; ++v) {
+                const int zc = std::min(h->Lz, zc0 << v);
+                int nb = 0, ok = 1;
+                const float t_fk = time3([&]() {
+                    if (launch_force_kick_tiled<T>(cfg, L, h->fire, h->partials, zc, h->stream, &nb) < 0) ok = 0;
+                });
+                h->launches += 4;
+                if (!ok || cudaGetLastError() != cudaSuccess) break;
+                const float ms = t_pred + t_der + t_fk;
+                h->tune_ms[kSepVariants + 2 * kFusedConfigs + 2 * cfg + v] = ms;
+                if (ms < best) {
+                    best = ms;
+                    h->path = 2;
+                    h->tiled_cfg = cfg;
+                    h->tiled_zc = zc;
+                    h->tiled_nblocks = nb;
+                }
+                if (zc >= h->Lz) break;
+            }
+        }
+        for (int cap = 0; try_sep && cap < kSepVariants; ++cap) {
             const float t_fk =
                 time3([&]() { launch_force_kick_only<T>(L, h->fire, h->partials, h->grid, h->stream, cap); });
             const float ms = t_pred + t_der + t_fk;
@@ -607,7 +640,7 @@ template <class T> static int tune_fire(qmin_ctx *h, const Lat<T> &L)
             }
         }
         CK(cudaMemcpyAsync(h->V, h->V2, bytes, cudaMemcpyDeviceToDevice, h->stream));
-        h->launches += 4 * (2 + (L.multi ? 1 : 0) + kSepVariants);
+        h->launches += 4 * (1 + (L.multi ? 1 : 0) + (try_sep ? kSepVariants : 0)) + 2;
     }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
@@ -631,13 +664,20 @@ template <class T> static int fire_impl(qmin_ctx *h, int max_iterations)
     LB.V = (T *)h->V2;
     LB.F = (T *)h->F2;
     int parity = 0;
-    const double args[4] = {(double)h->path, (double)(h->path ? h->fused_cfg : h->sep_cap), (double)h->fused_zc, 0};
+    const int variant = h->path == 0 ? h->sep_cap : (h->path == 1 ? h->fused_cfg : h->tiled_cfg);
+    const double args[4] = {(double)h->path, (double)variant, (double)(h->path == 2 ? h->tiled_zc : h->fused_zc), 0};
     r = capture_chunk(h, 0, args, [&]() {
         int n;
         if (h->path == 0) {
             n = launch_fire_pred<T>(L, h->fire, h->stream);
             n += launch_force_kick<T>(L, h->fire, h->partials, h->grid, h->stream, h->sep_cap);
             n += launch_fire_control(h->fire, h->partials, h->grid, h->stream);
+        } else if (h->path == 2) {
+            int nb = 0;
+            n = launch_fire_pred<T>(L, h->fire, h->stream);
+            if (L.multi) n += launch_derivs<T>(L, h->stream);
+            n += launch_force_kick_tiled<T>(h->tiled_cfg, L, h->fire, h->partials, h->tiled_zc, h->stream, &nb);
+            n += launch_fire_control(h->fire, h->partials, nb, h->stream);
         } else {
             int nb = 0;
             if (parity == 0)
@@ -869,7 +909,7 @@ template <class T> static int fire_profile_impl(qmin_ctx *h, int iterations, dou
     cudaEvent_t ev[5];
     for (auto &e : ev) CK(cudaEventCreate(&e));
     double acc[4] = {0, 0, 0, 0};
-    const bool fused = h->path == 1;
+    const bool fused = h->path == 1, tiled = h->path == 2;
     Lat<T> LB = L;
     LB.Q = (T *)h->Q2;
     LB.V = (T *)h->V2;
@@ -881,7 +921,10 @@ template <class T> static int fire_profile_impl(qmin_ctx *h, int iterations, dou
         if (!fused && L.multi) h->launches += launch_derivs<T>(L, h->stream);
         CK(cudaEventRecord(ev[2], h->stream));
         int nparts = h->grid;
-        if (!fused) {
+        if (tiled) {
+            h->launches += launch_force_kick_tiled<T>(h->tiled_cfg, L, h->fire, h->partials, h->tiled_zc, h->stream,
+                                                      &nparts);
+        } else if (!fused) {
             h->launches += launch_force_kick_only<T>(L, h->fire, h->partials, h->grid, h->stream, h->sep_cap);
         } else if ((it & 1) == 0) {
             h->launches += launch_fire_fused<T>(h->fused_cfg, L, (T *)h->Q2, (T *)h->V2, (T *)h->F2, h->fire,
@@ -932,8 +975,10 @@ int qmin_fire_profile(qmin_handle h, int iterations, double kernel_ms[4], int *f
 int qmin_set_fire_kernel(qmin_handle h, int mode)
 {
     if (!h) return fail(QMIN_EINVAL, "qmin_set_fire_kernel: null handle");
-    if (mode != QMIN_FIRE_SEPARATE && mode != QMIN_FIRE_FUSED && mode != QMIN_FIRE_AUTO)
-        return fail(QMIN_EINVAL, "qmin_set_fire_kernel: mode must be QMIN_FIRE_SEPARATE, _FUSED or _AUTO");
+    if (mode != QMIN_FIRE_SEPARATE && mode != QMIN_FIRE_FUSED && mode != QMIN_FIRE_AUTO && mode != QMIN_FIRE_TILED)
+        return fail(QMIN_EINVAL, "qmin_set_fire_kernel: mode must be QMIN_FIRE_SEPARATE, _FUSED, _TILED or _AUTO");
+    if (mode == QMIN_FIRE_TILED && h->prec != QMIN_FP32)
+        return fail(QMIN_EINVAL, "qmin_set_fire_kernel: the staged force + kick is built for the FP32 form only");
     if (h->fire_mode != mode) invalidate_graphs(h);
     h->fire_mode = mode;
     return QMIN_OK;
@@ -944,14 +989,15 @@ int qmin_fire_tuning(qmin_handle h, int *path, int *variant, int *tile_x, int *t
     if (!h) return fail(QMIN_EINVAL, "qmin_fire_tuning: null handle");
     if (h->path < 0) return fail(QMIN_ESTATE, "qmin_fire_tuning: no FIRE run has been tuned yet");
     if (path) *path = h->path;
-    if (variant) *variant = h->path ? h->fused_cfg : h->sep_cap;
+    if (variant) *variant = h->path == 0 ? h->sep_cap : (h->path == 1 ? h->fused_cfg : h->tiled_cfg);
     int tx = 0, ty = 0;
     if (h->path == 1) fused_tile_shape(h->fused_cfg, &tx, &ty);
+    if (h->path == 2) tiled_tile_shape(h->tiled_cfg, &tx, &ty);
     if (tile_x) *tile_x = tx;
     if (tile_y) *tile_y = ty;
-    if (zc) *zc = h->path == 1 ? h->fused_zc : 0;
+    if (zc) *zc = h->path == 1 ? h->fused_zc : (h->path == 2 ? h->tiled_zc : 0);
     if (ms)
-        for (int k = 0; k < kSepVariants + 2 * kFusedConfigs; ++k) ms[k] = h->tune_ms[k];
+        for (int k = 0; k < kTuneCandidates; ++k) ms[k] = h->tune_ms[k];
     return QMIN_OK;
 }
 

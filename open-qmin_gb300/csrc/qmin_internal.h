@@ -99,5 +99,13 @@ template <class T>
 int launch_fire_fused(int cfg, const Lat<T> &L, T *Qn, T *Vn, T *Fn, FireDev *fd, double *partials, int zc,
                       cudaStream_t s, int *nblocks);
 int fused_tile_shape(int cfg, int *tx, int *ty);
+// force + second half kick from shared-memory tiles (FP32 form): tile shape
+// cfg in [0, kTiledConfigs), zc z planes per block, *nblocks partial sums;
+// returns launches or -1 (FP64, or the shape could not be configured)
+constexpr int kTiledConfigs = 3;
+template <class T>
+int launch_force_kick_tiled(int cfg, const Lat<T> &L, FireDev *fd, double *partials, int zc, cudaStream_t s,
+                            int *nblocks);
+int tiled_tile_shape(int cfg, int *tx, int *ty);
 
 }  // namespace qmin

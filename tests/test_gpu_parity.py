@@ -189,16 +189,17 @@ def test_cpp_host_example_reproduces_cli_pin(qmin):
 
 
 @pytest.mark.parametrize("L", [(16, 9, 7), (40, 33, 21), (65, 17, 30)])
-@pytest.mark.parametrize("prec", [0, 1])
-def test_fused_matches_separate_kernels(qmin, oracle, L, prec):
-    """The fused tiled kernel on lattices that do not divide its tiles (partial
-    tiles, lattices narrower than a tile, odd z extents) tracks the separate
+@pytest.mark.parametrize("prec,other", [(0, 1), (1, 1), (1, 3)])
+def test_fused_matches_separate_kernels(qmin, oracle, L, prec, other):
+    """The fused tiled kernel (other = 1) and the staged force + kick
+    (other = 3, FP32 form) on lattices that do not divide their tiles (partial
+    tiles, lattices narrower than a tile, odd z extents) track the separate
     kernels: FP64 to 1e-12 after 7 iterations, FP32 to 1e-5."""
     cfg = parse_args([f"L={L[0]},{L[1]},{L[2]}", "seed=11", "Ls=2.32,1.0,0.5,0,0", "wall=2,0,h,5.3",
                       f"sphere={L[0] / 2},{L[1] / 2},{L[2] / 2},{min(L) / 4},p,2.0"])
     s = oracle_system(oracle, cfg)
     res = []
-    for mode in (0, 1):
+    for mode in (0, other):
         lat = gpu_lattice(qmin, s, prec)
         lat.set_fire_kernel(mode)
         lat.fire_init()
@@ -209,3 +210,30 @@ def test_fused_matches_separate_kernels(qmin, oracle, L, prec):
     assert abs(res[0][0]["forceMax"] - res[1][0]["forceMax"]) <= tol * res[0][0]["forceMax"]
     for a, b in zip(res[0][1], res[1][1]):
         assert rel_err(b, a) <= tol
+
+
+@pytest.mark.parametrize("Ls", ["2.32,0,0,0,0", "2.32,1.0,0.5,0,0"])
+def test_staged_force_kick_matches_separate(qmin, oracle, Ls):
+    """The staged force + kick (FP32 form) gives the separate kernels' forces
+    to FP32 rounding (1e-6 normwise; the two compilations may contract
+    different products into FMAs): one-constant and multi-constant, walls,
+    spheres, periodic wrap across tile edges; FIRE scalars and state to 1e-5
+    after 40 iterations."""
+    cfg = parse_args(["L=37,29,23", "seed=5", f"Ls={Ls}", "wall=2,0,h,5.3", "wall=0,30,p,1.5",
+                      "sphere=35.5,2.2,11.0,5.3,h,4.0", "sphere=12.0,20.0,20.5,4.1,p,0.8"])
+    s = oracle_system(oracle, cfg)
+    out = []
+    for mode in (0, 3):
+        lat = gpu_lattice(qmin, s, 1)
+        lat.set_fire_kernel(mode)
+        lat.fire_init()
+        r = lat.fire_run(1)
+        F1 = lat.get_state(Q=False, F=True)[2]
+        r = lat.fire_run(40)
+        out.append((F1, r, lat.get_state(Q=True, V=True, F=True), lat.fire_tuning()["path"]))
+    assert out[0][3] == "separate" and out[1][3] == "tiled"
+    assert rel_err(out[1][0], out[0][0]) <= 1e-6
+    assert out[0][1]["iterations"] == out[1][1]["iterations"] == 40
+    assert abs(out[0][1]["forceMax"] - out[1][1]["forceMax"]) <= 1e-5 * out[0][1]["forceMax"]
+    for a, b in zip(out[0][2], out[1][2]):
+        assert rel_err(b, a) <= 1e-5
