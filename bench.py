@@ -573,6 +573,36 @@ def run_c5(args):
         out[tag] = {"time_s": dt, "iterations": r["iterations"], "forceMax": r["forceMax"],
                     "converged": r["forceMax"] < 1e-6, "E_per_site": e, "site_steps_per_s": N * r["iterations"] / dt}
         lat.close()
+    if os.path.exists(WARMNET_WEIGHTS):
+        # learned warm start (net trained on c4 at 64^3, run on the whole 400^3 lattice) + FP32 FIRE
+        ws = importlib.import_module("qmin_gb300.warmstart")
+        net = q.WarmNet(1, d["L"])
+        net.set_params(np.load(WARMNET_WEIGHTS)["params"])
+        lat = lattice(q.FP32)
+        lat.warm_start(net)  # first call outside the timed region
+        lat.fire_init(force_cutoff=1e-6)
+        lat.fire_run(1)
+        lat.set_state(d["Q"], d["types"])
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        lat.warm_start(net)
+        t_inf = time.perf_counter() - t0
+        lat.fire_init(force_cutoff=1e-6)
+        r = lat.fire_run(args.c5_max_iterations)
+        torch.cuda.synchronize()
+        dt = time.perf_counter() - t0
+        Qf = lat.get_state()[0]
+        lat.close()
+        net.close()
+        fm64, e64 = ws.fp64_check(d, Qf)
+        ep = out["fire_fp64"]["E_per_site"]
+        rel = abs(e64 - ep) / abs(ep)
+        ok = bool(fm64 < 1e-6 and rel <= 1e-4)
+        out["warm_start_fp32"] = {"time_s": dt, "inference_s": t_inf, "iterations": r["iterations"],
+                                  "forceMax_fp64": fm64, "E_per_site_fp64": e64, "E_rel_vs_plain_fp64": rel,
+                                  "E_lower_than_plain": bool(e64 < ep), "protocol_pass": ok,
+                                  "protocol_time_s": dt + (0.0 if ok else out["fire_fp32"]["time_s"]),
+                                  "note": "net trained on c4 (64^3, walls + one sphere, no field); no retraining"}
     for name in ("adam", "lbfgs"):
         lat = lattice(q.FP32)
         torch.cuda.synchronize()

@@ -111,6 +111,36 @@ int qmin_set_state(qmin_handle h, const double *Q, const int32_t *types, int lay
 int qmin_get_state(qmin_handle h, double *Q, double *V, double *F, int layout);
 /* number of non-object sites (updater::getNTotal, baseUpdater.cpp:10-28) */
 int qmin_n_active(qmin_handle h, long long *n);
+/* lattice sides of the handle (cubicLattice::latticeSites) */
+int qmin_get_sides(qmin_handle h, int *Lx, int *Ly, int *Lz);
+/* site types as int32 (simpleModel::returnTypes) */
+int qmin_get_types(qmin_handle h, int32_t *types);
+/* overwrite Q only, keeping types, velocities and minimiser state (writing
+ * through simpleModel::returnPositions, as multirankSimulation::loadState does) */
+int qmin_set_positions(qmin_handle h, const double *Q, int layout);
+/* qTensorLatticeModel::computeDefectMeasures (qTensorLatticeModel.cpp:95-133):
+ * kind 0 largest eigenvalue of Q, 1 det Q, 2 (tr Q^2)^3 - 54 (det Q)^2, on
+ * sites with type <= 0; object sites get 0.  out: host, N doubles. */
+int qmin_defect_measures(qmin_handle h, int kind, double *out);
+
+/* ---- files ---- */
+/* multirankSimulation::saveState (multirankSimulation.cpp:616-665), single
+ * rank: writes <prefix>_x0y0z0.txt, one line per site whose x, y and z are
+ * multiples of lattice_skip: "x y z Qxx Qxy Qxz Qyy Qyz type defect"
+ * (tab-separated, numbers as C++ streams print them), defect =
+ * qmin_defect_measures(defect_kind). */
+int qmin_save_state(qmin_handle h, const char *prefix, int lattice_skip, int defect_kind);
+/* multirankSimulation::loadState (multirankSimulation.cpp:566-614), single
+ * rank: reads <prefix>_x0y0z0.txt and sets Q of every listed site; types and
+ * velocities are kept.  QMIN_EINVAL if the file cannot be opened or a listed
+ * site lies outside the lattice. */
+int qmin_load_state(qmin_handle h, const char *prefix);
+/* Binary exact-resume checkpoint (no reference counterpart): resident state,
+ * parameters, objects, FIRE / minimiser scalars and buffers, FIRE strategy.
+ * Loading needs a handle of the same sides, precision and metric mode; a run
+ * resumed from it repeats the saved run's iterations bit for bit. */
+int qmin_checkpoint_save(qmin_handle h, const char *path);
+int qmin_checkpoint_load(qmin_handle h, const char *path);
 
 /* ---- force and energy ---- */
 /* multirankSimulation::computeForces -> landauDeGennesLC::computeForces
@@ -143,6 +173,13 @@ int qmin_nesterov_run(qmin_handle h, double dt, double mu, double force_cutoff, 
  * (energyMinimizerLoLBFGS.h:29-44, .cpp:195-226); history reset when reset != 0 */
 int qmin_lbfgs_run(qmin_handle h, int m, double eta, double force_cutoff, int max_iterations, int reset,
                    int *iterations, double *force_max);
+
+/* energyMinimizerGradientDescent::setGradientDescentParameters + minimize
+ * (energyMinimizerGradientDescent.cpp:64-115): Q += dt F, forces at the new Q,
+ * forceMax = sqrt(sum F.F) / nTotal; at least one iteration; the iteration
+ * count restarts from 0 when reset != 0 (class defaults: dt 0.01, cutoff 1e-7) */
+int qmin_gd_run(qmin_handle h, double dt, double force_cutoff, int max_iterations, int reset, int *iterations,
+                double *force_max);
 
 /* ---- FIRE iteration strategy and diagnostics ---- */
 #define QMIN_FIRE_SEPARATE 0 /* predictor, derivative planes, force+kick, control as separate kernels */
@@ -284,6 +321,16 @@ int qmin_host_add_wall(int Lx, int Ly, int Lz, int xyz, int plane, int kind, dou
 /* multirankSimulation::createSphericalColloid (multirankSimulationBoundaries.cpp:169-215) */
 int qmin_host_add_sphere(int Lx, int Ly, int Lz, const double center[3], double radius, int kind, double W,
                          double S0, double *Q, int32_t *types, qmin_object *objs, int *nobj);
+
+/* multirankSimulation::createBoundaryFromFile (multirankSimulationBoundaries.cpp:7-96),
+ * single rank: reads a boundary file (first line the object count; per object
+ * a line "kind W S0 n" with kind 0 oriented / 1 degenerate planar, then n
+ * lines "x y z C1 C2 C3 C4 C5") and adds each object as qmin_host_add_wall
+ * does (sites wrapped periodically, their Q set to C1..C5, neighbours marked
+ * -1).  objs has room for max_objs entries; *nobj is updated.  QMIN_EINVAL on
+ * a missing file or a malformed line. */
+int qmin_host_boundary_file(int Lx, int Ly, int Lz, const char *path, double *Q, int32_t *types, qmin_object *objs,
+                            int max_objs, int *nobj);
 
 #ifdef __cplusplus
 }

@@ -31,6 +31,8 @@ EXPORTED_SYMBOLS = [
     "qmin_create", "qmin_destroy", "qmin_set_stream", "qmin_last_error_string", "qmin_kernel_launches",
     "qmin_set_params", "qmin_set_objects", "qmin_set_state", "qmin_get_state", "qmin_n_active", "qmin_force",
     "qmin_energy", "qmin_fire_init", "qmin_fire_run", "qmin_adam_run", "qmin_nesterov_run", "qmin_lbfgs_run",
+    "qmin_gd_run", "qmin_get_sides", "qmin_get_types", "qmin_set_positions", "qmin_defect_measures",
+    "qmin_save_state", "qmin_load_state", "qmin_checkpoint_save", "qmin_checkpoint_load", "qmin_host_boundary_file",
     "qmin_host_random_nematic", "qmin_host_add_wall", "qmin_host_add_sphere", "qmin_set_fire_kernel",
     "qmin_fire_profile", "qmin_fire_tuning", "qmin_energy_noalloc", "qmin_batch_create", "qmin_batch_destroy",
     "qmin_batch_set_params", "qmin_batch_set_solve", "qmin_batch_get_solve", "qmin_batch_fire_init",
@@ -100,6 +102,13 @@ def lib():
             "qmin_adam_run": [h, C.c_double, C.c_double, C.c_double, C.c_double, C.c_double, C.c_int, C.c_int, ip, dp],
             "qmin_nesterov_run": [h, C.c_double, C.c_double, C.c_double, C.c_int, C.c_int, ip, dp],
             "qmin_lbfgs_run": [h, C.c_int, C.c_double, C.c_double, C.c_int, C.c_int, ip, dp],
+            "qmin_gd_run": [h, C.c_double, C.c_double, C.c_int, C.c_int, ip, dp],
+            "qmin_get_sides": [h, ip, ip, ip], "qmin_get_types": [h, vp], "qmin_set_positions": [h, vp, C.c_int],
+            "qmin_defect_measures": [h, C.c_int, vp],
+            "qmin_save_state": [h, C.c_char_p, C.c_int, C.c_int], "qmin_load_state": [h, C.c_char_p],
+            "qmin_checkpoint_save": [h, C.c_char_p], "qmin_checkpoint_load": [h, C.c_char_p],
+            "qmin_host_boundary_file": [C.c_int, C.c_int, C.c_int, C.c_char_p, dp, ip, C.POINTER(Object), C.c_int,
+                                        ip],
             "qmin_host_random_nematic": [C.c_int, C.c_int, C.c_int, C.c_int, C.c_double, dp],
             "qmin_set_fire_kernel": [h, C.c_int],
             "qmin_batch_create": [C.c_int, ip, C.c_int, C.c_int, C.POINTER(C.c_void_p)],
@@ -185,6 +194,11 @@ class Geometry:
         c = (C.c_double * 3)(*[float(x) for x in center])
         _check(lib().qmin_host_add_sphere(*self.L, c, float(radius), int(kind), float(W), float(S0), _dp(self.Q),
                                           _ip(self.types), self.objs, C.byref(self.nobj)))
+
+    def add_boundary_file(self, path):
+        """Objects from a boundary file in the reference's format (createBoundaryFromFile)."""
+        _check(lib().qmin_host_boundary_file(*self.L, os.fsencode(path), _dp(self.Q), _ip(self.types), self.objs,
+                                             127, C.byref(self.nobj)))
 
     def objects(self):
         return [(self.objs[k].kind, self.objs[k].W, self.objs[k].S0) for k in range(self.nobj.value)]
@@ -296,6 +310,39 @@ class Lattice:
         _check(lib().qmin_lbfgs_run(self._h, int(m), eta, force_cutoff, int(max_iterations), int(reset), C.byref(it),
                                     C.byref(fm)))
         return dict(iterations=it.value, forceMax=fm.value)
+
+    def get_types(self):
+        t = np.zeros(self.N, dtype=np.int32)
+        _check(lib().qmin_get_types(self._h, t.ctypes.data))
+        return t
+
+    def set_positions(self, Q, layout=LAYOUT_AOS):
+        Q = np.ascontiguousarray(Q, dtype=np.float64)
+        _check(lib().qmin_set_positions(self._h, Q.ctypes.data, layout))
+
+    def defect_measures(self, kind=0):
+        """0 largest eigenvalue, 1 det Q, 2 (tr Q^2)^3 - 54 det(Q)^2 (object sites 0)."""
+        out = np.zeros(self.N)
+        _check(lib().qmin_defect_measures(self._h, int(kind), out.ctypes.data))
+        return out
+
+    def save_state(self, prefix, lattice_skip=1, defect_kind=0):
+        _check(lib().qmin_save_state(self._h, os.fsencode(prefix), int(lattice_skip), int(defect_kind)))
+
+    def load_state(self, prefix):
+        _check(lib().qmin_load_state(self._h, os.fsencode(prefix)))
+
+    def checkpoint_save(self, path):
+        _check(lib().qmin_checkpoint_save(self._h, os.fsencode(path)))
+
+    def checkpoint_load(self, path):
+        _check(lib().qmin_checkpoint_load(self._h, os.fsencode(path)))
+
+    def gd_run(self, max_iterations, dt=0.01, force_cutoff=1e-7, reset=True):
+        its, fm = C.c_int(), C.c_double()
+        _check(lib().qmin_gd_run(self._h, dt, force_cutoff, int(max_iterations), int(bool(reset)), C.byref(its),
+                                 C.byref(fm)))
+        return dict(iterations=its.value, forceMax=fm.value)
 
     def set_fire_kernel(self, mode):
         """FIRE_AUTO (default): autotuned; FIRE_FUSED: one tiled kernel per iteration; FIRE_SEPARATE;
@@ -528,6 +575,7 @@ class WarmNet:
         return n.value
 
 
-from .reference_api import (energyMinimizerAdam, energyMinimizerFIRE, energyMinimizerLoLBFGS,  # noqa: E402,F401
+from .reference_api import (energyMinimizerAdam, energyMinimizerFIRE, energyMinimizerGradientDescent,  # noqa: E402,F401
+                            energyMinimizerLoLBFGS,
                             energyMinimizerNesterovAG, landauDeGennesLC, multirankSimulation,
                             qTensorLatticeModel, boundaryObject, boundaryType)

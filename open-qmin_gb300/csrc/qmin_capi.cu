@@ -68,11 +68,11 @@ struct qmin_ctx {
     int max_type = 0;
     long long nTotal = 0;
     long long launches = 0;
-    // cached chunk graphs: 0 FIRE, 1 Adam, 2 Nesterov, 3 L-BFGS
-    cudaGraphExec_t graph[4] = {nullptr, nullptr, nullptr, nullptr};
-    int graph_per_iter[4] = {0, 0, 0, 0};
-    int graph_key[4] = {0, 0, 0, 0};
-    double graph_args[4][4] = {};  // scalar kernel arguments baked into each graph
+    // cached chunk graphs: 0 FIRE, 1 Adam, 2 Nesterov, 3 L-BFGS, 4 gradient descent
+    cudaGraphExec_t graph[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
+    int graph_per_iter[5] = {0, 0, 0, 0, 0};
+    int graph_key[5] = {0, 0, 0, 0, 0};
+    double graph_args[5][4] = {};  // scalar kernel arguments baked into each graph
     int version = 1;  // bumped whenever kernel arguments change
     // fused tiled FIRE path: second state buffer set (ping-pong) and the tile
     // configuration chosen by the autotuner for the current parameters
@@ -154,7 +154,7 @@ template <class T> static Lat<T> make_lat(qmin_ctx *h)
 
 static void free_ctx(qmin_ctx *h)
 {
-    for (int g = 0; g < 4; ++g)
+    for (int g = 0; g < 5; ++g)
         if (h->graph[g]) cudaGraphExecDestroy(h->graph[g]);
     void *bufs[] = {h->Q, h->V, h->F, h->D, h->types, h->objs, h->partials, h->stage, h->stage_t, h->fire, h->iter,
                     h->out5, h->M, h->S, h->alt, h->lbp, h->lbs, h->lby, h->Q2, h->V2, h->F2};
@@ -170,7 +170,7 @@ static void free_ctx(qmin_ctx *h)
 static void invalidate_graphs(qmin_ctx *h)
 {
     h->version++;
-    for (int g = 0; g < 4; ++g)
+    for (int g = 0; g < 5; ++g)
         if (h->graph[g]) {
             cudaGraphExecDestroy(h->graph[g]);
             h->graph[g] = nullptr;
@@ -366,6 +366,57 @@ int qmin_get_state(qmin_handle h, double *Q, double *V, double *F, int layout)
             h->launches += launch_soa_to_aos<float>((const float *)src[a], h->stage, h->N, h->P, layout, h->stream);
         CK(cudaMemcpyAsync(dst[a], h->stage, sizeof(double) * 5 * (size_t)h->N, cudaMemcpyDeviceToHost, h->stream));
     }
+    CK(cudaStreamSynchronize(h->stream));
+    return QMIN_OK;
+}
+
+int qmin_get_sides(qmin_handle h, int *Lx, int *Ly, int *Lz)
+{
+    if (!h) return fail(QMIN_EINVAL, "qmin_get_sides: null handle");
+    if (Lx) *Lx = h->Lx;
+    if (Ly) *Ly = h->Ly;
+    if (Lz) *Lz = h->Lz;
+    return QMIN_OK;
+}
+
+int qmin_get_types(qmin_handle h, int32_t *types)
+{
+    if (!h || !types) return fail(QMIN_EINVAL, "qmin_get_types: null argument");
+    if (!h->have_state) return fail(QMIN_ESTATE, "qmin_get_types: no state set");
+    std::vector<int8_t> t8((size_t)h->N);
+    CK(cudaMemcpyAsync(t8.data(), h->types, (size_t)h->N, cudaMemcpyDeviceToHost, h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+    for (int i = 0; i < h->N; ++i) types[i] = t8[i];
+    return QMIN_OK;
+}
+
+int qmin_set_positions(qmin_handle h, const double *Q, int layout)
+{
+    if (!h || !Q) return fail(QMIN_EINVAL, "qmin_set_positions: null argument");
+    if (layout != QMIN_LAYOUT_AOS && layout != QMIN_LAYOUT_SOA) return fail(QMIN_EINVAL, "qmin_set_positions: bad layout");
+    if (!h->have_state) return fail(QMIN_ESTATE, "qmin_set_positions: qmin_set_state has not been called");
+    int r = ensure_stage(h);
+    if (r) return r;
+    CK(cudaMemcpyAsync(h->stage, Q, sizeof(double) * 5 * (size_t)h->N, cudaMemcpyHostToDevice, h->stream));
+    if (h->prec == QMIN_FP64)
+        h->launches += launch_aos_to_soa<double>(h->stage, (double *)h->Q, h->N, h->P, layout, h->stream);
+    else
+        h->launches += launch_aos_to_soa<float>(h->stage, (float *)h->Q, h->N, h->P, layout, h->stream);
+    CK(cudaStreamSynchronize(h->stream));
+    return QMIN_OK;
+}
+
+int qmin_defect_measures(qmin_handle h, int kind, double *out)
+{
+    if (!h || !out) return fail(QMIN_EINVAL, "qmin_defect_measures: null argument");
+    if (kind < 0 || kind > 2) return fail(QMIN_EINVAL, "qmin_defect_measures: kind must be 0, 1 or 2");
+    if (!h->have_state) return fail(QMIN_ESTATE, "qmin_defect_measures: no state set");
+    int r = ensure_stage(h);
+    if (r) return r;
+    if (h->prec == QMIN_FP64) h->launches += launch_defects<double>(make_lat<double>(h), kind, h->stage, h->stream);
+    else h->launches += launch_defects<float>(make_lat<float>(h), kind, h->stage, h->stream);
+    CK(cudaGetLastError());
+    CK(cudaMemcpyAsync(out, h->stage, sizeof(double) * (size_t)h->N, cudaMemcpyDeviceToHost, h->stream));
     CK(cudaStreamSynchronize(h->stream));
     return QMIN_OK;
 }
@@ -847,6 +898,44 @@ int qmin_nesterov_run(qmin_handle h, double dt, double mu, double force_cutoff, 
     return QMIN_OK;
 }
 
+template <class T> static int gd_impl(qmin_ctx *h, double dt, int max_iterations)
+{
+    Lat<T> L = make_lat<T>(h);
+    const double args[4] = {dt, 0, 0, 0};
+    int r = capture_chunk(h, 4, args, [&]() {
+        int n = launch_gd_move<T>(L, h->iter, dt, h->stream);
+        n += launch_force<T>(L, h->grid, h->stream);
+        n += launch_ff_dot<T>(L, h->iter, h->partials, h->grid, h->stream);
+        n += launch_norm_control(h->iter, h->partials, h->grid, 0, 0.0, 0.0, h->stream);
+        return n;
+    });
+    if (r) return r;
+    return run_chunks(h, 4, h->iter, h->iter_h, max_iterations / kChunk + 2);
+}
+
+int qmin_gd_run(qmin_handle h, double dt, double force_cutoff, int max_iterations, int reset, int *iterations,
+                double *force_max)
+{
+    int r = ready(h, "qmin_gd_run");
+    if (r) return r;
+    // minimize(): forces at the current Q first, at least one iteration
+    // (energyMinimizerGradientDescent.cpp:91-98)
+    h->launches += h->prec == QMIN_FP64 ? launch_force<double>(make_lat<double>(h), h->grid, h->stream)
+                                        : launch_force<float>(make_lat<float>(h), h->grid, h->stream);
+    r = iter_begin(h, reset, 0.0, force_cutoff, max_iterations, true);
+    if (r) return r;
+    h->iter_h->ndof = h->nTotal;  // forceMax divides by nTotal (energyMinimizerGradientDescent.cpp:82)
+    CK(cudaMemcpyAsync(h->iter, h->iter_h, sizeof(IterDev), cudaMemcpyHostToDevice, h->stream));
+    r = h->prec == QMIN_FP64 ? gd_impl<double>(h, dt, max_iterations) : gd_impl<float>(h, dt, max_iterations);
+    if (r) return r;
+    CK(cudaMemcpyAsync(h->iter_h, h->iter, sizeof(IterDev), cudaMemcpyDeviceToHost, h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+    if (iterations) *iterations = h->iter_h->iterations;
+    if (force_max) *force_max = h->iter_h->forceMax;
+    if (h->iter_h->status) return fail(QMIN_ENONFINITE, "qmin_gd_run: non-finite force norm");
+    return QMIN_OK;
+}
+
 template <class T> static int lbfgs_impl(qmin_ctx *h, int m, double eta, int max_iterations)
 {
     Lat<T> L = make_lat<T>(h);
@@ -1017,4 +1106,158 @@ int qmin_warm_start(qmin_handle h, qmin_warmnet n)
     if (!rc) rc = qmin_warmnet_sync(n);
     h->fire_ready = false;
     return rc;
+}
+
+// ------------------------------------------------------------ checkpoint
+// Binary exact-resume checkpoint: the resident state in the device layout,
+// the force parameters and objects, the FIRE / minimiser scalars and optional
+// minimiser buffers, and the FIRE strategy in use (so a resumed run takes the
+// same reduction order).  Little-endian host format, version 1.
+namespace {
+struct CkpHeader {
+    char magic[8];
+    int32_t version, Lx, Ly, Lz, prec, metric_mode, nobj, have_params, fire_ready, lb_m, flags;
+    int32_t path, sep_cap, fused_cfg, fused_zc, fused_nblocks, tiled_cfg, tiled_zc, tiled_nblocks, fire_mode;
+    int64_t N, P;
+};
+enum { kCkpM = 1, kCkpS = 2, kCkpAlt = 4, kCkpLb = 8 };
+const char kCkpMagic[8] = {'Q', 'M', 'I', 'N', 'C', 'K', 'P', '1'};
+}  // namespace
+
+int qmin_checkpoint_save(qmin_handle h, const char *path)
+{
+    int r = ready(h, "qmin_checkpoint_save");
+    if (r) return r;
+    if (!path) return fail(QMIN_EINVAL, "qmin_checkpoint_save: null path");
+    CkpHeader hd;
+    memset(&hd, 0, sizeof hd);
+    memcpy(hd.magic, kCkpMagic, 8);
+    hd.version = 1;
+    hd.Lx = h->Lx; hd.Ly = h->Ly; hd.Lz = h->Lz;
+    hd.prec = h->prec; hd.metric_mode = h->metric_mode;
+    hd.nobj = (int32_t)h->objs_host.size();
+    hd.have_params = h->have_params; hd.fire_ready = h->fire_ready; hd.lb_m = h->lb_m;
+    hd.flags = (h->M ? kCkpM : 0) | (h->S ? kCkpS : 0) | (h->alt ? kCkpAlt : 0) | (h->lbp ? kCkpLb : 0);
+    hd.path = h->path; hd.sep_cap = h->sep_cap; hd.fused_cfg = h->fused_cfg; hd.fused_zc = h->fused_zc;
+    hd.fused_nblocks = h->fused_nblocks; hd.tiled_cfg = h->tiled_cfg; hd.tiled_zc = h->tiled_zc;
+    hd.tiled_nblocks = h->tiled_nblocks; hd.fire_mode = h->fire_mode;
+    hd.N = h->N; hd.P = h->P;
+    const size_t plane = 5 * (size_t)h->P * h->esz;
+    std::vector<char> buf(plane);
+    FILE *f = fopen(path, "wb");
+    if (!f) return fail(QMIN_EINVAL, std::string("qmin_checkpoint_save: cannot open ") + path);
+    bool ok = fwrite(&hd, sizeof hd, 1, f) == 1 && fwrite(&h->params, sizeof h->params, 1, f) == 1;
+    if (ok && hd.nobj) ok = fwrite(h->objs_host.data(), sizeof(qmin_object), hd.nobj, f) == (size_t)hd.nobj;
+    auto put = [&](const void *dev, size_t bytes) {
+        if (!ok) return;
+        if (buf.size() < bytes) buf.resize(bytes);
+        ok = cudaMemcpy(buf.data(), dev, bytes, cudaMemcpyDeviceToHost) == cudaSuccess &&
+             fwrite(buf.data(), 1, bytes, f) == bytes;
+    };
+    CK(cudaStreamSynchronize(h->stream));
+    put(h->Q, plane);
+    put(h->V, plane);
+    put(h->F, plane);
+    put(h->types, (size_t)h->N);
+    put(h->fire, sizeof(FireDev));
+    put(h->iter, sizeof(IterDev));
+    if (h->M) put(h->M, plane);
+    if (h->S) put(h->S, plane);
+    if (h->alt) put(h->alt, plane);
+    if (h->lbp) {
+        put(h->lbp, plane);
+        put(h->lbs, plane * h->lb_m);
+        put(h->lby, plane * h->lb_m);
+    }
+    ok = fclose(f) == 0 && ok;
+    if (!ok) return fail(QMIN_ECUDA, "qmin_checkpoint_save: write failed");
+    return QMIN_OK;
+}
+
+int qmin_checkpoint_load(qmin_handle h, const char *path)
+{
+    if (!h || !path) return fail(QMIN_EINVAL, "qmin_checkpoint_load: null argument");
+    FILE *f = fopen(path, "rb");
+    if (!f) return fail(QMIN_EINVAL, std::string("qmin_checkpoint_load: cannot open ") + path);
+    CkpHeader hd;
+    if (fread(&hd, sizeof hd, 1, f) != 1 || memcmp(hd.magic, kCkpMagic, 8) != 0 || hd.version != 1) {
+        fclose(f);
+        return fail(QMIN_EINVAL, "qmin_checkpoint_load: not a version-1 qmin checkpoint");
+    }
+    if (hd.Lx != h->Lx || hd.Ly != h->Ly || hd.Lz != h->Lz || hd.prec != h->prec || hd.metric_mode != h->metric_mode ||
+        hd.P != h->P) {
+        fclose(f);
+        return fail(QMIN_EINVAL, "qmin_checkpoint_load: lattice, precision or metric mode differ from the handle's");
+    }
+    qmin_ldg_params p;
+    std::vector<qmin_object> objs((size_t)std::max(hd.nobj, 0));
+    bool ok = fread(&p, sizeof p, 1, f) == 1 && hd.nobj >= 0 && hd.nobj <= 127;
+    if (ok && hd.nobj) ok = fread(objs.data(), sizeof(qmin_object), hd.nobj, f) == (size_t)hd.nobj;
+    if (ok && hd.have_params) ok = qmin_set_params(h, &p) == QMIN_OK;
+    if (ok) ok = qmin_set_objects(h, objs.data(), hd.nobj) == QMIN_OK;
+    const size_t plane = 5 * (size_t)h->P * h->esz;
+    std::vector<char> buf(plane);
+    auto get = [&](void *dev, size_t bytes) {
+        if (!ok) return;
+        if (buf.size() < bytes) buf.resize(bytes);
+        ok = fread(buf.data(), 1, bytes, f) == bytes &&
+             cudaMemcpy(dev, buf.data(), bytes, cudaMemcpyHostToDevice) == cudaSuccess;
+    };
+    CK(cudaStreamSynchronize(h->stream));
+    get(h->Q, plane);
+    get(h->V, plane);
+    get(h->F, plane);
+    get(h->types, (size_t)h->N);
+    get(h->fire, sizeof(FireDev));
+    get(h->iter, sizeof(IterDev));
+    if (ok && (hd.flags & kCkpM) && !alloc_planes(h, &h->M, 1)) get(h->M, plane);
+    if (ok && (hd.flags & kCkpS) && !alloc_planes(h, &h->S, 1)) get(h->S, plane);
+    if (ok && (hd.flags & kCkpAlt) && !alloc_planes(h, &h->alt, 1)) get(h->alt, plane);
+    if (ok && (hd.flags & kCkpLb)) {
+        if (h->lb_m != hd.lb_m) {
+            if (h->lbs) cudaFree(h->lbs);
+            if (h->lby) cudaFree(h->lby);
+            h->lbs = h->lby = nullptr;
+            h->lb_m = hd.lb_m;
+        }
+        ok = !alloc_planes(h, &h->lbp, 1) && !alloc_planes(h, &h->lbs, hd.lb_m) && !alloc_planes(h, &h->lby, hd.lb_m);
+        get(h->lbp, plane);
+        get(h->lbs, plane * hd.lb_m);
+        get(h->lby, plane * hd.lb_m);
+    }
+    fclose(f);
+    if (!ok) return fail(QMIN_EINVAL, "qmin_checkpoint_load: truncated or unreadable checkpoint");
+    // site counts from the restored types
+    std::vector<int8_t> t8((size_t)h->N);
+    CK(cudaMemcpy(t8.data(), h->types, (size_t)h->N, cudaMemcpyDeviceToHost));
+    long long nT = 0;
+    int mx = 0;
+    for (int i = 0; i < h->N; ++i) {
+        nT += t8[i] <= 0;
+        mx = std::max(mx, (int)t8[i]);
+    }
+    h->nTotal = nT;
+    h->max_type = mx;
+    h->have_state = true;
+    h->fire_ready = hd.fire_ready != 0;
+    CK(cudaMemcpy(h->fire_h, h->fire, sizeof(FireDev), cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(h->iter_h, h->iter, sizeof(IterDev), cudaMemcpyDeviceToHost));
+    invalidate_graphs(h);
+    // the FIRE strategy of the saved run, so the resumed run reduces in the same order
+    h->fire_mode = hd.fire_mode;
+    if (hd.path >= 0) {
+        int r = ensure_pingpong(h);
+        if (r) return r;
+        h->path = hd.path;
+        h->sep_cap = hd.sep_cap;
+        h->fused_cfg = hd.fused_cfg;
+        h->fused_zc = hd.fused_zc;
+        h->fused_nblocks = hd.fused_nblocks;
+        h->tiled_cfg = hd.tiled_cfg;
+        h->tiled_zc = hd.tiled_zc;
+        h->tiled_nblocks = hd.tiled_nblocks;
+        h->tuned_version = h->version;
+        h->tuned_mode = h->fire_mode;
+    }
+    return QMIN_OK;
 }

@@ -2,7 +2,10 @@
 // of these on the host even in GPU runs (openQmin.cpp:261-268); they are
 // one-time set-up, not part of the minimisation hot path.
 #include <cmath>
+#include <fstream>
 #include <random>
+#include <sstream>
+#include <string>
 #include <vector>
 
 #include "../../include/qmin_gb300.h"
@@ -153,3 +156,41 @@ int qmin_host_add_sphere(int Lx, int Ly, int Lz, const double center[3], double 
 }
 
 }  // extern "C"
+
+// multirankSimulation::createBoundaryFromFile (multirankSimulationBoundaries.cpp:43-96)
+// for one rank: every object's sites go through add_object (periodic wrap, Q
+// set from the file, neighbours marked -1).
+extern "C" int qmin_host_boundary_file(int Lx, int Ly, int Lz, const char *path, double *Q, int32_t *types,
+                                       qmin_object *objs, int max_objs, int *nobj)
+{
+    if (!path || !Q || !types || !objs || !nobj || Lx < 1 || Ly < 1 || Lz < 1) return QMIN_EINVAL;
+    std::ifstream in(path);
+    if (!in) return QMIN_EINVAL;
+    std::string line;
+    int count = 0;
+    if (!std::getline(in, line) || !(std::istringstream(line) >> count) || count < 0) return QMIN_EINVAL;
+    for (int o = 0; o < count; ++o) {
+        int kind = 0, n = 0;
+        double W = 0.0, S0 = 0.0;
+        if (!std::getline(in, line)) return QMIN_EINVAL;
+        std::istringstream hs(line);
+        if (!(hs >> kind >> W >> S0 >> n) || n < 0) return QMIN_EINVAL;
+        std::vector<int> xyz;
+        std::vector<double> qs;
+        xyz.reserve(3 * (size_t)n);
+        qs.reserve(5 * (size_t)n);
+        for (int e = 0; e < n && std::getline(in, line); ++e) {
+            std::istringstream ls(line);
+            int x, y, z;
+            double c[5];
+            if (!(ls >> x >> y >> z >> c[0] >> c[1] >> c[2] >> c[3] >> c[4])) return QMIN_EINVAL;
+            xyz.insert(xyz.end(), {x, y, z});
+            qs.insert(qs.end(), c, c + 5);
+        }
+        if (*nobj >= max_objs) return QMIN_EINVAL;
+        const int r = add_object(Lx, Ly, Lz, xyz, qs, kind == 0 ? QMIN_HOMEOTROPIC : QMIN_DEGENERATE_PLANAR, W, S0, Q,
+                                 types, objs, nobj);
+        if (r) return r;
+    }
+    return QMIN_OK;
+}

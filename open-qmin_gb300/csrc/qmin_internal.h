@@ -82,6 +82,9 @@ int launch_adam_step(const Lat<T> &L, T *M, T *S, IterDev *it, double beta1, dou
 template <class T>
 int launch_nesterov_step(const Lat<T> &L, T *alt, IterDev *it, double dt, double mu, double *partials, int grid,
                          cudaStream_t s);
+template <class T> int launch_defects(const Lat<T> &L, int kind, double *out, cudaStream_t s);
+template <class T> int launch_gd_move(const Lat<T> &L, IterDev *it, double dt, cudaStream_t s);
+template <class T> int launch_ff_dot(const Lat<T> &L, IterDev *it, double *partials, int grid, cudaStream_t s);
 int launch_norm_control(IterDev *it, const double *partials, int nparts, int adam, double beta1, double beta2,
                         cudaStream_t s);
 template <class T>

@@ -417,6 +417,86 @@ __global__ void __launch_bounds__(kBlock) k_nesterov(Lat<T> L, T *alt, const Ite
     if (threadIdx.x == 0) partials[blockIdx.x] = acc[0];
 }
 
+// energyMinimizerGradientDescent::gradientDescentCPU move (energyMinimizerGradientDescent.cpp:71):
+// Q += dt F on every site (object sites carry F = 0)
+template <class T>
+__global__ void __launch_bounds__(kBlock) k_gd_move(Lat<T> L, const IterDev *__restrict__ it, T dt)
+{
+    if (!it->active) return;
+    for (int i = blockIdx.x * kBlock + threadIdx.x; i < L.N; i += gridDim.x * kBlock)
+#pragma unroll
+        for (int k = 0; k < 5; ++k) L.Q[k * L.P + i] += dt * L.F[k * L.P + i];
+}
+
+// sum_i F_i . F_i (plain dot, energyMinimizerGradientDescent.cpp:75-79)
+template <class T>
+__global__ void __launch_bounds__(kBlock) k_ff_dot(Lat<T> L, const IterDev *__restrict__ it, double *partials)
+{
+    if (!it->active) return;
+    double acc[1] = {0.0};
+    for (int i = blockIdx.x * kBlock + threadIdx.x; i < L.N; i += gridDim.x * kBlock) {
+        T ff = T(0);
+#pragma unroll
+        for (int k = 0; k < 5; ++k) {
+            const T f = L.F[k * L.P + i];
+            ff += f * f;
+        }
+        acc[0] += (double)ff;
+    }
+    block_sum<1>(acc);
+    if (threadIdx.x == 0) partials[blockIdx.x] = acc[0];
+}
+
+// determinant of the traceless symmetric Q (Qzz = -Qxx - Qyy)
+template <class T> __device__ __forceinline__ double det_q(const T *qt)
+{
+    const double xx = qt[0], xy = qt[1], xz = qt[2], yy = qt[3], yz = qt[4], zz = -xx - yy;
+    return xx * (yy * zz - yz * yz) - xy * (xy * zz - yz * xz) + xz * (xy * yz - yy * xz);
+}
+
+// qTensorLatticeModel::computeDefectMeasures (qTensorLatticeModel.cpp:95-133) on
+// sites with type <= 0 (object sites get 0): 0 the largest eigenvalue
+// (trigonometric solution of the characteristic cubic, eigenvaluesOfQ,
+// qTensorFunctions.h:215-241), 1 det Q, 2 (tr Q^2)^3 - 54 (det Q)^2
+template <class T>
+__global__ void __launch_bounds__(kBlock) k_defects(Lat<T> L, int kind, double *out)
+{
+    const double pi = 3.14159265358979323846;
+    for (int i = blockIdx.x * kBlock + threadIdx.x; i < L.N; i += gridDim.x * kBlock) {
+        double v = 0.0;
+        if (L.types[i] <= 0) {
+            T qt[5];
+#pragma unroll
+            for (int k = 0; k < 5; ++k) qt[k] = L.Q[k * L.P + i];
+            if (kind == 0) {
+                const double q0 = qt[0], q1 = qt[1], q2 = qt[2], q3 = qt[3], q4 = qt[4];
+                const double off = q1 * q1 + q2 * q2 + q4 * q4;
+                if (off == 0.0) {
+                    v = fmax(fmax(q0, q3), -q0 - q3);
+                } else {
+                    // eigenvalues 2p cos(phi + 2 pi k / 3), p^2 = tr(Q^2) / 6, cos(3 phi) = det(Q / p) / 2
+                    const double p = sqrt((2.0 * (q0 * q0 + q3 * q3 + q0 * q3) + 2.0 * off) / 6.0);
+                    const double ip = 1.0 / p;
+                    const T b[5] = {T(ip * q0), T(ip * q1), T(ip * q2), T(ip * q3), T(ip * q4)};
+                    const double r = 0.5 * det_q(b);
+                    const double phi = r <= -1.0 ? pi / 3.0 : (r >= 1.0 ? 0.0 : acos(r) / 3.0);
+                    const double e1 = 2.0 * p * cos(phi), e3 = 2.0 * p * cos(phi + 2.0 * pi / 3.0);
+                    v = fmax(fmax(e1, -e1 - e3), e3);
+                }
+            } else {
+                const double d = det_q(qt);
+                if (kind == 1) {
+                    v = d;
+                } else {
+                    const double t2 = (double)tr_q2(qt);
+                    v = t2 * t2 * t2 - 54.0 * d * d;
+                }
+            }
+        }
+        out[i] = v;
+    }
+}
+
 // forceMax = sqrt(F.F) / Ndof and the while-condition of Adam / Nesterov
 __global__ void __launch_bounds__(kBlock) k_norm_control(IterDev *it, const double *partials, int nparts, int adam,
                                                          double beta1, double beta2)
@@ -667,6 +747,21 @@ int launch_nesterov_step(const Lat<T> &L, T *alt, IterDev *it, double dt, double
     k_nesterov<T><<<grid, kBlock, 0, s>>>(L, alt, it, T(dt), T(mu), partials);
     return 1;
 }
+template <class T> int launch_defects(const Lat<T> &L, int kind, double *out, cudaStream_t s)
+{
+    k_defects<T><<<elem_grid(L.N), kBlock, 0, s>>>(L, kind, out);
+    return 1;
+}
+template <class T> int launch_gd_move(const Lat<T> &L, IterDev *it, double dt, cudaStream_t s)
+{
+    k_gd_move<T><<<elem_grid(L.N), kBlock, 0, s>>>(L, it, T(dt));
+    return 1;
+}
+template <class T> int launch_ff_dot(const Lat<T> &L, IterDev *it, double *partials, int grid, cudaStream_t s)
+{
+    k_ff_dot<T><<<grid, kBlock, 0, s>>>(L, it, partials);
+    return 1;
+}
 int launch_norm_control(IterDev *it, const double *partials, int nparts, int adam, double beta1, double beta2,
                         cudaStream_t s)
 {
@@ -734,6 +829,9 @@ int launch_energy_full(const Lat<T> &L, double *partials, int grid, double *out5
                                      double *, int, cudaStream_t);                                                 \
     template int launch_nesterov_step<T>(const Lat<T> &, T *, IterDev *, double, double, double *, int,            \
                                          cudaStream_t);                                                            \
+    template int launch_defects<T>(const Lat<T> &, int, double *, cudaStream_t);                                   \
+    template int launch_gd_move<T>(const Lat<T> &, IterDev *, double, cudaStream_t);                                 \
+    template int launch_ff_dot<T>(const Lat<T> &, IterDev *, double *, int, cudaStream_t);                          \
     template int launch_lbfgs_first<T>(const Lat<T> &, T *, IterDev *, cudaStream_t);                              \
     template int launch_lbfgs_iteration<T>(const Lat<T> &, T *, T *, T *, IterDev *, int, double, double *, int,   \
                                            cudaStream_t);                                                          \

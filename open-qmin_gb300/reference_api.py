@@ -68,6 +68,11 @@ class qTensorLatticeModel:
     def returnTypes(self):
         return self.geometry.types.copy()
 
+    def computeDefectMeasures(self, defectType=0):
+        """qTensorLatticeModel::computeDefectMeasures; returns the per-site values."""
+        self.defectMeasures = self.lattice.defect_measures(defectType)
+        return self.defectMeasures
+
 
 class landauDeGennesLC:
     """Landau-de Gennes force: bulk A, B, C; L1-L4 distortion; anchoring; E/H fields."""
@@ -200,6 +205,24 @@ class energyMinimizerNesterovAG(_Updater):
         return r
 
 
+class energyMinimizerGradientDescent(_Updater):
+    def __init__(self, model=None):
+        super().__init__(model)
+        self.setGradientDescentParameters(0.01, 1e-7)
+        self.maxIterations = 1000  # energyMinimizerGradientDescent::initializeParameters
+
+    def setGradientDescentParameters(self, deltaT, forceCutoff):
+        self.deltaT, self.forceCutoff = deltaT, forceCutoff
+        self._fresh = True
+
+    def minimize(self):
+        r = self.sim.model.lattice.gd_run(self.maxIterations, dt=self.deltaT, force_cutoff=self.forceCutoff,
+                                          reset=self._fresh)
+        self._fresh = False
+        self.iterations, self.forceMax = r["iterations"], r["forceMax"]
+        return r
+
+
 class energyMinimizerLoLBFGS(_Updater):
     def __init__(self, model=None):
         super().__init__(model)
@@ -244,6 +267,15 @@ class multirankSimulation:
 
     def createSphericalColloid(self, center, radius, bObj):
         self.model.geometry.add_sphere(center, radius, bObj.boundary, bObj.P1, bObj.P2)
+
+    def createBoundaryFromFile(self, fname, verbose=False):
+        self.model.geometry.add_boundary_file(fname)
+
+    def saveState(self, fname, latticeSkip=1, defectType=0):
+        self.model.lattice.save_state(fname, latticeSkip, defectType)
+
+    def loadState(self, fname):
+        self.model.lattice.load_state(fname)
 
     def finalizeObjects(self):
         m = self.model

@@ -28,7 +28,7 @@ def _torch():
 def set_up_lattice(sol, precision, Q=None):
     lat = Lattice(sol["L"], precision)
     a, b, c = sol["consts"]
-    lat.set_params(a, b, c, *sol["Ls"])
+    lat.set_params(a, b, c, *sol["Ls"], E=sol.get("E"), H=sol.get("H"))
     lat.set_objects(sol["objects"])
     lat.set_state(sol["Q"] if Q is None else Q, sol["types"])
     return lat

@@ -148,6 +148,14 @@ static int add_object(const int L[3], int nsites, const int *xyz, const double *
     return nobj + 1;
 }
 
+/* one object from an explicit site list (the core of
+ * multirankSimulation::createBoundaryFromFile, multirankSimulationBoundaries.cpp:43-96) */
+int qo_add_sites(const int L[3], int nsites, const int *xyz, const double *qs, int kind, double W, double S0,
+                 double *Q, int *types, qo_object *objs, int nobj)
+{
+    return add_object(L, nsites, xyz, qs, kind, W, S0, Q, types, objs, nobj);
+}
+
 /* multirankSimulation::createWall (multirankSimulationBoundaries.cpp:101-167) */
 int qo_add_wall(const int L[3], int xyz, int plane, int kind, double W, double S0,
                 double *Q, int *types, qo_object *objs, int nobj)
@@ -850,6 +858,82 @@ int qo_nesterov(const qo_params *p, double *Q, double *F, const int *types, cons
         for (size_t i = 0; i < N; ++i) fn += tmp[i];
         forceMax = sqrt(fn) / N;
     }
+    free(tmp);
+    if (forcemax_out) *forcemax_out = forceMax;
+    return it;
+}
+
+/* determinantOfQ (qTensorFunctions.h:136-140) */
+static double det_q(const double *q)
+{
+    return q[3] * (q[1] * q[1] - q[0] * q[0] - q[2] * q[2]) + 2 * q[1] * q[2] * q[4] +
+           q[0] * (q[1] * q[1] - q[3] * q[3] - q[4] * q[4]);
+}
+
+/* qTensorLatticeModel::computeDefectMeasures (qTensorLatticeModel.cpp:95-133) with
+ * eigenvaluesOfQ (qTensorFunctions.h:215-241); object sites get 0 */
+void qo_defects(const qo_params *p, const double *Q, const int *types, int kind, double *out)
+{
+    const double pi = 3.14159265358979323846;
+    size_t N = (size_t)p->Lx * p->Ly * p->Lz;
+    for (size_t i = 0; i < N; ++i) {
+        const double *q = Q + 5 * i;
+        double v = 0.0;
+        if (types[i] <= 0) {
+            if (kind == 0) {
+                double a, b, c;
+                double p1 = q[1] * q[1] + q[2] * q[2] + q[4] * q[4];
+                if (p1 == 0) {
+                    a = q[0]; b = q[3]; c = -q[0] - q[3];
+                } else {
+                    double p2 = 2 * (q[0] * q[0] + q[3] * q[3] + q[0] * q[3]) + 2 * p1;
+                    double pp = sqrt(p2 / 6.0), ip = 1.0 / pp;
+                    double B[5] = {ip * q[0], ip * q[1], ip * q[2], ip * q[3], ip * q[4]};
+                    double r = 0.5 * det_q(B);
+                    double phi = r <= -1 ? pi / 3.0 : (r >= 1 ? 0.0 : acos(r) / 3.0);
+                    a = 2.0 * pp * cos(phi);
+                    c = 2.0 * pp * cos(phi + 2.0 * pi / 3.0);
+                    b = -a - c;
+                }
+                v = fmax(fmax(a, b), c);
+            } else if (kind == 1) {
+                v = det_q(q);
+            } else {
+                double t2 = 2.0 * (q[0] * q[0] + q[1] * q[1] + q[2] * q[2] + q[3] * q[3] + q[4] * q[4] + q[0] * q[3]);
+                double d = det_q(q);
+                v = t2 * t2 * t2 - 54.0 * d * d;
+            }
+        }
+        out[i] = v;
+    }
+}
+
+/* energyMinimizerGradientDescent::minimize / gradientDescentCPU
+ * (energyMinimizerGradientDescent.cpp:64-106): forces at Q on entry, then per
+ * iteration Q += dt F (qTensorLatticeModel::moveParticles), forces at the new Q,
+ * forceMax = sqrt(sum_i F_i.F_i) / nTotal with the plain dot product and
+ * nTotal = non-object sites; at least one iteration. */
+int qo_gd(const qo_params *p, double *Q, double *F, const int *types, const qo_object *objs, double dt, double fcut,
+          int max_iters, double *forcemax_out)
+{
+    size_t N = (size_t)p->Lx * p->Ly * p->Lz;
+    long long nTotal = 0;
+    for (size_t i = 0; i < N; ++i) nTotal += types[i] <= 0;
+    double *tmp = (double *)malloc(sizeof(double) * N);
+    double forceMax = 0.0;
+    int it = 0;
+    qo_force(p, Q, types, objs, F);
+    do {
+        it += 1;
+#pragma omp parallel for schedule(static)
+        for (long long j = 0; j < (long long)(5 * N); ++j) Q[j] += dt * F[j];
+        qo_force(p, Q, types, objs, F);
+#pragma omp parallel for schedule(static)
+        for (long long ii = 0; ii < (long long)N; ++ii) tmp[ii] = dot_plain(F + 5 * ii, F + 5 * ii);
+        double fn = 0.0;
+        for (size_t i = 0; i < N; ++i) fn += tmp[i];
+        forceMax = sqrt(fn) / (double)nTotal;
+    } while (it < max_iters && forceMax > fcut);
     free(tmp);
     if (forcemax_out) *forcemax_out = forceMax;
     return it;

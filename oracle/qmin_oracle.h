@@ -47,6 +47,9 @@ typedef struct {
 void qo_random_nematic(int N, unsigned seed, double S0, double *Q);
 int qo_add_wall(const int L[3], int xyz, int plane, int kind, double W, double S0,
                 double *Q, int *types, qo_object *objs, int nobj);
+int qo_add_sites(const int L[3], int nsites, const int *xyz, const double *qs, int kind, double W, double S0,
+                 double *Q, int *types, qo_object *objs, int nobj);
+void qo_defects(const qo_params *p, const double *Q, const int *types, int kind, double *out);
 int qo_add_sphere(const int L[3], const double center[3], double radius, int kind, double W, double S0,
                   double *Q, int *types, qo_object *objs, int nobj);
 int qo_count_active(int N, const int *types);
@@ -62,6 +65,8 @@ int qo_fire(const qo_params *p, double *Q, double *V, double *F, const int *type
 int qo_adam(const qo_params *p, double *Q, double *F, const int *types, const qo_object *objs,
             double beta1, double beta2, double eps, double dt, double fcut, int max_iters,
             double *M, double *S, double *forcemax_out);
+int qo_gd(const qo_params *p, double *Q, double *F, const int *types, const qo_object *objs, double dt, double fcut,
+          int max_iters, double *forcemax_out);
 int qo_nesterov(const qo_params *p, double *Q, double *F, const int *types, const qo_object *objs,
                 double dt, double mu, double fcut, int max_iters, double *alt, double *forcemax_out);
 int qo_lbfgs(const qo_params *p, double *Q, double *F, const int *types, const qo_object *objs,

@@ -56,6 +56,10 @@ def lib():
         dp, ip = C.POINTER(C.c_double), C.POINTER(C.c_int)
         L.qo_random_nematic.argtypes = [C.c_int, C.c_uint, C.c_double, dp]
         L.qo_add_wall.argtypes = [ip, C.c_int, C.c_int, C.c_int, C.c_double, C.c_double, dp, ip, C.POINTER(Object), C.c_int]
+        L.qo_add_sites.argtypes = [ip, C.c_int, ip, dp, C.c_int, C.c_double, C.c_double, dp, ip, C.POINTER(Object),
+                                   C.c_int]
+        L.qo_defects.argtypes = [C.POINTER(Params), dp, ip, C.c_int, dp]
+        L.qo_defects.restype = None
         L.qo_add_sphere.argtypes = [ip, dp, C.c_double, C.c_int, C.c_double, C.c_double, dp, ip, C.POINTER(Object), C.c_int]
         L.qo_count_active.argtypes = [C.c_int, ip]
         L.qo_force.argtypes = [C.POINTER(Params), dp, ip, C.POINTER(Object), dp]
@@ -68,6 +72,7 @@ def lib():
                               C.c_double, C.c_double, C.c_int, dp, dp, dp]
         L.qo_nesterov.argtypes = [C.POINTER(Params), dp, dp, ip, C.POINTER(Object), C.c_double, C.c_double,
                                   C.c_double, C.c_int, dp, dp]
+        L.qo_gd.argtypes = [C.POINTER(Params), dp, dp, ip, C.POINTER(Object), C.c_double, C.c_double, C.c_int, dp]
         L.qo_lbfgs.argtypes = [C.POINTER(Params), dp, dp, ip, C.POINTER(Object), C.c_int, C.c_double, C.c_double,
                                C.c_int, dp]
         L.qo_set_threads.argtypes = [C.c_int]
@@ -130,6 +135,35 @@ class System:
         self.nobj = lib().qo_add_sphere(Lc, cc, radius, kind, W, self.S0, _dp(self.Q), _ip(self.types), self.objs,
                                         self.nobj)
 
+    def add_sites(self, xyz, qs, kind, W, S0):
+        """One object from explicit sites (wrapped into the box) and their Q."""
+        Lc = (C.c_int * 3)(*self.L)
+        xyz = np.ascontiguousarray(xyz, dtype=np.int32).reshape(-1, 3)
+        qs = np.ascontiguousarray(qs, dtype=np.float64).reshape(-1, 5)
+        self.nobj = lib().qo_add_sites(Lc, len(xyz), _ip(xyz), _dp(qs), kind, W, S0, _dp(self.Q), _ip(self.types),
+                                       self.objs, self.nobj)
+
+    def add_boundary_file(self, path):
+        """multirankSimulation::createBoundaryFromFile (multirankSimulationBoundaries.cpp:43-96):
+        the object count, then per object "kind W S0 n" and n lines "x y z C1..C5"."""
+        lines = open(path).read().split("\n")
+        count = int(lines[0].split()[0])
+        pos = 1
+        for _ in range(count):
+            kind, W, S0, n = lines[pos].split()[:4]
+            pos += 1
+            rows = [ln.split() for ln in lines[pos:pos + int(n)] if ln.strip()]
+            pos += int(n)
+            xyz = [[int(r[0]), int(r[1]), int(r[2])] for r in rows]
+            qs = [[float(v) for v in r[3:8]] for r in rows]
+            self.add_sites(xyz, qs, 0 if int(kind) == 0 else 1, float(W), float(S0))
+
+    def defects(self, kind=0, Q=None):
+        out = np.zeros(self.N)
+        Q = self.Q if Q is None else np.ascontiguousarray(Q, dtype=np.float64)
+        lib().qo_defects(C.byref(self.p), _dp(Q), _ip(self.types), int(kind), _dp(out))
+        return out
+
     def n_active(self):
         return lib().qo_count_active(self.N, _ip(self.types))
 
@@ -174,6 +208,14 @@ class System:
         fm = C.c_double()
         n = lib().qo_nesterov(C.byref(self.p), _dp(self.Q), _dp(F), _ip(self.types), self.objs, dt, mu, fcut, iters,
                               _dp(alt), C.byref(fm))
+        return dict(iterations=n, forceMax=fm.value, F=F)
+
+    def gd(self, iters, dt=0.01, fcut=1e-7):
+        """energyMinimizerGradientDescent defaults: dt 0.01, cutoff 1e-7."""
+        F = np.zeros((self.N, 5))
+        fm = C.c_double()
+        n = lib().qo_gd(C.byref(self.p), _dp(self.Q), _dp(F), _ip(self.types), self.objs, dt, fcut, iters,
+                        C.byref(fm))
         return dict(iterations=n, forceMax=fm.value, F=F)
 
     def lbfgs(self, iters, eta=1e-4, m=5, fcut=1e-12):

@@ -9,7 +9,8 @@
 //   openQmin.cpp:173-175)  Ls=L1,L2,L3,L4,L6  wall=xyz,plane,kind,W
 //   sphere=cx,cy,cz,r,kind,W  (kind h = homeotropic, p = degenerate planar;
 //   S0 of every object is the bulk S0)  E=Ex,Ey,Ez,eps,eps0,deps
-//   H=Hx,Hy,Hz,chi,mu0,dchi  minimizer=fire|adam|nesterov|lbfgs|none  iters=N
+//   H=Hx,Hy,Hz,chi,mu0,dchi  minimizer=fire|adam|nesterov|lbfgs|gd|none  iters=N
+//   bfile=PATH (boundary file)  loadstate=PREFIX  savestate=PREFIX,SKIP,DEFECTTYPE  defects=1
 //   dt=DT  fc=cutoff  trace=1 (per-iteration trace, one minimize() call per
 //   iteration)  qin=file (load Q0 from a raw float64 AoS file instead of the
 //   random initialisation)
@@ -27,6 +28,7 @@
 #include "energyMinimizerFIRE.h"
 #include "energyMinimizerAdam.h"
 #include "energyMinimizerNesterovAG.h"
+#include "energyMinimizerGradientDescent.h"
 #include "energyMinimizerLoLBFGS.h"
 #include "noiseSource.h"
 #include <map>
@@ -101,6 +103,10 @@ int main(int argc, char **argv)
     double fc = atof(get("fc", "1e-12").c_str());
     bool trace = atoi(get("trace", "0").c_str()) != 0;
     string qin = get("qin", "");
+    string bfile = get("bfile", "");        // multirankSimulation::createBoundaryFromFile
+    string loadstate = get("loadstate", "");  // multirankSimulation::loadState prefix (before minimising)
+    string savestate = get("savestate", "");  // multirankSimulation::saveState prefix,skip,defectType (after)
+    bool defects = atoi(get("defects", "0").c_str()) != 0;  // dump computeDefectMeasures 0, 1, 2 (after)
 
     // openQmin.cpp:173-180
     double a = -1, b = -ABC[1] / ABC[0], c = -ABC[2] / ABC[0];
@@ -165,12 +171,15 @@ int main(int argc, char **argv)
         sim->createSphericalColloid(make_scalar3(atof(s[0].c_str()), atof(s[1].c_str()), atof(s[2].c_str())),
                                     atof(s[3].c_str()), bo);
     }
+    if (!bfile.empty()) sim->createBoundaryFromFile(bfile, false);
+    if (!loadstate.empty()) sim->loadState(loadstate);
     // minimisers are created after the initial state is in place, so that
     // state-copying constructors (Nesterov's alternate sequence) see Q0
     shared_ptr<FireProbe> fire;
     shared_ptr<energyMinimizerAdam> adam;
     shared_ptr<energyMinimizerNesterovAG> nest;
     shared_ptr<energyMinimizerLoLBFGS> lbfgs;
+    shared_ptr<energyMinimizerGradientDescent> gd;
     if (minimizer == "fire") {
         fire = make_shared<FireProbe>(Conf);
         fire->setMaximumIterations(iters);
@@ -188,6 +197,11 @@ int main(int argc, char **argv)
         nest->setNesterovAGParameters(dt, atof(get("mu", "0.01").c_str()), fc);
         nest->setMaximumIterations(iters);
         sim->addUpdater(nest, Conf);
+    } else if (minimizer == "gd") {
+        gd = make_shared<energyMinimizerGradientDescent>(Conf);
+        gd->setGradientDescentParameters(dt, fc);
+        gd->setMaximumIterations(iters);
+        sim->addUpdater(gd, Conf);
     } else if (minimizer == "lbfgs") {
         lbfgs = make_shared<energyMinimizerLoLBFGS>(Conf);
         lbfgs->setLoLBFGSParameters(5, dt, 1.0, fc, 10);
@@ -241,6 +255,18 @@ int main(int argc, char **argv)
         if (adam) { fmax = adam->getMaxForce(); done = adam->getCurrentIterations(); }
         if (nest) { fmax = nest->getMaxForce(); done = nest->getCurrentIterations(); }
         if (lbfgs) { fmax = lbfgs->getMaxForce(); done = lbfgs->getCurrentIterations(); }
+        if (gd) { fmax = gd->getMaxForce(); done = gd->getCurrentIterations(); }
+    }
+    if (defects) {
+        for (int dt2 = 0; dt2 < 3; ++dt2) {
+            Conf->computeDefectMeasures(dt2);
+            ArrayHandle<scalar> dm(Conf->returnDefectMeasures(), access_location::host, access_mode::read);
+            dump(out + "/defects" + to_string(dt2) + ".f64", dm.data, (size_t)N);
+        }
+    }
+    if (!savestate.empty()) {
+        vector<string> sv = parse_strs(savestate);
+        sim->saveState(sv[0], atoi(sv[1].c_str()), atoi(sv[2].c_str()));
     }
     dump_dvec(out + "/qfinal.f64", Conf->returnPositions(), N);
     dump_dvec(out + "/vfinal.f64", Conf->returnVelocities(), N);

@@ -8,8 +8,34 @@ import numpy as np
 GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
 
 
+_INPUT_DIR = None
+
+
+def _input_dir():
+    """A directory (removed at exit) holding the golden cases' input files."""
+    global _INPUT_DIR
+    if _INPUT_DIR is None:
+        import atexit
+        import shutil
+        import tempfile
+        _INPUT_DIR = tempfile.mkdtemp(prefix="qmin_golden_")
+        atexit.register(shutil.rmtree, _INPUT_DIR, True)
+    return _INPUT_DIR
+
+
 def load(name):
-    return dict(np.load(os.path.join(GOLDEN, name + ".npz")))
+    """A golden case; its input files (keys in_<file name with dots as _>) are
+    written to a temporary directory that replaces "{d}" in its arguments."""
+    g = dict(np.load(os.path.join(GOLDEN, name + ".npz")))
+    ins = [k for k in g if k.startswith("in_")]
+    if ins:
+        d = _input_dir()
+        for k in ins:
+            stem, _, ext = k[3:].rpartition("_")
+            with open(os.path.join(d, stem + "." + ext), "w") as f:
+                f.write(str(g[k]))
+        g["args"] = np.array(str(g["args"]).replace("{d}", d))
+    return g
 
 
 def parse_args(args):
@@ -40,6 +66,8 @@ def parse_args(args):
             cfg["iters"] = int(v)
         elif k == "dt":
             cfg["dt"] = float(v)
+        elif k in ("bfile", "loadstate"):
+            cfg[k] = v
     return cfg
 
 
@@ -50,7 +78,19 @@ def oracle_system(qo, cfg, metric_mode=0):
         s.add_wall(xyz, plane, kind, W)
     for c, r, kind, W in cfg["spheres"]:
         s.add_sphere(c, r, kind, W)
+    if "bfile" in cfg:
+        s.add_boundary_file(cfg["bfile"])
+    if "loadstate" in cfg:
+        load_state_text(s.Q, s.L, cfg["loadstate"] + "_x0y0z0.txt")
     return s
+
+
+def load_state_text(Q, L, path):
+    """multirankSimulation::loadState (multirankSimulation.cpp:581-613): Q of every listed site."""
+    vals = open(path).read().split()
+    for r in range(len(vals) // 10):
+        x, y, z = (int(v) for v in vals[10 * r:10 * r + 3])
+        Q[x + L[0] * (y + L[1] * z)] = [float(v) for v in vals[10 * r + 3:10 * r + 8]]
 
 
 def gpu_lattice(qmin, s, precision=0, metric_mode=0):
@@ -72,4 +112,4 @@ def rel_err(a, b):
 
 
 GOLDEN_CASES = ["l1_bulk_fire", "l123_walls_sphere_fire", "planar_sphere_fire", "l1234_planar_fields_fire",
-                "edges_gaps_wrap", "adam", "nesterov", "lbfgs"]
+                "edges_gaps_wrap", "adam", "nesterov", "lbfgs", "gd", "boundary_file_defects", "load_state"]

@@ -50,14 +50,68 @@ CASES = {
                   "minimizer=nesterov", "iters=25", "dt=0.0005"], True),
     "lbfgs": (["L=10,9,8", "seed=6", "Ls=2.32,0,0,0,0", "wall=0,0,p,1.0", "sphere=5,4,4,2.1,h,5.3",
                "minimizer=lbfgs", "iters=25", "dt=0.0005"], True),
+    # gradient descent (energyMinimizerGradientDescent, dt 0.01 is the class default)
+    "gd": (["L=10,9,8", "seed=8", "Ls=2.32,1.0,0.5,0,0", "wall=2,0,h,5.3", "sphere=5,4,4.5,2.3,p,1.2",
+            "minimizer=gd", "iters=30", "dt=0.01"], True),
+    # objects read from a boundary file, FIRE, defect measures and saveState (skip 2, largest eigenvalue)
+    "boundary_file_defects": (["L=12,10,9", "seed=31", "Ls=2.32,1.0,0.5,0,0", "bfile={d}/objects.txt",
+                               "minimizer=fire", "iters=15", "trace=1", "defects=1", "savestate={d}/st,2,0"], True),
+    # loadState of a state file (Q only; types are not loaded).  A FIRE updater is attached (with no
+    # iterations) because finalizeObjects takes NActive, the energy's divisor, from the updaters
+    "load_state": (["L=7,6,5", "seed=2", "Ls=2.32,0,0,0,0", "loadstate={d}/ld", "minimizer=fire", "iters=0"], True),
     # the 50^3 one-constant CLI run (openQmin -i 100 -l 50 --L1 2.32): scalars only
     "c1_50cube_fire100": (["L=50,50,50", "seed=13371", "Ls=2.32,0,0,0,0", "minimizer=fire", "iters=100",
                            "trace=1"], False),
 }
 
 
+def boundary_file_text():
+    """A boundary file in the reference's format (multirankSimulationBoundaries.cpp:7-41),
+    written here: a homeotropic 3x3x2 block with a tilted preferred director, and a
+    degenerate planar plate on z = 0 whose sites partly lie outside the box (x = -1
+    and x = 12 wrap periodically)."""
+    S0 = 0.53
+    n = np.array([0.3, -0.5, 0.81])
+    n = n / np.linalg.norm(n)
+    qb = 1.5 * S0 * (np.outer(n, n) - np.eye(3) / 3.0)
+    q5 = [qb[0, 0], qb[0, 1], qb[0, 2], qb[1, 1], qb[1, 2]]
+    block = [(x, y, z) for z in (6, 7) for y in (3, 4, 5) for x in (2, 3, 4)]
+    plate = [(x, y, 0) for y in range(0, 10, 3) for x in range(-1, 13)]
+    lines = ["2", f"0 4.0 {S0} {len(block)}"]
+    lines += [f"{x} {y} {z} " + " ".join(f"{v:.15g}" for v in q5) for (x, y, z) in block]
+    lines += [f"1 1.5 {S0} {len(plate)}"]
+    lines += [f"{x} {y} {z} 0 0 1 0 0" for (x, y, z) in plate]
+    return "\n".join(lines) + "\n"
+
+
+def state_file_text(L, seed):
+    """A state file in saveState's layout (multirankSimulation.cpp:616-665) for every
+    site of an L box, with seeded values, written here for the loadState case."""
+    rng = np.random.default_rng(seed)
+    rows = []
+    for z in range(L[2]):
+        for y in range(L[1]):
+            for x in range(L[0]):
+                q = rng.uniform(-0.3, 0.3, 5)
+                rows.append(f"{x}\t{y}\t{z}\t" + "\t".join(f"{v:g}" for v in q) + "\t0\t0")
+    return "\n".join(rows) + "\n"
+
+
+# cases that need input files (written into the run directory; "{d}" in an
+# argument is replaced by that directory) and collect output text files
+FILES = {
+    "boundary_file_defects": ({"objects.txt": boundary_file_text}, ["st_x0y0z0.txt"]),
+    "load_state": ({"ld_x0y0z0.txt": lambda: state_file_text((7, 6, 5), 3)}, []),
+}
+
+
 def run_case(name, args, full):
     with tempfile.TemporaryDirectory() as d:
+        pre, post = FILES.get(name, ({}, []))
+        for fn, make in pre.items():
+            with open(os.path.join(d, fn), "w") as f:
+                f.write(make())
+        args = [a.replace("{d}", d) for a in args]
         subprocess.run([DUMPER, d] + args, check=True, capture_output=True)
         ld = lambda f, dt=np.float64: np.fromfile(os.path.join(d, f), dtype=dt)
         out = {"args": np.array(json.dumps(args))}
@@ -75,14 +129,26 @@ def run_case(name, args, full):
             out["qfinal"] = ld("qfinal.f64").reshape(-1, 5)
             out["vfinal"] = ld("vfinal.f64").reshape(-1, 5)
             out["ffinal"] = ld("ffinal.f64").reshape(-1, 5)
+        for fn, make in pre.items():
+            out["in_" + fn.replace(".", "_")] = np.array(make())
+        for fn in post:
+            out["out_" + fn.replace(".", "_")] = np.array(open(os.path.join(d, fn)).read())
+        for k in range(3):
+            if os.path.exists(os.path.join(d, f"defects{k}.f64")):
+                out[f"defects{k}"] = ld(f"defects{k}.f64")
+        out["args"] = np.array(json.dumps([a.replace(d, "{d}") for a in args]))
         np.savez_compressed(os.path.join(HERE, name + ".npz"), **out)
 
 
-def main():
+def main(names=None):
+    """Regenerate every case, or only the named ones."""
     for name, (args, full) in CASES.items():
+        if names and name not in names:
+            continue
         run_case(name, args, full)
         print("wrote", name)
 
 
 if __name__ == "__main__":
-    main()
+    import sys
+    main(sys.argv[1:])

@@ -76,6 +76,11 @@ def test_host_setup_matches_reference(qmin, oracle, name):
         geo.add_wall(xyz, plane, kind, W, S0)
     for c, r, kind, W in cfg["spheres"]:
         geo.add_sphere(c, r, kind, W, S0)
+    if "bfile" in cfg:
+        geo.add_boundary_file(cfg["bfile"])
+    if "loadstate" in cfg:
+        from cases import load_state_text
+        load_state_text(geo.Q, cfg["L"], cfg["loadstate"] + "_x0y0z0.txt")
     np.testing.assert_array_equal(geo.types, g["types"].astype(np.int32))
     m = np.isfinite(g["q0"])
     np.testing.assert_array_equal(geo.Q[m], g["q0"][m])
@@ -94,3 +99,14 @@ def test_host_setup_rejects_bad_arguments(qmin):
     c = (C.c_double * 3)(1, 1, 1)
     assert lib.qmin_host_add_sphere(3, 3, 3, c, -1.0, 0, 1.0, 0.5, dp, ip, objs, C.byref(n)) == qmin.QMIN_EINVAL
     assert n.value == 0
+
+
+def test_boundary_file_rejects_malformed_input(qmin, tmp_path):
+    L = (6, 6, 6)
+    geo = qmin.Geometry(L, np.zeros((216, 5)))
+    with pytest.raises(qmin.QminError):
+        geo.add_boundary_file(str(tmp_path / "missing.txt"))
+    bad = tmp_path / "bad.txt"
+    bad.write_text("1\n0 1.0 0.5 2\n1 1 1 0 0 0 0 0\n1 2 x 0 0 0 0 0\n")
+    with pytest.raises(qmin.QminError):
+        geo.add_boundary_file(str(bad))

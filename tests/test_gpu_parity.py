@@ -93,7 +93,7 @@ def test_fire_per_iteration_trace(qmin, oracle, mode):
         assert r["nsince"] == int(row[5])
 
 
-@pytest.mark.parametrize("name", ["adam", "nesterov", "lbfgs"])
+@pytest.mark.parametrize("name", ["adam", "nesterov", "lbfgs", "gd"])
 def test_other_minimisers_fp64(qmin, oracle, name):
     g = load(name)
     cfg = parse_args(g["args"])
@@ -104,6 +104,9 @@ def test_other_minimisers_fp64(qmin, oracle, name):
         r = lat.adam_run(n, dt=dt)
     elif name == "nesterov":
         r = lat.nesterov_run(n, dt=dt)
+    elif name == "gd":
+        r = lat.gd_run(n, dt=dt)
+        assert rel_err(lat.get_state(Q=False, F=True)[2], g["ffinal"]) <= TOL_TRAJ
     else:
         r = lat.lbfgs_run(n, eta=dt)
     assert r["iterations"] == int(g["final"][0])

@@ -29,6 +29,9 @@ def test_minimiser(oracle, name):
     cfg = parse_args(g["args"])
     s = oracle_system(oracle, cfg)
     n = cfg["iters"]
+    if cfg["minimizer"] == "none" or n == 0:
+        np.testing.assert_array_equal(s.Q, g["qfinal"])
+        return
     if cfg["minimizer"] == "fire":
         r = s.fire(n, dt=cfg["dt"], trace=True)
         tr = g["trace"]
@@ -40,6 +43,9 @@ def test_minimiser(oracle, name):
         r = s.adam(n, dt=cfg["dt"])
     elif cfg["minimizer"] == "nesterov":
         r = s.nesterov(n, dt=cfg["dt"])
+    elif cfg["minimizer"] == "gd":
+        r = s.gd(n, dt=cfg["dt"])
+        assert rel_err(r["F"], g["ffinal"]) <= 1e-10
     else:
         r = s.lbfgs(n, eta=cfg["dt"])
     assert r["iterations"] == int(g["final"][0])
@@ -77,3 +83,13 @@ def test_metric_single_mode_is_one_correction(oracle):
     np.testing.assert_allclose(m0, Fc[:, 0], rtol=1e-12, atol=1e-14)
     np.testing.assert_allclose(m3, Fc[:, 3], rtol=1e-12, atol=1e-14)
     np.testing.assert_array_equal(F1[:, [1, 2, 4]], Fc[:, [1, 2, 4]])
+
+
+def test_defect_measures(oracle):
+    """computeDefectMeasures 0, 1, 2 on the reference's final state."""
+    g = load("boundary_file_defects")
+    s = oracle_system(oracle, parse_args(g["args"]))
+    for k in range(3):
+        d = s.defects(k, Q=g["qfinal"])
+        scale = np.abs(g[f"defects{k}"]).max()
+        np.testing.assert_allclose(d, g[f"defects{k}"], rtol=0, atol=1e-13 * scale)
