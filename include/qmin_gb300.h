@@ -123,7 +123,18 @@ int qmin_set_positions(qmin_handle h, const double *Q, int layout);
  * sites with type <= 0; object sites get 0.  out: host, N doubles. */
 int qmin_defect_measures(qmin_handle h, int kind, double *out);
 
+/* landauDeGennesLC::setSpatiallyVaryingField (landauDeGennesLC.cpp:81-123) with
+ * the field given directly: H is host AoS double[N][3] (NULL switches the
+ * field off); chi, mu0, dchi replace the H-field constants of qmin_set_params,
+ * as the reference's setter does.  Its force (landauDeGennesLCOtherForces.cpp:254-283)
+ * and energy (landauDeGennesLC.cpp:256-265) are the uniform H field's with
+ * each site's own H, on sites with type <= 0.  Call after qmin_set_params. */
+int qmin_set_field_map(qmin_handle h, const double *H, double chi, double mu0, double dchi);
+
 /* ---- files ---- */
+/* the same field read from <prefix>_x0y0z0.txt, lines "x y z Hx Hy Hz"
+ * (sites not listed get H = 0) */
+int qmin_load_field_map(qmin_handle h, const char *prefix, double chi, double mu0, double dchi);
 /* multirankSimulation::saveState (multirankSimulation.cpp:616-665), single
  * rank: writes <prefix>_x0y0z0.txt, one line per site whose x, y and z are
  * multiples of lattice_skip: "x y z Qxx Qxy Qxz Qyy Qyz type defect"

@@ -32,7 +32,7 @@ EXPORTED_SYMBOLS = [
     "qmin_set_params", "qmin_set_objects", "qmin_set_state", "qmin_get_state", "qmin_n_active", "qmin_force",
     "qmin_energy", "qmin_fire_init", "qmin_fire_run", "qmin_adam_run", "qmin_nesterov_run", "qmin_lbfgs_run",
     "qmin_gd_run", "qmin_get_sides", "qmin_get_types", "qmin_set_positions", "qmin_defect_measures",
-    "qmin_save_state", "qmin_load_state", "qmin_checkpoint_save", "qmin_checkpoint_load", "qmin_host_boundary_file",
+    "qmin_save_state", "qmin_load_state", "qmin_set_field_map", "qmin_load_field_map", "qmin_checkpoint_save", "qmin_checkpoint_load", "qmin_host_boundary_file",
     "qmin_host_random_nematic", "qmin_host_add_wall", "qmin_host_add_sphere", "qmin_set_fire_kernel",
     "qmin_fire_profile", "qmin_fire_tuning", "qmin_energy_noalloc", "qmin_batch_create", "qmin_batch_destroy",
     "qmin_batch_set_params", "qmin_batch_set_solve", "qmin_batch_get_solve", "qmin_batch_fire_init",
@@ -105,6 +105,8 @@ def lib():
             "qmin_gd_run": [h, C.c_double, C.c_double, C.c_int, C.c_int, ip, dp],
             "qmin_get_sides": [h, ip, ip, ip], "qmin_get_types": [h, vp], "qmin_set_positions": [h, vp, C.c_int],
             "qmin_defect_measures": [h, C.c_int, vp],
+            "qmin_set_field_map": [h, vp, C.c_double, C.c_double, C.c_double],
+            "qmin_load_field_map": [h, C.c_char_p, C.c_double, C.c_double, C.c_double],
             "qmin_save_state": [h, C.c_char_p, C.c_int, C.c_int], "qmin_load_state": [h, C.c_char_p],
             "qmin_checkpoint_save": [h, C.c_char_p], "qmin_checkpoint_load": [h, C.c_char_p],
             "qmin_host_boundary_file": [C.c_int, C.c_int, C.c_int, C.c_char_p, dp, ip, C.POINTER(Object), C.c_int,
@@ -325,6 +327,17 @@ class Lattice:
         out = np.zeros(self.N)
         _check(lib().qmin_defect_measures(self._h, int(kind), out.ctypes.data))
         return out
+
+    def set_field_map(self, H, chi, mu0, dchi):
+        """Per-site H field (N x 3; None switches it off); chi, mu0, dchi replace the H constants."""
+        if H is None:
+            _check(lib().qmin_set_field_map(self._h, None, chi, mu0, dchi))
+            return
+        H = np.ascontiguousarray(H, dtype=np.float64).reshape(self.N, 3)
+        _check(lib().qmin_set_field_map(self._h, H.ctypes.data, chi, mu0, dchi))
+
+    def load_field_map(self, prefix, chi, mu0, dchi):
+        _check(lib().qmin_load_field_map(self._h, os.fsencode(prefix), chi, mu0, dchi))
 
     def save_state(self, prefix, lattice_skip=1, defect_kind=0):
         _check(lib().qmin_save_state(self._h, os.fsencode(prefix), int(lattice_skip), int(defect_kind)))

@@ -77,6 +77,8 @@ struct qmin_ctx {
     // fused tiled FIRE path: second state buffer set (ping-pong) and the tile
     // configuration chosen by the autotuner for the current parameters
     void *Q2 = nullptr, *V2 = nullptr, *F2 = nullptr;
+    void *hvar = nullptr;  // spatially varying H field (3 planes), active when hvar_on
+    bool hvar_on = false;
     int fire_mode = QMIN_FIRE_AUTO;  // strategy requested by the caller
     // strategy chosen by the autotuner for the current parameters
     int path = -1;  // 0 separate kernels, 1 fused tiled kernel, 2 separate with the staged force + kick
@@ -149,6 +151,8 @@ template <class T> static Lat<T> make_lat(qmin_ctx *h)
     L.D = (T *)h->D;
     L.objs = (const ObjDev<T> *)h->objs;
     fill_lat_params(L, h->params, h->metric_mode);
+    L.Hv = h->hvar_on ? (const T *)h->hvar : nullptr;
+    L.hvp = T(h->params.dchi * h->params.mu0);
     return L;
 }
 
@@ -157,7 +161,7 @@ static void free_ctx(qmin_ctx *h)
     for (int g = 0; g < 5; ++g)
         if (h->graph[g]) cudaGraphExecDestroy(h->graph[g]);
     void *bufs[] = {h->Q, h->V, h->F, h->D, h->types, h->objs, h->partials, h->stage, h->stage_t, h->fire, h->iter,
-                    h->out5, h->M, h->S, h->alt, h->lbp, h->lbs, h->lby, h->Q2, h->V2, h->F2};
+                    h->out5, h->M, h->S, h->alt, h->lbp, h->lbs, h->lby, h->Q2, h->V2, h->F2, h->hvar};
     for (void *b : bufs)
         if (b) cudaFree(b);
     if (h->fire_h) cudaFreeHost(h->fire_h);
@@ -367,6 +371,39 @@ int qmin_get_state(qmin_handle h, double *Q, double *V, double *F, int layout)
         CK(cudaMemcpyAsync(dst[a], h->stage, sizeof(double) * 5 * (size_t)h->N, cudaMemcpyDeviceToHost, h->stream));
     }
     CK(cudaStreamSynchronize(h->stream));
+    return QMIN_OK;
+}
+
+int qmin_set_field_map(qmin_handle h, const double *H, double chi, double mu0, double dchi)
+{
+    if (!h) return fail(QMIN_EINVAL, "qmin_set_field_map: null handle");
+    if (!h->have_params) return fail(QMIN_ESTATE, "qmin_set_field_map: qmin_set_params has not been called");
+    h->params.chi = chi;  // setSpatiallyVaryingField replaces the field constants (landauDeGennesLC.cpp:83-85)
+    h->params.mu0 = mu0;
+    h->params.dchi = dchi;
+    invalidate_graphs(h);
+    if (!H) {
+        h->hvar_on = false;
+        return QMIN_OK;
+    }
+    if (!h->hvar && cudaMalloc(&h->hvar, 3 * (size_t)h->P * h->esz) != cudaSuccess) {
+        cudaGetLastError();
+        return fail(QMIN_ENOMEM, "qmin_set_field_map: allocation failed");
+    }
+    // AoS N x 3 -> 3 planes in the state precision
+    const size_t N = (size_t)h->N, P = (size_t)h->P;
+    if (h->prec == QMIN_FP64) {
+        std::vector<double> planes(3 * P, 0.0);
+        for (size_t i = 0; i < N; ++i)
+            for (int c = 0; c < 3; ++c) planes[c * P + i] = H[3 * i + c];
+        CK(cudaMemcpy(h->hvar, planes.data(), 3 * P * sizeof(double), cudaMemcpyHostToDevice));
+    } else {
+        std::vector<float> planes(3 * P, 0.0f);
+        for (size_t i = 0; i < N; ++i)
+            for (int c = 0; c < 3; ++c) planes[c * P + i] = (float)H[3 * i + c];
+        CK(cudaMemcpy(h->hvar, planes.data(), 3 * P * sizeof(float), cudaMemcpyHostToDevice));
+    }
+    h->hvar_on = true;
     return QMIN_OK;
 }
 

@@ -116,7 +116,7 @@ __device__ __forceinline__ T deriv2_rule(int t, int td, int tu, T qd, T q, T qu)
 //   type <0: F = M(-phase - distortion + anchoring - fields)
 // metric_mode 1 applies M once everywhere (the reference GPU branch).
 template <class T, class A>
-__device__ __forceinline__ void site_force_core(const Lat<T> &L, const A &acc, int t, T *f)
+__device__ __forceinline__ void site_force_core(const Lat<T> &L, const A &acc, int t, T *f, const T *hs = nullptr)
 {
     if (t > 0) {
 #pragma unroll
@@ -236,7 +236,26 @@ __device__ __forceinline__ void site_force_core(const Lat<T> &L, const A &acc, i
     if (L.hfield)
 #pragma unroll
         for (int k = 0; k < 5; ++k) f[k] -= L.fH[k];
+    if (hs) {
+        // landauDeGennesLC::computeSpatiallyVaryingFieldCPU (landauDeGennesLCOtherForces.cpp:254-283):
+        // the uniform-field force with this site's H
+        const T hx = hs[0], hy = hs[1], hz = hs[2], fp = L.hvp;
+        f[0] -= T(-0.5) * fp * (hx * hx - hz * hz);
+        f[1] -= -fp * hx * hy;
+        f[2] -= -fp * hx * hz;
+        f[3] -= T(-0.5) * fp * (hy * hy - hz * hz);
+        f[4] -= -fp * hy * hz;
+    }
     metric(f);
+}
+
+// this site's spatially varying field (3 values) when one is set, else null
+template <class T> __device__ __forceinline__ const T *site_field(const Lat<T> &L, long long i, T (&h)[3])
+{
+    if (!L.Hv) return nullptr;
+#pragma unroll
+    for (int c = 0; c < 3; ++c) h[c] = L.Hv[c * L.P + i];
+    return h;
 }
 
 // accessor over the global SoA planes; neighbour derivatives from the D planes.
@@ -271,7 +290,8 @@ __device__ __forceinline__ void site_force(const Lat<T> &L, int i, T *f)
         return;
     }
     GlobalAcc<T> acc(L, i);
-    site_force_core(L, acc, t, f);
+    T h[3];
+    site_force_core(L, acc, t, f, site_field(L, i, h));
 }
 
 }  // namespace qmin

@@ -181,9 +181,11 @@ __global__ void __launch_bounds__(TX *BY) k_fire_fused(Lat<T> L, T *__restrict__
                     bool deep = (t == 0);
 #pragma unroll
                     for (int sn = 0; sn < 6; ++sn) deep = deep && (a.B::tn(sn) == 0);
-                    if (deep) site_force_core(L, a, 0, f);
-                    else site_force_core(L, static_cast<const Acc &>(a), t, f);
                     const long long i = (long long)gx + (long long)L.Lx * gy + (long long)sxy * z;
+                    T hv[3];
+                    const T *hp = site_field(L, i, hv);
+                    if (deep) site_force_core(L, a, 0, f, hp);
+                    else site_force_core(L, static_cast<const Acc &>(a), t, f, hp);
                     T v2[5];
 #pragma unroll
                     for (int k = 0; k < 5; ++k) {

@@ -28,6 +28,8 @@ template <class T> struct Lat {
     T a, b, c;          // A/2, B/3, C/4
     T L1, L2, L3, L4;
     T fE[5], fH[5];     // uniform-field force vectors (subtracted, as the reference does)
+    const T *Hv;        // spatially varying H field, 3 planes of stride P, or null
+    T hvp;              // its dchi * mu0
     int metric_mode, multi, efield, hfield;
     T cb[5 * QMIN_BULK_W];  // combined bulk multi-constant coefficients
 };

@@ -79,3 +79,32 @@ extern "C" int qmin_load_state(qmin_handle h, const char *prefix)
     std::fclose(f);
     return qmin_set_positions(h, Q.data(), QMIN_LAYOUT_AOS);
 }
+
+extern "C" int qmin_load_field_map(qmin_handle h, const char *prefix, double chi, double mu0, double dchi)
+{
+    if (!h || !prefix) return set_error(QMIN_EINVAL, "qmin_load_field_map: null argument");
+    int Lx = 0, Ly = 0, Lz = 0;
+    int r = qmin_get_sides(h, &Lx, &Ly, &Lz);
+    if (r) return r;
+    const size_t N = (size_t)Lx * Ly * Lz;
+    std::vector<double> H(3 * N, 0.0);  // sites not listed keep a zero field
+    const std::string fn = state_file(prefix);
+    FILE *f = std::fopen(fn.c_str(), "r");
+    if (!f) return set_error(QMIN_EINVAL, "qmin_load_field_map: cannot open " + fn);
+    double fx, fy, fz, hx, hy, hz;
+    // landauDeGennesLC::setSpatiallyVaryingField: `while (file >> fx >> fy >> fz >> Hx >> Hy >> Hz)`,
+    // positions read as reals and truncated to int
+    while (std::fscanf(f, "%lf %lf %lf %lf %lf %lf", &fx, &fy, &fz, &hx, &hy, &hz) == 6) {
+        const int x = (int)fx, y = (int)fy, z = (int)fz;
+        if (x < 0 || y < 0 || z < 0 || x >= Lx || y >= Ly || z >= Lz) {
+            std::fclose(f);
+            return set_error(QMIN_EINVAL, "qmin_load_field_map: a site in " + fn + " lies outside the lattice");
+        }
+        const size_t i = (size_t)x + (size_t)Lx * ((size_t)y + (size_t)Ly * z);
+        H[3 * i] = hx;
+        H[3 * i + 1] = hy;
+        H[3 * i + 2] = hz;
+    }
+    std::fclose(f);
+    return qmin_set_field_map(h, H.data(), chi, mu0, dchi);
+}

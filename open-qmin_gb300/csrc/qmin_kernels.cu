@@ -240,6 +240,13 @@ __global__ void __launch_bounds__(kBlock) k_energy(Lat<T> L, double *partials, d
                                      T(0.5) * hz * hz * (c - dc * q[0] - dc * q[3]) -
                                      T(0.5) * hy * hy * (c + dc * q[3]) - dc * hy * hz * q[4]));
         }
+        if (L.Hv) {
+            // landauDeGennesLC.cpp:256-265: the H-field density with this site's H
+            const T hx = L.Hv[i], hy = L.Hv[P + i], hz = L.Hv[2 * P + i], c = T(chi), m0 = T(mu0), dc = T(dchi);
+            acc[4] += (double)(m0 * (T(-0.5) * hx * hx * (c + dc * q[0]) - dc * hx * hy * q[1] - dc * hx * hz * q[2] -
+                                     T(0.5) * hz * hz * (c - dc * q[0] - dc * q[3]) -
+                                     T(0.5) * hy * hy * (c + dc * q[3]) - dc * hy * hz * q[4]));
+        }
         const Nb b = neighbours(L, i);
         T d[15];
         site_derivs(L, i, t, b, d);

@@ -165,7 +165,8 @@ __global__ void __launch_bounds__(TX *BY, (sizeof(T) == 4 && MULTI) ? 2 : 1)
                     for (int k = 0; k < 5; ++k) vo[k] = L.V[k * P + i];
                     a.p = (ly + 1) * SX + (lx + 1);
                     T f[5], v[5];
-                    site_force_core(L, a, (int)sT[a.s0 * TS + a.p], f);
+                    T hv[3];
+                    site_force_core(L, a, (int)sT[a.s0 * TS + a.p], f, site_field(L, i, hv));
 #pragma unroll
                     for (int k = 0; k < 5; ++k) {
                         v[k] = vo[k] + hdt * f[k];

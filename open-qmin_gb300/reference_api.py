@@ -104,10 +104,16 @@ class landauDeGennesLC:
     def setHField(self, field, chi, mu0, deltaChi):
         self.H = (float(field[0]), float(field[1]), float(field[2]), chi, mu0, deltaChi)
 
+    def setSpatiallyVaryingField(self, fname, chi, mu0, deltaChi, rankParity=(0, 0, 0)):
+        """Per-site H field read from fname_x0y0z0.txt (single rank)."""
+        self.field_map = (fname, chi, mu0, deltaChi)
+
     def apply(self, lattice):
         multi = self.multi if self.multi is not None else any(x != 0 for x in (self.L2, self.L3, self.L4))
         lattice.set_params(self.A, self.B, self.C, self.L1, self.L2, self.L3, self.L4, multi_constant=multi,
                            E=self.E, H=self.H)
+        if getattr(self, "field_map", None):
+            lattice.load_field_map(*self.field_map)
 
     def computeForces(self):
         return self.sim.computeForces()

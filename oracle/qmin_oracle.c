@@ -571,6 +571,12 @@ void qo_force(const qo_params *p, const double *Q, const int *types, const qo_ob
             for (int k = 0; k < 5; ++k) f[k] -= fE[k];
         if (p->hfield)
             for (int k = 0; k < 5; ++k) f[k] -= fH[k];
+        if (p->hvar) {
+            /* landauDeGennesLC::computeSpatiallyVaryingFieldCPU (landauDeGennesLCOtherForces.cpp:254-283) */
+            double g[5];
+            field_force(p->hvar + 3 * i, p->dchi, p->mu0, g);
+            for (int k = 0; k < 5; ++k) f[k] -= g[k];
+        }
         metric(f);
     }
     free(D);
@@ -618,6 +624,14 @@ double qo_energy(const qo_params *p, const double *Q, const int *types, const qo
                               p->dchi * H[0] * H[2] * q[2] -
                               0.5 * H[2] * H[2] * (p->chi - p->dchi * q[0] - p->dchi * q[3]) -
                               0.5 * H[1] * H[1] * (p->chi + p->dchi * q[3]) - p->dchi * H[1] * H[2] * q[4]);
+        }
+        if (p->hvar) {
+            /* landauDeGennesLC.cpp:256-265: same density as the uniform H field, per-site H */
+            const double *H = p->hvar + 3 * i;
+            ei[4] += p->mu0 * (-0.5 * H[0] * H[0] * (p->chi + p->dchi * q[0]) - p->dchi * H[0] * H[1] * q[1] -
+                               p->dchi * H[0] * H[2] * q[2] -
+                               0.5 * H[2] * H[2] * (p->chi - p->dchi * q[0] - p->dchi * q[3]) -
+                               0.5 * H[1] * H[1] * (p->chi + p->dchi * q[3]) - p->dchi * H[1] * H[2] * q[4]);
         }
         qo_nbrs n;
         neighbours(L, i, &n);

@@ -28,6 +28,8 @@ typedef struct {
     double E[3], eps, eps0, deps;  /* setEField (landauDeGennesLC.h:76-83) */
     double H[3], chi, mu0, dchi;   /* setHField (landauDeGennesLC.h:84-91) */
     int metric_mode;         /* 0: CPU path (M^2 on type 0, M on type < 0), 1: M once everywhere */
+    const double *hvar;      /* spatially varying H field, N x 3 per site, or NULL
+                                (landauDeGennesLC::setSpatiallyVaryingField, landauDeGennesLC.cpp:81-123) */
 } qo_params;
 
 typedef struct { int kind; double W, S0; } qo_object; /* kind 0 homeotropic, 1 degenerate planar */

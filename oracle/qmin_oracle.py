@@ -22,7 +22,7 @@ class Params(C.Structure):
                 ("multi_constant", C.c_int), ("efield", C.c_int), ("hfield", C.c_int),
                 ("E", C.c_double * 3), ("eps", C.c_double), ("eps0", C.c_double), ("deps", C.c_double),
                 ("H", C.c_double * 3), ("chi", C.c_double), ("mu0", C.c_double), ("dchi", C.c_double),
-                ("metric_mode", C.c_int)]
+                ("metric_mode", C.c_int), ("hvar", C.POINTER(C.c_double))]
 
 
 class Object(C.Structure):
@@ -134,6 +134,13 @@ class System:
         cc = (C.c_double * 3)(*center)
         self.nobj = lib().qo_add_sphere(Lc, cc, radius, kind, W, self.S0, _dp(self.Q), _ip(self.types), self.objs,
                                         self.nobj)
+
+    def set_field_map(self, H, chi, mu0, dchi):
+        """landauDeGennesLC::setSpatiallyVaryingField: per-site H (N x 3); chi, mu0,
+        dchi replace the uniform field's constants."""
+        self._hvar = np.ascontiguousarray(H, dtype=np.float64).reshape(self.N, 3)
+        self.p.hvar = _dp(self._hvar)
+        self.p.chi, self.p.mu0, self.p.dchi = chi, mu0, dchi
 
     def add_sites(self, xyz, qs, kind, W, S0):
         """One object from explicit sites (wrapped into the box) and their Q."""

@@ -11,6 +11,7 @@
 //   S0 of every object is the bulk S0)  E=Ex,Ey,Ez,eps,eps0,deps
 //   H=Hx,Hy,Hz,chi,mu0,dchi  minimizer=fire|adam|nesterov|lbfgs|gd|none  iters=N
 //   bfile=PATH (boundary file)  loadstate=PREFIX  savestate=PREFIX,SKIP,DEFECTTYPE  defects=1
+//   hfile=PREFIX,chi,mu0,dchi (spatially varying H field)
 //   dt=DT  fc=cutoff  trace=1 (per-iteration trace, one minimize() call per
 //   iteration)  qin=file (load Q0 from a raw float64 AoS file instead of the
 //   random initialisation)
@@ -136,6 +137,13 @@ int main(int argc, char **argv)
         lc->setHField(make_scalar3(h[0], h[1], h[2]), h[3], h[4], h[5]);
     }
     lc->setModel(Conf);
+    if (kv.count("hfile")) {
+        // landauDeGennesLC::setSpatiallyVaryingField(prefix, chi, mu0, dchi, rank parity 0)
+        vector<string> hf = parse_strs(get("hfile", ""));
+        int3 parity;
+        parity.x = parity.y = parity.z = 0;
+        lc->setSpatiallyVaryingField(hf[0], atof(hf[1].c_str()), atof(hf[2].c_str()), atof(hf[3].c_str()), parity);
+    }
     sim->addForce(lc);
 
     // openQmin.cpp:261-268 and setInitialConditions.h:37-41

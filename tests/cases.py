@@ -68,6 +68,9 @@ def parse_args(args):
             cfg["dt"] = float(v)
         elif k in ("bfile", "loadstate"):
             cfg[k] = v
+        elif k == "hfile":
+            f = v.split(",")
+            cfg["hfile"] = (f[0], float(f[1]), float(f[2]), float(f[3]))
     return cfg
 
 
@@ -82,6 +85,15 @@ def oracle_system(qo, cfg, metric_mode=0):
         s.add_boundary_file(cfg["bfile"])
     if "loadstate" in cfg:
         load_state_text(s.Q, s.L, cfg["loadstate"] + "_x0y0z0.txt")
+    if "hfile" in cfg:
+        prefix, chi, mu0, dchi = cfg["hfile"]
+        H = np.zeros((s.N, 3))
+        vals = open(prefix + "_x0y0z0.txt").read().split()
+        for r in range(len(vals) // 6):
+            x, y, z = (int(float(v)) for v in vals[6 * r:6 * r + 3])
+            H[x + s.L[0] * (y + s.L[1] * z)] = [float(v) for v in vals[6 * r + 3:6 * r + 6]]
+        s.set_field_map(H, chi, mu0, dchi)
+        s.hfile = cfg["hfile"]
     return s
 
 
@@ -102,6 +114,8 @@ def gpu_lattice(qmin, s, precision=0, metric_mode=0):
                    H=(p.H[0], p.H[1], p.H[2], p.chi, p.mu0, p.dchi) if p.hfield else None)
     lat.set_objects([(s.objs[k].kind, s.objs[k].W, s.objs[k].S0) for k in range(s.nobj)])
     lat.set_state(s.Q, s.types)
+    if getattr(s, "hfile", None):
+        lat.load_field_map(*s.hfile)  # the library's own reader of the field file
     return lat
 
 
@@ -112,4 +126,5 @@ def rel_err(a, b):
 
 
 GOLDEN_CASES = ["l1_bulk_fire", "l123_walls_sphere_fire", "planar_sphere_fire", "l1234_planar_fields_fire",
-                "edges_gaps_wrap", "adam", "nesterov", "lbfgs", "gd", "boundary_file_defects", "load_state"]
+                "edges_gaps_wrap", "adam", "nesterov", "lbfgs", "gd", "boundary_file_defects", "load_state",
+                "field_map"]

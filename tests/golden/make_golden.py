@@ -59,6 +59,9 @@ CASES = {
     # loadState of a state file (Q only; types are not loaded).  A FIRE updater is attached (with no
     # iterations) because finalizeObjects takes NActive, the energy's divisor, from the updaters
     "load_state": (["L=7,6,5", "seed=2", "Ls=2.32,0,0,0,0", "loadstate={d}/ld", "minimizer=fire", "iters=0"], True),
+    # spatially varying H field read from a file, L1-L3, wall + planar sphere
+    "field_map": (["L=9,8,7", "seed=41", "Ls=2.32,1.0,0.5,0,0", "wall=2,0,h,5.3", "sphere=4.5,4,4,2.2,p,1.7",
+                   "hfile={d}/hf,1.3,0.8,0.6", "minimizer=fire", "iters=20", "trace=1"], True),
     # the 50^3 one-constant CLI run (openQmin -i 100 -l 50 --L1 2.32): scalars only
     "c1_50cube_fire100": (["L=50,50,50", "seed=13371", "Ls=2.32,0,0,0,0", "minimizer=fire", "iters=100",
                            "trace=1"], False),
@@ -97,11 +100,26 @@ def state_file_text(L, seed):
     return "\n".join(rows) + "\n"
 
 
+def field_file_text(L):
+    """A spatially varying H field file (landauDeGennesLC.cpp:81-123 layout: x y z Hx Hy Hz),
+    written here: a smooth field on every site with x + y even (the others keep H = 0)."""
+    rows = []
+    for z in range(L[2]):
+        for y in range(L[1]):
+            for x in range(L[0]):
+                if (x + y) % 2:
+                    continue
+                h = (0.4 * np.sin(2 * np.pi * x / L[0]), 0.15 + 0.05 * y, 0.3 * np.cos(2 * np.pi * z / L[2]))
+                rows.append(f"{x} {y} {z} {h[0]:.12g} {h[1]:.12g} {h[2]:.12g}")
+    return "\n".join(rows) + "\n"
+
+
 # cases that need input files (written into the run directory; "{d}" in an
 # argument is replaced by that directory) and collect output text files
 FILES = {
     "boundary_file_defects": ({"objects.txt": boundary_file_text}, ["st_x0y0z0.txt"]),
     "load_state": ({"ld_x0y0z0.txt": lambda: state_file_text((7, 6, 5), 3)}, []),
+    "field_map": ({"hf_x0y0z0.txt": lambda: field_file_text((9, 8, 7))}, []),
 }
 
 
