@@ -7,6 +7,7 @@
  * depend on the thread count. */
 #include "qmin_oracle.h"
 #include "distortion_coeffs.h"
+#include "distortion_coeffs_l6.h"
 
 #include <math.h>
 #include <stdint.h>
@@ -399,6 +400,42 @@ static void multi_term(int term, double Lc, int bcase, const double *x125, doubl
     }
 }
 
+/* L6 forms: (0.5 L6) * sum_{i<=j} (k/2) x_i x_j, the quadratic forms of
+ * lcForces.h's bulkL6Force / boundaryL6Force (tables in distortion_coeffs_l6.h;
+ * the bulk form equals boundary case 0).  qo_l6_start[(case + 1) * 5 + c] is
+ * the first entry of (case, component c); the entries are grouped that way. */
+static int qo_l6_start[65 * 5 + 1];
+static int qo_l6_ready;
+
+static void build_l6(void)
+{
+    if (qo_l6_ready) return;
+#pragma omp critical(qo_l6_init)
+    {
+        if (!qo_l6_ready) {
+            int count[65 * 5];
+            memset(count, 0, sizeof count);
+            for (int e = 0; e < QO_L6_N; ++e) count[(qo_l6_entries[e][0] + 1) * 5 + qo_l6_entries[e][1]]++;
+            qo_l6_start[0] = 0;
+            for (int slot = 0; slot < 65 * 5; ++slot) qo_l6_start[slot + 1] = qo_l6_start[slot] + count[slot];
+            qo_l6_ready = 1;
+        }
+    }
+}
+
+static void l6_term(double L6, int bcase, const double *x125, double *s)
+{
+    for (int k = 0; k < 5; ++k) {
+        const int slot = (bcase + 1) * 5 + k;
+        double acc = 0.0;
+        for (int e = qo_l6_start[slot]; e < qo_l6_start[slot + 1]; ++e) {
+            const short *r = qo_l6_entries[e];
+            acc += (double)r[4] / 2.0 * x125[r[2]] * x125[r[3]];
+        }
+        s[k] = (0.5 * L6) * acc;
+    }
+}
+
 /* boundary anchoring force on an LC site from one object neighbour
  * (landauDeGennesLCBoundary.h:26-74).
  * Homeotropic (Rapini-Papoular): E = W tr((q-qB)^2), F = -dE/dq.
@@ -503,6 +540,7 @@ void qo_force(const qo_params *p, const double *Q, const int *types, const qo_ob
     double *D = NULL;
     if (p->multi_constant) {
         build_forms();
+        build_l6();
         D = (double *)malloc(sizeof(double) * 15 * N);
         first_derivatives(L, Q, types, D);
     }
@@ -546,6 +584,11 @@ void qo_force(const qo_params *p, const double *Q, const int *types, const qo_ob
             for (int term = 0; term < 3; ++term) {
                 if (Lc[term] == 0) continue;
                 multi_term(term, Lc[term], bcase, x, ind);
+                for (int k = 0; k < 5; ++k) s[k] += ind[k];
+            }
+            if (p->L6 != 0) {
+                /* DT:183-187, 273-277, 315-319: bulk form on type 0 and -2, case form on -1 */
+                l6_term(p->L6, boundary_form ? bcase : -1, x, ind);
                 for (int k = 0; k < 5; ++k) s[k] += ind[k];
             }
         }
@@ -690,6 +733,20 @@ double qo_energy(const qo_params *p, const double *Q, const int *types, const qo
                 for (int y = 0; y < 3; ++y) s += lc[e6][3] * Qm[l][y] * G[k][x][y];
             }
             dist += 0.5 * p->L4 * s;
+        }
+        if (p->L6 != 0) {
+            /* cubic term L6/2 Q_ab da Q_ij db Q_ij */
+            double Qm[3][3];
+            tensor3(q, Qm);
+            double s = 0.0;
+            for (int a = 0; a < 3; ++a)
+                for (int b = 0; b < 3; ++b) {
+                    double g = 0.0;
+                    for (int x = 0; x < 3; ++x)
+                        for (int y = 0; y < 3; ++y) g += G[a][x][y] * G[b][x][y];
+                    s += Qm[a][b] * g;
+                }
+            dist += 0.5 * p->L6 * s;
         }
         ei[1] = dist;
     }

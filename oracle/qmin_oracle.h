@@ -30,6 +30,7 @@ typedef struct {
     int metric_mode;         /* 0: CPU path (M^2 on type 0, M on type < 0), 1: M once everywhere */
     const double *hvar;      /* spatially varying H field, N x 3 per site, or NULL
                                 (landauDeGennesLC::setSpatiallyVaryingField, landauDeGennesLC.cpp:81-123) */
+    double L6;               /* cubic elastic constant (landauDeGennesLC.h:35, lcForces.h:801-1047) */
 } qo_params;
 
 typedef struct { int kind; double W, S0; } qo_object; /* kind 0 homeotropic, 1 degenerate planar */

@@ -22,7 +22,7 @@ class Params(C.Structure):
                 ("multi_constant", C.c_int), ("efield", C.c_int), ("hfield", C.c_int),
                 ("E", C.c_double * 3), ("eps", C.c_double), ("eps0", C.c_double), ("deps", C.c_double),
                 ("H", C.c_double * 3), ("chi", C.c_double), ("mu0", C.c_double), ("dchi", C.c_double),
-                ("metric_mode", C.c_int), ("hvar", C.POINTER(C.c_double))]
+                ("metric_mode", C.c_int), ("hvar", C.POINTER(C.c_double)), ("L6", C.c_double)]
 
 
 class Object(C.Structure):
@@ -105,8 +105,8 @@ class System:
         p = Params()
         p.Lx, p.Ly, p.Lz = self.L
         p.A, p.B, p.C = a, b, c
-        Ls = tuple(Ls) + (0,) * (4 - len(Ls))
-        p.L1, p.L2, p.L3, p.L4 = Ls
+        Ls = tuple(Ls) + (0,) * (5 - len(Ls))
+        p.L1, p.L2, p.L3, p.L4, p.L6 = Ls[:5]
         p.multi_constant = int(any(x != 0 for x in Ls[1:]))
         if E is not None:
             p.efield = 1

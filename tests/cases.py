@@ -75,7 +75,7 @@ def parse_args(args):
 
 
 def oracle_system(qo, cfg, metric_mode=0):
-    s = qo.System(cfg["L"], Ls=cfg["Ls"][:4], E=cfg["E"], H=cfg["H"], metric_mode=metric_mode)
+    s = qo.System(cfg["L"], Ls=cfg["Ls"][:5], E=cfg["E"], H=cfg["H"], metric_mode=metric_mode)
     s.random_nematic(cfg["seed"])
     for xyz, plane, kind, W in cfg["walls"]:
         s.add_wall(xyz, plane, kind, W)
@@ -109,7 +109,7 @@ def gpu_lattice(qmin, s, precision=0, metric_mode=0):
     """A GPU lattice with the oracle system's parameters, objects and state."""
     lat = qmin.Lattice(s.L, precision, metric_mode)
     p = s.p
-    lat.set_params(p.A, p.B, p.C, p.L1, p.L2, p.L3, p.L4, multi_constant=p.multi_constant,
+    lat.set_params(p.A, p.B, p.C, p.L1, p.L2, p.L3, p.L4, multi_constant=p.multi_constant, L6=p.L6,
                    E=(p.E[0], p.E[1], p.E[2], p.eps, p.eps0, p.deps) if p.efield else None,
                    H=(p.H[0], p.H[1], p.H[2], p.chi, p.mu0, p.dchi) if p.hfield else None)
     lat.set_objects([(s.objs[k].kind, s.objs[k].W, s.objs[k].S0) for k in range(s.nobj)])
@@ -127,4 +127,4 @@ def rel_err(a, b):
 
 GOLDEN_CASES = ["l1_bulk_fire", "l123_walls_sphere_fire", "planar_sphere_fire", "l1234_planar_fields_fire",
                 "edges_gaps_wrap", "adam", "nesterov", "lbfgs", "gd", "boundary_file_defects", "load_state",
-                "field_map"]
+                "field_map", "l6_fire"]

@@ -62,6 +62,9 @@ CASES = {
     # spatially varying H field read from a file, L1-L3, wall + planar sphere
     "field_map": (["L=9,8,7", "seed=41", "Ls=2.32,1.0,0.5,0,0", "wall=2,0,h,5.3", "sphere=4.5,4,4,2.2,p,1.7",
                    "hfile={d}/hf,1.3,0.8,0.6", "minimizer=fire", "iters=20", "trace=1"], True),
+    # the cubic L6 term with L1-L3, homeotropic wall and sphere, planar sphere (bulk and boundary forms)
+    "l6_fire": (["L=11,10,9", "seed=53", "Ls=2.32,1.0,0.5,0,0.8", "wall=2,0,h,5.3", "sphere=5,5,4.5,2.4,h,4.0",
+                 "sphere=1.3,8.2,6.4,1.9,p,1.2", "minimizer=fire", "iters=20", "trace=1"], True),
     # the 50^3 one-constant CLI run (openQmin -i 100 -l 50 --L1 2.32): scalars only
     "c1_50cube_fire100": (["L=50,50,50", "seed=13371", "Ls=2.32,0,0,0,0", "minimizer=fire", "iters=100",
                            "trace=1"], False),
