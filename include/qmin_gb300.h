@@ -67,6 +67,8 @@ typedef struct {
     double E[3], eps, eps0, deps;
     int hfield;          /* uniform H field on */
     double H[3], chi, mu0, dchi;
+    double L6;           /* cubic elastic constant (setElasticConstants' l6); needs multi_constant;
+                            single-lattice handles only (a batch rejects it) */
 } qmin_ldg_params;
 
 /* boundaryObject{boundary, P1 = W, P2 = S0} (latticeBoundaries.h:20-39) */

@@ -61,7 +61,8 @@ class LdgParams(C.Structure):
                 ("multi_constant", C.c_int), ("efield", C.c_int),
                 ("E", C.c_double * 3), ("eps", C.c_double), ("eps0", C.c_double), ("deps", C.c_double),
                 ("hfield", C.c_int),
-                ("H", C.c_double * 3), ("chi", C.c_double), ("mu0", C.c_double), ("dchi", C.c_double)]
+                ("H", C.c_double * 3), ("chi", C.c_double), ("mu0", C.c_double), ("dchi", C.c_double),
+                ("L6", C.c_double)]
 
 
 class Object(C.Structure):
@@ -229,11 +230,12 @@ class Lattice:
         except Exception:
             pass
 
-    def set_params(self, A, B, Cc, L1=0.0, L2=0.0, L3=0.0, L4=0.0, multi_constant=None, E=None, H=None):
+    def set_params(self, A, B, Cc, L1=0.0, L2=0.0, L3=0.0, L4=0.0, multi_constant=None, E=None, H=None, L6=0.0):
         p = LdgParams()
         p.A, p.B, p.C = A, B, Cc
-        p.L1, p.L2, p.L3, p.L4 = L1, L2, L3, L4
-        p.multi_constant = int(any(x != 0 for x in (L2, L3, L4))) if multi_constant is None else int(multi_constant)
+        p.L1, p.L2, p.L3, p.L4, p.L6 = L1, L2, L3, L4, L6
+        p.multi_constant = (int(any(x != 0 for x in (L2, L3, L4, L6))) if multi_constant is None
+                            else int(multi_constant))
         if E is not None:
             p.efield = 1
             p.E[0], p.E[1], p.E[2], p.eps, p.eps0, p.deps = E
@@ -410,11 +412,12 @@ class Batch:
         except Exception:
             pass
 
-    def set_params(self, A, B, Cc, L1=0.0, L2=0.0, L3=0.0, L4=0.0, multi_constant=None, E=None, H=None):
+    def set_params(self, A, B, Cc, L1=0.0, L2=0.0, L3=0.0, L4=0.0, multi_constant=None, E=None, H=None, L6=0.0):
         p = LdgParams()
         p.A, p.B, p.C = A, B, Cc
-        p.L1, p.L2, p.L3, p.L4 = L1, L2, L3, L4
-        p.multi_constant = int(any(x != 0 for x in (L2, L3, L4))) if multi_constant is None else int(multi_constant)
+        p.L1, p.L2, p.L3, p.L4, p.L6 = L1, L2, L3, L4, L6
+        p.multi_constant = (int(any(x != 0 for x in (L2, L3, L4, L6))) if multi_constant is None
+                            else int(multi_constant))
         if E is not None:
             p.efield = 1
             p.E[0], p.E[1], p.E[2], p.eps, p.eps0, p.deps = E

@@ -427,6 +427,8 @@ int qmin_batch_destroy(qmin_batch b)
 int qmin_batch_set_params(qmin_batch b, const qmin_ldg_params *p)
 {
     if (!b || !p) return bfail(QMIN_EINVAL, "qmin_batch_set_params: null argument");
+    if (p->multi_constant && p->L6 != 0.0)
+        return bfail(QMIN_EINVAL, "qmin_batch_set_params: the L6 term is supported by single-lattice handles only");
     b->params = *p;
     if (p->multi_constant && !b->D) {
         if (cudaMalloc(&b->D, 15 * (size_t)b->P * b->esz) != cudaSuccess) {

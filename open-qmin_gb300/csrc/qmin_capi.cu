@@ -103,6 +103,7 @@ template <class T> void fill_lat_params(Lat<T> &L, const qmin_ldg_params &p, int
     L.L2 = T(p.L2);
     L.L3 = T(p.L3);
     L.L4 = T(p.L4);
+    L.L6 = T(p.L6);
     // uniform-field force vectors (landauDeGennesLCOtherForces.cpp:297-303)
     auto field = [](const double *fld, double aniso, double perm, T *out) {
         double pr = aniso * perm;
@@ -651,7 +652,9 @@ template <class T> static int tune_fire(qmin_ctx *h, const Lat<T> &L)
     LB.Q = (T *)h->Q2;
     LB.V = (T *)h->V2;
     LB.F = (T *)h->F2;
-    if (h->fire_mode == QMIN_FIRE_AUTO || h->fire_mode == QMIN_FIRE_FUSED) {
+    // the L6 forms are compiled into the uncapped separate kernels only
+    const bool l6 = L.multi && L.L6 != T(0);
+    if (!l6 && (h->fire_mode == QMIN_FIRE_AUTO || h->fire_mode == QMIN_FIRE_FUSED)) {
         for (int cfg = 0; cfg < kFusedConfigs; ++cfg) {
             int tx, ty;
             fused_tile_shape(cfg, &tx, &ty);
@@ -682,8 +685,9 @@ template <class T> static int tune_fire(qmin_ctx *h, const Lat<T> &L)
             }
         }
     }
-    const bool try_sep = h->fire_mode == QMIN_FIRE_AUTO || h->fire_mode == QMIN_FIRE_SEPARATE;
-    const bool try_tiled = (h->fire_mode == QMIN_FIRE_AUTO || h->fire_mode == QMIN_FIRE_TILED) && sizeof(T) == 4;
+    const bool try_sep = l6 || h->fire_mode == QMIN_FIRE_AUTO || h->fire_mode == QMIN_FIRE_SEPARATE;
+    const bool try_tiled =
+        !l6 && (h->fire_mode == QMIN_FIRE_AUTO || h->fire_mode == QMIN_FIRE_TILED) && sizeof(T) == 4;
     if (try_sep || try_tiled) {
         const float t_pred = time3([&]() { launch_fire_pred<T>(LB, h->fire, h->stream); });
         const float t_der = L.multi ? time3([&]() { launch_derivs<T>(L, h->stream); }) : 0.f;

@@ -14,6 +14,7 @@
 #pragma once
 #include "qmin_device.cuh"
 #include "qmin_distortion_tables.h"
+#include "qmin_l6_forms.h"
 #include "qmin_internal.h"
 
 namespace qmin {
@@ -22,6 +23,19 @@ namespace qmin {
 static __device__ const uint16_t g_dt_offset[3 * 64 * 5 + 1] = QMIN_DT_OFFSET_INIT;
 static __device__ const uint8_t g_dt_input[QMIN_DT_NPAIRS] = QMIN_DT_INPUT_INIT;
 static __device__ const int8_t g_dt_k[QMIN_DT_NPAIRS] = QMIN_DT_K_INIT;
+// L6 quadratic forms of the 27 boundary cases: (case, component) -> (i, j, k), value (k/2) x_i x_j
+static __device__ const uint16_t g_l6_offset[64 * 5 + 1] = QMIN_L6_OFFSET_INIT;
+static __device__ const uint8_t g_l6_i[QMIN_L6_NPAIRS] = QMIN_L6_I_INIT;
+static __device__ const uint8_t g_l6_j[QMIN_L6_NPAIRS] = QMIN_L6_J_INIT;
+static __device__ const int8_t g_l6_k[QMIN_L6_NPAIRS] = QMIN_L6_K_INIT;
+
+// input x of the 125-input stencils, derivatives as true derivatives
+template <class T, class A> __device__ __forceinline__ T stencil_input(const A &acc, int j)
+{
+    if (j < 5) return acc.q(j);
+    if (j < 35) return acc.nq((j - 5) / 5, (j - 5) % 5);
+    return T(0.5) * acc.dn((j - 35) / 15, (j - 35) % 15);
+}
 
 template <class T>
 __device__ __forceinline__ T ld(const T *p)
@@ -115,7 +129,9 @@ __device__ __forceinline__ T deriv2_rule(int t, int td, int tu, T qd, T q, T qu)
 //   type 0:  F = M( M(-phase - distortion) - fields )
 //   type <0: F = M(-phase - distortion + anchoring - fields)
 // metric_mode 1 applies M once everywhere (the reference GPU branch).
-template <class T, class A>
+// WITH_L6 compiles the cubic L6 forms in; kernels without it leave L6 out
+// (it is a runtime-zero branch that would still cost registers)
+template <class T, class A, bool WITH_L6 = false>
 __device__ __forceinline__ void site_force_core(const Lat<T> &L, const A &acc, int t, T *f, const T *hs = nullptr)
 {
     if (t > 0) {
@@ -181,11 +197,18 @@ __device__ __forceinline__ void site_force_core(const Lat<T> &L, const A &acc, i
             } else {
                 QMIN_BULK_FORMS(L.cb, s2);
             }
+#pragma unroll
+            for (int k = 0; k < 5; ++k) sp[k] += s2[k];
+            if (WITH_L6 && L.L6 != T(0)) {
+                // lcForce::bulkL6Force (lcForces.h:801-815): quadratic in the same inputs
+                T s6[5];
+                QMIN_L6_BULK(T, s6);
+#pragma unroll
+                for (int k = 0; k < 5; ++k) sp[k] += (T(0.5) * L.L6) * s6[k];
+            }
 #undef QIN
 #undef QN
 #undef DN
-#pragma unroll
-            for (int k = 0; k < 5; ++k) sp[k] += s2[k];
         } else {
             // boundary forms: lcForce::getBoundaryCase (lcForces.h:13-25), down wins
             int xx = 0, yy = 0, zz = 0;
@@ -212,6 +235,16 @@ __device__ __forceinline__ void site_force_core(const Lat<T> &L, const A &acc, i
                         acc_k += T(g_dt_k[e]) * x;
                     }
                     sp[k] += (T(0.5) * Lt[term]) * (acc_k / T(2));
+                }
+            }
+            if (WITH_L6 && L.L6 != T(0)) {
+                // lcForce::boundaryL6Force (lcForces.h:818-1047)
+                for (int k = 0; k < 5; ++k) {
+                    const int o0 = g_l6_offset[bcase * 5 + k], o1 = g_l6_offset[bcase * 5 + k + 1];
+                    T acc_k = T(0);
+                    for (int e = o0; e < o1; ++e)
+                        acc_k += T(g_l6_k[e]) * stencil_input<T>(acc, g_l6_i[e]) * stencil_input<T>(acc, g_l6_j[e]);
+                    sp[k] += (T(0.5) * L.L6) * (acc_k / T(2));
                 }
             }
         }
@@ -280,7 +313,7 @@ template <class T> struct GlobalAcc {
     __device__ __forceinline__ T dn(int s, int d) const { return ld(D + (long long)d * P + b.n[s]); }
 };
 
-template <class T>
+template <class T, bool WITH_L6 = false>
 __device__ __forceinline__ void site_force(const Lat<T> &L, int i, T *f)
 {
     const int t = L.types[i];
@@ -291,7 +324,7 @@ __device__ __forceinline__ void site_force(const Lat<T> &L, int i, T *f)
     }
     GlobalAcc<T> acc(L, i);
     T h[3];
-    site_force_core(L, acc, t, f, site_field(L, i, h));
+    site_force_core<T, GlobalAcc<T>, WITH_L6>(L, acc, t, f, site_field(L, i, h));
 }
 
 }  // namespace qmin

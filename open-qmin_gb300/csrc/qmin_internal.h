@@ -26,7 +26,7 @@ template <class T> struct Lat {
     T *D;  // 15 derivative planes (multi-constant only)
     const ObjDev<T> *objs;
     T a, b, c;          // A/2, B/3, C/4
-    T L1, L2, L3, L4;
+    T L1, L2, L3, L4, L6;
     T fE[5], fH[5];     // uniform-field force vectors (subtracted, as the reference does)
     const T *Hv;        // spatially varying H field, 3 planes of stride P, or null
     T hvp;              // its dchi * mu0

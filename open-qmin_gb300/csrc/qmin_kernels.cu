@@ -67,12 +67,12 @@ __global__ void __launch_bounds__(kBlock) k_derivs(Lat<T> L)
 }
 
 // ------------------------------------------------------------------- force
-template <class T>
+template <class T, bool WITH_L6 = false>
 __global__ void __launch_bounds__(kBlock) k_force(Lat<T> L)
 {
     for (int i = blockIdx.x * kBlock + threadIdx.x; i < L.N; i += gridDim.x * kBlock) {
         T f[5];
-        site_force(L, i, f);
+        site_force<T, WITH_L6>(L, i, f);
 #pragma unroll
         for (int k = 0; k < 5; ++k) L.F[k * L.P + i] = f[k];
     }
@@ -117,7 +117,7 @@ __global__ void __launch_bounds__(kBlock) k_fire_pred(Lat<T> L, const FireDev *_
 // force at the moved Q, second half kick (velocityVerlet.cpp:33-37) and the
 // three FIRE reductions F.F, v.v, F.v in the QT metric (energyMinimizerFIRE.cpp:94-103)
 // CAP limits registers so that CAP + 1 blocks of 256 threads fit per SM
-template <class T, int CAP>
+template <class T, int CAP, bool WITH_L6 = false>
 __global__ void __launch_bounds__(kBlock, CAP + 1)
     k_force_kick(Lat<T> L, const FireDev *__restrict__ fd, double *partials)
 {
@@ -126,7 +126,7 @@ __global__ void __launch_bounds__(kBlock, CAP + 1)
     double acc[3] = {0.0, 0.0, 0.0};
     for (int i = blockIdx.x * kBlock + threadIdx.x; i < L.N; i += gridDim.x * kBlock) {
         T f[5], v[5];
-        site_force(L, i, f);
+        site_force<T, WITH_L6>(L, i, f);
 #pragma unroll
         for (int k = 0; k < 5; ++k) {
             v[k] = L.V[k * L.P + i] + hdt * f[k];
@@ -312,6 +312,24 @@ __global__ void __launch_bounds__(kBlock) k_energy(Lat<T> L, double *partials, d
                 for (int y = 0; y < 3; ++y) s += sg * Qm[perm[e][0]][y] * G[perm[e][2]][perm[e][1]][y];
             }
             dist += T(0.5) * L.L4 * s;
+        }
+        if (L.L6 != T(0)) {
+            // cubic term L6/2 Q_ab da Q_ij db Q_ij (landauDeGennesLC.cpp:331-334)
+            T Qm[3][3];
+            sym3(q, Qm);
+            T s = T(0);
+#pragma unroll
+            for (int a = 0; a < 3; ++a)
+#pragma unroll
+                for (int bb = 0; bb < 3; ++bb) {
+                    T g = T(0);
+#pragma unroll
+                    for (int x = 0; x < 3; ++x)
+#pragma unroll
+                        for (int y = 0; y < 3; ++y) g += G[a][x][y] * G[bb][x][y];
+                    s += Qm[a][bb] * g;
+                }
+            dist += T(0.5) * L.L6 * s;
         }
         acc[1] += (double)dist;
     }
@@ -686,7 +704,8 @@ template <class T> int launch_force(const Lat<T> &L, int grid, cudaStream_t s)
 {
     int n = 0;
     if (L.multi) n += launch_derivs(L, s);
-    k_force<T><<<grid, kBlock, 0, s>>>(L);
+    if (L.L6 != T(0)) k_force<T, true><<<grid, kBlock, 0, s>>>(L);
+    else k_force<T><<<grid, kBlock, 0, s>>>(L);
     return n + 1;
 }
 template <class T> int launch_fire_pred(const Lat<T> &L, FireDev *fd, cudaStream_t s)
@@ -704,7 +723,9 @@ int launch_force_kick(const Lat<T> &L, FireDev *fd, double *partials, int grid, 
 template <class T>
 int launch_force_kick_only(const Lat<T> &L, FireDev *fd, double *partials, int grid, cudaStream_t s, int cap)
 {
-    if (cap == 2) k_force_kick<T, 2><<<grid, kBlock, 0, s>>>(L, fd, partials);
+    // the L6 forms exist only in the uncapped kernel
+    if (L.L6 != T(0) && L.multi) k_force_kick<T, 0, true><<<grid, kBlock, 0, s>>>(L, fd, partials);
+    else if (cap == 2) k_force_kick<T, 2><<<grid, kBlock, 0, s>>>(L, fd, partials);
     else if (cap == 1) k_force_kick<T, 1><<<grid, kBlock, 0, s>>>(L, fd, partials);
     else k_force_kick<T, 0><<<grid, kBlock, 0, s>>>(L, fd, partials);
     return 1;

@@ -153,6 +153,7 @@ int qmin_energy_noalloc(const qmin_lattice_desc *desc, const qmin_ldg_params *p,
     L.L2 = p->L2;
     L.L3 = p->L3;
     L.L4 = p->L4;
+    L.L6 = p->L6;
     L.multi = p->multi_constant;
     L.efield = p->efield;
     L.hfield = p->hfield;

@@ -50,7 +50,7 @@ def test_force_fp32(qmin, oracle, name):
 
 
 @pytest.mark.parametrize("name", ["l1_bulk_fire", "l123_walls_sphere_fire", "planar_sphere_fire",
-                                  "l1234_planar_fields_fire", "edges_gaps_wrap"])
+                                  "l1234_planar_fields_fire", "edges_gaps_wrap", "field_map", "l6_fire"])
 @pytest.mark.parametrize("mode", [0, 1])
 def test_fire_trajectory_fp64(qmin, oracle, name, mode):
     """Both FIRE execution paths (separate kernels, fused tiled kernel) against the reference."""
@@ -240,3 +240,10 @@ def test_staged_force_kick_matches_separate(qmin, oracle, Ls):
     assert abs(out[0][1]["forceMax"] - out[1][1]["forceMax"]) <= 1e-5 * out[0][1]["forceMax"]
     for a, b in zip(out[0][2], out[1][2]):
         assert rel_err(b, a) <= 1e-5
+
+
+def test_l6_batch_rejected(qmin):
+    """The batched path has no L6 forms and says so."""
+    b = qmin.Batch([(8, 8, 8)])
+    with pytest.raises(qmin.QminError):
+        b.set_params(-1.0, -12.3, 10.1, 2.32, 1.0, 0.5, L6=0.8)
