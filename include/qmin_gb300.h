@@ -125,6 +125,15 @@ int qmin_set_positions(qmin_handle h, const double *Q, int layout);
  * sites with type <= 0; object sites get 0.  out: host, N doubles. */
 int qmin_defect_measures(qmin_handle h, int kind, double *out);
 
+/* landauDeGennesLC::computeObjectForces (landauDeGennesLCOtherForces.cpp:147-251):
+ * the force on every object from the stress tensor of the LC sites next to it,
+ * forces[3*j .. 3*j+2] for object j (host; capacity = number of objects it
+ * holds; *nobj_out, may be NULL, receives the object count).  One-constant
+ * form only, as in the reference (QMIN_EINVAL otherwise).  Each call returns
+ * the force of the current state; the reference instead adds it to a running
+ * per-object total (cubicLattice::boundaryForce) on every call. */
+int qmin_object_forces(qmin_handle h, double *forces, int capacity, int *nobj_out);
+
 /* landauDeGennesLC::setSpatiallyVaryingField (landauDeGennesLC.cpp:81-123) with
  * the field given directly: H is host AoS double[N][3] (NULL switches the
  * field off); chi, mu0, dchi replace the H-field constants of qmin_set_params,

@@ -31,7 +31,7 @@ EXPORTED_SYMBOLS = [
     "qmin_create", "qmin_destroy", "qmin_set_stream", "qmin_last_error_string", "qmin_kernel_launches",
     "qmin_set_params", "qmin_set_objects", "qmin_set_state", "qmin_get_state", "qmin_n_active", "qmin_force",
     "qmin_energy", "qmin_fire_init", "qmin_fire_run", "qmin_adam_run", "qmin_nesterov_run", "qmin_lbfgs_run",
-    "qmin_gd_run", "qmin_get_sides", "qmin_get_types", "qmin_set_positions", "qmin_defect_measures",
+    "qmin_gd_run", "qmin_get_sides", "qmin_get_types", "qmin_set_positions", "qmin_defect_measures", "qmin_object_forces",
     "qmin_save_state", "qmin_load_state", "qmin_set_field_map", "qmin_load_field_map", "qmin_checkpoint_save", "qmin_checkpoint_load", "qmin_host_boundary_file",
     "qmin_host_random_nematic", "qmin_host_add_wall", "qmin_host_add_sphere", "qmin_set_fire_kernel",
     "qmin_fire_profile", "qmin_fire_tuning", "qmin_energy_noalloc", "qmin_batch_create", "qmin_batch_destroy",
@@ -105,7 +105,7 @@ def lib():
             "qmin_lbfgs_run": [h, C.c_int, C.c_double, C.c_double, C.c_int, C.c_int, ip, dp],
             "qmin_gd_run": [h, C.c_double, C.c_double, C.c_int, C.c_int, ip, dp],
             "qmin_get_sides": [h, ip, ip, ip], "qmin_get_types": [h, vp], "qmin_set_positions": [h, vp, C.c_int],
-            "qmin_defect_measures": [h, C.c_int, vp],
+            "qmin_defect_measures": [h, C.c_int, vp], "qmin_object_forces": [h, vp, C.c_int, ip],
             "qmin_set_field_map": [h, vp, C.c_double, C.c_double, C.c_double],
             "qmin_load_field_map": [h, C.c_char_p, C.c_double, C.c_double, C.c_double],
             "qmin_save_state": [h, C.c_char_p, C.c_int, C.c_int], "qmin_load_state": [h, C.c_char_p],
@@ -340,6 +340,13 @@ class Lattice:
 
     def load_field_map(self, prefix, chi, mu0, dchi):
         _check(lib().qmin_load_field_map(self._h, os.fsencode(prefix), chi, mu0, dchi))
+
+    def object_forces(self):
+        """Force on every object from the stress tensor (one-constant form): array [nobj, 3]."""
+        out = np.zeros((127, 3))
+        n = C.c_int()
+        _check(lib().qmin_object_forces(self._h, out.ctypes.data, 127, C.byref(n)))
+        return out[:n.value].copy()
 
     def save_state(self, prefix, lattice_skip=1, defect_kind=0):
         _check(lib().qmin_save_state(self._h, os.fsencode(prefix), int(lattice_skip), int(defect_kind)))

@@ -1302,3 +1302,36 @@ int qmin_checkpoint_load(qmin_handle h, const char *path)
     }
     return QMIN_OK;
 }
+
+int qmin_object_forces(qmin_handle h, double *forces, int capacity, int *nobj_out)
+{
+    int r = ready(h, "qmin_object_forces");
+    if (r) return r;
+    if (h->params.multi_constant)
+        return fail(QMIN_EINVAL, "qmin_object_forces: the stress tensor is defined for the one-constant form only");
+    const int nobj = (int)h->objs_host.size();
+    if (nobj_out) *nobj_out = nobj;
+    if (nobj == 0) return QMIN_OK;
+    if (!forces || capacity < nobj)
+        return fail(QMIN_EINVAL, "qmin_object_forces: forces must hold 3 doubles for every object");
+    double *out = nullptr;
+    if (cudaMalloc(&out, sizeof(double) * 3 * nobj) != cudaSuccess) {
+        cudaGetLastError();
+        return fail(QMIN_ENOMEM, "qmin_object_forces: allocation failed");
+    }
+    const qmin_ldg_params &p = h->params;
+    double E0[3] = {0, 0, 0}, H0[3] = {0, 0, 0};
+    const double *E = p.efield ? p.E : E0, *H = p.hfield ? p.H : H0;
+    if (h->prec == QMIN_FP64)
+        h->launches += launch_object_forces<double>(make_lat<double>(h), nobj, E, p.eps, p.eps0, p.deps, H, p.chi,
+                                                    p.mu0, p.dchi, h->partials, h->grid, out, h->stream);
+    else
+        h->launches += launch_object_forces<float>(make_lat<float>(h), nobj, E, p.eps, p.eps0, p.deps, H, p.chi,
+                                                   p.mu0, p.dchi, h->partials, h->grid, out, h->stream);
+    cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaMemcpyAsync(forces, out, sizeof(double) * 3 * nobj, cudaMemcpyDeviceToHost, h->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+    cudaFree(out);
+    if (e != cudaSuccess) return fail(QMIN_ECUDA, std::string("qmin_object_forces: ") + cudaGetErrorString(e));
+    return QMIN_OK;
+}

@@ -85,6 +85,10 @@ template <class T>
 int launch_nesterov_step(const Lat<T> &L, T *alt, IterDev *it, double dt, double mu, double *partials, int grid,
                          cudaStream_t s);
 template <class T> int launch_defects(const Lat<T> &L, int kind, double *out, cudaStream_t s);
+template <class T>
+int launch_object_forces(const Lat<T> &L, int nobj, const double *E, double eps, double eps0, double deps,
+                         const double *H, double chi, double mu0, double dchi, double *partials, int grid,
+                         double *out, cudaStream_t s);
 template <class T> int launch_gd_move(const Lat<T> &L, IterDev *it, double dt, cudaStream_t s);
 template <class T> int launch_ff_dot(const Lat<T> &L, IterDev *it, double *partials, int grid, cudaStream_t s);
 int launch_norm_control(IterDev *it, const double *partials, int nparts, int adam, double beta1, double beta2,

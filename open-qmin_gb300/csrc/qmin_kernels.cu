@@ -213,130 +213,207 @@ __device__ __forceinline__ void sym3(const T *d, T G[3][3])
     G[2][0] = d[2]; G[2][1] = d[4]; G[2][2] = -d[0] - d[3];
 }
 
+// the energy densities of one LC site (type t <= 0), added to acc[5] = phase,
+// distortion, anchoring, E field, H field (landauDeGennesLC::computeEnergyCPU,
+// landauDeGennesLC.cpp:204-353)
+struct FieldArgs {
+    double Ex, Ey, Ez, eps, eps0, deps, Hx, Hy, Hz, chi, mu0, dchi;
+};
 template <class T>
-__global__ void __launch_bounds__(kBlock) k_energy(Lat<T> L, double *partials, double Ex, double Ey, double Ez,
-                                                   double eps, double eps0, double deps, double Hx, double Hy,
-                                                   double Hz, double chi, double mu0, double dchi)
+__device__ __forceinline__ void site_energy(const Lat<T> &L, int i, int t, const FieldArgs &fa, double *acc)
+{
+    const long long P = L.P;
+    const double Ex = fa.Ex, Ey = fa.Ey, Ez = fa.Ez, eps = fa.eps, eps0 = fa.eps0, deps = fa.deps;
+    const double Hx = fa.Hx, Hy = fa.Hy, Hz = fa.Hz, chi = fa.chi, mu0 = fa.mu0, dchi = fa.dchi;
+    T q[5];
+#pragma unroll
+    for (int k = 0; k < 5; ++k) q[k] = ld(L.Q + k * P + i);
+    const T t2 = tr_q2(q);
+    acc[0] += (double)(L.a * t2 + L.b * tr_q3(q) + L.c * (t2 * t2));
+    if (L.efield) {
+        const T ex = T(Ex), ey = T(Ey), ez = T(Ez), e = T(eps), e0 = T(eps0), de = T(deps);
+        acc[3] += (double)(e0 * (T(-0.5) * ex * ex * (e + de * q[0]) - de * ex * ey * q[1] - de * ex * ez * q[2] -
+                                 T(0.5) * ez * ez * (e - de * q[0] - de * q[3]) -
+                                 T(0.5) * ey * ey * (e + de * q[3]) - de * ey * ez * q[4]));
+    }
+    if (L.hfield) {
+        const T hx = T(Hx), hy = T(Hy), hz = T(Hz), c = T(chi), m0 = T(mu0), dc = T(dchi);
+        acc[4] += (double)(m0 * (T(-0.5) * hx * hx * (c + dc * q[0]) - dc * hx * hy * q[1] - dc * hx * hz * q[2] -
+                                 T(0.5) * hz * hz * (c - dc * q[0] - dc * q[3]) -
+                                 T(0.5) * hy * hy * (c + dc * q[3]) - dc * hy * hz * q[4]));
+    }
+    if (L.Hv) {
+        // landauDeGennesLC.cpp:256-265: the H-field density with this site's H
+        const T hx = L.Hv[i], hy = L.Hv[P + i], hz = L.Hv[2 * P + i], c = T(chi), m0 = T(mu0), dc = T(dchi);
+        acc[4] += (double)(m0 * (T(-0.5) * hx * hx * (c + dc * q[0]) - dc * hx * hy * q[1] - dc * hx * hz * q[2] -
+                                 T(0.5) * hz * hz * (c - dc * q[0] - dc * q[3]) -
+                                 T(0.5) * hy * hy * (c + dc * q[3]) - dc * hy * hz * q[4]));
+    }
+    const Nb b = neighbours(L, i);
+    T d[15];
+    site_derivs(L, i, t, b, d);
+    if (t < 0) {
+        T anch = T(0);
+#pragma unroll
+        for (int s = 0; s < 6; ++s) {
+            const int ts = L.types[b.n[s]];
+            if (ts > 0) {
+                T qb[5];
+#pragma unroll
+                for (int k = 0; k < 5; ++k) qb[k] = ld(L.Q + k * P + b.n[s]);
+                const ObjDev<T> o = L.objs[ts - 1];
+                anch += anchoring_energy(o.kind, o.W, o.S0, q, qb);
+            }
+        }
+        acc[2] += (double)anch;
+    }
+    T G[3][3][3];
+    sym3(d, G[0]);
+    sym3(d + 5, G[1]);
+    sym3(d + 10, G[2]);
+    T dist = T(0);
+    if (L.L1 != T(0)) {
+        T s = T(0);
+#pragma unroll
+        for (int k = 0; k < 3; ++k)
+#pragma unroll
+            for (int x = 0; x < 3; ++x)
+#pragma unroll
+                for (int y = 0; y < 3; ++y) s += G[k][x][y] * G[k][x][y];
+        dist += T(0.5) * L.L1 * s;
+    }
+    if (L.L2 != T(0)) {
+        T s = T(0);
+#pragma unroll
+        for (int x = 0; x < 3; ++x) {
+            const T dv = G[0][x][0] + G[1][x][1] + G[2][x][2];
+            s += dv * dv;
+        }
+        dist += T(0.5) * L.L2 * s;
+    }
+    if (L.L3 != T(0)) {
+        T s = T(0);
+#pragma unroll
+        for (int k = 0; k < 3; ++k)
+#pragma unroll
+            for (int x = 0; x < 3; ++x)
+#pragma unroll
+                for (int y = 0; y < 3; ++y) s += G[k][x][y] * G[y][x][k];
+        dist += T(0.5) * L.L3 * s;
+    }
+    if (L.L4 != T(0)) {
+        T Qm[3][3];
+        sym3(q, Qm);
+        // eps_lik Q_lj dk Q_ij over the six permutations (l, i, k)
+        const int perm[6][3] = {{0, 1, 2}, {1, 2, 0}, {2, 0, 1}, {0, 2, 1}, {2, 1, 0}, {1, 0, 2}};
+        T s = T(0);
+#pragma unroll
+        for (int e = 0; e < 6; ++e) {
+            const T sg = e < 3 ? T(1) : T(-1);
+#pragma unroll
+            for (int y = 0; y < 3; ++y) s += sg * Qm[perm[e][0]][y] * G[perm[e][2]][perm[e][1]][y];
+        }
+        dist += T(0.5) * L.L4 * s;
+    }
+    if (L.L6 != T(0)) {
+        // cubic term L6/2 Q_ab da Q_ij db Q_ij (landauDeGennesLC.cpp:331-334)
+        T Qm[3][3];
+        sym3(q, Qm);
+        T s = T(0);
+#pragma unroll
+        for (int a = 0; a < 3; ++a)
+#pragma unroll
+            for (int bb = 0; bb < 3; ++bb) {
+                T g = T(0);
+#pragma unroll
+                for (int x = 0; x < 3; ++x)
+#pragma unroll
+                    for (int y = 0; y < 3; ++y) g += G[a][x][y] * G[bb][x][y];
+                s += Qm[a][bb] * g;
+            }
+        dist += T(0.5) * L.L6 * s;
+    }
+    acc[1] += (double)dist;
+}
+
+template <class T>
+__global__ void __launch_bounds__(kBlock) k_energy(Lat<T> L, double *partials, FieldArgs fa)
 {
     double acc[5] = {0, 0, 0, 0, 0};
-    const long long P = L.P;
     for (int i = blockIdx.x * kBlock + threadIdx.x; i < L.N; i += gridDim.x * kBlock) {
         const int t = L.types[i];
         if (t > 0) continue;
-        T q[5];
-#pragma unroll
-        for (int k = 0; k < 5; ++k) q[k] = ld(L.Q + k * P + i);
-        const T t2 = tr_q2(q);
-        acc[0] += (double)(L.a * t2 + L.b * tr_q3(q) + L.c * (t2 * t2));
-        if (L.efield) {
-            const T ex = T(Ex), ey = T(Ey), ez = T(Ez), e = T(eps), e0 = T(eps0), de = T(deps);
-            acc[3] += (double)(e0 * (T(-0.5) * ex * ex * (e + de * q[0]) - de * ex * ey * q[1] - de * ex * ez * q[2] -
-                                     T(0.5) * ez * ez * (e - de * q[0] - de * q[3]) -
-                                     T(0.5) * ey * ey * (e + de * q[3]) - de * ey * ez * q[4]));
-        }
-        if (L.hfield) {
-            const T hx = T(Hx), hy = T(Hy), hz = T(Hz), c = T(chi), m0 = T(mu0), dc = T(dchi);
-            acc[4] += (double)(m0 * (T(-0.5) * hx * hx * (c + dc * q[0]) - dc * hx * hy * q[1] - dc * hx * hz * q[2] -
-                                     T(0.5) * hz * hz * (c - dc * q[0] - dc * q[3]) -
-                                     T(0.5) * hy * hy * (c + dc * q[3]) - dc * hy * hz * q[4]));
-        }
-        if (L.Hv) {
-            // landauDeGennesLC.cpp:256-265: the H-field density with this site's H
-            const T hx = L.Hv[i], hy = L.Hv[P + i], hz = L.Hv[2 * P + i], c = T(chi), m0 = T(mu0), dc = T(dchi);
-            acc[4] += (double)(m0 * (T(-0.5) * hx * hx * (c + dc * q[0]) - dc * hx * hy * q[1] - dc * hx * hz * q[2] -
-                                     T(0.5) * hz * hz * (c - dc * q[0] - dc * q[3]) -
-                                     T(0.5) * hy * hy * (c + dc * q[3]) - dc * hy * hz * q[4]));
-        }
-        const Nb b = neighbours(L, i);
-        T d[15];
-        site_derivs(L, i, t, b, d);
-        if (t < 0) {
-            T anch = T(0);
-#pragma unroll
-            for (int s = 0; s < 6; ++s) {
-                const int ts = L.types[b.n[s]];
-                if (ts > 0) {
-                    T qb[5];
-#pragma unroll
-                    for (int k = 0; k < 5; ++k) qb[k] = ld(L.Q + k * P + b.n[s]);
-                    const ObjDev<T> o = L.objs[ts - 1];
-                    anch += anchoring_energy(o.kind, o.W, o.S0, q, qb);
-                }
-            }
-            acc[2] += (double)anch;
-        }
-        T G[3][3][3];
-        sym3(d, G[0]);
-        sym3(d + 5, G[1]);
-        sym3(d + 10, G[2]);
-        T dist = T(0);
-        if (L.L1 != T(0)) {
-            T s = T(0);
-#pragma unroll
-            for (int k = 0; k < 3; ++k)
-#pragma unroll
-                for (int x = 0; x < 3; ++x)
-#pragma unroll
-                    for (int y = 0; y < 3; ++y) s += G[k][x][y] * G[k][x][y];
-            dist += T(0.5) * L.L1 * s;
-        }
-        if (L.L2 != T(0)) {
-            T s = T(0);
-#pragma unroll
-            for (int x = 0; x < 3; ++x) {
-                const T dv = G[0][x][0] + G[1][x][1] + G[2][x][2];
-                s += dv * dv;
-            }
-            dist += T(0.5) * L.L2 * s;
-        }
-        if (L.L3 != T(0)) {
-            T s = T(0);
-#pragma unroll
-            for (int k = 0; k < 3; ++k)
-#pragma unroll
-                for (int x = 0; x < 3; ++x)
-#pragma unroll
-                    for (int y = 0; y < 3; ++y) s += G[k][x][y] * G[y][x][k];
-            dist += T(0.5) * L.L3 * s;
-        }
-        if (L.L4 != T(0)) {
-            T Qm[3][3];
-            sym3(q, Qm);
-            // eps_lik Q_lj dk Q_ij over the six permutations (l, i, k)
-            const int perm[6][3] = {{0, 1, 2}, {1, 2, 0}, {2, 0, 1}, {0, 2, 1}, {2, 1, 0}, {1, 0, 2}};
-            T s = T(0);
-#pragma unroll
-            for (int e = 0; e < 6; ++e) {
-                const T sg = e < 3 ? T(1) : T(-1);
-#pragma unroll
-                for (int y = 0; y < 3; ++y) s += sg * Qm[perm[e][0]][y] * G[perm[e][2]][perm[e][1]][y];
-            }
-            dist += T(0.5) * L.L4 * s;
-        }
-        if (L.L6 != T(0)) {
-            // cubic term L6/2 Q_ab da Q_ij db Q_ij (landauDeGennesLC.cpp:331-334)
-            T Qm[3][3];
-            sym3(q, Qm);
-            T s = T(0);
-#pragma unroll
-            for (int a = 0; a < 3; ++a)
-#pragma unroll
-                for (int bb = 0; bb < 3; ++bb) {
-                    T g = T(0);
-#pragma unroll
-                    for (int x = 0; x < 3; ++x)
-#pragma unroll
-                        for (int y = 0; y < 3; ++y) g += G[a][x][y] * G[bb][x][y];
-                    s += Qm[a][bb] * g;
-                }
-            dist += T(0.5) * L.L6 * s;
-        }
-        acc[1] += (double)dist;
+        site_energy(L, i, t, fa, acc);
     }
     block_sum<5>(acc);
     if (threadIdx.x == 0)
 #pragma unroll
         for (int k = 0; k < 5; ++k) partials[5 * blockIdx.x + k] = acc[k];
+}
+
+// landauDeGennesLC::computeObjectForces with computeStressTensors, one-constant form
+// (landauDeGennesLCOtherForces.cpp:147-251): the force on the object whose sites
+// have type j is the sum, over the LC sites next to it, of sigma . a, where
+//   sigma_ab = e delta_ab - L1 B(d_a q, d_b q),
+//   B(u, v)  = 2 (u0 v0 + u3 v3) + u0 v3 + u3 v0 + 4 (u1 v1 + u2 v2 + u4 v4),
+// e is the site's total energy density, d_a q its first derivatives (one-sided
+// next to objects) and a the unit direction (+-1 per axis) to its object
+// neighbours, the up neighbour taking precedence.
+template <class T>
+__global__ void __launch_bounds__(kBlock) k_object_force(Lat<T> L, int j, FieldArgs fa, double *partials)
+{
+    double acc[3] = {0.0, 0.0, 0.0};
+    for (int i = blockIdx.x * kBlock + threadIdx.x; i < L.N; i += gridDim.x * kBlock) {
+        const int t = L.types[i];
+        if (t > 0) continue;
+        const Nb b = neighbours(L, i);
+        int tn[6];
+        bool next_to_j = false;
+#pragma unroll
+        for (int s = 0; s < 6; ++s) {
+            tn[s] = L.types[b.n[s]];
+            next_to_j = next_to_j || tn[s] == j;
+        }
+        if (!next_to_j) continue;
+        double e5[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
+        site_energy(L, i, t, fa, e5);
+        const double e = e5[0] + e5[3] + e5[4] + e5[2] + e5[1];  // phase, fields, anchoring, distortion
+        T d[15];
+        site_derivs(L, i, t, b, d);
+        double a[3];
+#pragma unroll
+        for (int ax = 0; ax < 3; ++ax) {
+            a[ax] = 0.0;
+            if (tn[2 * ax] > 0) a[ax] = -1.0;
+            if (tn[2 * ax + 1] > 0) a[ax] = 1.0;
+        }
+        double sig[3][3];
+#pragma unroll
+        for (int p = 0; p < 3; ++p)
+#pragma unroll
+            for (int r = 0; r < 3; ++r) {
+                const T *u = d + 5 * p, *v = d + 5 * r;
+                const double B = 2.0 * ((double)u[0] * v[0] + (double)u[3] * v[3]) + (double)u[0] * v[3] +
+                                 (double)u[3] * v[0] +
+                                 4.0 * ((double)u[1] * v[1] + (double)u[2] * v[2] + (double)u[4] * v[4]);
+                sig[p][r] = -(double)L.L1 * B + (p == r ? e : 0.0);
+            }
+#pragma unroll
+        for (int p = 0; p < 3; ++p) acc[p] += sig[p][0] * a[0] + sig[p][1] * a[1] + sig[p][2] * a[2];
+    }
+    block_sum<3>(acc);
+    if (threadIdx.x == 0)
+#pragma unroll
+        for (int k = 0; k < 3; ++k) partials[3 * blockIdx.x + k] = acc[k];
+}
+
+__global__ void __launch_bounds__(kBlock) k_sum3(const double *partials, int nparts, double *out)
+{
+    double v[3];
+    sum_partials<3>(partials, nparts, v);
+    if (threadIdx.x == 0)
+#pragma unroll
+        for (int k = 0; k < 3; ++k) out[k] = v[k];
 }
 
 __global__ void __launch_bounds__(kBlock) k_sum5(const double *partials, int nparts, double *out)
@@ -775,6 +852,18 @@ int launch_nesterov_step(const Lat<T> &L, T *alt, IterDev *it, double dt, double
     k_nesterov<T><<<grid, kBlock, 0, s>>>(L, alt, it, T(dt), T(mu), partials);
     return 1;
 }
+template <class T>
+int launch_object_forces(const Lat<T> &L, int nobj, const double *E, double eps, double eps0, double deps,
+                         const double *H, double chi, double mu0, double dchi, double *partials, int grid,
+                         double *out, cudaStream_t s)
+{
+    const FieldArgs fa = {E[0], E[1], E[2], eps, eps0, deps, H[0], H[1], H[2], chi, mu0, dchi};
+    for (int j = 1; j <= nobj; ++j) {
+        k_object_force<T><<<grid, kBlock, 0, s>>>(L, j, fa, partials);
+        k_sum3<<<1, kBlock, 0, s>>>(partials, grid, out + 3 * (j - 1));
+    }
+    return 2 * nobj;
+}
 template <class T> int launch_defects(const Lat<T> &L, int kind, double *out, cudaStream_t s)
 {
     k_defects<T><<<elem_grid(L.N), kBlock, 0, s>>>(L, kind, out);
@@ -837,8 +926,8 @@ template <class T>
 int launch_energy_full(const Lat<T> &L, double *partials, int grid, double *out5, const double *E, double eps,
                        double eps0, double deps, const double *H, double chi, double mu0, double dchi, cudaStream_t s)
 {
-    k_energy<T><<<grid, kBlock, 0, s>>>(L, partials, E[0], E[1], E[2], eps, eps0, deps, H[0], H[1], H[2], chi, mu0,
-                                         dchi);
+    const FieldArgs fa = {E[0], E[1], E[2], eps, eps0, deps, H[0], H[1], H[2], chi, mu0, dchi};
+    k_energy<T><<<grid, kBlock, 0, s>>>(L, partials, fa);
     k_sum5<<<1, kBlock, 0, s>>>(partials, grid, out5);
     return 2;
 }
@@ -858,6 +947,9 @@ int launch_energy_full(const Lat<T> &L, double *partials, int grid, double *out5
     template int launch_nesterov_step<T>(const Lat<T> &, T *, IterDev *, double, double, double *, int,            \
                                          cudaStream_t);                                                            \
     template int launch_defects<T>(const Lat<T> &, int, double *, cudaStream_t);                                   \
+    template int launch_object_forces<T>(const Lat<T> &, int, const double *, double, double, double,               \
+                                         const double *, double, double, double, double *, int, double *,          \
+                                         cudaStream_t);                                   \
     template int launch_gd_move<T>(const Lat<T> &, IterDev *, double, cudaStream_t);                                 \
     template int launch_ff_dot<T>(const Lat<T> &, IterDev *, double *, int, cudaStream_t);                          \
     template int launch_lbfgs_first<T>(const Lat<T> &, T *, IterDev *, cudaStream_t);                              \

@@ -638,11 +638,11 @@ static void grad_tensor(const double *dx, const double *dy, const double *dz, do
     tensor3(dz, G[2]);
 }
 
-double qo_energy(const qo_params *p, const double *Q, const int *types, const qo_object *objs, double comps[5])
+/* per-site energy densities e[5 i + k] (phase, distortion, anchoring, E, H) */
+static void site_energies(const qo_params *p, const double *Q, const int *types, const qo_object *objs, double *e)
 {
     const int L[3] = {p->Lx, p->Ly, p->Lz};
     size_t N = (size_t)L[0] * L[1] * L[2];
-    double *e = (double *)malloc(sizeof(double) * 5 * N);
     double a = 0.5 * p->A, b = p->B / 3.0, c = 0.25 * p->C;
 #pragma omp parallel for schedule(static)
     for (long long ii = 0; ii < (long long)N; ++ii) {
@@ -750,6 +750,13 @@ double qo_energy(const qo_params *p, const double *Q, const int *types, const qo
         }
         ei[1] = dist;
     }
+}
+
+double qo_energy(const qo_params *p, const double *Q, const int *types, const qo_object *objs, double comps[5])
+{
+    size_t N = (size_t)p->Lx * p->Ly * p->Lz;
+    double *e = (double *)malloc(sizeof(double) * 5 * N);
+    site_energies(p, Q, types, objs, e);
     double cs[5] = {0, 0, 0, 0, 0};
     for (size_t i = 0; i < N; ++i)
         for (int k = 0; k < 5; ++k) cs[k] += e[5 * i + k];
@@ -757,6 +764,57 @@ double qo_energy(const qo_params *p, const double *Q, const int *types, const qo
     if (comps)
         for (int k = 0; k < 5; ++k) comps[k] = cs[k];
     return cs[0] + cs[1] + cs[2] + cs[3] + cs[4];
+}
+
+/* landauDeGennesLC::computeObjectForces / computeStressTensors, one-constant
+ * (landauDeGennesLCOtherForces.cpp:147-251): for object j, the sum over its
+ * surface sites (LC sites with an object-j neighbour) of sigma . a with
+ * sigma_ab = e delta_ab - L1 B(d_a q, d_b q), B(u, v) = 2 (u0 v0 + u3 v3) +
+ * u0 v3 + u3 v0 + 4 (u1 v1 + u2 v2 + u4 v4), e the site's total energy density,
+ * d_a q the first derivatives, a the +-1 direction to object neighbours (up wins). */
+void qo_object_forces(const qo_params *p, const double *Q, const int *types, const qo_object *objs, int nobj,
+                      double *out)
+{
+    const int L[3] = {p->Lx, p->Ly, p->Lz};
+    size_t N = (size_t)L[0] * L[1] * L[2];
+    double *e = (double *)malloc(sizeof(double) * 5 * N);
+    double *D = (double *)malloc(sizeof(double) * 15 * N);
+    site_energies(p, Q, types, objs, e);
+    first_derivatives(L, Q, types, D);
+    for (int j = 0; j < 3 * nobj; ++j) out[j] = 0.0;
+    for (size_t i = 0; i < N; ++i) {
+        if (types[i] > 0) continue;
+        qo_nbrs n;
+        neighbours(L, i, &n);
+        int tn[6];
+        for (int s = 0; s < 6; ++s) tn[s] = types[n.nb[s]];
+        const double *ei = e + 5 * i;
+        double et = ei[0] + ei[3] + ei[4] + ei[2] + ei[1];
+        double a[3];
+        for (int ax = 0; ax < 3; ++ax) {
+            a[ax] = 0.0;
+            if (tn[2 * ax] > 0) a[ax] = -1.0;
+            if (tn[2 * ax + 1] > 0) a[ax] = 1.0;
+        }
+        double f[3];
+        for (int r = 0; r < 3; ++r) {
+            f[r] = 0.0;
+            for (int cc = 0; cc < 3; ++cc) {
+                const double *u = D + 15 * i + 5 * r, *v = D + 15 * i + 5 * cc;
+                double B = 2.0 * (u[0] * v[0] + u[3] * v[3]) + u[0] * v[3] + u[3] * v[0] +
+                           4.0 * (u[1] * v[1] + u[2] * v[2] + u[4] * v[4]);
+                f[r] += (-p->L1 * B + (r == cc ? et : 0.0)) * a[cc];
+            }
+        }
+        for (int obj = 1; obj <= nobj; ++obj) {
+            int next = 0;
+            for (int s = 0; s < 6; ++s) next |= tn[s] == obj;
+            if (next)
+                for (int r = 0; r < 3; ++r) out[3 * (obj - 1) + r] += f[r];
+        }
+    }
+    free(e);
+    free(D);
 }
 
 /* ------------------------------------------------------------- FIRE ---- */

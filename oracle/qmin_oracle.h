@@ -53,6 +53,8 @@ int qo_add_wall(const int L[3], int xyz, int plane, int kind, double W, double S
 int qo_add_sites(const int L[3], int nsites, const int *xyz, const double *qs, int kind, double W, double S0,
                  double *Q, int *types, qo_object *objs, int nobj);
 void qo_defects(const qo_params *p, const double *Q, const int *types, int kind, double *out);
+void qo_object_forces(const qo_params *p, const double *Q, const int *types, const qo_object *objs, int nobj,
+                      double *out);
 int qo_add_sphere(const int L[3], const double center[3], double radius, int kind, double W, double S0,
                   double *Q, int *types, qo_object *objs, int nobj);
 int qo_count_active(int N, const int *types);

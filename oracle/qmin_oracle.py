@@ -59,6 +59,8 @@ def lib():
         L.qo_add_sites.argtypes = [ip, C.c_int, ip, dp, C.c_int, C.c_double, C.c_double, dp, ip, C.POINTER(Object),
                                    C.c_int]
         L.qo_defects.argtypes = [C.POINTER(Params), dp, ip, C.c_int, dp]
+        L.qo_object_forces.argtypes = [C.POINTER(Params), dp, ip, C.POINTER(Object), C.c_int, dp]
+        L.qo_object_forces.restype = None
         L.qo_defects.restype = None
         L.qo_add_sphere.argtypes = [ip, dp, C.c_double, C.c_int, C.c_double, C.c_double, dp, ip, C.POINTER(Object), C.c_int]
         L.qo_count_active.argtypes = [C.c_int, ip]
@@ -170,6 +172,13 @@ class System:
         Q = self.Q if Q is None else np.ascontiguousarray(Q, dtype=np.float64)
         lib().qo_defects(C.byref(self.p), _dp(Q), _ip(self.types), int(kind), _dp(out))
         return out
+
+    def object_forces(self, Q=None):
+        """Force on every object from the one-constant stress tensor: [nobj, 3]."""
+        out = np.zeros((max(self.nobj, 1), 3))
+        Q = self.Q if Q is None else np.ascontiguousarray(Q, dtype=np.float64)
+        lib().qo_object_forces(C.byref(self.p), _dp(Q), _ip(self.types), self.objs, self.nobj, _dp(out))
+        return out[:self.nobj]
 
     def n_active(self):
         return lib().qo_count_active(self.N, _ip(self.types))

@@ -11,7 +11,7 @@
 //   S0 of every object is the bulk S0)  E=Ex,Ey,Ez,eps,eps0,deps
 //   H=Hx,Hy,Hz,chi,mu0,dchi  minimizer=fire|adam|nesterov|lbfgs|gd|none  iters=N
 //   bfile=PATH (boundary file)  loadstate=PREFIX  savestate=PREFIX,SKIP,DEFECTTYPE  defects=1
-//   hfile=PREFIX,chi,mu0,dchi (spatially varying H field)
+//   hfile=PREFIX,chi,mu0,dchi (spatially varying H field)  objforce=1
 //   dt=DT  fc=cutoff  trace=1 (per-iteration trace, one minimize() call per
 //   iteration)  qin=file (load Q0 from a raw float64 AoS file instead of the
 //   random initialisation)
@@ -108,6 +108,7 @@ int main(int argc, char **argv)
     string loadstate = get("loadstate", "");  // multirankSimulation::loadState prefix (before minimising)
     string savestate = get("savestate", "");  // multirankSimulation::saveState prefix,skip,defectType (after)
     bool defects = atoi(get("defects", "0").c_str()) != 0;  // dump computeDefectMeasures 0, 1, 2 (after)
+    bool objforce = atoi(get("objforce", "0").c_str()) != 0;  // dump computeObjectForces of every object (after)
 
     // openQmin.cpp:173-180
     double a = -1, b = -ABC[1] / ABC[0], c = -ABC[2] / ABC[0];
@@ -271,6 +272,15 @@ int main(int argc, char **argv)
             ArrayHandle<scalar> dm(Conf->returnDefectMeasures(), access_location::host, access_mode::read);
             dump(out + "/defects" + to_string(dt2) + ".f64", dm.data, (size_t)N);
         }
+    }
+    if (objforce) {
+        FILE *f = fopen((out + "/objforce.txt").c_str(), "w");
+        for (int j = 0; j < (int)Conf->boundaryForce.size(); ++j) {
+            lc->computeObjectForces(j);
+            fprintf(f, "%.17g %.17g %.17g\n", Conf->boundaryForce[j].x, Conf->boundaryForce[j].y,
+                    Conf->boundaryForce[j].z);
+        }
+        fclose(f);
     }
     if (!savestate.empty()) {
         vector<string> sv = parse_strs(savestate);

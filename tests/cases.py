@@ -127,4 +127,4 @@ def rel_err(a, b):
 
 GOLDEN_CASES = ["l1_bulk_fire", "l123_walls_sphere_fire", "planar_sphere_fire", "l1234_planar_fields_fire",
                 "edges_gaps_wrap", "adam", "nesterov", "lbfgs", "gd", "boundary_file_defects", "load_state",
-                "field_map", "l6_fire"]
+                "field_map", "l6_fire", "object_forces"]

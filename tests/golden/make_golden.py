@@ -65,6 +65,11 @@ CASES = {
     # the cubic L6 term with L1-L3, homeotropic wall and sphere, planar sphere (bulk and boundary forms)
     "l6_fire": (["L=11,10,9", "seed=53", "Ls=2.32,1.0,0.5,0,0.8", "wall=2,0,h,5.3", "sphere=5,5,4.5,2.4,h,4.0",
                  "sphere=1.3,8.2,6.4,1.9,p,1.2", "minimizer=fire", "iters=20", "trace=1"], True),
+    # forces on objects from the stress tensor (one-constant): a homeotropic sphere, a planar sphere
+    # and a wall, after FIRE
+    "object_forces": (["L=14,12,11", "seed=61", "Ls=2.32,0,0,0,0", "wall=2,0,h,5.3", "sphere=4.3,5.2,5.6,2.6,h,4.0",
+                       "sphere=10.2,6.4,5.1,2.2,p,1.5", "minimizer=fire", "iters=25", "trace=1", "objforce=1"],
+                      True),
     # the 50^3 one-constant CLI run (openQmin -i 100 -l 50 --L1 2.32): scalars only
     "c1_50cube_fire100": (["L=50,50,50", "seed=13371", "Ls=2.32,0,0,0,0", "minimizer=fire", "iters=100",
                            "trace=1"], False),
@@ -154,6 +159,8 @@ def run_case(name, args, full):
             out["in_" + fn.replace(".", "_")] = np.array(make())
         for fn in post:
             out["out_" + fn.replace(".", "_")] = np.array(open(os.path.join(d, fn)).read())
+        if os.path.exists(os.path.join(d, "objforce.txt")):
+            out["objforce"] = np.loadtxt(os.path.join(d, "objforce.txt"), ndmin=2)
         for k in range(3):
             if os.path.exists(os.path.join(d, f"defects{k}.f64")):
                 out[f"defects{k}"] = ld(f"defects{k}.f64")

@@ -143,3 +143,16 @@ def test_reference_shaped_file_calls(qmin, oracle, tmp_path):
     d = model.computeDefectMeasures(1)
     assert np.abs(d - oracle_system(oracle, cfg).defects(1)).max() <= 1e-13
     sim.loadState(str(tmp_path / "x"))
+
+
+def test_object_forces_match_reference(qmin, oracle):
+    """Force on each object from the one-constant stress tensor, on the
+    reference's final state; the multi-constant form is refused."""
+    g, s, lat = _reference_case(qmin, oracle, "object_forces")
+    lat.set_positions(g["qfinal"])
+    f = lat.object_forces()
+    assert f.shape == g["objforce"].shape
+    np.testing.assert_allclose(f, g["objforce"], rtol=0, atol=1e-12 * np.abs(g["objforce"]).max())
+    g2, s2, lat2 = _reference_case(qmin, oracle, "l123_walls_sphere_fire")
+    with pytest.raises(qmin.QminError):
+        lat2.object_forces()

@@ -93,3 +93,11 @@ def test_defect_measures(oracle):
         d = s.defects(k, Q=g["qfinal"])
         scale = np.abs(g[f"defects{k}"]).max()
         np.testing.assert_allclose(d, g[f"defects{k}"], rtol=0, atol=1e-13 * scale)
+
+
+def test_object_forces(oracle):
+    """computeObjectForces of every object on the reference's final state."""
+    g = load("object_forces")
+    s = oracle_system(oracle, parse_args(g["args"]))
+    f = s.object_forces(Q=g["qfinal"])
+    np.testing.assert_allclose(f, g["objforce"], rtol=0, atol=1e-12 * np.abs(g["objforce"]).max())
