@@ -131,6 +131,12 @@ template <class T> void fill_lat_params(Lat<T> &L, const qmin_ldg_params &p, int
             }
             L.cb[k * QMIN_BULK_W + n] = T(c);
         }
+    for (int k = 0; k < 5; ++k)
+        for (int n = 0; n < QMIN_Q25_W; ++n) {
+            double c = 0.0;  // k L / 8 per stencil value
+            for (int t = 0; t < 4; ++t) c += Lt[t] * (double)qmin_q25_k[t][k][n] * 0.125;
+            L.cq[k * QMIN_Q25_W + n] = T(c);
+        }
 }
 template void fill_lat_params<double>(Lat<double> &, const qmin_ldg_params &, int);
 template void fill_lat_params<float>(Lat<float> &, const qmin_ldg_params &, int);

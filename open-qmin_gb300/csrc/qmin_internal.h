@@ -7,6 +7,7 @@
 
 #include "../../include/qmin_gb300.h"
 #include "qmin_bulk_forms.h"
+#include "qmin_bulk_q25.h"
 
 namespace qmin {
 
@@ -32,6 +33,7 @@ template <class T> struct Lat {
     T hvp;              // its dchi * mu0
     int metric_mode, multi, efield, hfield;
     T cb[5 * QMIN_BULK_W];  // combined bulk multi-constant coefficients
+    T cq[5 * QMIN_Q25_W];   // the same form over Q on the 25-point stencil (deep bulk sites)
 };
 
 // force parameters shared by every kernel (qmin_capi.cu)
@@ -116,5 +118,21 @@ template <class T>
 int launch_force_kick_tiled(int cfg, const Lat<T> &L, FireDev *fd, double *partials, int zc, cudaStream_t s,
                             int *nblocks);
 int tiled_tile_shape(int cfg, int *tx, int *ty);
+
+// split force + kick (multi-constant, no L6): site classes (0 deep bulk, 1 other
+// LC site, 2 object), the class-1 sites, and the sites whose derivative planes
+// the class-1 forms read
+struct SplitLists {
+    const uint8_t *cls;
+    const int *sites;
+    int n_sites;
+    const int *derivs;
+    int n_derivs;
+};
+template <class T> int launch_split_derivs(const Lat<T> &L, const SplitLists &sl, FireDev *fd, cudaStream_t s);
+// partials: the deep kernel's grid blocks, then the list kernel's; *nparts their total
+template <class T>
+int launch_split_force_kick(const Lat<T> &L, const SplitLists &sl, FireDev *fd, double *partials, int grid, int cap,
+                            cudaStream_t s, int *nparts);
 
 }  // namespace qmin
