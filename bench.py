@@ -188,7 +188,8 @@ def run_ours(args, rank, world):
         lat = make_lattice(q, consts, g, precision)
         pinned = args.fire_kernel_fp64 if precision == q.FP64 else args.fire_kernel_fp32
         if pinned != "auto":
-            lat.set_fire_kernel({"separate": q.FIRE_SEPARATE, "fused": q.FIRE_FUSED, "tiled": q.FIRE_TILED}[pinned])
+            lat.set_fire_kernel({"separate": q.FIRE_SEPARATE, "fused": q.FIRE_FUSED, "tiled": q.FIRE_TILED,
+                                 "split": q.FIRE_SPLIT}[pinned])
         stream = torch.cuda.Stream()
         lat_stream = stream.cuda_stream
         q._check(q.lib().qmin_set_stream(lat._h, lat_stream))
@@ -642,8 +643,8 @@ def main():
     ap.add_argument("--c4-test", type=int, default=64, help="c4 test solves for the warm-start protocol (0: skip)")
     # a fixed FIRE strategy instead of the autotuner's choice (for profiling runs, where the
     # profiler's serialised launches would bias the autotuner's timings)
-    ap.add_argument("--fire-kernel-fp64", default="auto", choices=["auto", "separate", "fused"])
-    ap.add_argument("--fire-kernel-fp32", default="auto", choices=["auto", "separate", "fused", "tiled"])
+    ap.add_argument("--fire-kernel-fp64", default="auto", choices=["auto", "separate", "fused", "split"])
+    ap.add_argument("--fire-kernel-fp32", default="auto", choices=["auto", "separate", "fused", "tiled", "split"])
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", 0))
     world = int(os.environ.get("WORLD_SIZE", 1))

@@ -209,6 +209,9 @@ int qmin_gd_run(qmin_handle h, double dt, double force_cutoff, int max_iteration
 #define QMIN_FIRE_AUTO 2     /* the autotuner picks the fastest of the others (default) */
 #define QMIN_FIRE_TILED 3    /* separate predictor and derivative planes, force + kick from shared-memory
                                 tiles (FP32 form only) */
+#define QMIN_FIRE_SPLIT 4    /* deep bulk sites' force + kick over Q on the 25-point stencil (no derivative
+                                planes), the sites near objects through the plane forms (multi-constant
+                                form without L6; otherwise the separate kernels run) */
 /* Choose how qmin_fire_run executes an iteration; all strategies give the
  * same results to rounding.  No reference counterpart (execution strategy). */
 int qmin_set_fire_kernel(qmin_handle h, int mode);
@@ -223,13 +226,14 @@ int qmin_fire_profile(qmin_handle h, int iterations, double kernel_ms[4], int *f
 /* The FIRE strategy the autotuner chose on the first run (path 0 separate
  * kernels sized for `variant` + 1 blocks per SM; path 1 fused kernel and
  * path 2 staged force + kick, each with tile shape `variant` = tile_x x tile_y
- * and `zc` z planes per block) and the measured ms per iteration of every
- * candidate: ms[0..2] separate (1, 2, 3 blocks per SM), ms[3 + 2*cfg + v]
- * fused (4 shapes, v = 0/1 for the two z extents tried), ms[11 + 2*cfg + v]
- * staged (3 shapes); -1 = not run.
+ * and `zc` z planes per block; path 3 split force + kick with its deep-site
+ * kernel sized for `variant` + 1 blocks per SM) and the measured ms per
+ * iteration of every candidate: ms[0..2] separate (1, 2, 3 blocks per SM),
+ * ms[3 + 2*cfg + v] fused (4 shapes, v = 0/1 for the two z extents tried),
+ * ms[11 + 2*cfg + v] staged (3 shapes), ms[17 + v] split; -1 = not run.
  * No reference counterpart (the reference's kernelTuner scans block sizes,
  * src/utilities/kernelTuner.cpp:5-125). */
-#define QMIN_TUNE_CANDIDATES 17
+#define QMIN_TUNE_CANDIDATES 19
 int qmin_fire_tuning(qmin_handle h, int *path, int *variant, int *tile_x, int *tile_y, int *zc,
                      double ms[QMIN_TUNE_CANDIDATES]);
 

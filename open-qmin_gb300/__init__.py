@@ -42,7 +42,7 @@ EXPORTED_SYMBOLS = [
     "qmin_warmnet_backward", "qmin_warmnet_adam_step", "qmin_warmnet_write_state", "qmin_warmnet_sync",
     "qmin_warmnet_kernel_launches", "qmin_warm_start",
 ]
-FIRE_SEPARATE, FIRE_FUSED, FIRE_AUTO, FIRE_TILED = 0, 1, 2, 3
+FIRE_SEPARATE, FIRE_FUSED, FIRE_AUTO, FIRE_TILED, FIRE_SPLIT = 0, 1, 2, 3, 4
 
 
 class QminError(RuntimeError):
@@ -368,7 +368,8 @@ class Lattice:
 
     def set_fire_kernel(self, mode):
         """FIRE_AUTO (default): autotuned; FIRE_FUSED: one tiled kernel per iteration; FIRE_SEPARATE;
-        FIRE_TILED: separate predictor and derivatives, force + kick from shared-memory tiles (FP32)."""
+        FIRE_TILED: separate predictor and derivatives, force + kick from shared-memory tiles (FP32);
+        FIRE_SPLIT: deep bulk sites over Q on the 25-point stencil, the rest through derivative planes."""
         _check(lib().qmin_set_fire_kernel(self._h, int(mode)))
 
     def fire_profile(self, iterations=20):
@@ -379,13 +380,14 @@ class Lattice:
 
     def fire_tuning(self):
         path, var, tx, ty, zc = C.c_int(), C.c_int(), C.c_int(), C.c_int(), C.c_int()
-        ms = (C.c_double * 17)()
+        ms = (C.c_double * 19)()
         _check(lib().qmin_fire_tuning(self._h, C.byref(path), C.byref(var), C.byref(tx), C.byref(ty), C.byref(zc),
                                       ms))
         names = (["separate_1blk", "separate_2blk", "separate_3blk"]
                  + [f"fused_{a}x{b}_z{v}" for a, b in ((32, 8), (32, 16), (64, 8), (32, 4)) for v in (0, 1)]
-                 + [f"tiled_{a}x{b}_z{v}" for a, b in ((32, 8), (32, 4), (16, 16)) for v in (0, 1)])
-        return dict(path=["separate", "fused", "tiled"][path.value], variant=var.value, tile=(tx.value, ty.value),
+                 + [f"tiled_{a}x{b}_z{v}" for a, b in ((32, 8), (32, 4), (16, 16)) for v in (0, 1)]
+                 + ["split_1blk", "split_2blk"])
+        return dict(path=["separate", "fused", "tiled", "split"][path.value], variant=var.value, tile=(tx.value, ty.value),
                     zc=zc.value, candidates_ms={n: m for n, m in zip(names, ms) if m >= 0})
 
     def launches(self):

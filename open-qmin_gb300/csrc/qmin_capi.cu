@@ -36,7 +36,8 @@ static int fail(int code, const std::string &msg)
     } while (0)
 
 static const int kSepVariants = 3;  // separate-kernel force + kick with 1, 2, 3 blocks per SM
-static const int kTuneCandidates = kSepVariants + 2 * kFusedConfigs + 2 * kTiledConfigs;
+static const int kSplitVariants = 2;  // deep-site kernel with 1 or 2 blocks per SM
+static const int kTuneCandidates = kSepVariants + 2 * kFusedConfigs + 2 * kTiledConfigs + kSplitVariants;
 static_assert(kTuneCandidates == QMIN_TUNE_CANDIDATES, "tuning candidate count");
 
 struct qmin_ctx {
@@ -84,6 +85,12 @@ struct qmin_ctx {
     int path = -1;  // 0 separate kernels, 1 fused tiled kernel, 2 separate with the staged force + kick
     int sep_cap = 0, fused_cfg = -1, fused_zc = 0, fused_nblocks = 0, tuned_version = 0, tuned_mode = -1;
     int tiled_cfg = -1, tiled_zc = 0, tiled_nblocks = 0;
+    int split_cap = 0;  // path 3: register cap of the deep-site kernel
+    // split path: site classes (0 deep bulk, 1 other LC, 2 object), the class-1
+    // sites and the sites whose derivative planes they read
+    uint8_t *split_cls = nullptr;
+    int *split_sites = nullptr, *split_derivs = nullptr;
+    int n_split_sites = 0, n_split_derivs = 0;
     // separate (register caps), fused (cfg, z extent), staged force + kick (cfg, z extent)
     double tune_ms[kTuneCandidates] = {};
 };
@@ -168,7 +175,8 @@ static void free_ctx(qmin_ctx *h)
     for (int g = 0; g < 5; ++g)
         if (h->graph[g]) cudaGraphExecDestroy(h->graph[g]);
     void *bufs[] = {h->Q, h->V, h->F, h->D, h->types, h->objs, h->partials, h->stage, h->stage_t, h->fire, h->iter,
-                    h->out5, h->M, h->S, h->alt, h->lbp, h->lbs, h->lby, h->Q2, h->V2, h->F2, h->hvar};
+                    h->out5, h->M, h->S, h->alt, h->lbp, h->lbs, h->lby, h->Q2, h->V2, h->F2, h->hvar,
+                    h->split_cls, h->split_sites, h->split_derivs};
     for (void *b : bufs)
         if (b) cudaFree(b);
     if (h->fire_h) cudaFreeHost(h->fire_h);
@@ -331,6 +339,62 @@ static int ensure_stage(qmin_ctx *h)
     return QMIN_OK;
 }
 
+// classes and index lists of the split force + kick, from host site types
+static int build_split_lists(qmin_ctx *h, const int8_t *t8)
+{
+    const int Lx = h->Lx, Ly = h->Ly, Lz = h->Lz, N = h->N;
+    std::vector<uint8_t> cls((size_t)N);
+    std::vector<int> sites, derivs;
+    std::vector<char> need((size_t)N, 0);
+    auto nb = [&](int i, int s) {
+        const int x = i % Lx, r = i / Lx, y = r % Ly, z = r / Ly;
+        switch (s) {
+        case 0: return (x == 0 ? Lx - 1 : x - 1) + Lx * (y + Ly * z);
+        case 1: return (x == Lx - 1 ? 0 : x + 1) + Lx * (y + Ly * z);
+        case 2: return x + Lx * ((y == 0 ? Ly - 1 : y - 1) + Ly * z);
+        case 3: return x + Lx * ((y == Ly - 1 ? 0 : y + 1) + Ly * z);
+        case 4: return x + Lx * (y + Ly * (z == 0 ? Lz - 1 : z - 1));
+        default: return x + Lx * (y + Ly * (z == Lz - 1 ? 0 : z + 1));
+        }
+    };
+    for (int i = 0; i < N; ++i) {
+        if (t8[i] > 0) {
+            cls[i] = 2;
+            continue;
+        }
+        bool deep = t8[i] == 0;
+        for (int s = 0; s < 6 && deep; ++s) deep = t8[nb(i, s)] == 0;
+        cls[i] = deep ? 0 : 1;
+        if (!deep) {
+            sites.push_back(i);
+            for (int s = 0; s < 6; ++s) need[nb(i, s)] = 1;
+        }
+    }
+    for (int i = 0; i < N; ++i)
+        if (need[i]) derivs.push_back(i);
+    auto upload = [&](void **dst, const void *src, size_t bytes) -> bool {
+        if (*dst) cudaFree(*dst);
+        *dst = nullptr;
+        if (bytes == 0) return true;
+        return cudaMalloc(dst, bytes) == cudaSuccess &&
+               cudaMemcpy(*dst, src, bytes, cudaMemcpyHostToDevice) == cudaSuccess;
+    };
+    if (!upload((void **)&h->split_cls, cls.data(), cls.size()) ||
+        !upload((void **)&h->split_sites, sites.data(), sites.size() * sizeof(int)) ||
+        !upload((void **)&h->split_derivs, derivs.data(), derivs.size() * sizeof(int))) {
+        cudaGetLastError();
+        return fail(QMIN_ENOMEM, "split site lists: allocation failed");
+    }
+    h->n_split_sites = (int)sites.size();
+    h->n_split_derivs = (int)derivs.size();
+    return QMIN_OK;
+}
+
+static SplitLists split_lists(const qmin_ctx *h)
+{
+    return SplitLists{h->split_cls, h->split_sites, h->n_split_sites, h->split_derivs, h->n_split_derivs};
+}
+
 int qmin_set_state(qmin_handle h, const double *Q, const int32_t *types, int layout)
 {
     if (!h || !Q || !types) return fail(QMIN_EINVAL, "qmin_set_state: null argument");
@@ -357,6 +421,13 @@ int qmin_set_state(qmin_handle h, const double *Q, const int32_t *types, int lay
     CK(cudaMemsetAsync(h->V, 0, 5 * (size_t)h->P * h->esz, h->stream));
     CK(cudaMemsetAsync(h->F, 0, 5 * (size_t)h->P * h->esz, h->stream));
     CK(cudaGetLastError());
+    {
+        std::vector<int8_t> t8((size_t)h->N);
+        for (int i = 0; i < h->N; ++i) t8[i] = (int8_t)types[i];
+        CK(cudaStreamSynchronize(h->stream));
+        if ((r = build_split_lists(h, t8.data()))) return r;
+    }
+    invalidate_graphs(h);
     h->have_state = true;
     return QMIN_OK;
 }
@@ -691,10 +762,11 @@ template <class T> static int tune_fire(qmin_ctx *h, const Lat<T> &L)
             }
         }
     }
-    const bool try_sep = l6 || h->fire_mode == QMIN_FIRE_AUTO || h->fire_mode == QMIN_FIRE_SEPARATE;
+    const bool try_sep = l6 || h->fire_mode == QMIN_FIRE_AUTO || h->fire_mode == QMIN_FIRE_SEPARATE ||
+                         (h->fire_mode == QMIN_FIRE_SPLIT && !L.multi);
     const bool try_tiled =
         !l6 && (h->fire_mode == QMIN_FIRE_AUTO || h->fire_mode == QMIN_FIRE_TILED) && sizeof(T) == 4;
-    if (try_sep || try_tiled) {
+    if (try_sep || try_tiled || (L.multi && !l6 && h->fire_mode == QMIN_FIRE_SPLIT)) {
         const float t_pred = time3([&]() { launch_fire_pred<T>(LB, h->fire, h->stream); });
         const float t_der = L.multi ? time3([&]() { launch_derivs<T>(L, h->stream); }) : 0.f;
         const size_t bytes = 5 * (size_t)h->P * h->esz;
@@ -737,6 +809,25 @@ template <class T> static int tune_fire(qmin_ctx *h, const Lat<T> &L)
                 h->sep_cap = cap;
             }
         }
+        const bool try_split = L.multi && !l6 && h->split_cls &&
+                               (h->fire_mode == QMIN_FIRE_AUTO || h->fire_mode == QMIN_FIRE_SPLIT);
+        if (try_split) {
+            const SplitLists sl = split_lists(h);
+            const float t_dl = time3([&]() { launch_split_derivs<T>(L, sl, h->fire, h->stream); });
+            for (int cap = 0; cap < kSplitVariants; ++cap) {
+                int np = 0;
+                const float t_fk = time3(
+                    [&]() { launch_split_force_kick<T>(L, sl, h->fire, h->partials, h->grid, cap, h->stream, &np); });
+                const float ms = t_pred + t_dl + t_fk;
+                h->tune_ms[kSepVariants + 2 * kFusedConfigs + 2 * kTiledConfigs + cap] = ms;
+                if (ms < best) {
+                    best = ms;
+                    h->path = 3;
+                    h->split_cap = cap;
+                }
+            }
+            h->launches += 4 * (1 + 2 * kSplitVariants);
+        }
         CK(cudaMemcpyAsync(h->V, h->V2, bytes, cudaMemcpyDeviceToDevice, h->stream));
         h->launches += 4 * (1 + (L.multi ? 1 : 0) + (try_sep ? kSepVariants : 0)) + 2;
     }
@@ -762,7 +853,10 @@ template <class T> static int fire_impl(qmin_ctx *h, int max_iterations)
     LB.V = (T *)h->V2;
     LB.F = (T *)h->F2;
     int parity = 0;
-    const int variant = h->path == 0 ? h->sep_cap : (h->path == 1 ? h->fused_cfg : h->tiled_cfg);
+    const int variant = h->path == 0 ? h->sep_cap
+                        : h->path == 1 ? h->fused_cfg
+                        : h->path == 2 ? h->tiled_cfg
+                                       : h->split_cap;
     const double args[4] = {(double)h->path, (double)variant, (double)(h->path == 2 ? h->tiled_zc : h->fused_zc), 0};
     r = capture_chunk(h, 0, args, [&]() {
         int n;
@@ -770,6 +864,13 @@ template <class T> static int fire_impl(qmin_ctx *h, int max_iterations)
             n = launch_fire_pred<T>(L, h->fire, h->stream);
             n += launch_force_kick<T>(L, h->fire, h->partials, h->grid, h->stream, h->sep_cap);
             n += launch_fire_control(h->fire, h->partials, h->grid, h->stream);
+        } else if (h->path == 3) {
+            int nb = 0;
+            const SplitLists sl = split_lists(h);
+            n = launch_fire_pred<T>(L, h->fire, h->stream);
+            n += launch_split_derivs<T>(L, sl, h->fire, h->stream);
+            n += launch_split_force_kick<T>(L, sl, h->fire, h->partials, h->grid, h->split_cap, h->stream, &nb);
+            n += launch_fire_control(h->fire, h->partials, nb, h->stream);
         } else if (h->path == 2) {
             int nb = 0;
             n = launch_fire_pred<T>(L, h->fire, h->stream);
@@ -1045,7 +1146,8 @@ template <class T> static int fire_profile_impl(qmin_ctx *h, int iterations, dou
     cudaEvent_t ev[5];
     for (auto &e : ev) CK(cudaEventCreate(&e));
     double acc[4] = {0, 0, 0, 0};
-    const bool fused = h->path == 1, tiled = h->path == 2;
+    const bool fused = h->path == 1, tiled = h->path == 2, split = h->path == 3;
+    const SplitLists sl = split_lists(h);
     Lat<T> LB = L;
     LB.Q = (T *)h->Q2;
     LB.V = (T *)h->V2;
@@ -1054,10 +1156,14 @@ template <class T> static int fire_profile_impl(qmin_ctx *h, int iterations, dou
         CK(cudaEventRecord(ev[0], h->stream));
         if (!fused) h->launches += launch_fire_pred<T>(L, h->fire, h->stream);
         CK(cudaEventRecord(ev[1], h->stream));
-        if (!fused && L.multi) h->launches += launch_derivs<T>(L, h->stream);
+        if (split) h->launches += launch_split_derivs<T>(L, sl, h->fire, h->stream);
+        else if (!fused && L.multi) h->launches += launch_derivs<T>(L, h->stream);
         CK(cudaEventRecord(ev[2], h->stream));
         int nparts = h->grid;
-        if (tiled) {
+        if (split) {
+            h->launches += launch_split_force_kick<T>(L, sl, h->fire, h->partials, h->grid, h->split_cap, h->stream,
+                                                      &nparts);
+        } else if (tiled) {
             h->launches += launch_force_kick_tiled<T>(h->tiled_cfg, L, h->fire, h->partials, h->tiled_zc, h->stream,
                                                       &nparts);
         } else if (!fused) {
@@ -1111,8 +1217,10 @@ int qmin_fire_profile(qmin_handle h, int iterations, double kernel_ms[4], int *f
 int qmin_set_fire_kernel(qmin_handle h, int mode)
 {
     if (!h) return fail(QMIN_EINVAL, "qmin_set_fire_kernel: null handle");
-    if (mode != QMIN_FIRE_SEPARATE && mode != QMIN_FIRE_FUSED && mode != QMIN_FIRE_AUTO && mode != QMIN_FIRE_TILED)
-        return fail(QMIN_EINVAL, "qmin_set_fire_kernel: mode must be QMIN_FIRE_SEPARATE, _FUSED, _TILED or _AUTO");
+    if (mode != QMIN_FIRE_SEPARATE && mode != QMIN_FIRE_FUSED && mode != QMIN_FIRE_AUTO && mode != QMIN_FIRE_TILED &&
+        mode != QMIN_FIRE_SPLIT)
+        return fail(QMIN_EINVAL,
+                    "qmin_set_fire_kernel: mode must be QMIN_FIRE_SEPARATE, _FUSED, _TILED, _SPLIT or _AUTO");
     if (mode == QMIN_FIRE_TILED && h->prec != QMIN_FP32)
         return fail(QMIN_EINVAL, "qmin_set_fire_kernel: the staged force + kick is built for the FP32 form only");
     if (h->fire_mode != mode) invalidate_graphs(h);
@@ -1125,7 +1233,8 @@ int qmin_fire_tuning(qmin_handle h, int *path, int *variant, int *tile_x, int *t
     if (!h) return fail(QMIN_EINVAL, "qmin_fire_tuning: null handle");
     if (h->path < 0) return fail(QMIN_ESTATE, "qmin_fire_tuning: no FIRE run has been tuned yet");
     if (path) *path = h->path;
-    if (variant) *variant = h->path == 0 ? h->sep_cap : (h->path == 1 ? h->fused_cfg : h->tiled_cfg);
+    if (variant)
+        *variant = h->path == 0 ? h->sep_cap : (h->path == 1 ? h->fused_cfg : (h->path == 2 ? h->tiled_cfg : h->split_cap));
     int tx = 0, ty = 0;
     if (h->path == 1) fused_tile_shape(h->fused_cfg, &tx, &ty);
     if (h->path == 2) tiled_tile_shape(h->tiled_cfg, &tx, &ty);
@@ -1165,6 +1274,7 @@ struct CkpHeader {
     char magic[8];
     int32_t version, Lx, Ly, Lz, prec, metric_mode, nobj, have_params, fire_ready, lb_m, flags;
     int32_t path, sep_cap, fused_cfg, fused_zc, fused_nblocks, tiled_cfg, tiled_zc, tiled_nblocks, fire_mode;
+    int32_t split_cap, pad;
     int64_t N, P;
 };
 enum { kCkpM = 1, kCkpS = 2, kCkpAlt = 4, kCkpLb = 8 };
@@ -1187,7 +1297,7 @@ int qmin_checkpoint_save(qmin_handle h, const char *path)
     hd.flags = (h->M ? kCkpM : 0) | (h->S ? kCkpS : 0) | (h->alt ? kCkpAlt : 0) | (h->lbp ? kCkpLb : 0);
     hd.path = h->path; hd.sep_cap = h->sep_cap; hd.fused_cfg = h->fused_cfg; hd.fused_zc = h->fused_zc;
     hd.fused_nblocks = h->fused_nblocks; hd.tiled_cfg = h->tiled_cfg; hd.tiled_zc = h->tiled_zc;
-    hd.tiled_nblocks = h->tiled_nblocks; hd.fire_mode = h->fire_mode;
+    hd.tiled_nblocks = h->tiled_nblocks; hd.fire_mode = h->fire_mode; hd.split_cap = h->split_cap;
     hd.N = h->N; hd.P = h->P;
     const size_t plane = 5 * (size_t)h->P * h->esz;
     std::vector<char> buf(plane);
@@ -1285,6 +1395,7 @@ int qmin_checkpoint_load(qmin_handle h, const char *path)
     }
     h->nTotal = nT;
     h->max_type = mx;
+    if (int rr = build_split_lists(h, t8.data())) return rr;
     h->have_state = true;
     h->fire_ready = hd.fire_ready != 0;
     CK(cudaMemcpy(h->fire_h, h->fire, sizeof(FireDev), cudaMemcpyDeviceToHost));
@@ -1303,6 +1414,7 @@ int qmin_checkpoint_load(qmin_handle h, const char *path)
         h->tiled_cfg = hd.tiled_cfg;
         h->tiled_zc = hd.tiled_zc;
         h->tiled_nblocks = hd.tiled_nblocks;
+        h->split_cap = hd.split_cap;
         h->tuned_version = h->version;
         h->tuned_mode = h->fire_mode;
     }

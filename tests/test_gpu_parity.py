@@ -51,9 +51,10 @@ def test_force_fp32(qmin, oracle, name):
 
 @pytest.mark.parametrize("name", ["l1_bulk_fire", "l123_walls_sphere_fire", "planar_sphere_fire",
                                   "l1234_planar_fields_fire", "edges_gaps_wrap", "field_map", "l6_fire"])
-@pytest.mark.parametrize("mode", [0, 1])
+@pytest.mark.parametrize("mode", [0, 1, 4])
 def test_fire_trajectory_fp64(qmin, oracle, name, mode):
-    """Both FIRE execution paths (separate kernels, fused tiled kernel) against the reference."""
+    """The FIRE execution paths (separate kernels, fused tiled kernel, split
+    deep/listed force + kick) against the reference."""
     g = load(name)
     cfg = parse_args(g["args"])
     s = oracle_system(oracle, cfg)
@@ -192,10 +193,10 @@ def test_cpp_host_example_reproduces_cli_pin(qmin):
 
 
 @pytest.mark.parametrize("L", [(16, 9, 7), (40, 33, 21), (65, 17, 30)])
-@pytest.mark.parametrize("prec,other", [(0, 1), (1, 1), (1, 3)])
+@pytest.mark.parametrize("prec,other", [(0, 1), (1, 1), (1, 3), (0, 4), (1, 4)])
 def test_fused_matches_separate_kernels(qmin, oracle, L, prec, other):
-    """The fused tiled kernel (other = 1) and the staged force + kick
-    (other = 3, FP32 form) on lattices that do not divide their tiles (partial
+    """The fused tiled kernel (other = 1), the staged force + kick
+    (other = 3, FP32 form) and the split force + kick (other = 4) on lattices that do not divide their tiles (partial
     tiles, lattices narrower than a tile, odd z extents) track the separate
     kernels: FP64 to 1e-12 after 7 iterations, FP32 to 1e-5."""
     cfg = parse_args([f"L={L[0]},{L[1]},{L[2]}", "seed=11", "Ls=2.32,1.0,0.5,0,0", "wall=2,0,h,5.3",
