@@ -54,6 +54,10 @@ def kernel_roofline(lat, esz, N, peak, peak_kind, tag):
         nbytes[2] = FUSED_BYTES[esz]
     elif tuning["path"] == "tiled":
         names[2] = "force_kick_tiled"
+    elif tuning["path"] == "split":
+        # deep bulk sites over Q (no derivative planes) + the listed sites; derivative planes only at the list
+        names[1] = "first_derivatives_listed"
+        names[2] = "force_kick_split"
     dom = int(np.argmax(kms))
     achieved = nbytes[dom] * N / (kms[dom] / 1e3) / 1e9
     out = {"bound": "hbm", "kernel": names[dom], "achieved": achieved, "peak": peak, "unit": "GB/s",
