@@ -194,6 +194,9 @@ def run_ours(args, rank, world):
         if pinned != "auto":
             lat.set_fire_kernel({"separate": q.FIRE_SEPARATE, "fused": q.FIRE_FUSED, "tiled": q.FIRE_TILED,
                                  "split": q.FIRE_SPLIT}[pinned])
+            variant = args.fire_variant_fp64 if precision == q.FP64 else args.fire_variant_fp32
+            if variant >= 0:
+                lat.set_fire_variant(variant)
         stream = torch.cuda.Stream()
         lat_stream = stream.cuda_stream
         q._check(q.lib().qmin_set_stream(lat._h, lat_stream))
@@ -649,6 +652,8 @@ def main():
     # profiler's serialised launches would bias the autotuner's timings)
     ap.add_argument("--fire-kernel-fp64", default="auto", choices=["auto", "separate", "fused", "split"])
     ap.add_argument("--fire-kernel-fp32", default="auto", choices=["auto", "separate", "fused", "tiled", "split"])
+    ap.add_argument("--fire-variant-fp64", type=int, default=-1, help="variant index of the pinned FP64 strategy")
+    ap.add_argument("--fire-variant-fp32", type=int, default=-1, help="variant index of the pinned FP32 strategy")
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", 0))
     world = int(os.environ.get("WORLD_SIZE", 1))

@@ -223,17 +223,26 @@ int qmin_set_fire_kernel(qmin_handle h, int mode);
  * advances exactly as in qmin_fire_run.  No reference counterpart (profiling). */
 int qmin_fire_profile(qmin_handle h, int iterations, double kernel_ms[4], int *fused);
 /* (kernel_ms[2] is the staged force + kick when path 2 runs; *fused is 1 only for path 1) */
+/* Pin one variant of the strategy chosen with qmin_set_fire_kernel (its index
+ * among that strategy's candidates in qmin_fire_tuning's ms[]: 0-2 separate,
+ * 0-3 fused, 0-2 staged, 0-3 split), or -1 to let the autotuner pick (the
+ * default; qmin_set_fire_kernel resets it).  QMIN_EINVAL for an index the
+ * strategy does not have or when no strategy is pinned.  No reference
+ * counterpart (execution strategy). */
+int qmin_set_fire_variant(qmin_handle h, int variant);
 /* The FIRE strategy the autotuner chose on the first run (path 0 separate
  * kernels sized for `variant` + 1 blocks per SM; path 1 fused kernel and
  * path 2 staged force + kick, each with tile shape `variant` = tile_x x tile_y
- * and `zc` z planes per block; path 3 split force + kick with its deep-site
- * kernel sized for `variant` + 1 blocks per SM) and the measured ms per
+ * and `zc` z planes per block; path 3 split force + kick with deep-site
+ * kernel `variant`, as in ms[17 + v] below) and the measured ms per
  * iteration of every candidate: ms[0..2] separate (1, 2, 3 blocks per SM),
  * ms[3 + 2*cfg + v] fused (4 shapes, v = 0/1 for the two z extents tried),
- * ms[11 + 2*cfg + v] staged (3 shapes), ms[17 + v] split; -1 = not run.
+ * ms[11 + 2*cfg + v] staged (3 shapes), ms[17 + v] split (v = 0, 1: deep
+ * sites from global memory at 1 or 2 blocks per SM; v = 2, 3: deep sites
+ * from shared-memory tiles of 32 x 8 or 16 x 16 sites); -1 = not run.
  * No reference counterpart (the reference's kernelTuner scans block sizes,
  * src/utilities/kernelTuner.cpp:5-125). */
-#define QMIN_TUNE_CANDIDATES 19
+#define QMIN_TUNE_CANDIDATES 21
 int qmin_fire_tuning(qmin_handle h, int *path, int *variant, int *tile_x, int *tile_y, int *zc,
                      double ms[QMIN_TUNE_CANDIDATES]);
 

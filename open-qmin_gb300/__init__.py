@@ -34,6 +34,7 @@ EXPORTED_SYMBOLS = [
     "qmin_gd_run", "qmin_get_sides", "qmin_get_types", "qmin_set_positions", "qmin_defect_measures", "qmin_object_forces",
     "qmin_save_state", "qmin_load_state", "qmin_set_field_map", "qmin_load_field_map", "qmin_checkpoint_save", "qmin_checkpoint_load", "qmin_host_boundary_file",
     "qmin_host_random_nematic", "qmin_host_add_wall", "qmin_host_add_sphere", "qmin_set_fire_kernel",
+    "qmin_set_fire_variant",
     "qmin_fire_profile", "qmin_fire_tuning", "qmin_energy_noalloc", "qmin_batch_create", "qmin_batch_destroy",
     "qmin_batch_set_params", "qmin_batch_set_solve", "qmin_batch_get_solve", "qmin_batch_fire_init",
     "qmin_batch_fire_run", "qmin_batch_kernel_launches", "qmin_warmnet_create", "qmin_warmnet_destroy",
@@ -114,6 +115,7 @@ def lib():
                                         ip],
             "qmin_host_random_nematic": [C.c_int, C.c_int, C.c_int, C.c_int, C.c_double, dp],
             "qmin_set_fire_kernel": [h, C.c_int],
+            "qmin_set_fire_variant": [h, C.c_int],
             "qmin_batch_create": [C.c_int, ip, C.c_int, C.c_int, C.POINTER(C.c_void_p)],
             "qmin_batch_destroy": [h], "qmin_batch_set_params": [h, C.POINTER(LdgParams)],
             "qmin_batch_set_solve": [h, C.c_int, vp, vp, C.POINTER(Object), C.c_int],
@@ -372,6 +374,10 @@ class Lattice:
         FIRE_SPLIT: deep bulk sites over Q on the 25-point stencil, the rest through derivative planes."""
         _check(lib().qmin_set_fire_kernel(self._h, int(mode)))
 
+    def set_fire_variant(self, variant):
+        """Pin one variant (index within the strategy set by set_fire_kernel), or -1 for the autotuner's choice."""
+        _check(lib().qmin_set_fire_variant(self._h, int(variant)))
+
     def fire_profile(self, iterations=20):
         ms = (C.c_double * 4)()
         fused = C.c_int()
@@ -380,13 +386,13 @@ class Lattice:
 
     def fire_tuning(self):
         path, var, tx, ty, zc = C.c_int(), C.c_int(), C.c_int(), C.c_int(), C.c_int()
-        ms = (C.c_double * 19)()
+        ms = (C.c_double * 21)()
         _check(lib().qmin_fire_tuning(self._h, C.byref(path), C.byref(var), C.byref(tx), C.byref(ty), C.byref(zc),
                                       ms))
         names = (["separate_1blk", "separate_2blk", "separate_3blk"]
                  + [f"fused_{a}x{b}_z{v}" for a, b in ((32, 8), (32, 16), (64, 8), (32, 4)) for v in (0, 1)]
                  + [f"tiled_{a}x{b}_z{v}" for a, b in ((32, 8), (32, 4), (16, 16)) for v in (0, 1)]
-                 + ["split_1blk", "split_2blk"])
+                 + ["split_1blk", "split_2blk", "split_smem_32x8", "split_smem_16x16"])
         return dict(path=["separate", "fused", "tiled", "split"][path.value], variant=var.value, tile=(tx.value, ty.value),
                     zc=zc.value, candidates_ms={n: m for n, m in zip(names, ms) if m >= 0})
 

@@ -36,7 +36,7 @@ static int fail(int code, const std::string &msg)
     } while (0)
 
 static const int kSepVariants = 3;  // separate-kernel force + kick with 1, 2, 3 blocks per SM
-static const int kSplitVariants = 2;  // deep-site kernel with 1 or 2 blocks per SM
+static const int kSplitVariants = 4;  // deep-site kernel: 1 or 2 blocks per SM, shared-memory 32x8 or 16x16
 static const int kTuneCandidates = kSepVariants + 2 * kFusedConfigs + 2 * kTiledConfigs + kSplitVariants;
 static_assert(kTuneCandidates == QMIN_TUNE_CANDIDATES, "tuning candidate count");
 
@@ -81,6 +81,8 @@ struct qmin_ctx {
     void *hvar = nullptr;  // spatially varying H field (3 planes), active when hvar_on
     bool hvar_on = false;
     int fire_mode = QMIN_FIRE_AUTO;  // strategy requested by the caller
+    int fire_variant = -1;           // variant of that strategy the caller pinned (-1: the tuner picks)
+    int tuned_variant = -1;
     // strategy chosen by the autotuner for the current parameters
     int path = -1;  // 0 separate kernels, 1 fused tiled kernel, 2 separate with the staged force + kick
     int sep_cap = 0, fused_cfg = -1, fused_zc = 0, fused_nblocks = 0, tuned_version = 0, tuned_mode = -1;
@@ -706,7 +708,11 @@ static int settle_pingpong(qmin_ctx *h, int executed)
 // timings (whose forces equal the ones already resident).
 template <class T> static int tune_fire(qmin_ctx *h, const Lat<T> &L)
 {
-    if (h->path >= 0 && h->tuned_version == h->version && h->tuned_mode == h->fire_mode) return QMIN_OK;
+    if (h->path >= 0 && h->tuned_version == h->version && h->tuned_mode == h->fire_mode &&
+        h->tuned_variant == h->fire_variant)
+        return QMIN_OK;
+    // a pinned variant restricts every loop below to that index
+    auto pinned_out = [&](int v) { return h->fire_variant >= 0 && v != h->fire_variant; };
     int r = ensure_pingpong(h);
     if (r) return r;
     cudaEvent_t e0, e1;
@@ -733,6 +739,7 @@ template <class T> static int tune_fire(qmin_ctx *h, const Lat<T> &L)
     const bool l6 = L.multi && L.L6 != T(0);
     if (!l6 && (h->fire_mode == QMIN_FIRE_AUTO || h->fire_mode == QMIN_FIRE_FUSED)) {
         for (int cfg = 0; cfg < kFusedConfigs; ++cfg) {
+            if (pinned_out(cfg)) continue;
             int tx, ty;
             fused_tile_shape(cfg, &tx, &ty);
             const int ntiles = ((h->Lx + tx - 1) / tx) * ((h->Ly + ty - 1) / ty);
@@ -772,6 +779,7 @@ template <class T> static int tune_fire(qmin_ctx *h, const Lat<T> &L)
         const size_t bytes = 5 * (size_t)h->P * h->esz;
         CK(cudaMemcpyAsync(h->V2, h->V, bytes, cudaMemcpyDeviceToDevice, h->stream));
         for (int cfg = 0; try_tiled && cfg < kTiledConfigs; ++cfg) {
+            if (pinned_out(cfg)) continue;
             int tx, ty;
             tiled_tile_shape(cfg, &tx, &ty);
             const int ntiles = ((h->Lx + tx - 1) / tx) * ((h->Ly + ty - 1) / ty);
@@ -799,6 +807,7 @@ template <class T> static int tune_fire(qmin_ctx *h, const Lat<T> &L)
             }
         }
         for (int cap = 0; try_sep && cap < kSepVariants; ++cap) {
+            if (pinned_out(cap)) continue;
             const float t_fk =
                 time3([&]() { launch_force_kick_only<T>(L, h->fire, h->partials, h->grid, h->stream, cap); });
             const float ms = t_pred + t_der + t_fk;
@@ -815,6 +824,7 @@ template <class T> static int tune_fire(qmin_ctx *h, const Lat<T> &L)
             const SplitLists sl = split_lists(h);
             const float t_dl = time3([&]() { launch_split_derivs<T>(L, sl, h->fire, h->stream); });
             for (int cap = 0; cap < kSplitVariants; ++cap) {
+                if (pinned_out(cap)) continue;
                 int np = 0;
                 const float t_fk = time3(
                     [&]() { launch_split_force_kick<T>(L, sl, h->fire, h->partials, h->grid, cap, h->stream, &np); });
@@ -837,6 +847,7 @@ template <class T> static int tune_fire(qmin_ctx *h, const Lat<T> &L)
     if (h->path < 0) return fail(QMIN_ECUDA, "FIRE autotuner: no strategy could be launched");
     h->tuned_version = h->version;
     h->tuned_mode = h->fire_mode;
+    h->tuned_variant = h->fire_variant;
     return QMIN_OK;
 }
 
@@ -1225,6 +1236,25 @@ int qmin_set_fire_kernel(qmin_handle h, int mode)
         return fail(QMIN_EINVAL, "qmin_set_fire_kernel: the staged force + kick is built for the FP32 form only");
     if (h->fire_mode != mode) invalidate_graphs(h);
     h->fire_mode = mode;
+    h->fire_variant = -1;
+    return QMIN_OK;
+}
+
+int qmin_set_fire_variant(qmin_handle h, int variant)
+{
+    if (!h) return fail(QMIN_EINVAL, "qmin_set_fire_variant: null handle");
+    if (variant < -1) return fail(QMIN_EINVAL, "qmin_set_fire_variant: variant must be -1 or an index");
+    if (variant >= 0) {
+        const int n = h->fire_mode == QMIN_FIRE_SEPARATE ? kSepVariants
+                      : h->fire_mode == QMIN_FIRE_FUSED  ? kFusedConfigs
+                      : h->fire_mode == QMIN_FIRE_TILED  ? kTiledConfigs
+                      : h->fire_mode == QMIN_FIRE_SPLIT  ? kSplitVariants
+                                                         : 0;
+        if (n == 0) return fail(QMIN_EINVAL, "qmin_set_fire_variant: pin a strategy with qmin_set_fire_kernel first");
+        if (variant >= n) return fail(QMIN_EINVAL, "qmin_set_fire_variant: no such variant of this strategy");
+    }
+    if (h->fire_variant != variant) invalidate_graphs(h);
+    h->fire_variant = variant;
     return QMIN_OK;
 }
 
@@ -1238,6 +1268,7 @@ int qmin_fire_tuning(qmin_handle h, int *path, int *variant, int *tile_x, int *t
     int tx = 0, ty = 0;
     if (h->path == 1) fused_tile_shape(h->fused_cfg, &tx, &ty);
     if (h->path == 2) tiled_tile_shape(h->tiled_cfg, &tx, &ty);
+    if (h->path == 3 && h->split_cap >= 2) tx = h->split_cap == 2 ? 32 : 16, ty = h->split_cap == 2 ? 8 : 16;
     if (tile_x) *tile_x = tx;
     if (tile_y) *tile_y = ty;
     if (zc) *zc = h->path == 1 ? h->fused_zc : (h->path == 2 ? h->tiled_zc : 0);
@@ -1274,7 +1305,7 @@ struct CkpHeader {
     char magic[8];
     int32_t version, Lx, Ly, Lz, prec, metric_mode, nobj, have_params, fire_ready, lb_m, flags;
     int32_t path, sep_cap, fused_cfg, fused_zc, fused_nblocks, tiled_cfg, tiled_zc, tiled_nblocks, fire_mode;
-    int32_t split_cap, pad;
+    int32_t split_cap, fire_variant1;  // pinned variant + 1 (0: none)
     int64_t N, P;
 };
 enum { kCkpM = 1, kCkpS = 2, kCkpAlt = 4, kCkpLb = 8 };
@@ -1298,6 +1329,7 @@ int qmin_checkpoint_save(qmin_handle h, const char *path)
     hd.path = h->path; hd.sep_cap = h->sep_cap; hd.fused_cfg = h->fused_cfg; hd.fused_zc = h->fused_zc;
     hd.fused_nblocks = h->fused_nblocks; hd.tiled_cfg = h->tiled_cfg; hd.tiled_zc = h->tiled_zc;
     hd.tiled_nblocks = h->tiled_nblocks; hd.fire_mode = h->fire_mode; hd.split_cap = h->split_cap;
+    hd.fire_variant1 = h->fire_variant + 1;
     hd.N = h->N; hd.P = h->P;
     const size_t plane = 5 * (size_t)h->P * h->esz;
     std::vector<char> buf(plane);
@@ -1403,6 +1435,7 @@ int qmin_checkpoint_load(qmin_handle h, const char *path)
     invalidate_graphs(h);
     // the FIRE strategy of the saved run, so the resumed run reduces in the same order
     h->fire_mode = hd.fire_mode;
+    h->fire_variant = hd.fire_variant1 - 1;
     if (hd.path >= 0) {
         int r = ensure_pingpong(h);
         if (r) return r;
@@ -1417,6 +1450,7 @@ int qmin_checkpoint_load(qmin_handle h, const char *path)
         h->split_cap = hd.split_cap;
         h->tuned_version = h->version;
         h->tuned_mode = h->fire_mode;
+        h->tuned_variant = h->fire_variant;
     }
     return QMIN_OK;
 }

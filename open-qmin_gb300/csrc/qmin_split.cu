@@ -152,6 +152,149 @@ __global__ void __launch_bounds__(kBlock)
     }
 }
 
+// Deep bulk sites from shared memory: a block owns a TX x TY column and walks
+// zc planes, keeping Q of the tile plus a two-site halo in a ring of six planes
+// (z-2 .. z+2 in use, z+3 arriving by cp.async while z is computed).
+namespace {
+template <class T> __device__ __forceinline__ void cp_async_q(T *smem, const T *gmem)
+{
+    const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
+    if constexpr (sizeof(T) == 4)
+        asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(sa), "l"(gmem) : "memory");
+    else
+        asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(sa), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ int wrap_any(int v, int m)
+{
+    int r = v % m;
+    return r < 0 ? r + m : r;
+}
+constexpr int kDeepNS = 6, kDeepZc = 8;
+template <class T, int TX, int TY> constexpr size_t deep_tiled_smem()
+{
+    return (size_t)kDeepNS * 5 * (TX + 4) * (TY + 4) * sizeof(T);
+}
+// FP64 keeps 2 blocks (16 warps) per SM, FP32 4 (32 warps)
+template <class T> constexpr int deep_tiled_minb() { return sizeof(T) == 4 ? 4 : 2; }
+}  // namespace
+
+template <class T, int TX, int TY>
+__global__ void __launch_bounds__(TX *TY, deep_tiled_minb<T>())
+    k_force_kick_deep_tiled(Lat<T> L, const uint8_t *__restrict__ cls, const FireDev *__restrict__ fd,
+                            double *partials, int zc)
+{
+    constexpr int NT = TX * TY, SX = TX + 4, TS = SX * (TY + 4), NS = kDeepNS;
+    constexpr int NPOS = (TS + NT - 1) / NT;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    T *sQ = reinterpret_cast<T *>(smem_raw);  // [NS][5][TS]
+    if (!fd->active) return;
+    const T hdt = T(0.5) * T(fd->dt);
+    const int ntx = (L.Lx + TX - 1) / TX;
+    const int gx0 = (blockIdx.x % ntx) * TX, gy0 = (blockIdx.x / ntx) * TY;
+    const int zs = blockIdx.y * zc, ze = min(L.Lz, zs + zc);
+    const long long P = L.P;
+    const int sxy = L.Lx * L.Ly;
+    int off[NPOS];
+#pragma unroll
+    for (int j = 0; j < NPOS; ++j) {
+        const int pp = threadIdx.x + j * NT;
+        off[j] = pp < TS ? wrap_any(gx0 + pp % SX - 2, L.Lx) + L.Lx * wrap_any(gy0 + pp / SX - 2, L.Ly) : -1;
+    }
+    auto slot_of = [&](int z) { return (z - zs + 2) % NS; };  // z >= zs - 2
+    auto issue = [&](int z) {
+        const int sl = slot_of(z);
+        const long long base = (long long)sxy * wrap_any(z, L.Lz);
+#pragma unroll
+        for (int j = 0; j < NPOS; ++j) {
+            if (off[j] < 0) continue;
+            const int pp = threadIdx.x + j * NT;
+#pragma unroll
+            for (int k = 0; k < 5; ++k) cp_async_q(&sQ[(sl * 5 + k) * TS + pp], L.Q + k * P + base + off[j]);
+        }
+    };
+    double acc[3] = {0.0, 0.0, 0.0};
+    if (zs < L.Lz) {
+        for (int z = zs - 2; z <= zs + 2; ++z) {
+            issue(z);
+            asm volatile("cp.async.commit_group;\n" ::: "memory");
+        }
+        const int lx = threadIdx.x % TX, ly = threadIdx.x / TX;
+        const int gx = gx0 + lx, gy = gy0 + ly;
+        const int p = (ly + 2) * SX + (lx + 2);
+        for (int z = zs; z < ze; ++z) {
+            if (z + 3 <= ze + 1) issue(z + 3);
+            asm volatile("cp.async.commit_group;\n" ::: "memory");
+            asm volatile("cp.async.wait_group 1;\n" ::: "memory");
+            __syncthreads();
+            const long long i = (long long)gx + (long long)L.Lx * gy + (long long)sxy * z;
+            if (gx < L.Lx && gy < L.Ly && cls[i] == 0) {
+                int sb[5];
+#pragma unroll
+                for (int d = 0; d < 5; ++d) sb[d] = slot_of(z + d - 2) * 5 * TS + p;
+#define QQ(dx, dy, dz, c) sQ[sb[(dz) + 2] + (c) * TS + (dy) * SX + (dx)]
+                T q[5];
+#pragma unroll
+                for (int k = 0; k < 5; ++k) q[k] = QQ(0, 0, 0, k);
+                T f[5], force[5], s2[5];
+                phase_force(L.a, L.b, L.c, q, force);
+                if (L.L4 == T(0)) {
+                    QMIN_BULK_Q25_NO_L4(L.cq, s2);
+                } else {
+                    QMIN_BULK_Q25(L.cq, s2);
+                }
+#undef QQ
+#pragma unroll
+                for (int k = 0; k < 5; ++k) f[k] = force[k] - s2[k];
+                if (L.metric_mode == 0) metric(f);
+                if (L.efield)
+#pragma unroll
+                    for (int k = 0; k < 5; ++k) f[k] -= L.fE[k];
+                if (L.hfield)
+#pragma unroll
+                    for (int k = 0; k < 5; ++k) f[k] -= L.fH[k];
+                T h[3];
+                if (const T *hs = site_field(L, i, h)) {
+                    const T hx = hs[0], hy = hs[1], hz = hs[2], fp = L.hvp;
+                    f[0] -= T(-0.5) * fp * (hx * hx - hz * hz);
+                    f[1] -= -fp * hx * hy;
+                    f[2] -= -fp * hx * hz;
+                    f[3] -= T(-0.5) * fp * (hy * hy - hz * hz);
+                    f[4] -= -fp * hy * hz;
+                }
+                metric(f);
+                kick_and_sum(L, i, hdt, f, acc);
+            }
+            __syncthreads();
+        }
+    }
+    block_sum<3, NT>(acc);
+    if (threadIdx.x == 0) {
+        const int b = blockIdx.y * gridDim.x + blockIdx.x;
+#pragma unroll
+        for (int k = 0; k < 3; ++k) partials[3 * b + k] = acc[k];
+    }
+}
+
+// shared-memory deep kernel over TX x TY columns of kDeepZc planes (more when
+// the grid would not fit the partials buffer); returns its block count
+template <class T, int TX, int TY>
+static int launch_deep_tiled(const Lat<T> &L, const SplitLists &sl, FireDev *fd, double *partials, cudaStream_t s)
+{
+    constexpr size_t sm = deep_tiled_smem<T, TX, TY>();
+    static bool attr_set = false;
+    if (!attr_set) {
+        // a failure here surfaces as the launch's error
+        attr_set = cudaFuncSetAttribute(k_force_kick_deep_tiled<T, TX, TY>,
+                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm) == cudaSuccess;
+    }
+    const int ntiles = ((L.Lx + TX - 1) / TX) * ((L.Ly + TY - 1) / TY);
+    int zc = kDeepZc;
+    while ((long long)ntiles * ((L.Lz + zc - 1) / zc) > kMaxFusedBlocks - 1024) ++zc;
+    const int nz = (L.Lz + zc - 1) / zc;
+    k_force_kick_deep_tiled<T, TX, TY><<<dim3(ntiles, nz), TX * TY, sm, s>>>(L, sl.cls, fd, partials, zc);
+    return ntiles * nz;
+}
+
 template <class T> int launch_split_derivs(const Lat<T> &L, const SplitLists &sl, FireDev *fd, cudaStream_t s)
 {
     if (sl.n_derivs == 0) return 0;
@@ -163,12 +306,21 @@ template <class T>
 int launch_split_force_kick(const Lat<T> &L, const SplitLists &sl, FireDev *fd, double *partials, int grid, int cap,
                             cudaStream_t s, int *nparts)
 {
-    if (cap == 1) k_force_kick_deep<T, 1><<<grid, kBlock, 0, s>>>(L, sl.cls, fd, partials);
-    else k_force_kick_deep<T, 0><<<grid, kBlock, 0, s>>>(L, sl.cls, fd, partials);
-    int n = 1, np = grid;
+    int np = grid;
+    if (cap == 2) {
+        np = launch_deep_tiled<T, 32, 8>(L, sl, fd, partials, s);
+    } else if (cap == 3) {
+        np = launch_deep_tiled<T, 16, 16>(L, sl, fd, partials, s);
+    } else if (cap == 1) {
+        k_force_kick_deep<T, 1><<<grid, kBlock, 0, s>>>(L, sl.cls, fd, partials);
+    } else {
+        k_force_kick_deep<T, 0><<<grid, kBlock, 0, s>>>(L, sl.cls, fd, partials);
+    }
+    const int grid_used = np;
+    int n = 1;
     if (sl.n_sites > 0) {
         const int g2 = list_grid(sl.n_sites);
-        k_force_kick_list<T><<<g2, kBlock, 0, s>>>(L, sl.sites, sl.n_sites, fd, partials + 3 * grid);
+        k_force_kick_list<T><<<g2, kBlock, 0, s>>>(L, sl.sites, sl.n_sites, fd, partials + 3 * grid_used);
         np += g2;
         ++n;
     }
