@@ -10,6 +10,7 @@
 // keeps the plane-based forms; their derivative planes are refreshed only at
 // the sites that list reads.  Results equal the separate kernels' to rounding.
 #include <algorithm>
+#include <type_traits>
 
 #include "qmin_force_core.cuh"
 
@@ -178,6 +179,56 @@ template <class T, int TX, int TY> constexpr size_t deep_tiled_smem()
 template <class T> constexpr int deep_tiled_minb() { return sizeof(T) == 4 ? 4 : 2; }
 }  // namespace
 
+// site of thread t in a TX-wide tile.  A warp covers 32 x 1 sites of a 32-wide
+// tile, 4 x 8 sites of a 16-wide one: with the staged rows TX + 4 = 20 words
+// apart, the 8 rows of 4 fall into disjoint shared-memory banks for every
+// stencil offset (a 16 x 2 footprint would put 4 banks of its two rows together).
+template <int TX> __device__ __forceinline__ void tile_site(int t, int &lx, int &ly)
+{
+    constexpr int WX = TX >= 32 ? 32 : 4, WY = 32 / WX, NWX = TX / WX;
+    const int lane = t & 31, w = t >> 5;
+    lx = (w % NWX) * WX + lane % WX;
+    ly = (w / NWX) * WY + lane / WX;
+}
+
+// force of a deep bulk site from Q staged in shared memory: plane dz of the
+// site's column starts at sb[dz + 2], components TS apart, rows SX apart
+template <class T, int TS, int SX>
+__device__ __forceinline__ void deep_force_tile(const Lat<T> &L, const T *sQ, const int (&sb)[5], long long i, T *f)
+{
+#define QQ(dx, dy, dz, c) sQ[sb[(dz) + 2] + (c) * TS + (dy) * SX + (dx)]
+    T q[5];
+#pragma unroll
+    for (int k = 0; k < 5; ++k) q[k] = QQ(0, 0, 0, k);
+    T force[5], s2[5];
+    phase_force(L.a, L.b, L.c, q, force);
+    if (L.L4 == T(0)) {
+        QMIN_BULK_Q25_NO_L4(L.cq, s2);
+    } else {
+        QMIN_BULK_Q25(L.cq, s2);
+    }
+#undef QQ
+#pragma unroll
+    for (int k = 0; k < 5; ++k) f[k] = force[k] - s2[k];
+    if (L.metric_mode == 0) metric(f);
+    if (L.efield)
+#pragma unroll
+        for (int k = 0; k < 5; ++k) f[k] -= L.fE[k];
+    if (L.hfield)
+#pragma unroll
+        for (int k = 0; k < 5; ++k) f[k] -= L.fH[k];
+    T h[3];
+    if (const T *hs = site_field(L, i, h)) {
+        const T hx = hs[0], hy = hs[1], hz = hs[2], fp = L.hvp;
+        f[0] -= T(-0.5) * fp * (hx * hx - hz * hz);
+        f[1] -= -fp * hx * hy;
+        f[2] -= -fp * hx * hz;
+        f[3] -= T(-0.5) * fp * (hy * hy - hz * hz);
+        f[4] -= -fp * hy * hz;
+    }
+    metric(f);
+}
+
 template <class T, int TX, int TY>
 __global__ void __launch_bounds__(TX *TY, deep_tiled_minb<T>())
     k_force_kick_deep_tiled(Lat<T> L, const uint8_t *__restrict__ cls, const FireDev *__restrict__ fd,
@@ -212,61 +263,66 @@ __global__ void __launch_bounds__(TX *TY, deep_tiled_minb<T>())
             for (int k = 0; k < 5; ++k) cp_async_q(&sQ[(sl * 5 + k) * TS + pp], L.Q + k * P + base + off[j]);
         }
     };
-    double acc[3] = {0.0, 0.0, 0.0};
+    // per-thread sums over the column in the site precision (at most a few
+    // tens of terms, each already rounded to it), FP64 across threads and blocks
+    using Acc = typename std::conditional<sizeof(T) == 4, float, double>::type;
+    Acc sacc[3] = {Acc(0), Acc(0), Acc(0)};
     if (zs < L.Lz) {
         for (int z = zs - 2; z <= zs + 2; ++z) {
             issue(z);
             asm volatile("cp.async.commit_group;\n" ::: "memory");
         }
-        const int lx = threadIdx.x % TX, ly = threadIdx.x / TX;
+        int lx, ly;
+        tile_site<TX>(threadIdx.x, lx, ly);
         const int gx = gx0 + lx, gy = gy0 + ly;
+        const bool inside = gx < L.Lx && gy < L.Ly;
+        const long long i0 = (long long)gx + (long long)L.Lx * gy;
         const int p = (ly + 2) * SX + (lx + 2);
+        // class and velocity of the next plane's site, loaded one plane ahead
+        uint8_t c_next = 1;
+        T v_next[5];
+        auto fetch = [&](int z) {
+            c_next = 1;
+            if (inside && z < ze) {
+                const long long i = i0 + (long long)sxy * z;
+                c_next = cls[i];
+#pragma unroll
+                for (int k = 0; k < 5; ++k) v_next[k] = L.V[k * P + i];
+            }
+        };
+        fetch(zs);
         for (int z = zs; z < ze; ++z) {
             if (z + 3 <= ze + 1) issue(z + 3);
             asm volatile("cp.async.commit_group;\n" ::: "memory");
+            const uint8_t c_here = c_next;
+            T v_here[5];
+#pragma unroll
+            for (int k = 0; k < 5; ++k) v_here[k] = v_next[k];
+            fetch(z + 1);
             asm volatile("cp.async.wait_group 1;\n" ::: "memory");
             __syncthreads();
-            const long long i = (long long)gx + (long long)L.Lx * gy + (long long)sxy * z;
-            if (gx < L.Lx && gy < L.Ly && cls[i] == 0) {
+            const long long i = i0 + (long long)sxy * z;
+            if (c_here == 0) {
                 int sb[5];
 #pragma unroll
                 for (int d = 0; d < 5; ++d) sb[d] = slot_of(z + d - 2) * 5 * TS + p;
-#define QQ(dx, dy, dz, c) sQ[sb[(dz) + 2] + (c) * TS + (dy) * SX + (dx)]
-                T q[5];
+                T f[5];
+                deep_force_tile<T, TS, SX>(L, sQ, sb, i, f);
+                T v[5];
 #pragma unroll
-                for (int k = 0; k < 5; ++k) q[k] = QQ(0, 0, 0, k);
-                T f[5], force[5], s2[5];
-                phase_force(L.a, L.b, L.c, q, force);
-                if (L.L4 == T(0)) {
-                    QMIN_BULK_Q25_NO_L4(L.cq, s2);
-                } else {
-                    QMIN_BULK_Q25(L.cq, s2);
+                for (int k = 0; k < 5; ++k) {
+                    v[k] = v_here[k] + hdt * f[k];
+                    L.F[k * P + i] = f[k];
+                    L.V[k * P + i] = v[k];
                 }
-#undef QQ
-#pragma unroll
-                for (int k = 0; k < 5; ++k) f[k] = force[k] - s2[k];
-                if (L.metric_mode == 0) metric(f);
-                if (L.efield)
-#pragma unroll
-                    for (int k = 0; k < 5; ++k) f[k] -= L.fE[k];
-                if (L.hfield)
-#pragma unroll
-                    for (int k = 0; k < 5; ++k) f[k] -= L.fH[k];
-                T h[3];
-                if (const T *hs = site_field(L, i, h)) {
-                    const T hx = hs[0], hy = hs[1], hz = hs[2], fp = L.hvp;
-                    f[0] -= T(-0.5) * fp * (hx * hx - hz * hz);
-                    f[1] -= -fp * hx * hy;
-                    f[2] -= -fp * hx * hz;
-                    f[3] -= T(-0.5) * fp * (hy * hy - hz * hz);
-                    f[4] -= -fp * hy * hz;
-                }
-                metric(f);
-                kick_and_sum(L, i, hdt, f, acc);
+                sacc[0] += (Acc)dot_qt(f, f);
+                sacc[1] += (Acc)dot_qt(v, v);
+                sacc[2] += (Acc)dot_qt(f, v);
             }
             __syncthreads();
         }
     }
+    double acc[3] = {(double)sacc[0], (double)sacc[1], (double)sacc[2]};
     block_sum<3, NT>(acc);
     if (threadIdx.x == 0) {
         const int b = blockIdx.y * gridDim.x + blockIdx.x;
