@@ -36,7 +36,10 @@ static int fail(int code, const std::string &msg)
     } while (0)
 
 static const int kSepVariants = 3;  // separate-kernel force + kick with 1, 2, 3 blocks per SM
-static const int kSplitVariants = 4;  // deep-site kernel: 1 or 2 blocks per SM, shared-memory 32x8 or 16x16
+// deep-site kernel: 1 or 2 blocks per SM, shared-memory 32x8 or 16x16, and
+// (FP32 only) two sites per thread on 32x8 tiles, z chunks of 8 planes or about two waves of columns
+static const int kSplitVariants = 6;
+static const int kSplitFp32First = 4;
 static const int kTuneCandidates = kSepVariants + 2 * kFusedConfigs + 2 * kTiledConfigs + kSplitVariants;
 static_assert(kTuneCandidates == QMIN_TUNE_CANDIDATES, "tuning candidate count");
 
@@ -824,7 +827,7 @@ template <class T> static int tune_fire(qmin_ctx *h, const Lat<T> &L)
             const SplitLists sl = split_lists(h);
             const float t_dl = time3([&]() { launch_split_derivs<T>(L, sl, h->fire, h->stream); });
             for (int cap = 0; cap < kSplitVariants; ++cap) {
-                if (pinned_out(cap)) continue;
+                if (pinned_out(cap) || (sizeof(T) == 8 && cap >= kSplitFp32First)) continue;
                 int np = 0;
                 const float t_fk = time3(
                     [&]() { launch_split_force_kick<T>(L, sl, h->fire, h->partials, h->grid, cap, h->stream, &np); });
@@ -1252,6 +1255,8 @@ int qmin_set_fire_variant(qmin_handle h, int variant)
                                                          : 0;
         if (n == 0) return fail(QMIN_EINVAL, "qmin_set_fire_variant: pin a strategy with qmin_set_fire_kernel first");
         if (variant >= n) return fail(QMIN_EINVAL, "qmin_set_fire_variant: no such variant of this strategy");
+        if (h->fire_mode == QMIN_FIRE_SPLIT && variant >= kSplitFp32First && h->prec != QMIN_FP32)
+            return fail(QMIN_EINVAL, "qmin_set_fire_variant: the two-sites-per-thread kernels are FP32 only");
     }
     if (h->fire_variant != variant) invalidate_graphs(h);
     h->fire_variant = variant;
@@ -1268,7 +1273,7 @@ int qmin_fire_tuning(qmin_handle h, int *path, int *variant, int *tile_x, int *t
     int tx = 0, ty = 0;
     if (h->path == 1) fused_tile_shape(h->fused_cfg, &tx, &ty);
     if (h->path == 2) tiled_tile_shape(h->tiled_cfg, &tx, &ty);
-    if (h->path == 3 && h->split_cap >= 2) tx = h->split_cap == 2 ? 32 : 16, ty = h->split_cap == 2 ? 8 : 16;
+    if (h->path == 3 && h->split_cap >= 2) tx = h->split_cap == 3 ? 16 : 32, ty = h->split_cap == 3 ? 16 : 8;
     if (tile_x) *tile_x = tx;
     if (tile_y) *tile_y = ty;
     if (zc) *zc = h->path == 1 ? h->fused_zc : (h->path == 2 ? h->tiled_zc : 0);

@@ -191,23 +191,13 @@ template <int TX> __device__ __forceinline__ void tile_site(int t, int &lx, int 
     ly = (w / NWX) * WY + lane / WX;
 }
 
-// force of a deep bulk site from Q staged in shared memory: plane dz of the
-// site's column starts at sb[dz + 2], components TS apart, rows SX apart
-template <class T, int TS, int SX>
-__device__ __forceinline__ void deep_force_tile(const Lat<T> &L, const T *sQ, const int (&sb)[5], long long i, T *f)
+// force of a deep bulk site from its Q and its combined bulk form s2, M
+// applied as for type-0 sites (twice in CPU mode, the fields between the two)
+template <class T>
+__device__ __forceinline__ void deep_force_finish(const Lat<T> &L, const T *q, const T *s2, long long i, T *f)
 {
-#define QQ(dx, dy, dz, c) sQ[sb[(dz) + 2] + (c) * TS + (dy) * SX + (dx)]
-    T q[5];
-#pragma unroll
-    for (int k = 0; k < 5; ++k) q[k] = QQ(0, 0, 0, k);
-    T force[5], s2[5];
+    T force[5];
     phase_force(L.a, L.b, L.c, q, force);
-    if (L.L4 == T(0)) {
-        QMIN_BULK_Q25_NO_L4(L.cq, s2);
-    } else {
-        QMIN_BULK_Q25(L.cq, s2);
-    }
-#undef QQ
 #pragma unroll
     for (int k = 0; k < 5; ++k) f[k] = force[k] - s2[k];
     if (L.metric_mode == 0) metric(f);
@@ -227,6 +217,61 @@ __device__ __forceinline__ void deep_force_tile(const Lat<T> &L, const T *sQ, co
         f[4] -= -fp * hy * hz;
     }
     metric(f);
+}
+
+// force of a deep bulk site from Q staged in shared memory: plane dz of the
+// site's column starts at sb[dz + 2], components TS apart, rows SX apart
+template <class T, int TS, int SX>
+__device__ __forceinline__ void deep_force_tile(const Lat<T> &L, const T *sQ, const int (&sb)[5], long long i, T *f)
+{
+#define QQ(dx, dy, dz, c) sQ[sb[(dz) + 2] + (c) * TS + (dy) * SX + (dx)]
+    T q[5], s2[5];
+#pragma unroll
+    for (int k = 0; k < 5; ++k) q[k] = QQ(0, 0, 0, k);
+    if (L.L4 == T(0)) {
+        QMIN_BULK_Q25_NO_L4(L.cq, s2);
+    } else {
+        QMIN_BULK_Q25(L.cq, s2);
+    }
+#undef QQ
+    deep_force_finish(L, q, s2, i, f);
+}
+
+// the same for the two x-adjacent sites of an even-aligned pair (site indices
+// i and ib): every value comes from a float2 load of an aligned pair of x
+// positions (one load serves both sites wherever their stencils overlap)
+template <int TS, int SX>
+__device__ __forceinline__ void deep_force_pair_tile(const Lat<float> &L, const float *sQ, const int (&sb)[5],
+                                                     long long i, long long ib, float *fa, float *fb)
+{
+#define QMIN_LD2(dz, off) (*reinterpret_cast<const float2 *>(sQ + sb[(dz) + 2] + (off)))
+#define QMIN_EVEN(dx) ((dx) >= 0 ? ((dx) & ~1) : -((1 - (dx)) & ~1))
+#define QMIN_PICK(v, e) ((e) ? (v).y : (v).x)
+#define QQ(dx, dy, dz, c) QMIN_PICK(QMIN_LD2(dz, (c) * TS + (dy) * SX + QMIN_EVEN(dx)), (dx) & 1)
+    float qa[5], sa[5];
+#pragma unroll
+    for (int k = 0; k < 5; ++k) qa[k] = QQ(0, 0, 0, k);
+    if (L.L4 == 0.f) {
+        QMIN_BULK_Q25_NO_L4(L.cq, sa);
+    } else {
+        QMIN_BULK_Q25(L.cq, sa);
+    }
+#undef QQ
+#define QQ(dx, dy, dz, c) QMIN_PICK(QMIN_LD2(dz, (c) * TS + (dy) * SX + QMIN_EVEN((dx) + 1)), ((dx) + 1) & 1)
+    float qb[5], sbv[5];
+#pragma unroll
+    for (int k = 0; k < 5; ++k) qb[k] = QQ(0, 0, 0, k);
+    if (L.L4 == 0.f) {
+        QMIN_BULK_Q25_NO_L4(L.cq, sbv);
+    } else {
+        QMIN_BULK_Q25(L.cq, sbv);
+    }
+#undef QQ
+#undef QMIN_PICK
+#undef QMIN_EVEN
+#undef QMIN_LD2
+    deep_force_finish(L, qa, sa, i, fa);
+    deep_force_finish(L, qb, sbv, ib, fb);
 }
 
 template <class T, int TX, int TY>
@@ -331,6 +376,133 @@ __global__ void __launch_bounds__(TX *TY, deep_tiled_minb<T>())
     }
 }
 
+// FP32 deep sites two per thread: thread (px, ly) of a TX x TY tile owns the
+// x-adjacent sites 2 px and 2 px + 1, reads every staged value as an aligned
+// float2 (a half-warp reads one 32-word row: no bank conflicts) and shares the
+// loads where the two stencils overlap.  Staging and plane ring as in
+// k_force_kick_deep_tiled.
+template <int TX, int TY, int MINB>
+__global__ void __launch_bounds__(TX / 2 * TY, MINB)
+    k_force_kick_deep_pair(Lat<float> L, const uint8_t *__restrict__ cls, const FireDev *__restrict__ fd,
+                           double *partials, int zc)
+{
+    static_assert(TX % 2 == 0 && (TX + 4) % 2 == 0, "pairs need even rows");
+    constexpr int NT = TX / 2 * TY, SX = TX + 4, TS = SX * (TY + 4), NS = kDeepNS;
+    constexpr int NPOS = (TS + NT - 1) / NT;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    float *sQ = reinterpret_cast<float *>(smem_raw);  // [NS][5][TS]
+    if (!fd->active) return;
+    const float hdt = 0.5f * float(fd->dt);
+    const int ntx = (L.Lx + TX - 1) / TX;
+    const int gx0 = (blockIdx.x % ntx) * TX, gy0 = (blockIdx.x / ntx) * TY;
+    const int zs = blockIdx.y * zc, ze = min(L.Lz, zs + zc);
+    const long long P = L.P;
+    const int sxy = L.Lx * L.Ly;
+    int off[NPOS];
+#pragma unroll
+    for (int j = 0; j < NPOS; ++j) {
+        const int pp = threadIdx.x + j * NT;
+        off[j] = pp < TS ? wrap_any(gx0 + pp % SX - 2, L.Lx) + L.Lx * wrap_any(gy0 + pp / SX - 2, L.Ly) : -1;
+    }
+    auto slot_of = [&](int z) { return (z - zs + 2) % NS; };  // z >= zs - 2
+    auto issue = [&](int z) {
+        const int sl = slot_of(z);
+        const long long base = (long long)sxy * wrap_any(z, L.Lz);
+#pragma unroll
+        for (int j = 0; j < NPOS; ++j) {
+            if (off[j] < 0) continue;
+            const int pp = threadIdx.x + j * NT;
+#pragma unroll
+            for (int k = 0; k < 5; ++k) cp_async_q(&sQ[(sl * 5 + k) * TS + pp], L.Q + k * P + base + off[j]);
+        }
+    };
+    float sacc[3] = {0.f, 0.f, 0.f};
+    if (zs < L.Lz) {
+        for (int z = zs - 2; z <= zs + 2; ++z) {
+            issue(z);
+            asm volatile("cp.async.commit_group;\n" ::: "memory");
+        }
+        const int px = threadIdx.x % (TX / 2), ly = threadIdx.x / (TX / 2);
+        const int gx = gx0 + 2 * px, gy = gy0 + ly;
+        // sites a = (gx, gy) and b = (gx + 1, gy); b may lie past an odd Lx
+        const bool in_a = gx < L.Lx && gy < L.Ly, in_b = gx + 1 < L.Lx && gy < L.Ly;
+        const long long i0 = (long long)gx + (long long)L.Lx * gy;
+        const int p = (ly + 2) * SX + (2 * px + 2);
+        uint8_t ca_next = 1, cb_next = 1;
+        float va_next[5], vb_next[5];
+        auto fetch = [&](int z) {
+            ca_next = cb_next = 1;
+            if (z < ze) {
+                const long long i = i0 + (long long)sxy * z;
+                if (in_a) {
+                    ca_next = cls[i];
+#pragma unroll
+                    for (int k = 0; k < 5; ++k) va_next[k] = L.V[k * P + i];
+                }
+                if (in_b) {
+                    cb_next = cls[i + 1];
+#pragma unroll
+                    for (int k = 0; k < 5; ++k) vb_next[k] = L.V[k * P + i + 1];
+                }
+            }
+        };
+        fetch(zs);
+        for (int z = zs; z < ze; ++z) {
+            if (z + 3 <= ze + 1) issue(z + 3);
+            asm volatile("cp.async.commit_group;\n" ::: "memory");
+            const uint8_t ca = ca_next, cb = cb_next;
+            float va[5], vb[5];
+#pragma unroll
+            for (int k = 0; k < 5; ++k) {
+                va[k] = va_next[k];
+                vb[k] = vb_next[k];
+            }
+            fetch(z + 1);
+            asm volatile("cp.async.wait_group 1;\n" ::: "memory");
+            __syncthreads();
+            if (ca == 0 || cb == 0) {
+                const long long i = i0 + (long long)sxy * z;
+                int sb[5];
+#pragma unroll
+                for (int d = 0; d < 5; ++d) sb[d] = slot_of(z + d - 2) * 5 * TS + p;
+                float fa[5], fb[5];
+                // b past the lattice's x edge: computed and dropped, its field read at a
+                deep_force_pair_tile<TS, SX>(L, sQ, sb, i, in_b ? i + 1 : i, fa, fb);
+                if (ca == 0) {
+#pragma unroll
+                    for (int k = 0; k < 5; ++k) {
+                        va[k] += hdt * fa[k];
+                        L.F[k * P + i] = fa[k];
+                        L.V[k * P + i] = va[k];
+                    }
+                    sacc[0] += dot_qt(fa, fa);
+                    sacc[1] += dot_qt(va, va);
+                    sacc[2] += dot_qt(fa, va);
+                }
+                if (cb == 0) {
+#pragma unroll
+                    for (int k = 0; k < 5; ++k) {
+                        vb[k] += hdt * fb[k];
+                        L.F[k * P + i + 1] = fb[k];
+                        L.V[k * P + i + 1] = vb[k];
+                    }
+                    sacc[0] += dot_qt(fb, fb);
+                    sacc[1] += dot_qt(vb, vb);
+                    sacc[2] += dot_qt(fb, vb);
+                }
+            }
+            __syncthreads();
+        }
+    }
+    double acc[3] = {(double)sacc[0], (double)sacc[1], (double)sacc[2]};
+    block_sum<3, NT>(acc);
+    if (threadIdx.x == 0) {
+        const int b = blockIdx.y * gridDim.x + blockIdx.x;
+#pragma unroll
+        for (int k = 0; k < 3; ++k) partials[3 * b + k] = acc[k];
+    }
+}
+
 // shared-memory deep kernel over TX x TY columns of kDeepZc planes (more when
 // the grid would not fit the partials buffer); returns its block count
 template <class T, int TX, int TY>
@@ -351,6 +523,33 @@ static int launch_deep_tiled(const Lat<T> &L, const SplitLists &sl, FireDev *fd,
     return ntiles * nz;
 }
 
+// the FP32 two-sites-per-thread deep kernel over TX x TY columns
+// fitted = true: z chunks sized so that the grid is about two waves of MINB
+// blocks on each of the 152 SMs (fewer, longer columns), else kDeepZc planes
+template <int TX, int TY, int MINB>
+static int launch_deep_pair(const Lat<float> &L, const SplitLists &sl, FireDev *fd, double *partials, bool fitted,
+                            cudaStream_t s)
+{
+    constexpr size_t sm = deep_tiled_smem<float, TX, TY>();
+    static bool attr_set = false;
+    if (!attr_set) {
+        // a failure here surfaces as the launch's error
+        attr_set = cudaFuncSetAttribute(k_force_kick_deep_pair<TX, TY, MINB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        (int)sm) == cudaSuccess;
+    }
+    const int ntiles = ((L.Lx + TX - 1) / TX) * ((L.Ly + TY - 1) / TY);
+    int zc = kDeepZc;
+    if (fitted) {
+        // about two waves: each block walks a long column
+        const long long nz = std::max(1LL, 2LL * 152 * MINB / ntiles);
+        zc = std::max(kDeepZc, (int)((L.Lz + nz - 1) / nz));
+    }
+    while ((long long)ntiles * ((L.Lz + zc - 1) / zc) > kMaxFusedBlocks - 1024) ++zc;
+    const int nz = (L.Lz + zc - 1) / zc;
+    k_force_kick_deep_pair<TX, TY, MINB><<<dim3(ntiles, nz), TX / 2 * TY, sm, s>>>(L, sl.cls, fd, partials, zc);
+    return ntiles * nz;
+}
+
 template <class T> int launch_split_derivs(const Lat<T> &L, const SplitLists &sl, FireDev *fd, cudaStream_t s)
 {
     if (sl.n_derivs == 0) return 0;
@@ -367,6 +566,12 @@ int launch_split_force_kick(const Lat<T> &L, const SplitLists &sl, FireDev *fd, 
         np = launch_deep_tiled<T, 32, 8>(L, sl, fd, partials, s);
     } else if (cap == 3) {
         np = launch_deep_tiled<T, 16, 16>(L, sl, fd, partials, s);
+    } else if (cap == 4 || cap == 5) {
+        if constexpr (sizeof(T) == 4) {
+            np = launch_deep_pair<32, 8, 3>(L, sl, fd, partials, cap == 5, s);
+        } else {
+            return -1;  // FP32 only (the autotuner does not offer it for FP64)
+        }
     } else if (cap == 1) {
         k_force_kick_deep<T, 1><<<grid, kBlock, 0, s>>>(L, sl.cls, fd, partials);
     } else {
