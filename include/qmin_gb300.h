@@ -206,7 +206,8 @@ int qmin_gd_run(qmin_handle h, double dt, double force_cutoff, int max_iteration
 /* ---- FIRE iteration strategy and diagnostics ---- */
 #define QMIN_FIRE_SEPARATE 0 /* predictor, derivative planes, force+kick, control as separate kernels */
 #define QMIN_FIRE_FUSED 1    /* one shared-memory tiled kernel per iteration */
-#define QMIN_FIRE_AUTO 2     /* the autotuner picks the fastest of the others (default) */
+#define QMIN_FIRE_AUTO 2     /* the autotuner picks the fastest (default): of the split and separate
+                                strategies where the split path applies, of all the others elsewhere */
 #define QMIN_FIRE_TILED 3    /* separate predictor and derivative planes, force + kick from shared-memory
                                 tiles (FP32 form only) */
 #define QMIN_FIRE_SPLIT 4    /* deep bulk sites' force + kick over Q on the 25-point stencil (no derivative

@@ -701,14 +701,16 @@ static int settle_pingpong(qmin_ctx *h, int executed)
     return QMIN_OK;
 }
 
-// Autotuner for the FIRE iteration: times every candidate strategy on the live
-// lattice with CUDA events and keeps the fastest.  Candidates: the separate
-// kernels (predictor, derivative planes, force + kick) with and without a
-// register cap, and the fused tiled kernel for each tile shape and two z
-// extents.  The timing launches leave the state as it was: the fused kernel
-// writes only the second buffer set and the partials, the predictor is timed on
-// the second buffer set, and the velocities are restored after the force + kick
-// timings (whose forces equal the ones already resident).
+// Autotuner for the FIRE iteration: times the candidate strategies on the live
+// lattice with CUDA events and keeps the fastest.  Candidates: the split force
+// + kick (deep-site kernel variants), the separate kernels (predictor,
+// derivative planes, force + kick) with and without a register cap, the staged
+// FP32 force + kick and the fused tiled kernel for each tile shape and two z
+// extents; a candidate whose first launch takes more than twice the best time
+// so far is not timed further.  The timing launches leave the state as it was:
+// the fused kernel writes only the second buffer set and the partials, the
+// predictor is timed on the second buffer set, and the velocities are restored
+// after the force + kick timings (whose forces equal the ones already resident).
 template <class T> static int tune_fire(qmin_ctx *h, const Lat<T> &L)
 {
     if (h->path >= 0 && h->tuned_version == h->version && h->tuned_mode == h->fire_mode &&
@@ -721,18 +723,29 @@ template <class T> static int tune_fire(qmin_ctx *h, const Lat<T> &L)
     cudaEvent_t e0, e1;
     CK(cudaEventCreate(&e0));
     CK(cudaEventCreate(&e1));
-    auto time3 = [&](auto &&launch) -> float {
-        launch();  // warm-up (also sets kernel attributes)
+    auto elapsed = [&](auto &&body) -> float {
         cudaEventRecord(e0, h->stream);
-        for (int k = 0; k < 3; ++k) launch();
+        body();
         cudaEventRecord(e1, h->stream);
         cudaEventSynchronize(e1);
         float ms = 0;
         cudaEventElapsedTime(&ms, e0, e1);
-        return ms / 3;
+        return ms;
     };
+    // mean of three launches after a warm-up (which also sets kernel
+    // attributes); a candidate whose warm-up already exceeds `budget` ms cannot
+    // win and keeps that time.  `launch` returns its kernel count.
+    auto timed = [&](auto &&launch, float budget) -> float {
+        const float warm = elapsed([&]() { h->launches += launch(); });
+        if (warm > budget) return warm;
+        return elapsed([&]() {
+                   for (int k = 0; k < 3; ++k) h->launches += launch();
+               }) / 3;
+    };
+    const float kNoBudget = 1e30f;
     const int H = L.multi ? 2 : 1;
-    float best = 1e30f;
+    float best = kNoBudget;
+    auto budget_for = [&](float fixed) { return best < kNoBudget ? 2.f * best - fixed : kNoBudget; };
     for (int k = 0; k < kTuneCandidates; ++k) h->tune_ms[k] = -1;
     Lat<T> LB = L;
     LB.Q = (T *)h->Q2;
@@ -740,47 +753,57 @@ template <class T> static int tune_fire(qmin_ctx *h, const Lat<T> &L)
     LB.F = (T *)h->F2;
     // the L6 forms are compiled into the uncapped separate kernels only
     const bool l6 = L.multi && L.L6 != T(0);
-    if (!l6 && (h->fire_mode == QMIN_FIRE_AUTO || h->fire_mode == QMIN_FIRE_FUSED)) {
-        for (int cfg = 0; cfg < kFusedConfigs; ++cfg) {
-            if (pinned_out(cfg)) continue;
-            int tx, ty;
-            fused_tile_shape(cfg, &tx, &ty);
-            const int ntiles = ((h->Lx + tx - 1) / tx) * ((h->Ly + ty - 1) / ty);
-            int zc0 = (int)std::ceil((double)h->Lz * ntiles / (152.0 * 4.0));
-            zc0 = std::max(zc0, 2 * H + 2);
-            for (int v = 0; v < 2; ++v) {
-                const int zc = std::min(h->Lz, zc0 << v);
-                const int nz = (h->Lz + zc - 1) / zc;
-                if ((long long)ntiles * nz > kMaxFusedBlocks) continue;
-                int nb = 0, ok = 1;
-                const float ms = time3([&]() {
-                    if (launch_fire_fused<T>(cfg, L, (T *)h->Q2, (T *)h->V2, (T *)h->F2, h->fire, h->partials, zc,
-                                             h->stream, &nb) < 0)
-                        ok = 0;
-                });
-                h->launches += 4;
-                if (!ok || cudaGetLastError() != cudaSuccess) continue;
-                h->tune_ms[kSepVariants + 2 * cfg + v] = ms;
+    const bool auto_mode = h->fire_mode == QMIN_FIRE_AUTO;
+    const bool split_ok = L.multi && !l6 && h->split_cls;
+    // automatic choice: the split path and the separate kernels where the split
+    // path exists (the fused and staged paths are measured slower there on
+    // GB300 and stay available when pinned), every strategy elsewhere
+    const bool try_split = split_ok && (auto_mode || h->fire_mode == QMIN_FIRE_SPLIT);
+    const bool try_sep = l6 || auto_mode || h->fire_mode == QMIN_FIRE_SEPARATE ||
+                         (h->fire_mode == QMIN_FIRE_SPLIT && !split_ok);
+    const bool try_tiled = !l6 && sizeof(T) == 4 && ((auto_mode && !split_ok) || h->fire_mode == QMIN_FIRE_TILED);
+    const bool try_fused = !l6 && ((auto_mode && !split_ok) || h->fire_mode == QMIN_FIRE_FUSED);
+    if (try_sep || try_tiled || try_split) {
+        const float t_pred = timed([&]() { return launch_fire_pred<T>(LB, h->fire, h->stream); }, kNoBudget);
+        const size_t bytes = 5 * (size_t)h->P * h->esz;
+        // the force + kick candidates kick V; it is restored afterwards (their forces equal the resident ones)
+        CK(cudaMemcpyAsync(h->V2, h->V, bytes, cudaMemcpyDeviceToDevice, h->stream));
+        if (try_split) {
+            const SplitLists sl = split_lists(h);
+            const float t_dl = timed([&]() { return launch_split_derivs<T>(L, sl, h->fire, h->stream); }, kNoBudget);
+            for (int cap = 0; cap < kSplitVariants; ++cap) {
+                if (pinned_out(cap) || (sizeof(T) == 8 && cap >= kSplitFp32First)) continue;
+                int np = 0;
+                const float t_fk = timed(
+                    [&]() {
+                        return launch_split_force_kick<T>(L, sl, h->fire, h->partials, h->grid, cap, h->stream, &np);
+                    },
+                    budget_for(t_pred + t_dl));
+                const float ms = t_pred + t_dl + t_fk;
+                h->tune_ms[kSepVariants + 2 * kFusedConfigs + 2 * kTiledConfigs + cap] = ms;
                 if (ms < best) {
                     best = ms;
-                    h->path = 1;
-                    h->fused_cfg = cfg;
-                    h->fused_zc = zc;
-                    h->fused_nblocks = nb;
+                    h->path = 3;
+                    h->split_cap = cap;
                 }
-                if (zc >= h->Lz) break;
             }
         }
-    }
-    const bool try_sep = l6 || h->fire_mode == QMIN_FIRE_AUTO || h->fire_mode == QMIN_FIRE_SEPARATE ||
-                         (h->fire_mode == QMIN_FIRE_SPLIT && !L.multi);
-    const bool try_tiled =
-        !l6 && (h->fire_mode == QMIN_FIRE_AUTO || h->fire_mode == QMIN_FIRE_TILED) && sizeof(T) == 4;
-    if (try_sep || try_tiled || (L.multi && !l6 && h->fire_mode == QMIN_FIRE_SPLIT)) {
-        const float t_pred = time3([&]() { launch_fire_pred<T>(LB, h->fire, h->stream); });
-        const float t_der = L.multi ? time3([&]() { launch_derivs<T>(L, h->stream); }) : 0.f;
-        const size_t bytes = 5 * (size_t)h->P * h->esz;
-        CK(cudaMemcpyAsync(h->V2, h->V, bytes, cudaMemcpyDeviceToDevice, h->stream));
+        const float t_der = (try_sep || try_tiled) && L.multi
+                                ? timed([&]() { return launch_derivs<T>(L, h->stream); }, kNoBudget)
+                                : 0.f;
+        for (int cap = 0; try_sep && cap < kSepVariants; ++cap) {
+            if (pinned_out(cap)) continue;
+            const float t_fk = timed(
+                [&]() { return launch_force_kick_only<T>(L, h->fire, h->partials, h->grid, h->stream, cap); },
+                budget_for(t_pred + t_der));
+            const float ms = t_pred + t_der + t_fk;
+            h->tune_ms[cap] = ms;
+            if (ms < best) {
+                best = ms;
+                h->path = 0;
+                h->sep_cap = cap;
+            }
+        }
         for (int cfg = 0; try_tiled && cfg < kTiledConfigs; ++cfg) {
             if (pinned_out(cfg)) continue;
             int tx, ty;
@@ -792,10 +815,13 @@ template <class T> static int tune_fire(qmin_ctx *h, const Lat<T> &L)
             for (int v = 0; v < 2; ++v) {
                 const int zc = std::min(h->Lz, zc0 << v);
                 int nb = 0, ok = 1;
-                const float t_fk = time3([&]() {
-                    if (launch_force_kick_tiled<T>(cfg, L, h->fire, h->partials, zc, h->stream, &nb) < 0) ok = 0;
-                });
-                h->launches += 4;
+                const float t_fk = timed(
+                    [&]() {
+                        const int n = launch_force_kick_tiled<T>(cfg, L, h->fire, h->partials, zc, h->stream, &nb);
+                        if (n < 0) ok = 0;
+                        return n < 0 ? 0 : n;
+                    },
+                    budget_for(t_pred + t_der));
                 if (!ok || cudaGetLastError() != cudaSuccess) break;
                 const float ms = t_pred + t_der + t_fk;
                 h->tune_ms[kSepVariants + 2 * kFusedConfigs + 2 * cfg + v] = ms;
@@ -809,40 +835,40 @@ template <class T> static int tune_fire(qmin_ctx *h, const Lat<T> &L)
                 if (zc >= h->Lz) break;
             }
         }
-        for (int cap = 0; try_sep && cap < kSepVariants; ++cap) {
-            if (pinned_out(cap)) continue;
-            const float t_fk =
-                time3([&]() { launch_force_kick_only<T>(L, h->fire, h->partials, h->grid, h->stream, cap); });
-            const float ms = t_pred + t_der + t_fk;
-            h->tune_ms[cap] = ms;
+        CK(cudaMemcpyAsync(h->V, h->V2, bytes, cudaMemcpyDeviceToDevice, h->stream));
+    }
+    // the fused kernel writes only the second buffer set and the partials
+    for (int cfg = 0; try_fused && cfg < kFusedConfigs; ++cfg) {
+        if (pinned_out(cfg)) continue;
+        int tx, ty;
+        fused_tile_shape(cfg, &tx, &ty);
+        const int ntiles = ((h->Lx + tx - 1) / tx) * ((h->Ly + ty - 1) / ty);
+        int zc0 = (int)std::ceil((double)h->Lz * ntiles / (152.0 * 4.0));
+        zc0 = std::max(zc0, 2 * H + 2);
+        for (int v = 0; v < 2; ++v) {
+            const int zc = std::min(h->Lz, zc0 << v);
+            const int nz = (h->Lz + zc - 1) / zc;
+            if ((long long)ntiles * nz > kMaxFusedBlocks) continue;
+            int nb = 0, ok = 1;
+            const float ms = timed(
+                [&]() {
+                    const int n = launch_fire_fused<T>(cfg, L, (T *)h->Q2, (T *)h->V2, (T *)h->F2, h->fire,
+                                                       h->partials, zc, h->stream, &nb);
+                    if (n < 0) ok = 0;
+                    return n < 0 ? 0 : n;
+                },
+                budget_for(0.f));
+            if (!ok || cudaGetLastError() != cudaSuccess) continue;
+            h->tune_ms[kSepVariants + 2 * cfg + v] = ms;
             if (ms < best) {
                 best = ms;
-                h->path = 0;
-                h->sep_cap = cap;
+                h->path = 1;
+                h->fused_cfg = cfg;
+                h->fused_zc = zc;
+                h->fused_nblocks = nb;
             }
+            if (zc >= h->Lz) break;
         }
-        const bool try_split = L.multi && !l6 && h->split_cls &&
-                               (h->fire_mode == QMIN_FIRE_AUTO || h->fire_mode == QMIN_FIRE_SPLIT);
-        if (try_split) {
-            const SplitLists sl = split_lists(h);
-            const float t_dl = time3([&]() { launch_split_derivs<T>(L, sl, h->fire, h->stream); });
-            for (int cap = 0; cap < kSplitVariants; ++cap) {
-                if (pinned_out(cap) || (sizeof(T) == 8 && cap >= kSplitFp32First)) continue;
-                int np = 0;
-                const float t_fk = time3(
-                    [&]() { launch_split_force_kick<T>(L, sl, h->fire, h->partials, h->grid, cap, h->stream, &np); });
-                const float ms = t_pred + t_dl + t_fk;
-                h->tune_ms[kSepVariants + 2 * kFusedConfigs + 2 * kTiledConfigs + cap] = ms;
-                if (ms < best) {
-                    best = ms;
-                    h->path = 3;
-                    h->split_cap = cap;
-                }
-            }
-            h->launches += 4 * (1 + 2 * kSplitVariants);
-        }
-        CK(cudaMemcpyAsync(h->V, h->V2, bytes, cudaMemcpyDeviceToDevice, h->stream));
-        h->launches += 4 * (1 + (L.multi ? 1 : 0) + (try_sep ? kSepVariants : 0)) + 2;
     }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
