@@ -50,7 +50,11 @@ struct qmin_ctx {
     size_t esz = 8;
     cudaStream_t stream = nullptr;
     bool own_stream = false;
+    // side stream (highest priority) and fork/join events for the listed sites of the split path
+    cudaStream_t aux = nullptr;
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
     void *Q = nullptr, *V = nullptr, *F = nullptr, *D = nullptr;
+    void *cbd = nullptr;  // merged boundary coefficients (multi-constant)
     int8_t *types = nullptr;
     void *objs = nullptr;
     int nobj = 0;
@@ -152,6 +156,21 @@ template <class T> void fill_lat_params(Lat<T> &L, const qmin_ldg_params &p, int
 }
 template void fill_lat_params<double>(Lat<double> &, const qmin_ldg_params &, int);
 template void fill_lat_params<float>(Lat<float> &, const qmin_ldg_params &, int);
+
+// k L / 4 per input of the merged boundary forms; halved for derivative inputs
+template <class T> void fill_boundary_coeffs(const qmin_ldg_params &p, T *out)
+{
+    const double Lt[3] = {p.L2, p.L3, p.L4};
+    for (int n = 0; n < QMIN_BND_CASES; ++n)
+        for (int k = 0; k < 5; ++k)
+            for (int m = 0; m < QMIN_BND_W; ++m) {
+                double c = 0.0;
+                for (int t = 0; t < 3; ++t) c += Lt[t] * (double)qmin_bnd_k[n][k][m][t];
+                out[(n * 5 + k) * QMIN_BND_W + m] = T(c * (qmin_bnd_dn[n][k][m] ? 0.125 : 0.25));
+            }
+}
+template void fill_boundary_coeffs<double>(const qmin_ldg_params &, double *);
+template void fill_boundary_coeffs<float>(const qmin_ldg_params &, float *);
 }  // namespace qmin
 
 template <class T> static Lat<T> make_lat(qmin_ctx *h)
@@ -172,6 +191,7 @@ template <class T> static Lat<T> make_lat(qmin_ctx *h)
     fill_lat_params(L, h->params, h->metric_mode);
     L.Hv = h->hvar_on ? (const T *)h->hvar : nullptr;
     L.hvp = T(h->params.dchi * h->params.mu0);
+    L.cbd = (const T *)h->cbd;
     return L;
 }
 
@@ -181,13 +201,16 @@ static void free_ctx(qmin_ctx *h)
         if (h->graph[g]) cudaGraphExecDestroy(h->graph[g]);
     void *bufs[] = {h->Q, h->V, h->F, h->D, h->types, h->objs, h->partials, h->stage, h->stage_t, h->fire, h->iter,
                     h->out5, h->M, h->S, h->alt, h->lbp, h->lbs, h->lby, h->Q2, h->V2, h->F2, h->hvar,
-                    h->split_cls, h->split_sites, h->split_derivs};
+                    h->split_cls, h->split_sites, h->split_derivs, h->cbd};
     for (void *b : bufs)
         if (b) cudaFree(b);
     if (h->fire_h) cudaFreeHost(h->fire_h);
     if (h->iter_h) cudaFreeHost(h->iter_h);
     if (h->out5_h) cudaFreeHost(h->out5_h);
     if (h->own_stream && h->stream) cudaStreamDestroy(h->stream);
+    if (h->aux) cudaStreamDestroy(h->aux);
+    if (h->ev_fork) cudaEventDestroy(h->ev_fork);
+    if (h->ev_join) cudaEventDestroy(h->ev_join);
     delete h;
 }
 
@@ -301,6 +324,24 @@ int qmin_set_params(qmin_handle h, const qmin_ldg_params *p)
         }
         CK(cudaMemsetAsync(h->D, 0, 15 * (size_t)h->P * h->esz, h->stream));
     }
+    if (p->multi_constant) {
+        const size_t n = (size_t)QMIN_BND_CASES * 5 * QMIN_BND_W;
+        if (!h->cbd && cudaMalloc(&h->cbd, n * h->esz) != cudaSuccess) {
+            cudaGetLastError();
+            return fail(QMIN_ENOMEM, "qmin_set_params: boundary coefficient allocation failed");
+        }
+        if (h->prec == QMIN_FP64) {
+            std::vector<double> c(n);
+            fill_boundary_coeffs(*p, c.data());
+            CK(cudaMemcpyAsync(h->cbd, c.data(), n * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+            CK(cudaStreamSynchronize(h->stream));
+        } else {
+            std::vector<float> c(n);
+            fill_boundary_coeffs(*p, c.data());
+            CK(cudaMemcpyAsync(h->cbd, c.data(), n * sizeof(float), cudaMemcpyHostToDevice, h->stream));
+            CK(cudaStreamSynchronize(h->stream));
+        }
+    }
     h->have_params = true;
     invalidate_graphs(h);
     return QMIN_OK;
@@ -377,6 +418,20 @@ static int build_split_lists(qmin_ctx *h, const int8_t *t8)
     }
     for (int i = 0; i < N; ++i)
         if (need[i]) derivs.push_back(i);
+    // listed sites grouped by form (bulk-like first, then each boundary case),
+    // so that the warps of the listed-site kernel take one branch
+    auto form_of = [&](int i) {
+        if (t8[i] != -1) return 0;
+        int xx = 0, yy = 0, zz = 0;  // lcForce::getBoundaryCase: the down neighbour wins
+        if (t8[nb(i, 1)] > 0) xx = 1;
+        if (t8[nb(i, 0)] > 0) xx = 2;
+        if (t8[nb(i, 3)] > 0) yy = 1;
+        if (t8[nb(i, 2)] > 0) yy = 2;
+        if (t8[nb(i, 5)] > 0) zz = 1;
+        if (t8[nb(i, 4)] > 0) zz = 2;
+        return 1 + xx + 3 * yy + 9 * zz;
+    };
+    std::stable_sort(sites.begin(), sites.end(), [&](int a, int b) { return form_of(a) < form_of(b); });
     auto upload = [&](void **dst, const void *src, size_t bytes) -> bool {
         if (*dst) cudaFree(*dst);
         *dst = nullptr;
@@ -674,6 +729,17 @@ int qmin_fire_init(qmin_handle h, const qmin_fire_params *p)
     return QMIN_OK;
 }
 
+static int ensure_aux(qmin_ctx *h)
+{
+    if (h->aux) return QMIN_OK;
+    int least = 0, greatest = 0;
+    CK(cudaDeviceGetStreamPriorityRange(&least, &greatest));
+    CK(cudaStreamCreateWithPriority(&h->aux, cudaStreamNonBlocking, greatest));
+    CK(cudaEventCreateWithFlags(&h->ev_fork, cudaEventDisableTiming));
+    CK(cudaEventCreateWithFlags(&h->ev_join, cudaEventDisableTiming));
+    return QMIN_OK;
+}
+
 static int ensure_pingpong(qmin_ctx *h)
 {
     if (h->Q2) return QMIN_OK;
@@ -888,6 +954,7 @@ template <class T> static int fire_impl(qmin_ctx *h, int max_iterations)
     h->launches += launch_force<T>(L, h->grid, h->stream);
     int r = tune_fire<T>(h, L);
     if (r) return r;
+    if (h->path == 3 && (r = ensure_aux(h))) return r;
     Lat<T> LB = L;  // the second buffer set as input
     LB.Q = (T *)h->Q2;
     LB.V = (T *)h->V2;
@@ -905,12 +972,20 @@ template <class T> static int fire_impl(qmin_ctx *h, int max_iterations)
             n += launch_force_kick<T>(L, h->fire, h->partials, h->grid, h->stream, h->sep_cap);
             n += launch_fire_control(h->fire, h->partials, h->grid, h->stream);
         } else if (h->path == 3) {
-            int nb = 0;
+            // the listed sites (derivative planes, then force + kick) on the
+            // high-priority side stream, beside the deep-site kernel
             const SplitLists sl = split_lists(h);
             n = launch_fire_pred<T>(L, h->fire, h->stream);
-            n += launch_split_derivs<T>(L, sl, h->fire, h->stream);
-            n += launch_split_force_kick<T>(L, sl, h->fire, h->partials, h->grid, h->split_cap, h->stream, &nb);
-            n += launch_fire_control(h->fire, h->partials, nb, h->stream);
+            cudaEventRecord(h->ev_fork, h->stream);
+            cudaStreamWaitEvent(h->aux, h->ev_fork, 0);
+            const int nd = launch_split_deep<T>(L, sl, h->fire, h->partials, h->grid, h->split_cap, h->stream);
+            n += 1;
+            n += launch_split_derivs<T>(L, sl, h->fire, h->aux);
+            const int nl = launch_split_list<T>(L, sl, h->fire, h->partials + 3 * nd, h->aux);
+            n += nl > 0 ? 1 : 0;
+            cudaEventRecord(h->ev_join, h->aux);
+            cudaStreamWaitEvent(h->stream, h->ev_join, 0);
+            n += launch_fire_control(h->fire, h->partials, nd + nl, h->stream);
         } else if (h->path == 2) {
             int nb = 0;
             n = launch_fire_pred<T>(L, h->fire, h->stream);

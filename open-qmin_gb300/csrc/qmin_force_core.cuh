@@ -131,7 +131,10 @@ __device__ __forceinline__ T deriv2_rule(int t, int td, int tu, T qd, T q, T qu)
 // metric_mode 1 applies M once everywhere (the reference GPU branch).
 // WITH_L6 compiles the cubic L6 forms in; kernels without it leave L6 out
 // (it is a runtime-zero branch that would still cost registers)
-template <class T, class A, bool WITH_L6 = false>
+// BND_LINES evaluates the boundary L2-L4 forms as straight-line code per case
+// (merged coefficients L.cbd) instead of walking the sparse tables; it needs
+// L.cbd and costs code size, so only the listed-site kernel takes it
+template <class T, class A, bool WITH_L6 = false, bool BND_LINES = false>
 __device__ __forceinline__ void site_force_core(const Lat<T> &L, const A &acc, int t, T *f, const T *hs = nullptr)
 {
     if (t > 0) {
@@ -219,8 +222,21 @@ __device__ __forceinline__ void site_force_core(const Lat<T> &L, const A &acc, i
             if (mask & 32) zz = 1;
             if (mask & 16) zz = 2;
             const int bcase = xx + 4 * yy + 16 * zz;
+            if constexpr (BND_LINES) {
+                T s3[5];
+                const T *cbd = L.cbd;
+#define QIN(c) q[c]
+#define QN(slot, c) nq[slot][c]
+#define DN(slot, d) acc.dn(slot, d)
+                QMIN_BOUNDARY_FORMS(xx + 3 * yy + 9 * zz, cbd, s3);
+#undef QIN
+#undef QN
+#undef DN
+#pragma unroll
+                for (int k = 0; k < 5; ++k) sp[k] += s3[k];
+            }
             const T Lt[3] = {L.L2, L.L3, L.L4};
-            for (int term = 0; term < 3; ++term) {
+            for (int term = 0; !BND_LINES && term < 3; ++term) {
                 if (Lt[term] == T(0)) continue;
                 for (int k = 0; k < 5; ++k) {
                     const int o0 = g_dt_offset[(term * 64 + bcase) * 5 + k];
@@ -313,7 +329,7 @@ template <class T> struct GlobalAcc {
     __device__ __forceinline__ T dn(int s, int d) const { return ld(D + (long long)d * P + b.n[s]); }
 };
 
-template <class T, bool WITH_L6 = false>
+template <class T, bool WITH_L6 = false, bool BND_LINES = false>
 __device__ __forceinline__ void site_force(const Lat<T> &L, int i, T *f)
 {
     const int t = L.types[i];
@@ -324,7 +340,7 @@ __device__ __forceinline__ void site_force(const Lat<T> &L, int i, T *f)
     }
     GlobalAcc<T> acc(L, i);
     T h[3];
-    site_force_core<T, GlobalAcc<T>, WITH_L6>(L, acc, t, f, site_field(L, i, h));
+    site_force_core<T, GlobalAcc<T>, WITH_L6, BND_LINES>(L, acc, t, f, site_field(L, i, h));
 }
 
 }  // namespace qmin

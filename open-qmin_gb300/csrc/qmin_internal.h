@@ -8,6 +8,7 @@
 #include "../../include/qmin_gb300.h"
 #include "qmin_bulk_forms.h"
 #include "qmin_bulk_q25.h"
+#include "qmin_boundary_forms.h"
 
 namespace qmin {
 
@@ -34,10 +35,13 @@ template <class T> struct Lat {
     int metric_mode, multi, efield, hfield;
     T cb[5 * QMIN_BULK_W];  // combined bulk multi-constant coefficients
     T cq[5 * QMIN_Q25_W];   // the same form over Q on the 25-point stencil (deep bulk sites)
+    const T *cbd;           // merged boundary L2-L4 coefficients [27][5][QMIN_BND_W] in device memory, or null
 };
 
 // force parameters shared by every kernel (qmin_capi.cu)
 template <class T> void fill_lat_params(Lat<T> &L, const qmin_ldg_params &p, int metric_mode);
+// the merged boundary coefficients for one parameter set, [27][5][QMIN_BND_W] (qmin_capi.cu)
+template <class T> void fill_boundary_coeffs(const qmin_ldg_params &p, T *out);
 
 // FIRE state resident on the device.  The velocity mix that ends one
 // iteration is deferred into the next iteration's first kernel.
@@ -134,5 +138,13 @@ template <class T> int launch_split_derivs(const Lat<T> &L, const SplitLists &sl
 template <class T>
 int launch_split_force_kick(const Lat<T> &L, const SplitLists &sl, FireDev *fd, double *partials, int grid, int cap,
                             cudaStream_t s, int *nparts);
+// the two halves separately: the deep-site kernel `cap` (returns its block
+// count, partials[0 .. 3 count)) and the listed sites (returns its block count,
+// 0 without listed sites); they touch disjoint sites and may run concurrently
+template <class T>
+int launch_split_deep(const Lat<T> &L, const SplitLists &sl, FireDev *fd, double *partials, int grid, int cap,
+                      cudaStream_t s);
+template <class T>
+int launch_split_list(const Lat<T> &L, const SplitLists &sl, FireDev *fd, double *partials, cudaStream_t s);
 
 }  // namespace qmin

@@ -121,7 +121,7 @@ __global__ void __launch_bounds__(kBlock)
     for (int e = blockIdx.x * kBlock + threadIdx.x; e < n; e += gridDim.x * kBlock) {
         const int i = list[e];
         T f[5];
-        site_force(L, i, f);
+        site_force<T, false, true>(L, i, f);
         kick_and_sum(L, i, hdt, f, acc);
     }
     block_sum<3>(acc);
@@ -558,35 +558,38 @@ template <class T> int launch_split_derivs(const Lat<T> &L, const SplitLists &sl
 }
 
 template <class T>
+int launch_split_deep(const Lat<T> &L, const SplitLists &sl, FireDev *fd, double *partials, int grid, int cap,
+                      cudaStream_t s)
+{
+    if (cap == 2) return launch_deep_tiled<T, 32, 8>(L, sl, fd, partials, s);
+    if (cap == 3) return launch_deep_tiled<T, 16, 16>(L, sl, fd, partials, s);
+    if (cap == 4 || cap == 5) {
+        if constexpr (sizeof(T) == 4) return launch_deep_pair<32, 8, 3>(L, sl, fd, partials, cap == 5, s);
+        else return -1;  // FP32 only (the autotuner does not offer it for FP64)
+    }
+    if (cap == 1) k_force_kick_deep<T, 1><<<grid, kBlock, 0, s>>>(L, sl.cls, fd, partials);
+    else k_force_kick_deep<T, 0><<<grid, kBlock, 0, s>>>(L, sl.cls, fd, partials);
+    return grid;
+}
+
+template <class T>
+int launch_split_list(const Lat<T> &L, const SplitLists &sl, FireDev *fd, double *partials, cudaStream_t s)
+{
+    if (sl.n_sites <= 0) return 0;
+    const int g = list_grid(sl.n_sites);
+    k_force_kick_list<T><<<g, kBlock, 0, s>>>(L, sl.sites, sl.n_sites, fd, partials);
+    return g;
+}
+
+template <class T>
 int launch_split_force_kick(const Lat<T> &L, const SplitLists &sl, FireDev *fd, double *partials, int grid, int cap,
                             cudaStream_t s, int *nparts)
 {
-    int np = grid;
-    if (cap == 2) {
-        np = launch_deep_tiled<T, 32, 8>(L, sl, fd, partials, s);
-    } else if (cap == 3) {
-        np = launch_deep_tiled<T, 16, 16>(L, sl, fd, partials, s);
-    } else if (cap == 4 || cap == 5) {
-        if constexpr (sizeof(T) == 4) {
-            np = launch_deep_pair<32, 8, 3>(L, sl, fd, partials, cap == 5, s);
-        } else {
-            return -1;  // FP32 only (the autotuner does not offer it for FP64)
-        }
-    } else if (cap == 1) {
-        k_force_kick_deep<T, 1><<<grid, kBlock, 0, s>>>(L, sl.cls, fd, partials);
-    } else {
-        k_force_kick_deep<T, 0><<<grid, kBlock, 0, s>>>(L, sl.cls, fd, partials);
-    }
-    const int grid_used = np;
-    int n = 1;
-    if (sl.n_sites > 0) {
-        const int g2 = list_grid(sl.n_sites);
-        k_force_kick_list<T><<<g2, kBlock, 0, s>>>(L, sl.sites, sl.n_sites, fd, partials + 3 * grid_used);
-        np += g2;
-        ++n;
-    }
-    *nparts = np;
-    return n;
+    const int nd = launch_split_deep<T>(L, sl, fd, partials, grid, cap, s);
+    if (nd < 0) return -1;
+    const int nl = launch_split_list<T>(L, sl, fd, partials + 3 * nd, s);
+    *nparts = nd + nl;
+    return 1 + (nl > 0 ? 1 : 0);
 }
 
 template int launch_split_derivs<double>(const Lat<double> &, const SplitLists &, FireDev *, cudaStream_t);
@@ -595,5 +598,11 @@ template int launch_split_force_kick<double>(const Lat<double> &, const SplitLis
                                              cudaStream_t, int *);
 template int launch_split_force_kick<float>(const Lat<float> &, const SplitLists &, FireDev *, double *, int, int,
                                             cudaStream_t, int *);
+template int launch_split_deep<double>(const Lat<double> &, const SplitLists &, FireDev *, double *, int, int,
+                                       cudaStream_t);
+template int launch_split_deep<float>(const Lat<float> &, const SplitLists &, FireDev *, double *, int, int,
+                                      cudaStream_t);
+template int launch_split_list<double>(const Lat<double> &, const SplitLists &, FireDev *, double *, cudaStream_t);
+template int launch_split_list<float>(const Lat<float> &, const SplitLists &, FireDev *, double *, cudaStream_t);
 
 }  // namespace qmin
