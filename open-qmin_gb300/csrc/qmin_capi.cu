@@ -192,6 +192,7 @@ template <class T> static Lat<T> make_lat(qmin_ctx *h)
     L.Hv = h->hvar_on ? (const T *)h->hvar : nullptr;
     L.hvp = T(h->params.dchi * h->params.mu0);
     L.cbd = (const T *)h->cbd;
+    L.split = SplitLists{h->split_cls, h->split_sites, h->n_split_sites, h->split_derivs, h->n_split_derivs};
     return L;
 }
 
@@ -799,14 +800,16 @@ template <class T> static int tune_fire(qmin_ctx *h, const Lat<T> &L)
         return ms;
     };
     // mean of three launches after a warm-up (which also sets kernel
-    // attributes); a candidate whose warm-up already exceeds `budget` ms cannot
-    // win and keeps that time.  `launch` returns its kernel count.
+    // attributes), one launch when the warm-up took over 2 ms; a candidate
+    // whose warm-up already exceeds `budget` ms cannot win and keeps that
+    // time.  `launch` returns its kernel count.
     auto timed = [&](auto &&launch, float budget) -> float {
         const float warm = elapsed([&]() { h->launches += launch(); });
         if (warm > budget) return warm;
+        const int reps = warm > 2.f ? 1 : 3;
         return elapsed([&]() {
-                   for (int k = 0; k < 3; ++k) h->launches += launch();
-               }) / 3;
+                   for (int k = 0; k < reps; ++k) h->launches += launch();
+               }) / reps;
     };
     const float kNoBudget = 1e30f;
     const int H = L.multi ? 2 : 1;

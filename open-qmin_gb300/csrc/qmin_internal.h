@@ -18,6 +18,17 @@ template <class T> struct ObjDev {
     T W, S0;
 };
 
+// split force + kick (multi-constant, no L6): site classes (0 deep bulk, 1 other
+// LC site, 2 object), the class-1 sites, and the sites whose derivative planes
+// the class-1 forms read
+struct SplitLists {
+    const uint8_t *cls;
+    const int *sites;
+    int n_sites;
+    const int *derivs;
+    int n_derivs;
+};
+
 // Everything a lattice kernel needs, passed by value.  Planes are SoA:
 // component k of site i lives at X[k * P + i]; P = N rounded up to 32.
 template <class T> struct Lat {
@@ -36,6 +47,7 @@ template <class T> struct Lat {
     T cb[5 * QMIN_BULK_W];  // combined bulk multi-constant coefficients
     T cq[5 * QMIN_Q25_W];   // the same form over Q on the 25-point stencil (deep bulk sites)
     const T *cbd;           // merged boundary L2-L4 coefficients [27][5][QMIN_BND_W] in device memory, or null
+    SplitLists split;       // deep / listed site classes and lists (all null when not built)
 };
 
 // force parameters shared by every kernel (qmin_capi.cu)
@@ -67,7 +79,11 @@ extern thread_local std::string g_last_error;
 
 // launchers (qmin_kernels.cu); each returns the number of kernels launched
 template <class T> int launch_derivs(const Lat<T> &L, cudaStream_t s);
+// forces at Q: the split kernels (deep sites over Q, listed sites through the
+// plane forms) where L.split is built and the form is multi-constant without
+// L6, else the derivative planes and the full-lattice force kernel
 template <class T> int launch_force(const Lat<T> &L, int grid, cudaStream_t s);
+template <class T> int launch_split_force(const Lat<T> &L, int grid, cudaStream_t s);
 template <class T> int launch_fire_pred(const Lat<T> &L, FireDev *fd, cudaStream_t s);
 template <class T>
 int launch_force_kick(const Lat<T> &L, FireDev *fd, double *partials, int grid, cudaStream_t s, int cap);
@@ -123,16 +139,6 @@ int launch_force_kick_tiled(int cfg, const Lat<T> &L, FireDev *fd, double *parti
                             int *nblocks);
 int tiled_tile_shape(int cfg, int *tx, int *ty);
 
-// split force + kick (multi-constant, no L6): site classes (0 deep bulk, 1 other
-// LC site, 2 object), the class-1 sites, and the sites whose derivative planes
-// the class-1 forms read
-struct SplitLists {
-    const uint8_t *cls;
-    const int *sites;
-    int n_sites;
-    const int *derivs;
-    int n_derivs;
-};
 template <class T> int launch_split_derivs(const Lat<T> &L, const SplitLists &sl, FireDev *fd, cudaStream_t s);
 // partials: the deep kernel's grid blocks, then the list kernel's; *nparts their total
 template <class T>

@@ -779,6 +779,7 @@ template <class T> int launch_derivs(const Lat<T> &L, cudaStream_t s)
 }
 template <class T> int launch_force(const Lat<T> &L, int grid, cudaStream_t s)
 {
+    if (L.multi && L.L6 == T(0) && L.split.cls) return launch_split_force(L, grid, s);
     int n = 0;
     if (L.multi) n += launch_derivs(L, s);
     if (L.L6 != T(0)) k_force<T, true><<<grid, kBlock, 0, s>>>(L);

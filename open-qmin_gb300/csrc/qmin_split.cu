@@ -90,44 +90,63 @@ int list_grid(int n) { return std::max(1, std::min((n + kBlock - 1) / kBlock, 15
 
 }  // namespace
 
-// every deep bulk site (cls == 0); partials[0 .. gridDim.x)
-template <class T, int CAP>
+// every deep bulk site (cls == 0); partials[0 .. gridDim.x).  KICK = false:
+// forces only (no FIRE state), object sites' forces set to zero
+template <class T, int CAP, bool KICK = true>
 __global__ void __launch_bounds__(kBlock, CAP + 1)
     k_force_kick_deep(Lat<T> L, const uint8_t *__restrict__ cls, const FireDev *__restrict__ fd, double *partials)
 {
-    if (!fd->active) return;
-    const T hdt = T(0.5) * T(fd->dt);
+    if (KICK && !fd->active) return;
+    const T hdt = KICK ? T(0.5) * T(fd->dt) : T(0);
     double acc[3] = {0.0, 0.0, 0.0};
     for (int i = blockIdx.x * kBlock + threadIdx.x; i < L.N; i += gridDim.x * kBlock) {
-        if (cls[i] != 0) continue;
+        const int c = cls[i];
+        if (!KICK && c == 2)
+#pragma unroll
+            for (int k = 0; k < 5; ++k) L.F[k * L.P + i] = T(0);
+        if (c != 0) continue;
         T f[5];
         deep_force(L, i, f);
-        kick_and_sum(L, i, hdt, f, acc);
-    }
-    block_sum<3>(acc);
-    if (threadIdx.x == 0)
+        if constexpr (KICK) {
+            kick_and_sum(L, i, hdt, f, acc);
+        } else {
 #pragma unroll
-        for (int k = 0; k < 3; ++k) partials[3 * blockIdx.x + k] = acc[k];
+            for (int k = 0; k < 5; ++k) L.F[k * L.P + i] = f[k];
+        }
+    }
+    if constexpr (KICK) {
+        block_sum<3>(acc);
+        if (threadIdx.x == 0)
+#pragma unroll
+            for (int k = 0; k < 3; ++k) partials[3 * blockIdx.x + k] = acc[k];
+    }
 }
 
-// the listed LC sites through the derivative-plane forms
-template <class T>
+// the listed LC sites through the derivative-plane forms (KICK = false: forces only)
+template <class T, bool KICK = true>
 __global__ void __launch_bounds__(kBlock)
     k_force_kick_list(Lat<T> L, const int *__restrict__ list, int n, const FireDev *__restrict__ fd, double *partials)
 {
-    if (!fd->active) return;
-    const T hdt = T(0.5) * T(fd->dt);
+    if (KICK && !fd->active) return;
+    const T hdt = KICK ? T(0.5) * T(fd->dt) : T(0);
     double acc[3] = {0.0, 0.0, 0.0};
     for (int e = blockIdx.x * kBlock + threadIdx.x; e < n; e += gridDim.x * kBlock) {
         const int i = list[e];
         T f[5];
         site_force<T, false, true>(L, i, f);
-        kick_and_sum(L, i, hdt, f, acc);
-    }
-    block_sum<3>(acc);
-    if (threadIdx.x == 0)
+        if constexpr (KICK) {
+            kick_and_sum(L, i, hdt, f, acc);
+        } else {
 #pragma unroll
-        for (int k = 0; k < 3; ++k) partials[3 * blockIdx.x + k] = acc[k];
+            for (int k = 0; k < 5; ++k) L.F[k * L.P + i] = f[k];
+        }
+    }
+    if constexpr (KICK) {
+        block_sum<3>(acc);
+        if (threadIdx.x == 0)
+#pragma unroll
+            for (int k = 0; k < 3; ++k) partials[3 * blockIdx.x + k] = acc[k];
+    }
 }
 
 // twice the first derivatives (k_derivs' rules) at the listed sites only
@@ -135,7 +154,7 @@ template <class T>
 __global__ void __launch_bounds__(kBlock)
     k_derivs_list(Lat<T> L, const int *__restrict__ list, int n, const FireDev *__restrict__ fd)
 {
-    if (!fd->active) return;
+    if (fd && !fd->active) return;  // fd null: a force-only evaluation
     const long long P = L.P;
     for (int e = blockIdx.x * kBlock + threadIdx.x; e < n; e += gridDim.x * kBlock) {
         const int i = list[e];
@@ -381,7 +400,7 @@ __global__ void __launch_bounds__(TX *TY, deep_tiled_minb<T>())
 // float2 (a half-warp reads one 32-word row: no bank conflicts) and shares the
 // loads where the two stencils overlap.  Staging and plane ring as in
 // k_force_kick_deep_tiled.
-template <int TX, int TY, int MINB>
+template <int TX, int TY, int MINB, bool KICK = true>
 __global__ void __launch_bounds__(TX / 2 * TY, MINB)
     k_force_kick_deep_pair(Lat<float> L, const uint8_t *__restrict__ cls, const FireDev *__restrict__ fd,
                            double *partials, int zc)
@@ -391,8 +410,8 @@ __global__ void __launch_bounds__(TX / 2 * TY, MINB)
     constexpr int NPOS = (TS + NT - 1) / NT;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     float *sQ = reinterpret_cast<float *>(smem_raw);  // [NS][5][TS]
-    if (!fd->active) return;
-    const float hdt = 0.5f * float(fd->dt);
+    if (KICK && !fd->active) return;
+    const float hdt = KICK ? 0.5f * float(fd->dt) : 0.f;
     const int ntx = (L.Lx + TX - 1) / TX;
     const int gx0 = (blockIdx.x % ntx) * TX, gy0 = (blockIdx.x / ntx) * TY;
     const int zs = blockIdx.y * zc, ze = min(L.Lz, zs + zc);
@@ -436,13 +455,15 @@ __global__ void __launch_bounds__(TX / 2 * TY, MINB)
                 const long long i = i0 + (long long)sxy * z;
                 if (in_a) {
                     ca_next = cls[i];
+                    if (KICK)
 #pragma unroll
-                    for (int k = 0; k < 5; ++k) va_next[k] = L.V[k * P + i];
+                        for (int k = 0; k < 5; ++k) va_next[k] = L.V[k * P + i];
                 }
                 if (in_b) {
                     cb_next = cls[i + 1];
+                    if (KICK)
 #pragma unroll
-                    for (int k = 0; k < 5; ++k) vb_next[k] = L.V[k * P + i + 1];
+                        for (int k = 0; k < 5; ++k) vb_next[k] = L.V[k * P + i + 1];
                 }
             }
         };
@@ -460,6 +481,16 @@ __global__ void __launch_bounds__(TX / 2 * TY, MINB)
             fetch(z + 1);
             asm volatile("cp.async.wait_group 1;\n" ::: "memory");
             __syncthreads();
+            if (!KICK) {
+                // forces only: object sites get zero force
+                const long long i = i0 + (long long)sxy * z;
+                if (ca == 2)
+#pragma unroll
+                    for (int k = 0; k < 5; ++k) L.F[k * P + i] = 0.f;
+                if (cb == 2)
+#pragma unroll
+                    for (int k = 0; k < 5; ++k) L.F[k * P + i + 1] = 0.f;
+            }
             if (ca == 0 || cb == 0) {
                 const long long i = i0 + (long long)sxy * z;
                 int sb[5];
@@ -470,36 +501,44 @@ __global__ void __launch_bounds__(TX / 2 * TY, MINB)
                 deep_force_pair_tile<TS, SX>(L, sQ, sb, i, in_b ? i + 1 : i, fa, fb);
                 if (ca == 0) {
 #pragma unroll
-                    for (int k = 0; k < 5; ++k) {
-                        va[k] += hdt * fa[k];
-                        L.F[k * P + i] = fa[k];
-                        L.V[k * P + i] = va[k];
+                    for (int k = 0; k < 5; ++k) L.F[k * P + i] = fa[k];
+                    if (KICK) {
+#pragma unroll
+                        for (int k = 0; k < 5; ++k) {
+                            va[k] += hdt * fa[k];
+                            L.V[k * P + i] = va[k];
+                        }
+                        sacc[0] += dot_qt(fa, fa);
+                        sacc[1] += dot_qt(va, va);
+                        sacc[2] += dot_qt(fa, va);
                     }
-                    sacc[0] += dot_qt(fa, fa);
-                    sacc[1] += dot_qt(va, va);
-                    sacc[2] += dot_qt(fa, va);
                 }
                 if (cb == 0) {
 #pragma unroll
-                    for (int k = 0; k < 5; ++k) {
-                        vb[k] += hdt * fb[k];
-                        L.F[k * P + i + 1] = fb[k];
-                        L.V[k * P + i + 1] = vb[k];
+                    for (int k = 0; k < 5; ++k) L.F[k * P + i + 1] = fb[k];
+                    if (KICK) {
+#pragma unroll
+                        for (int k = 0; k < 5; ++k) {
+                            vb[k] += hdt * fb[k];
+                            L.V[k * P + i + 1] = vb[k];
+                        }
+                        sacc[0] += dot_qt(fb, fb);
+                        sacc[1] += dot_qt(vb, vb);
+                        sacc[2] += dot_qt(fb, vb);
                     }
-                    sacc[0] += dot_qt(fb, fb);
-                    sacc[1] += dot_qt(vb, vb);
-                    sacc[2] += dot_qt(fb, vb);
                 }
             }
             __syncthreads();
         }
     }
-    double acc[3] = {(double)sacc[0], (double)sacc[1], (double)sacc[2]};
-    block_sum<3, NT>(acc);
-    if (threadIdx.x == 0) {
-        const int b = blockIdx.y * gridDim.x + blockIdx.x;
+    if constexpr (KICK) {
+        double acc[3] = {(double)sacc[0], (double)sacc[1], (double)sacc[2]};
+        block_sum<3, NT>(acc);
+        if (threadIdx.x == 0) {
+            const int b = blockIdx.y * gridDim.x + blockIdx.x;
 #pragma unroll
-        for (int k = 0; k < 3; ++k) partials[3 * b + k] = acc[k];
+            for (int k = 0; k < 3; ++k) partials[3 * b + k] = acc[k];
+        }
     }
 }
 
@@ -526,7 +565,7 @@ static int launch_deep_tiled(const Lat<T> &L, const SplitLists &sl, FireDev *fd,
 // the FP32 two-sites-per-thread deep kernel over TX x TY columns
 // fitted = true: z chunks sized so that the grid is about two waves of MINB
 // blocks on each of the 152 SMs (fewer, longer columns), else kDeepZc planes
-template <int TX, int TY, int MINB>
+template <int TX, int TY, int MINB, bool KICK = true>
 static int launch_deep_pair(const Lat<float> &L, const SplitLists &sl, FireDev *fd, double *partials, bool fitted,
                             cudaStream_t s)
 {
@@ -534,8 +573,8 @@ static int launch_deep_pair(const Lat<float> &L, const SplitLists &sl, FireDev *
     static bool attr_set = false;
     if (!attr_set) {
         // a failure here surfaces as the launch's error
-        attr_set = cudaFuncSetAttribute(k_force_kick_deep_pair<TX, TY, MINB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                        (int)sm) == cudaSuccess;
+        attr_set = cudaFuncSetAttribute(k_force_kick_deep_pair<TX, TY, MINB, KICK>,
+                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm) == cudaSuccess;
     }
     const int ntiles = ((L.Lx + TX - 1) / TX) * ((L.Ly + TY - 1) / TY);
     int zc = kDeepZc;
@@ -546,7 +585,7 @@ static int launch_deep_pair(const Lat<float> &L, const SplitLists &sl, FireDev *
     }
     while ((long long)ntiles * ((L.Lz + zc - 1) / zc) > kMaxFusedBlocks - 1024) ++zc;
     const int nz = (L.Lz + zc - 1) / zc;
-    k_force_kick_deep_pair<TX, TY, MINB><<<dim3(ntiles, nz), TX / 2 * TY, sm, s>>>(L, sl.cls, fd, partials, zc);
+    k_force_kick_deep_pair<TX, TY, MINB, KICK><<<dim3(ntiles, nz), TX / 2 * TY, sm, s>>>(L, sl.cls, fd, partials, zc);
     return ntiles * nz;
 }
 
@@ -592,6 +631,23 @@ int launch_split_force_kick(const Lat<T> &L, const SplitLists &sl, FireDev *fd, 
     return 1 + (nl > 0 ? 1 : 0);
 }
 
+// forces only at Q (no FIRE state): derivative planes at the listed sites'
+// neighbours, the deep sites (FP64 from global memory at 2 blocks per SM, FP32
+// two per thread on 32x8 tiles), then the listed sites; object sites get zero
+template <class T> int launch_split_force(const Lat<T> &L, int grid, cudaStream_t s)
+{
+    const SplitLists &sl = L.split;
+    int n = launch_split_derivs<T>(L, sl, nullptr, s);
+    if constexpr (sizeof(T) == 4) launch_deep_pair<32, 8, 3, false>(L, sl, nullptr, nullptr, true, s);
+    else k_force_kick_deep<T, 1, false><<<grid, kBlock, 0, s>>>(L, sl.cls, nullptr, nullptr);
+    ++n;
+    if (sl.n_sites > 0) {
+        k_force_kick_list<T, false><<<list_grid(sl.n_sites), kBlock, 0, s>>>(L, sl.sites, sl.n_sites, nullptr, nullptr);
+        ++n;
+    }
+    return n;
+}
+
 template int launch_split_derivs<double>(const Lat<double> &, const SplitLists &, FireDev *, cudaStream_t);
 template int launch_split_derivs<float>(const Lat<float> &, const SplitLists &, FireDev *, cudaStream_t);
 template int launch_split_force_kick<double>(const Lat<double> &, const SplitLists &, FireDev *, double *, int, int,
@@ -604,5 +660,7 @@ template int launch_split_deep<float>(const Lat<float> &, const SplitLists &, Fi
                                       cudaStream_t);
 template int launch_split_list<double>(const Lat<double> &, const SplitLists &, FireDev *, double *, cudaStream_t);
 template int launch_split_list<float>(const Lat<float> &, const SplitLists &, FireDev *, double *, cudaStream_t);
+template int launch_split_force<double>(const Lat<double> &, int, cudaStream_t);
+template int launch_split_force<float>(const Lat<float> &, int, cudaStream_t);
 
 }  // namespace qmin
