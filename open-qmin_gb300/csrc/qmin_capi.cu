@@ -59,6 +59,7 @@ struct qmin_ctx {
     void *objs = nullptr;
     int nobj = 0;
     std::vector<qmin_object> objs_host;
+    std::vector<int8_t> types_host;  // site types of the last qmin_set_state (split lists built from them)
     double *partials = nullptr;
     int grid = 1;
     double *stage = nullptr;
@@ -482,12 +483,16 @@ int qmin_set_state(qmin_handle h, const double *Q, const int32_t *types, int lay
     CK(cudaMemsetAsync(h->V, 0, 5 * (size_t)h->P * h->esz, h->stream));
     CK(cudaMemsetAsync(h->F, 0, 5 * (size_t)h->P * h->esz, h->stream));
     CK(cudaGetLastError());
-    {
-        std::vector<int8_t> t8((size_t)h->N);
-        for (int i = 0; i < h->N; ++i) t8[i] = (int8_t)types[i];
-        CK(cudaStreamSynchronize(h->stream));
-        if ((r = build_split_lists(h, t8.data()))) return r;
+    std::vector<int8_t> t8((size_t)h->N);
+    for (int i = 0; i < h->N; ++i) t8[i] = (int8_t)types[i];
+    CK(cudaStreamSynchronize(h->stream));
+    if (h->have_state && t8 == h->types_host) {
+        // same geometry: the split lists, the tuned strategy and the captured
+        // graphs (which hold buffer pointers, not contents) stay valid
+        return QMIN_OK;
     }
+    if ((r = build_split_lists(h, t8.data()))) return r;
+    h->types_host.swap(t8);
     invalidate_graphs(h);
     h->have_state = true;
     return QMIN_OK;
@@ -1537,6 +1542,7 @@ int qmin_checkpoint_load(qmin_handle h, const char *path)
     h->nTotal = nT;
     h->max_type = mx;
     if (int rr = build_split_lists(h, t8.data())) return rr;
+    h->types_host = t8;
     h->have_state = true;
     h->fire_ready = hd.fire_ready != 0;
     CK(cudaMemcpy(h->fire_h, h->fire, sizeof(FireDev), cudaMemcpyDeviceToHost));
