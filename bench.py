@@ -43,6 +43,11 @@ KERNEL_NAMES = ["fire_predictor", "first_derivatives", "force_kick_reduce", "fir
 FUSED_BYTES = {8: 241, 4: 121}
 
 
+# FP64 instructions per deep bulk site of the split force + kick (156 DFMA, 33 DMUL,
+# 21 DADD counted by ncu; 121 of them the 25-point form)
+FP64_OPS_PER_DEEP_SITE = 210
+
+
 def kernel_roofline(lat, esz, N, peak, peak_kind, tag):
     """Dominant kernel of the FIRE iteration, timed with CUDA events per launch."""
     kms, fused = lat.fire_profile(20)
@@ -238,6 +243,19 @@ def run_ours(args, rank, world):
     # whole-iteration view: 241 B/site for the fused ideal (read Q,V,F,types; write Q,V,F)
     it_ms = ms / (K)
     roofline["iteration_achieved_gbs_at_241B"] = 241 * N / (it_ms / 1e3) / 1e9
+    if roofline["kernel"] == "force_kick_split":
+        # the FP64 force + kick is bound by the FP64 pipe, not by HBM: the same launch
+        # against GB300's FP64 instruction rate (2 per SM per cycle, 304 per cycle over
+        # the 152 SMs) at the SM clock sampled during the timed region
+        mhz = (clocks or {}).get("sm_mhz") or 2070.0
+        t = roofline["kernel_ms"]["force_kick_split"] / 1e3
+        achieved = FP64_OPS_PER_DEEP_SITE * N / t / 1e9
+        peak_ops = 304 * mhz * 1e6 / 1e9
+        roofline["fp64_pipe"] = {"ops_per_site": FP64_OPS_PER_DEEP_SITE, "achieved": achieved, "peak": peak_ops,
+                                 "unit": "G FP64 instructions/s", "frac": achieved / peak_ops,
+                                 "source": "ncu dfma + dmul + dadd per deep site "
+                                           "(profiles/k_force_kick_deep_fp64_128cube.md); every site counted at "
+                                           "the deep-site figure"}
     fire_state = {"forceMax": r["forceMax"], "iterations": r["iterations"]}
     lat.close()
     if args.forms == "fp64":
