@@ -12,6 +12,8 @@
 #include <string>
 #include <vector>
 
+#include <cudaTypedefs.h>
+
 #include "../../include/qmin_gb300.h"
 #include "qmin_bulk_forms.h"
 #include "qmin_internal.h"
@@ -37,8 +39,10 @@ static int fail(int code, const std::string &msg)
 
 static const int kSepVariants = 3;  // separate-kernel force + kick with 1, 2, 3 blocks per SM
 // deep-site kernel: 1 or 2 blocks per SM, shared-memory 32x8 or 16x16, and
-// (FP32 only) two sites per thread on 32x8 tiles, z chunks of 8 planes or about two waves of columns
-static const int kSplitVariants = 6;
+// (FP32 only) two sites per thread on 32x8 tiles, z chunks of 8 planes or about
+// two waves of columns, the latter also with TMA staging of interior tiles
+static const int kSplitVariants = 7;
+static const int kSplitTma = 6;
 static const int kSplitFp32First = 4;
 static const int kTuneCandidates = kSepVariants + 2 * kFusedConfigs + 2 * kTiledConfigs + kSplitVariants;
 static_assert(kTuneCandidates == QMIN_TUNE_CANDIDATES, "tuning candidate count");
@@ -50,6 +54,10 @@ struct qmin_ctx {
     size_t esz = 8;
     cudaStream_t stream = nullptr;
     bool own_stream = false;
+    // FP32 Q planes as a TMA tensor map (interior tiles of the split path), built on first use
+    CUtensorMap tmap_q;
+    bool tmap_tried = false, tmap_ok = false;
+    int *dev_err = nullptr;  // set by a kernel whose bounded TMA wait gave up
     // side stream (highest priority) and fork/join events for the listed sites of the split path
     cudaStream_t aux = nullptr;
     cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
@@ -174,6 +182,43 @@ template void fill_boundary_coeffs<double>(const qmin_ldg_params &, double *);
 template void fill_boundary_coeffs<float>(const qmin_ldg_params &, float *);
 }  // namespace qmin
 
+// The FP32 Q planes as a 4-D tensor map (x, y, z, component) for the TMA-staged
+// deep kernel: boxes of 40 x 12 x 1 x 5 floats.  Needs x extent % 4 == 0 (the
+// row pitch must be a multiple of 16 bytes) and a lattice that has interior
+// tiles; the encoder comes from the driver (no link-time dependency).
+static bool ensure_tmap(qmin_ctx *h)
+{
+    if (h->tmap_tried) return h->tmap_ok;
+    h->tmap_tried = true;
+    h->tmap_ok = false;
+    if (h->prec != QMIN_FP32 || h->Lx % 4 != 0 || h->Lx < 40 || h->Ly < 12) return false;
+    void *fn = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+        q != cudaDriverEntryPointSuccess || !fn) {
+        cudaGetLastError();
+        return false;
+    }
+    if (!h->dev_err) {
+        if (cudaMalloc(&h->dev_err, sizeof(int)) != cudaSuccess) {
+            cudaGetLastError();
+            h->dev_err = nullptr;
+            return false;
+        }
+        cudaMemset(h->dev_err, 0, sizeof(int));
+    }
+    auto encode = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(fn);
+    const cuuint64_t dims[4] = {(cuuint64_t)h->Lx, (cuuint64_t)h->Ly, (cuuint64_t)h->Lz, 5};
+    const cuuint64_t strides[3] = {(cuuint64_t)h->Lx * 4, (cuuint64_t)h->Lx * h->Ly * 4, (cuuint64_t)h->P * 4};
+    const cuuint32_t box[4] = {40, 12, 1, 5};
+    const cuuint32_t estr[4] = {1, 1, 1, 1};
+    const CUresult r = encode(&h->tmap_q, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, h->Q, dims, strides, box, estr,
+                              CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                              CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    h->tmap_ok = r == CUDA_SUCCESS;
+    return h->tmap_ok;
+}
+
 template <class T> static Lat<T> make_lat(qmin_ctx *h)
 {
     Lat<T> L;
@@ -193,7 +238,9 @@ template <class T> static Lat<T> make_lat(qmin_ctx *h)
     L.Hv = h->hvar_on ? (const T *)h->hvar : nullptr;
     L.hvp = T(h->params.dchi * h->params.mu0);
     L.cbd = (const T *)h->cbd;
-    L.split = SplitLists{h->split_cls, h->split_sites, h->n_split_sites, h->split_derivs, h->n_split_derivs};
+    if (h->prec == QMIN_FP32) ensure_tmap(h);
+    L.split = SplitLists{h->split_cls, h->split_sites, h->n_split_sites, h->split_derivs, h->n_split_derivs,
+                         h->tmap_ok ? &h->tmap_q : nullptr, h->dev_err};
     return L;
 }
 
@@ -203,7 +250,7 @@ static void free_ctx(qmin_ctx *h)
         if (h->graph[g]) cudaGraphExecDestroy(h->graph[g]);
     void *bufs[] = {h->Q, h->V, h->F, h->D, h->types, h->objs, h->partials, h->stage, h->stage_t, h->fire, h->iter,
                     h->out5, h->M, h->S, h->alt, h->lbp, h->lbs, h->lby, h->Q2, h->V2, h->F2, h->hvar,
-                    h->split_cls, h->split_sites, h->split_derivs, h->cbd};
+                    h->split_cls, h->split_sites, h->split_derivs, h->cbd, h->dev_err};
     for (void *b : bufs)
         if (b) cudaFree(b);
     if (h->fire_h) cudaFreeHost(h->fire_h);
@@ -454,7 +501,8 @@ static int build_split_lists(qmin_ctx *h, const int8_t *t8)
 
 static SplitLists split_lists(const qmin_ctx *h)
 {
-    return SplitLists{h->split_cls, h->split_sites, h->n_split_sites, h->split_derivs, h->n_split_derivs};
+    return SplitLists{h->split_cls, h->split_sites, h->n_split_sites, h->split_derivs, h->n_split_derivs,
+                      h->tmap_ok ? &h->tmap_q : nullptr, h->dev_err};
 }
 
 int qmin_set_state(qmin_handle h, const double *Q, const int32_t *types, int layout)
@@ -847,6 +895,7 @@ template <class T> static int tune_fire(qmin_ctx *h, const Lat<T> &L)
             const float t_dl = timed([&]() { return launch_split_derivs<T>(L, sl, h->fire, h->stream); }, kNoBudget);
             for (int cap = 0; cap < kSplitVariants; ++cap) {
                 if (pinned_out(cap) || (sizeof(T) == 8 && cap >= kSplitFp32First)) continue;
+                if (cap == kSplitTma && !h->tmap_ok) continue;
                 int np = 0;
                 const float t_fk = timed(
                     [&]() {
@@ -1018,6 +1067,15 @@ template <class T> static int fire_impl(qmin_ctx *h, int max_iterations)
     r = run_chunks(h, 0, h->fire, h->fire_h, (remaining + kChunk - 1) / kChunk + 1);
     if (r) return r;
     if (h->path == 1 && (r = settle_pingpong(h, h->fire_h->iterations - it0))) return r;
+    if (h->path == 3 && h->split_cap == kSplitTma && h->dev_err) {
+        int e = 0;
+        CK(cudaMemcpyAsync(&e, h->dev_err, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
+        CK(cudaStreamSynchronize(h->stream));
+        if (e) {
+            cudaMemsetAsync(h->dev_err, 0, sizeof(int), h->stream);
+            return fail(QMIN_ECUDA, "qmin_fire_run: a TMA wait in the deep-site kernel gave up");
+        }
+    }
     h->launches += launch_fire_finish<T>(L, h->fire, h->stream);
     CK(cudaGetLastError());
     CK(cudaMemcpyAsync(h->fire_h, h->fire, sizeof(FireDev), cudaMemcpyDeviceToHost, h->stream));
@@ -1366,6 +1424,9 @@ int qmin_set_fire_variant(qmin_handle h, int variant)
         if (variant >= n) return fail(QMIN_EINVAL, "qmin_set_fire_variant: no such variant of this strategy");
         if (h->fire_mode == QMIN_FIRE_SPLIT && variant >= kSplitFp32First && h->prec != QMIN_FP32)
             return fail(QMIN_EINVAL, "qmin_set_fire_variant: the two-sites-per-thread kernels are FP32 only");
+        if (h->fire_mode == QMIN_FIRE_SPLIT && variant == kSplitTma && !ensure_tmap(h))
+            return fail(QMIN_EINVAL, "qmin_set_fire_variant: TMA staging needs an x extent that is a multiple of 4 "
+                                     "and at least 40 (and a driver that encodes tensor maps)");
     }
     if (h->fire_variant != variant) invalidate_graphs(h);
     h->fire_variant = variant;

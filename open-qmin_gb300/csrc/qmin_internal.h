@@ -1,5 +1,6 @@
 // Internal declarations shared by the qmin_gb300 translation units.
 #pragma once
+#include <cuda.h>  // CUtensorMap (the type only; the encoder is fetched from the driver at run time)
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -27,6 +28,8 @@ struct SplitLists {
     int n_sites;
     const int *derivs;
     int n_derivs;
+    const CUtensorMap *tmap_q;  // host copy of the FP32 Q planes' tensor map (interior tiles by TMA), or null
+    int *err;                   // device word set when a TMA wait gives up
 };
 
 // Everything a lattice kernel needs, passed by value.  Planes are SoA:

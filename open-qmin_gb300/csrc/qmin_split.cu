@@ -542,6 +542,238 @@ __global__ void __launch_bounds__(TX / 2 * TY, MINB)
     }
 }
 
+// TMA staging for the two-sites-per-thread kernel.  An interior tile (its
+// halo inside the lattice, no periodic wrap) takes each plane of Q as one
+// cp.async.bulk.tensor box of (TX + 8) x (TY + 4) sites x 5 components,
+// starting at x = gx0 - 4 so that the box's x coordinate is 16-byte aligned;
+// one thread issues it against an mbarrier per ring slot.  Tiles on the
+// lattice's x or y faces stage the same box with cp.async and the periodic
+// wrap.  Waits are bounded: a wait that gives up sets *err, lets the copies in
+// flight land (bounded again) and leaves the block's partials unwritten.
+namespace {
+__device__ __forceinline__ unsigned smem_addr(const void *p) { return (unsigned)__cvta_generic_to_shared(p); }
+__device__ __forceinline__ void mbar_init(uint64_t *b, unsigned count)
+{
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n" ::"r"(smem_addr(b)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint64_t *b, unsigned bytes)
+{
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(smem_addr(b)), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t *b, unsigned parity)
+{
+    unsigned ok;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(ok)
+        : "r"(smem_addr(b)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+// bounded wait (about a second at most)
+__device__ __forceinline__ bool mbar_wait(uint64_t *b, unsigned parity)
+{
+    for (int it = 0; it < (1 << 22); ++it)
+        if (mbar_try_wait(b, parity)) return true;
+    return false;
+}
+__device__ __forceinline__ void tma_load_4d(void *dst, const CUtensorMap *map, int c0, int c1, int c2, int c3,
+                                            uint64_t *bar)
+{
+    asm volatile(
+        "cp.async.bulk.tensor.4d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4, %5}], "
+        "[%6];\n" ::"r"(smem_addr(dst)),
+        "l"(map), "r"(c0), "r"(c1), "r"(c2), "r"(c3), "r"(smem_addr(bar))
+        : "memory");
+}
+template <int TX, int TY> constexpr size_t deep_pair_tma_smem()
+{
+    return (size_t)kDeepNS * 5 * (TX + 8) * (TY + 4) * sizeof(float) + kDeepNS * sizeof(uint64_t) + 128;
+}
+}  // namespace
+
+template <int TX, int TY, int MINB, bool KICK>
+__global__ void __launch_bounds__(TX / 2 * TY, MINB)
+    k_force_kick_deep_pair_tma(Lat<float> L, const __grid_constant__ CUtensorMap tmap, const uint8_t *__restrict__ cls,
+                               const FireDev *__restrict__ fd, double *partials, int zc, int *err)
+{
+    constexpr int NT = TX / 2 * TY, SX = TX + 8, ROWS = TY + 4, TS = SX * ROWS, NS = kDeepNS;
+    constexpr int NPOS = (TS + NT - 1) / NT;
+    constexpr unsigned kSlotBytes = 5u * TS * sizeof(float);
+    static_assert(kSlotBytes % 128 == 0, "ring slots stay 128-byte aligned");
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    // TMA boxes land on 128-byte boundaries: round the dynamic area up (128 bytes spare are allocated)
+    unsigned char *smem_al = smem_raw + ((128u - (smem_addr(smem_raw) & 127u)) & 127u);
+    float *sQ = reinterpret_cast<float *>(smem_al);                   // [NS][5][ROWS][SX]
+    uint64_t *bar = reinterpret_cast<uint64_t *>(smem_al + NS * kSlotBytes);
+    if (KICK && !fd->active) return;
+    const float hdt = KICK ? 0.5f * float(fd->dt) : 0.f;
+    const int ntx = (L.Lx + TX - 1) / TX;
+    const int gx0 = (blockIdx.x % ntx) * TX, gy0 = (blockIdx.x / ntx) * TY;
+    const int zs = blockIdx.y * zc, ze = min(L.Lz, zs + zc);
+    const long long P = L.P;
+    const int sxy = L.Lx * L.Ly;
+    // the box [gx0 - 4, gx0 + TX + 4) x [gy0 - 2, gy0 + TY + 2) lies inside the lattice
+    const bool use_tma = gx0 >= 4 && gx0 + TX + 4 <= L.Lx && gy0 >= 2 && gy0 + TY + 2 <= L.Ly;
+    if (zs >= L.Lz) return;
+    if (use_tma && threadIdx.x == 0) {
+        for (int k = 0; k < NS; ++k) mbar_init(&bar[k], 1);
+        asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+    }
+    __syncthreads();
+    int off[NPOS];
+#pragma unroll
+    for (int j = 0; j < NPOS; ++j) {
+        const int pp = threadIdx.x + j * NT;
+        off[j] = (!use_tma && pp < TS)
+                     ? wrap_any(gx0 - 4 + pp % SX, L.Lx) + L.Lx * wrap_any(gy0 - 2 + pp / SX, L.Ly)
+                     : -1;
+    }
+    auto slot_of = [&](int z) { return (z - zs + 2) % NS; };            // z >= zs - 2
+    auto parity_of = [&](int z) { return (unsigned)((z - zs + 2) / NS) & 1u; };
+    auto issue = [&](int z) {
+        const int sl = slot_of(z);
+        if (use_tma) {
+            if (threadIdx.x == 0) {
+                mbar_expect_tx(&bar[sl], kSlotBytes);
+                tma_load_4d(sQ + sl * 5 * TS, &tmap, gx0 - 4, gy0 - 2, wrap_any(z, L.Lz), 0, &bar[sl]);
+            }
+        } else {
+            const long long base = (long long)sxy * wrap_any(z, L.Lz);
+#pragma unroll
+            for (int j = 0; j < NPOS; ++j) {
+                if (off[j] < 0) continue;
+                const int pp = threadIdx.x + j * NT;
+#pragma unroll
+                for (int k = 0; k < 5; ++k) cp_async_q(&sQ[(sl * 5 + k) * TS + pp], L.Q + k * P + base + off[j]);
+            }
+        }
+        asm volatile("cp.async.commit_group;\n" ::: "memory");
+    };
+    int issued = zs + 2, waited = zs - 3;  // planes issued / known complete (TMA)
+    float sacc[3] = {0.f, 0.f, 0.f};
+    bool aborted = false;
+    for (int z = zs - 2; z <= zs + 2; ++z) issue(z);
+    const int px = threadIdx.x % (TX / 2), ly = threadIdx.x / (TX / 2);
+    const int gx = gx0 + 2 * px, gy = gy0 + ly;
+    const bool in_a = gx < L.Lx && gy < L.Ly, in_b = gx + 1 < L.Lx && gy < L.Ly;
+    const long long i0 = (long long)gx + (long long)L.Lx * gy;
+    const int p = (ly + 2) * SX + (2 * px + 4);
+    uint8_t ca_next = 1, cb_next = 1;
+    float va_next[5], vb_next[5];
+    auto fetch = [&](int z) {
+        ca_next = cb_next = 1;
+        if (z < ze) {
+            const long long i = i0 + (long long)sxy * z;
+            if (in_a) {
+                ca_next = cls[i];
+                if (KICK)
+#pragma unroll
+                    for (int k = 0; k < 5; ++k) va_next[k] = L.V[k * P + i];
+            }
+            if (in_b) {
+                cb_next = cls[i + 1];
+                if (KICK)
+#pragma unroll
+                    for (int k = 0; k < 5; ++k) vb_next[k] = L.V[k * P + i + 1];
+            }
+        }
+    };
+    fetch(zs);
+    for (int z = zs; z < ze; ++z) {
+        if (z + 3 <= ze + 1) {
+            issue(z + 3);
+            issued = z + 3;
+        } else {
+            asm volatile("cp.async.commit_group;\n" ::: "memory");
+        }
+        const uint8_t ca = ca_next, cb = cb_next;
+        float va[5], vb[5];
+#pragma unroll
+        for (int k = 0; k < 5; ++k) {
+            va[k] = va_next[k];
+            vb[k] = vb_next[k];
+        }
+        fetch(z + 1);
+        bool ok = true;
+        if (use_tma) {
+            for (int w = waited + 1; w <= z + 2 && ok; ++w) ok = mbar_wait(&bar[slot_of(w)], parity_of(w));
+            if (ok) waited = z + 2;
+        } else {
+            asm volatile("cp.async.wait_group 1;\n" ::: "memory");
+        }
+        if (__syncthreads_or(!ok)) {
+            aborted = true;
+            break;
+        }
+        if (!KICK) {
+            const long long i = i0 + (long long)sxy * z;
+            if (ca == 2)
+#pragma unroll
+                for (int k = 0; k < 5; ++k) L.F[k * P + i] = 0.f;
+            if (cb == 2)
+#pragma unroll
+                for (int k = 0; k < 5; ++k) L.F[k * P + i + 1] = 0.f;
+        }
+        if (ca == 0 || cb == 0) {
+            const long long i = i0 + (long long)sxy * z;
+            int sb[5];
+#pragma unroll
+            for (int d = 0; d < 5; ++d) sb[d] = slot_of(z + d - 2) * 5 * TS + p;
+            float fa[5], fb[5];
+            deep_force_pair_tile<TS, SX>(L, sQ, sb, i, in_b ? i + 1 : i, fa, fb);
+            if (ca == 0) {
+#pragma unroll
+                for (int k = 0; k < 5; ++k) L.F[k * P + i] = fa[k];
+                if (KICK) {
+#pragma unroll
+                    for (int k = 0; k < 5; ++k) {
+                        va[k] += hdt * fa[k];
+                        L.V[k * P + i] = va[k];
+                    }
+                    sacc[0] += dot_qt(fa, fa);
+                    sacc[1] += dot_qt(va, va);
+                    sacc[2] += dot_qt(fa, va);
+                }
+            }
+            if (cb == 0) {
+#pragma unroll
+                for (int k = 0; k < 5; ++k) L.F[k * P + i + 1] = fb[k];
+                if (KICK) {
+#pragma unroll
+                    for (int k = 0; k < 5; ++k) {
+                        vb[k] += hdt * fb[k];
+                        L.V[k * P + i + 1] = vb[k];
+                    }
+                    sacc[0] += dot_qt(fb, fb);
+                    sacc[1] += dot_qt(vb, vb);
+                    sacc[2] += dot_qt(fb, vb);
+                }
+            }
+        }
+        __syncthreads();
+    }
+    if (aborted) {
+        // let the boxes still in flight land before the block's shared memory goes away
+        if (use_tma && threadIdx.x == 0) {
+            for (int w = waited + 1; w <= issued; ++w) mbar_wait(&bar[slot_of(w)], parity_of(w));
+            atomicExch(err, 1);
+        }
+        asm volatile("cp.async.wait_all;\n" ::: "memory");
+        return;
+    }
+    asm volatile("cp.async.wait_all;\n" ::: "memory");
+    if constexpr (KICK) {
+        double acc[3] = {(double)sacc[0], (double)sacc[1], (double)sacc[2]};
+        block_sum<3, NT>(acc);
+        if (threadIdx.x == 0) {
+            const int b = blockIdx.y * gridDim.x + blockIdx.x;
+#pragma unroll
+            for (int k = 0; k < 3; ++k) partials[3 * b + k] = acc[k];
+        }
+    }
+}
+
 // shared-memory deep kernel over TX x TY columns of kDeepZc planes (more when
 // the grid would not fit the partials buffer); returns its block count
 template <class T, int TX, int TY>
@@ -589,6 +821,30 @@ static int launch_deep_pair(const Lat<float> &L, const SplitLists &sl, FireDev *
     return ntiles * nz;
 }
 
+// the TMA-staged two-sites-per-thread kernel (FP32, z chunks of about two
+// waves); -1 when the lattice has no tensor map (x extent not a multiple of 4)
+template <int TX, int TY, int MINB, bool KICK = true>
+static int launch_deep_pair_tma(const Lat<float> &L, const SplitLists &sl, FireDev *fd, double *partials,
+                                cudaStream_t s)
+{
+    if (!sl.tmap_q || !sl.err) return -1;
+    constexpr size_t sm = deep_pair_tma_smem<TX, TY>();
+    static bool attr_set = false;
+    if (!attr_set) {
+        // a failure here surfaces as the launch's error
+        attr_set = cudaFuncSetAttribute(k_force_kick_deep_pair_tma<TX, TY, MINB, KICK>,
+                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm) == cudaSuccess;
+    }
+    const int ntiles = ((L.Lx + TX - 1) / TX) * ((L.Ly + TY - 1) / TY);
+    const long long nzt = std::max(1LL, 2LL * 152 * MINB / ntiles);
+    int zc = std::max(kDeepZc, (int)((L.Lz + nzt - 1) / nzt));
+    while ((long long)ntiles * ((L.Lz + zc - 1) / zc) > kMaxFusedBlocks - 1024) ++zc;
+    const int nz = (L.Lz + zc - 1) / zc;
+    k_force_kick_deep_pair_tma<TX, TY, MINB, KICK>
+        <<<dim3(ntiles, nz), TX / 2 * TY, sm, s>>>(L, *sl.tmap_q, sl.cls, fd, partials, zc, sl.err);
+    return ntiles * nz;
+}
+
 template <class T> int launch_split_derivs(const Lat<T> &L, const SplitLists &sl, FireDev *fd, cudaStream_t s)
 {
     if (sl.n_derivs == 0) return 0;
@@ -602,9 +858,13 @@ int launch_split_deep(const Lat<T> &L, const SplitLists &sl, FireDev *fd, double
 {
     if (cap == 2) return launch_deep_tiled<T, 32, 8>(L, sl, fd, partials, s);
     if (cap == 3) return launch_deep_tiled<T, 16, 16>(L, sl, fd, partials, s);
-    if (cap == 4 || cap == 5) {
-        if constexpr (sizeof(T) == 4) return launch_deep_pair<32, 8, 3>(L, sl, fd, partials, cap == 5, s);
-        else return -1;  // FP32 only (the autotuner does not offer it for FP64)
+    if (cap == 4 || cap == 5 || cap == 6) {
+        if constexpr (sizeof(T) == 4) {
+            if (cap == 6) return launch_deep_pair_tma<32, 8, 3>(L, sl, fd, partials, s);
+            return launch_deep_pair<32, 8, 3>(L, sl, fd, partials, cap == 5, s);
+        } else {
+            return -1;  // FP32 only (the autotuner does not offer it for FP64)
+        }
     }
     if (cap == 1) k_force_kick_deep<T, 1><<<grid, kBlock, 0, s>>>(L, sl.cls, fd, partials);
     else k_force_kick_deep<T, 0><<<grid, kBlock, 0, s>>>(L, sl.cls, fd, partials);

@@ -216,21 +216,24 @@ def test_fused_matches_separate_kernels(qmin, oracle, L, prec, other):
         assert rel_err(b, a) <= tol
 
 
-@pytest.mark.parametrize("L", [(16, 9, 7), (40, 33, 21), (65, 17, 30)])
+@pytest.mark.parametrize("L", [(16, 9, 7), (40, 33, 21), (65, 17, 30), (104, 30, 20)])
 @pytest.mark.parametrize("prec", [0, 1])
-@pytest.mark.parametrize("variant", [0, 1, 2, 3, 4, 5])
+@pytest.mark.parametrize("variant", [0, 1, 2, 3, 4, 5, 6])
 def test_split_variants_match_separate(qmin, oracle, L, prec, variant):
     """Each pinned deep-site kernel of the split force + kick (0, 1: global
     memory at 1 or 2 blocks per SM; 2, 3: shared-memory tiles of 32 x 8 and
     16 x 16 sites, whose halos wrap across the periodic faces of lattices
     narrower than a tile; 4, 5, FP32 only: two x-adjacent sites per thread,
-    the second past the edge of an odd Lx) tracks the separate kernels, with
-    an L4 term and an external field: FP64 to 1e-12 after 7 iterations, FP32
-    to 1e-5."""
+    the second past the edge of an odd Lx; 6, FP32 only: the same with the
+    interior tiles' planes staged by TMA, which the 104 x 30 x 20 lattice has
+    beside its periodic edge tiles) tracks the separate kernels, with an L4
+    term and an external field: FP64 to 1e-12 after 7 iterations, FP32 to
+    1e-5."""
     cfg = parse_args([f"L={L[0]},{L[1]},{L[2]}", "seed=13", "Ls=2.32,1.0,0.5,0.3,0", "wall=2,0,h,5.3",
                       f"sphere={L[0] / 2},{L[1] / 2},{L[2] / 2},{min(L) / 4},p,2.0", "H=0.1,0.2,0.3,0.5,1.0,0.2"])
     s = oracle_system(oracle, cfg)
-    if variant >= 4 and prec == 0:
+    tma_ok = L[0] % 4 == 0 and L[0] >= 40 and L[1] >= 12
+    if (variant >= 4 and prec == 0) or (variant == 6 and not tma_ok):
         lat = gpu_lattice(qmin, s, prec)
         lat.set_fire_kernel(4)
         with pytest.raises(qmin.QminError):
@@ -248,7 +251,8 @@ def test_split_variants_match_separate(qmin, oracle, L, prec, variant):
     t = res[1][2]
     assert t["path"] == "split" and t["variant"] == variant
     assert list(t["candidates_ms"]) == [["split_1blk", "split_2blk", "split_smem_32x8", "split_smem_16x16",
-                                         "split_pair_32x8_z8", "split_pair_32x8_zfit"][variant]]
+                                         "split_pair_32x8_z8", "split_pair_32x8_zfit",
+                                         "split_pair_tma_32x8"][variant]]
     tol = 1e-12 if prec == 0 else 1e-5
     assert res[0][0]["iterations"] == res[1][0]["iterations"] == 7
     assert abs(res[0][0]["forceMax"] - res[1][0]["forceMax"]) <= tol * res[0][0]["forceMax"]
@@ -265,7 +269,7 @@ def test_fire_variant_pin_errors(qmin, oracle):
         lat.set_fire_variant(0)  # FIRE_AUTO
     lat.set_fire_kernel(4)
     with pytest.raises(qmin.QminError):
-        lat.set_fire_variant(6)
+        lat.set_fire_variant(7)
     with pytest.raises(qmin.QminError):
         lat.set_fire_variant(-2)
     lat.set_fire_variant(3)
