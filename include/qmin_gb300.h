@@ -341,6 +341,10 @@ int qmin_warmnet_adam_step(qmin_warmnet n, double lr, double beta1, double beta2
 int qmin_warmnet_write_state(qmin_warmnet n, int sample, void *Q_dev, int precision, long long plane_stride,
                              const int8_t *types_dev);
 int qmin_warmnet_sync(qmin_warmnet n);
+/* Tensor-core instruction family of the convolutions: 1 (default) the
+ * 5th-generation tcgen05.mma with tensor-memory accumulators, 0 the mma.sync
+ * kernels.  Both compute BF16 x BF16 -> FP32.  No reference counterpart. */
+int qmin_warmnet_set_tensor_path(qmin_warmnet n, int tcgen05);
 int qmin_warmnet_kernel_launches(qmin_warmnet n, long long *count);
 /* Warm-start a lattice in place: features from its current Q, types and
  * objects, one forward pass, the prediction written into its Q on the sites

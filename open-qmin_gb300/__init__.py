@@ -41,6 +41,7 @@ EXPORTED_SYMBOLS = [
     "qmin_warmnet_set_stream", "qmin_warmnet_param_count", "qmin_warmnet_shape", "qmin_warmnet_buffers",
     "qmin_warmnet_set_params", "qmin_warmnet_get_params", "qmin_warmnet_features", "qmin_warmnet_forward",
     "qmin_warmnet_backward", "qmin_warmnet_adam_step", "qmin_warmnet_write_state", "qmin_warmnet_sync",
+    "qmin_warmnet_set_tensor_path",
     "qmin_warmnet_kernel_launches", "qmin_warm_start",
 ]
 FIRE_SEPARATE, FIRE_FUSED, FIRE_AUTO, FIRE_TILED, FIRE_SPLIT = 0, 1, 2, 3, 4
@@ -136,6 +137,7 @@ def lib():
             "qmin_warmnet_adam_step": [h, C.c_double, C.c_double, C.c_double, C.c_double],
             "qmin_warmnet_write_state": [h, C.c_int, vp, C.c_int, C.c_longlong, vp],
             "qmin_warmnet_sync": [h], "qmin_warmnet_kernel_launches": [h, C.POINTER(C.c_longlong)],
+            "qmin_warmnet_set_tensor_path": [h, C.c_int],
             "qmin_warm_start": [h, h],
             "qmin_host_add_wall": [C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_double, C.c_double, dp,
                                    ip, C.POINTER(Object), ip],
@@ -544,6 +546,10 @@ class WarmNet:
             self.close()
         except Exception:
             pass
+
+    def set_tensor_path(self, tcgen05=True):
+        """Convolutions on tcgen05.mma with tensor-memory accumulators (default) or on mma.sync."""
+        _check(lib().qmin_warmnet_set_tensor_path(self._h, 1 if tcgen05 else 0))
 
     def set_stream(self, stream_ptr):
         _check(lib().qmin_warmnet_set_stream(self._h, C.c_void_p(stream_ptr)))

@@ -167,6 +167,206 @@ __global__ void __launch_bounds__(128) k_conv_gemm(Geo g, const bf16 *__restrict
     }
 }
 
+// ---- the same implicit GEMM on the 5th-generation tensor cores (tcgen05)
+//
+// A CTA computes 128 GEMM rows x all cout columns.  Per tap, the 128
+// gathered activation rows (A, 128 x cin) and the tap's weights (B, cout x
+// cin) are staged in shared memory in the canonical no-swizzle K-major
+// layout: 8-row x 16-byte core matrices, core matrix (m8, k8) at
+// (m8 * cin/8 + k8) * 128 bytes, so the descriptors' leading (K) byte offset is
+// 128 and their stride (M/N) byte offset cin/8 * 128.  One thread issues
+// cin/16 tcgen05.mma (kind::f16, BF16 x BF16 -> FP32, M = 128, N = cout,
+// K = 16) into an accumulator in tensor memory and commits them to the
+// stage's mbarrier; two stage buffers let the next tap's gather overlap the
+// MMAs.  The epilogue reads each warp's 32 accumulator rows with tcgen05.ld.
+// Every wait is bounded; a wait that gives up sets g_conv_err, and the CTA
+// still frees its tensor memory.
+__device__ int g_conv_err;
+
+namespace {
+__device__ __forceinline__ unsigned s_addr(const void *p) { return (unsigned)__cvta_generic_to_shared(p); }
+
+// shared-memory matrix descriptor, no swizzle, K-major (SM100 format: version 1 at bits 46-47)
+__device__ __forceinline__ uint64_t umma_desc(unsigned saddr, unsigned lbo, unsigned sbo)
+{
+    return (uint64_t)((saddr >> 4) & 0x3FFFu) | ((uint64_t)((lbo >> 4) & 0x3FFFu) << 16) |
+           ((uint64_t)((sbo >> 4) & 0x3FFFu) << 32) | ((uint64_t)1 << 46);
+}
+// instruction descriptor, kind::f16: FP32 accumulator, BF16 A and B, both K-major, N, M = 128
+__host__ __device__ constexpr uint32_t umma_idesc(int n)
+{
+    return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(n >> 3) << 17) | ((uint32_t)(128 >> 4) << 24);
+}
+__device__ __forceinline__ bool mbar_wait_bounded(unsigned bar, unsigned parity)
+{
+    for (int it = 0; it < (1 << 22); ++it) {
+        unsigned ok;
+        asm volatile(
+            "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+            : "=r"(ok)
+            : "r"(bar), "r"(parity)
+            : "memory");
+        if (ok) return true;
+    }
+    return false;
+}
+}  // namespace
+
+// tensor-memory columns for an accumulator of n FP32 columns (a power of two >= 32)
+static int umma_cols(int n)
+{
+    int c = 32;
+    while (c < n) c <<= 1;
+    return c;
+}
+// dynamic shared memory of k_conv_umma: two stages of A and B, two mbarriers,
+// the tensor-memory address; padded so that at most 512 / cols CTAs share an SM
+// and a tcgen05.alloc never waits
+static size_t umma_smem(int cin, int n)
+{
+    const size_t need = 2 * (size_t)(128 + n) * cin * 2 + 64;
+    const int per_sm = 512 / umma_cols(n);
+    const size_t floor_bytes = (size_t)(232448 / per_sm) - 1024 + 1;  // more than 1/(per_sm+1) of the SM's 227 KB
+    return std::max(need, std::min<size_t>(floor_bytes, 232448 - 1024));
+}
+
+template <int N, bool OUT_BF16>
+__global__ void __launch_bounds__(128) k_conv_umma(Geo g, const bf16 *__restrict__ in, const bf16 *__restrict__ w,
+                                                   const float *__restrict__ bias, const float *__restrict__ addend,
+                                                   void *out, int relu, int rows)
+{
+    static_assert(N % 16 == 0 && N >= 16 && N <= 256, "tcgen05 M=128 needs N a multiple of 16 in [16, 256]");
+    constexpr int COLS = N <= 32 ? 32 : (N <= 64 ? 64 : (N <= 128 ? 128 : 256));
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    const int cin = g.cin, kc8 = cin >> 3, K = g.taps * cin;
+    const size_t a_bytes = (size_t)128 * cin * 2, b_bytes = (size_t)N * cin * 2;
+    unsigned char *bufA[2] = {smem_raw, smem_raw + a_bytes + b_bytes};
+    unsigned char *bufB[2] = {smem_raw + a_bytes, smem_raw + 2 * a_bytes + b_bytes};
+    uint64_t *bar = reinterpret_cast<uint64_t *>(smem_raw + 2 * (a_bytes + b_bytes));
+    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(bar + 2);
+    const int tid = threadIdx.x, warp = tid >> 5;
+    const int row = blockIdx.x * 128 + tid;
+    // an earlier CTA's wait gave up: the launch's results are void, do no more work
+    if (*(volatile int *)&g_conv_err) return;
+
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(s_addr(tmem_slot)),
+                     "r"(COLS)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n" ::: "memory");
+    }
+    if (tid == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(s_addr(&bar[0])) : "memory");
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(s_addr(&bar[1])) : "memory");
+        asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+    const uint32_t tmem = *tmem_slot;
+
+    bool ok = true;
+    for (int tap = 0; tap < g.taps; ++tap) {
+        const int b = tap & 1;
+        if (tap >= 2) {
+            // the MMAs of tap - 2 have read this buffer
+            const bool w_ok = mbar_wait_bounded(s_addr(&bar[b]), (unsigned)((tap - 2) >> 1) & 1u);
+            if (__syncthreads_or(!w_ok)) {
+                ok = false;
+                break;
+            }
+        }
+        // A: this thread's row, cin channels of the tap's source voxel (zeros outside)
+        {
+            const int src = row < rows ? gather_src(g, row, tap) : -1;
+            const uint4 *sp = reinterpret_cast<const uint4 *>(in + (size_t)(src < 0 ? 0 : src) * cin);
+            unsigned char *dst = bufA[b] + (size_t)(tid >> 3) * kc8 * 128 + (tid & 7) * 16;
+            for (int k8 = 0; k8 < kc8; ++k8) {
+                const uint4 v = src >= 0 ? sp[k8] : make_uint4(0, 0, 0, 0);
+                *reinterpret_cast<uint4 *>(dst + k8 * 128) = v;
+            }
+        }
+        // B: the tap's weights, N x cin
+        for (int e = tid; e < N * kc8; e += 128) {
+            const int co = e / kc8, k8 = e - co * kc8;
+            const uint4 v = *reinterpret_cast<const uint4 *>(w + (size_t)co * K + (size_t)tap * cin + k8 * 8);
+            *reinterpret_cast<uint4 *>(bufB[b] + ((size_t)(co >> 3) * kc8 + k8) * 128 + (co & 7) * 16) = v;
+        }
+        // generic-proxy stores -> visible to the tensor cores' async proxy
+        asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+        __syncthreads();
+        if (tid == 0) {
+            asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+            const unsigned sa = s_addr(bufA[b]), sb = s_addr(bufB[b]);
+            const unsigned sbo = (unsigned)kc8 * 128u;
+            for (int kk = 0; kk < (cin >> 4); ++kk) {
+                const uint64_t da = umma_desc(sa + kk * 256, 128, sbo);
+                const uint64_t db = umma_desc(sb + kk * 256, 128, sbo);
+                const unsigned acc = (tap > 0 || kk > 0) ? 1u : 0u;
+                asm volatile(
+                    "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+                    " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem),
+                    "l"(da), "l"(db), "r"(umma_idesc(N)), "r"(acc)
+                    : "memory");
+            }
+            asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(
+                             s_addr(&bar[b]))
+                         : "memory");
+        }
+    }
+    if (ok) {
+        // the last commit covers every MMA this CTA issued
+        const int last = g.taps - 1;
+        const bool w_ok = mbar_wait_bounded(s_addr(&bar[last & 1]), (unsigned)(last >> 1) & 1u);
+        ok = !__syncthreads_or(!w_ok);
+    }
+    if (ok) {
+        asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+        const uint32_t taddr = tmem + ((uint32_t)(warp * 32) << 16);
+#pragma unroll
+        for (int c0 = 0; c0 < N; c0 += 8) {
+            uint32_t r[8];
+            asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];\n"
+                         : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+                           "=r"(r[7])
+                         : "r"(taddr + c0));
+            asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
+            float v[8];
+#pragma unroll
+            for (int e = 0; e < 8; ++e) {
+                v[e] = __uint_as_float(r[e]) + (bias ? bias[c0 + e] : 0.f);
+                if (relu) v[e] = fmaxf(v[e], 0.f);
+            }
+            if (row < rows) {
+                if (OUT_BF16) {
+                    bf16 *o = reinterpret_cast<bf16 *>(out) + (size_t)row * N + c0;
+                    __nv_bfloat162 h[4];
+#pragma unroll
+                    for (int e = 0; e < 4; ++e) h[e] = __floats2bfloat162_rn(v[2 * e], v[2 * e + 1]);
+                    *reinterpret_cast<uint4 *>(o) = *reinterpret_cast<const uint4 *>(h);
+                } else {
+                    float *o = reinterpret_cast<float *>(out) + (size_t)row * N + c0;
+                    if (addend) {
+                        const float *a = addend + (size_t)row * N + c0;
+#pragma unroll
+                        for (int e = 0; e < 8; ++e) v[e] += a[e];
+                    }
+                    *reinterpret_cast<float4 *>(o) = make_float4(v[0], v[1], v[2], v[3]);
+                    *reinterpret_cast<float4 *>(o + 4) = make_float4(v[4], v[5], v[6], v[7]);
+                }
+            }
+        }
+    } else if (tid == 0) {
+        // a wait gave up: let the MMAs in flight finish (bounded) before the buffers go away
+        for (int b = 0; b < 2; ++b) mbar_wait_bounded(s_addr(&bar[b]), 0u), mbar_wait_bounded(s_addr(&bar[b]), 1u);
+        atomicExch(&g_conv_err, 1);
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+    __syncthreads();
+    if (warp == 0)
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "r"(COLS) : "memory");
+}
+
 // dW[co][tap][ci] += sum_v dout[v][co] * in[src(v,tap)][ci] over rows
 // [blockIdx.x * chunk, +chunk): block tile 64 co x 64 ci for one tap, the
 // row dimension staged through shared memory 16 rows at a time; each block
@@ -426,10 +626,36 @@ __global__ void k_write_state(const float *y, T *Q, long long P, const int8_t *t
 
 static int grid1(long long n) { return (int)std::max<long long>(1, std::min<long long>((n + 255) / 256, 152 * 16)); }
 
-template <bool OB>
-static void conv_gemm(const Geo &g, const bf16 *in, const bf16 *w, const float *bias, const float *addend, void *out,
+template <int N, bool OB>
+static void conv_umma(const Geo &g, const bf16 *in, const bf16 *w, const float *bias, const float *addend, void *out,
                       int relu, int rows, cudaStream_t s)
 {
+    static int attr_bytes = 0;
+    const size_t sm = umma_smem(g.cin, N);
+    if ((int)sm > attr_bytes) {
+        // a failure here surfaces as the launch's error
+        if (cudaFuncSetAttribute(k_conv_umma<N, OB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm) ==
+            cudaSuccess)
+            attr_bytes = (int)sm;
+    }
+    k_conv_umma<N, OB><<<(rows + 127) / 128, 128, sm, s>>>(g, in, w, bias, addend, out, relu, rows);
+}
+
+// tcgen05: the 5th-generation tensor-core kernel above; otherwise mma.sync
+template <bool OB>
+static void conv_gemm(const Geo &g, const bf16 *in, const bf16 *w, const float *bias, const float *addend, void *out,
+                      int relu, int rows, cudaStream_t s, bool tcgen05)
+{
+    if (tcgen05) {
+        switch (g.cout) {
+        case 16: conv_umma<16, OB>(g, in, w, bias, addend, out, relu, rows, s); return;
+        case 32: conv_umma<32, OB>(g, in, w, bias, addend, out, relu, rows, s); return;
+        case 48: conv_umma<48, OB>(g, in, w, bias, addend, out, relu, rows, s); return;
+        case 64: conv_umma<64, OB>(g, in, w, bias, addend, out, relu, rows, s); return;
+        case 128: conv_umma<128, OB>(g, in, w, bias, addend, out, relu, rows, s); return;
+        default: break;
+        }
+    }
     const int blocks = (rows + 63) / 64;
     switch (g.cout / 8) {
     case 2: k_conv_gemm<2, OB><<<blocks, 128, 0, s>>>(g, in, w, bias, addend, out, relu, rows); break;
@@ -474,6 +700,7 @@ struct qmin_warmnet_ctx {
     bool own_stream = false;
     long long adam_t = 0;
     long long launches = 0;
+    bool tcgen05 = true;  // convolutions on tcgen05 (else mma.sync)
 };
 
 namespace {
@@ -552,8 +779,11 @@ void run_layer(qmin_warmnet_ctx *n, int i, const bf16 *in, float *f32out)
     const Layer &L = n->layers[i];
     const Geo g = fwd_geo(n, L);
     const int rows = (int)rows_at(n, out_level(L));
-    if (f32out) conv_gemm<false>(g, in, n->pb + L.woff, n->p + L.boff, nullptr, f32out, L.relu, rows, n->stream);
-    else conv_gemm<true>(g, in, n->pb + L.woff, n->p + L.boff, nullptr, n->act[i], L.relu, rows, n->stream);
+    if (f32out)
+        conv_gemm<false>(g, in, n->pb + L.woff, n->p + L.boff, nullptr, f32out, L.relu, rows, n->stream, n->tcgen05);
+    else
+        conv_gemm<true>(g, in, n->pb + L.woff, n->p + L.boff, nullptr, n->act[i], L.relu, rows, n->stream,
+                        n->tcgen05);
 }
 
 // backward of layer i: gout is the FP32 gradient w.r.t. the layer's output
@@ -596,7 +826,7 @@ void layer_backward(qmin_warmnet_ctx *n, int i, const float *gout, const bf16 *a
     const int flip = (L.stride == 1 && L.taps == 27) ? 1 : 0;
     k_dgrad_weights<<<grid1((long long)L.cout * L.cin * L.taps), 256, 0, s>>>(n->pb + L.woff, n->wd, L.cout, L.cin,
                                                                               L.taps, flip);
-    conv_gemm<false>(d, n->gbf, n->wd, nullptr, addend, gin, 0, (int)rows_in, s);
+    conv_gemm<false>(d, n->gbf, n->wd, nullptr, addend, gin, 0, (int)rows_in, s, n->tcgen05);
     n->launches += 2;
 }
 
@@ -878,7 +1108,25 @@ int qmin_warmnet_sync(qmin_warmnet n)
 {
     if (!n) return nfail(QMIN_EINVAL, "qmin_warmnet_sync: null handle");
     const cudaError_t e = cudaStreamSynchronize(n->stream);
-    return e == cudaSuccess ? QMIN_OK : nfail(QMIN_ECUDA, std::string("qmin_warmnet_sync: ") + cudaGetErrorString(e));
+    if (e != cudaSuccess) return nfail(QMIN_ECUDA, std::string("qmin_warmnet_sync: ") + cudaGetErrorString(e));
+    int err = 0;
+    if (cudaMemcpyFromSymbol(&err, g_conv_err, sizeof(int)) != cudaSuccess) {
+        cudaGetLastError();
+        return QMIN_OK;
+    }
+    if (err) {
+        const int zero = 0;
+        cudaMemcpyToSymbol(g_conv_err, &zero, sizeof(int));
+        return nfail(QMIN_ECUDA, "qmin_warmnet_sync: a tensor-core wait in a convolution gave up");
+    }
+    return QMIN_OK;
+}
+
+int qmin_warmnet_set_tensor_path(qmin_warmnet n, int tcgen05)
+{
+    if (!n) return nfail(QMIN_EINVAL, "qmin_warmnet_set_tensor_path: null handle");
+    n->tcgen05 = tcgen05 != 0;
+    return QMIN_OK;
 }
 
 int qmin_warmnet_kernel_launches(qmin_warmnet n, long long *count)

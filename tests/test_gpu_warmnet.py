@@ -97,6 +97,41 @@ def test_forward_matches_torch_fp64(qmin, L):
     assert err <= 3e-2, err
 
 
+@pytest.mark.parametrize("L", [(16, 16, 16), (24, 8, 16)])
+def test_tcgen05_matches_mma_sync(qmin, L):
+    """The tcgen05 convolutions (tensor-memory accumulators) against the
+    mma.sync ones on the same BF16 operands: every layer's output agrees to
+    FP32 accumulation order and the BF16 rounding of the activations between
+    layers (final output normwise relative difference <= 1e-2), the loss to
+    1e-2 and every parameter gradient to 2e-2."""
+    sols = []
+    for seed in (71, 72):
+        s = _lattice(qmin, seed, max(L))
+        if L != (max(L),) * 3:
+            side = max(L)
+            idx = np.arange(side ** 3).reshape(side, side, side)[:L[2], :L[1], :L[0]].ravel()
+            s = dict(s, L=L, Q=np.ascontiguousarray(s["Q"][idx]), types=np.ascontiguousarray(s["types"][idx]))
+        sols.append(s)
+    rng = np.random.default_rng(9)
+    n = L[0] * L[1] * L[2]
+    tgt = torch.as_tensor((0.3 * rng.standard_normal((2, n, 5))).astype(np.float32)).cuda()
+    outs = []
+    for tc in (False, True):
+        net, _keep = _net_with_inputs(qmin, sols, train=True)
+        net.set_tensor_path(tc)
+        net.forward()
+        torch.cuda.synchronize()
+        loss = net.backward(tgt.data_ptr())
+        net.sync()
+        _x, y, _m = net.torch_views()
+        outs.append((y.float().cpu().numpy().astype(np.float64), loss, net.get_params(grads=True)[1]))
+    (y0, l0, g0), (y1, l1, g1) = outs
+    assert np.isfinite(y1).all()
+    assert np.linalg.norm(y1 - y0) <= 1e-2 * np.linalg.norm(y0)
+    assert abs(l1 - l0) <= 1e-2 * abs(l0)
+    assert np.linalg.norm(g1 - g0) <= 2e-2 * np.linalg.norm(g0)
+
+
 def test_backward_matches_torch_fp64(qmin):
     L = (16, 16, 16)
     sols = [_lattice(qmin, s, 16) for s in (31, 32)]
