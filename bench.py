@@ -479,6 +479,54 @@ def warm_start_c2(q, consts, g, t64, t32):
     return w
 
 
+def run_warmnet(args):
+    """The warm-start net's forward pass on the c2 lattice (or --lattice N^3):
+    W untimed passes, then K passes timed with CUDA events on the net's
+    stream, for the tcgen05 and the mma.sync convolutions.  FLOPs are the
+    convolutions' 2 x rows x cout x taps x cin."""
+    import torch
+    import __graft_entry__ as ge
+    q = ge.load_package()
+    consts, g = build_workload_host(q)
+    L = WORKLOAD["L"]
+    lat = make_lattice(q, consts, g, q.FP32)
+    lat.set_state(g.Q, g.types)
+    params = np.load(WARMNET_WEIGHTS)["params"]
+    flops = 0
+    for cin, cout, taps, stride, level in [(16, 32, 27, 1, 0), (32, 48, 27, 2, 0), (48, 64, 27, 2, 1),
+                                           (64, 128, 27, 2, 2), (128, 64, 1, 1, 3), (64, 64, 27, 1, 2),
+                                           (64, 48, 1, 1, 2), (48, 48, 27, 1, 1), (48, 32, 1, 1, 1),
+                                           (32, 32, 27, 1, 0), (32, 16, 1, 1, 0)]:
+        out_level = level + (1 if stride == 2 else 0)
+        rows = (L[0] >> out_level) * (L[1] >> out_level) * (L[2] >> out_level)
+        flops += 2 * rows * cout * taps * cin
+    out = {"metric": "warm-start net forward", "unit": "TFLOP/s", "sites": L[0] * L[1] * L[2],
+           "conv_gflop_per_forward": flops / 1e9, "config": {"workload": f"{L[0]}^3 c2 geometry, batch 1"}}
+    for tc in (True, False):
+        net = q.WarmNet(1, L)
+        net.set_params(params)
+        net.set_tensor_path(tc)
+        st = torch.cuda.Stream()
+        net.set_stream(st.cuda_stream)
+        lat.warm_start(net)  # features + forward + write-back once
+        for _ in range(args.warmup):
+            net.forward()
+        net.sync()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record(st)
+        for _ in range(args.steps):
+            net.forward()
+        e1.record(st)
+        net.sync()
+        ms = e0.elapsed_time(e1) / args.steps
+        out["tcgen05" if tc else "mma_sync"] = {"ms_per_forward": ms, "tflops": flops / (ms / 1e3) / 1e12}
+        net.close()
+    out["value"] = out["tcgen05"]["tflops"]
+    lat.close()
+    return out
+
+
 def run_c4(q, ntest=64):
     """The learned warm start on c4 test solves (64^3, seeds 100000..), judged by the protocol."""
     import importlib
@@ -663,7 +711,8 @@ def main():
     ap.add_argument("--no-configs", action="store_true", help="skip the c1 and c3 runs")
     ap.add_argument("--lattice", type=int, default=200, help="cube side (profiling of smaller cases)")
     ap.add_argument("--forms", default="both", choices=["both", "fp64", "fp32"])
-    ap.add_argument("--workload", default="c2", choices=["c2", "c5"], help="c5: the 400^3 multi-sphere E-field case")
+    ap.add_argument("--workload", default="c2", choices=["c2", "c5", "warmnet"],
+                    help="c5: the 400^3 multi-sphere E-field case; warmnet: the warm-start net's forward pass")
     ap.add_argument("--c5-max-iterations", type=int, default=20000)
     ap.add_argument("--c4-test", type=int, default=64, help="c4 test solves for the warm-start protocol (0: skip)")
     # a fixed FIRE strategy instead of the autotuner's choice (for profiling runs, where the
@@ -681,6 +730,10 @@ def main():
         return 0
     if args.lattice != 200:
         scale_workload(args.lattice)
+    if args.workload == "warmnet":
+        if rank == 0:
+            print(json.dumps(run_warmnet(args)))
+        return 0
 
     if args.impl == "reference":
         if rank != 0:

@@ -51,6 +51,7 @@ struct Geo {
     int taps;        // 27 or 1
     int stride;      // 1 or 2
     int mode;        // 0 forward gather; 1 the transposed gather of a stride-2 conv
+    int nb;          // samples (rows = nb * Do * Ho * Wo)
 };
 
 // flat source voxel (sample offset included) of GEMM row r for one tap, or -1
@@ -367,6 +368,169 @@ __global__ void __launch_bounds__(128) k_conv_umma(Geo g, const bf16 *__restrict
         asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "r"(COLS) : "memory");
 }
 
+// ---- direct 3x3x3 stride-1 convolution on tcgen05 (no per-tap gather)
+//
+// A CTA computes an 8 (x) x 16 (y) x 1 (z) tile of output voxels = 128 GEMM
+// rows, row r = (x0 + r % 8, y0 + r / 8).  It stages the input halo (10 x 18
+// x 3 voxels, zero outside the volume) once, in the layout
+// [cin/8][3][18][10][8 channels]: 8 consecutive x voxels of one 8-channel
+// group form a canonical 8-row x 16-byte core matrix, and for tap (dx, dy,
+// dz) the A operand is that staged tile seen from (dx, dy, dz): the start
+// address moves by the tap, the stride (M) byte offset is one halo row (160
+// bytes, the next output y) and the leading (K) byte offset one 8-channel
+// group (3 * 18 * 160 bytes).  The weights of the 9 taps of one dz plane are
+// staged per stage ([tap][cout][cin] in the canonical layout), two buffers;
+// one thread issues 27 * cin/16 tcgen05.mma into tensor memory.  Every wait is
+// bounded and reports through g_conv_err; the CTA always frees its tensor memory.
+static size_t direct_smem(int cin, int n)
+{
+    const size_t need = (size_t)540 * cin * 2 + 2 * (size_t)9 * n * cin * 2 + 64;
+    const int per_sm = 512 / umma_cols(n);
+    const size_t floor_bytes = (size_t)(232448 / per_sm) - 1024 + 1;
+    return std::max(need, std::min<size_t>(floor_bytes, 232448 - 1024));
+}
+
+template <int N>
+__global__ void __launch_bounds__(128) k_conv3_direct(Geo g, const bf16 *__restrict__ in, const bf16 *__restrict__ w,
+                                                      const float *__restrict__ bias, bf16 *__restrict__ out, int relu)
+{
+    static_assert(N % 16 == 0 && N >= 16 && N <= 256, "tcgen05 M=128 needs N a multiple of 16 in [16, 256]");
+    constexpr int COLS = N <= 32 ? 32 : (N <= 64 ? 64 : (N <= 128 ? 128 : 256));
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    const int cin = g.cin, kc8 = cin >> 3, K = 27 * cin;
+    const int W = g.Wo, H = g.Ho, D = g.Do;  // stride 1: the input grid is the output grid
+    const size_t tile_bytes = (size_t)540 * cin * 2, wstage_bytes = (size_t)9 * N * cin * 2;
+    unsigned char *tile = smem_raw;
+    unsigned char *wbuf[2] = {smem_raw + tile_bytes, smem_raw + tile_bytes + wstage_bytes};
+    uint64_t *bar = reinterpret_cast<uint64_t *>(smem_raw + tile_bytes + 2 * wstage_bytes);
+    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(bar + 2);
+    const int tid = threadIdx.x, warp = tid >> 5;
+    const int tx = (W + 7) >> 3, ty = (H + 15) >> 4;
+    int bidx = blockIdx.x;
+    const int x0 = (bidx % tx) * 8;
+    bidx /= tx;
+    const int y0 = (bidx % ty) * 16;
+    bidx /= ty;
+    const int z = bidx % D, b = bidx / D;
+    if (*(volatile int *)&g_conv_err) return;
+
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(s_addr(tmem_slot)),
+                     "r"(COLS)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n" ::: "memory");
+    }
+    if (tid == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(s_addr(&bar[0])) : "memory");
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(s_addr(&bar[1])) : "memory");
+        asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+    }
+    // the input halo: (hx, hy, hz) -> input (x0 - 1 + hx, y0 - 1 + hy, z - 1 + hz)
+    for (int e = tid; e < 540 * kc8; e += 128) {
+        const int vox = e / kc8, k8 = e - vox * kc8;
+        const int hx = vox % 10, hy = (vox / 10) % 18, hz = vox / 180;
+        const int ix = x0 - 1 + hx, iy = y0 - 1 + hy, iz = z - 1 + hz;
+        uint4 v = make_uint4(0, 0, 0, 0);
+        if (ix >= 0 && iy >= 0 && iz >= 0 && ix < W && iy < H && iz < D)
+            v = *reinterpret_cast<const uint4 *>(in + ((((size_t)b * D + iz) * H + iy) * W + ix) * cin + k8 * 8);
+        *reinterpret_cast<uint4 *>(tile + (((size_t)(k8 * 3 + hz) * 18 + hy) * 10 + hx) * 16) = v;
+    }
+    auto load_weights = [&](int dz, unsigned char *dst) {
+        // taps dz*9 .. dz*9+8, [tap][co][cin] with each tap's [co][cin] in the canonical layout
+        for (int e = tid; e < 9 * N * kc8; e += 128) {
+            const int t9 = e / (N * kc8), rem = e - t9 * N * kc8, co = rem / kc8, k8 = rem - co * kc8;
+            const int tap = dz * 9 + t9;
+            const uint4 v = *reinterpret_cast<const uint4 *>(w + (size_t)co * K + (size_t)tap * cin + k8 * 8);
+            *reinterpret_cast<uint4 *>(dst + (size_t)t9 * N * cin * 2 + ((size_t)(co >> 3) * kc8 + k8) * 128 +
+                                       (co & 7) * 16) = v;
+        }
+    };
+    auto issue = [&](int dz, const unsigned char *wb, int b_idx) {
+        asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+        const unsigned st = s_addr(tile), sw = s_addr(wb);
+        const unsigned lbo_a = 3u * 18u * 160u, sbo_a = 160u, sbo_b = (unsigned)kc8 * 128u;
+        for (int t9 = 0; t9 < 9; ++t9) {
+            const int dy = t9 / 3, dx = t9 % 3;
+            for (int kk = 0; kk < (cin >> 4); ++kk) {
+                const unsigned a0 = st + ((unsigned)((2 * kk * 3 + dz) * 18 + dy) * 160u) + (unsigned)dx * 16u;
+                const unsigned b0 = sw + (unsigned)t9 * (unsigned)(N * cin * 2) + (unsigned)kk * 256u;
+                const uint64_t da = umma_desc(a0, lbo_a, sbo_a), db = umma_desc(b0, 128, sbo_b);
+                const unsigned acc = (dz > 0 || t9 > 0 || kk > 0) ? 1u : 0u;
+                asm volatile(
+                    "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+                    " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(*tmem_slot),
+                    "l"(da), "l"(db), "r"(umma_idesc(N)), "r"(acc)
+                    : "memory");
+            }
+        }
+        asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(
+                         s_addr(&bar[b_idx]))
+                     : "memory");
+    };
+    load_weights(0, wbuf[0]);
+    asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+    asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+    const uint32_t tmem = *tmem_slot;
+    if (tid == 0) issue(0, wbuf[0], 0);
+    load_weights(1, wbuf[1]);
+    asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+    __syncthreads();
+    if (tid == 0) issue(1, wbuf[1], 1);
+    // wbuf[0] is free once the dz = 0 MMAs have completed
+    bool ok = mbar_wait_bounded(s_addr(&bar[0]), 0u);
+    if (!__syncthreads_or(!ok)) {
+        load_weights(2, wbuf[0]);
+        asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+        __syncthreads();
+        if (tid == 0) issue(2, wbuf[0], 0);
+        // the second commit to bar[0] covers every MMA of this CTA
+        ok = mbar_wait_bounded(s_addr(&bar[0]), 1u);
+        ok = !__syncthreads_or(!ok);
+    } else {
+        ok = false;
+    }
+    if (ok) {
+        asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+        const uint32_t taddr = tmem + ((uint32_t)(warp * 32) << 16);
+        const int ox = x0 + (tid & 7), oy = y0 + (tid >> 3);
+        const bool inside = ox < W && oy < H;
+        bf16 *o = out + ((((size_t)b * D + z) * H + oy) * W + ox) * N;
+#pragma unroll
+        for (int c0 = 0; c0 < N; c0 += 8) {
+            uint32_t r[8];
+            asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];\n"
+                         : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+                           "=r"(r[7])
+                         : "r"(taddr + c0));
+            asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
+            if (inside) {
+                __nv_bfloat162 h[4];
+#pragma unroll
+                for (int e = 0; e < 4; ++e) {
+                    float v0 = __uint_as_float(r[2 * e]) + bias[c0 + 2 * e];
+                    float v1 = __uint_as_float(r[2 * e + 1]) + bias[c0 + 2 * e + 1];
+                    if (relu) {
+                        v0 = fmaxf(v0, 0.f);
+                        v1 = fmaxf(v1, 0.f);
+                    }
+                    h[e] = __floats2bfloat162_rn(v0, v1);
+                }
+                *reinterpret_cast<uint4 *>(o + c0) = *reinterpret_cast<const uint4 *>(h);
+            }
+        }
+    } else if (tid == 0) {
+        // a wait gave up: let the MMAs in flight finish (bounded) before the buffers go away
+        for (int k = 0; k < 2; ++k) mbar_wait_bounded(s_addr(&bar[k]), 0u), mbar_wait_bounded(s_addr(&bar[k]), 1u);
+        atomicExch(&g_conv_err, 1);
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+    __syncthreads();
+    if (warp == 0)
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "r"(COLS) : "memory");
+}
+
 // dW[co][tap][ci] += sum_v dout[v][co] * in[src(v,tap)][ci] over rows
 // [blockIdx.x * chunk, +chunk): block tile 64 co x 64 ci for one tap, the
 // row dimension staged through shared memory 16 rows at a time; each block
@@ -465,12 +629,15 @@ struct Dims {
 // nearest x2 upsampling of h (coarse, FP32) plus a BF16 skip on the fine grid, into BF16
 __global__ void k_up2_add(const float *h, const bf16 *skip, bf16 *out, Dims d, int c)
 {
-    const int X = 2 * d.x, Y = 2 * d.y, Z = 2 * d.z;
-    const long long n = (long long)d.B * X * Y * Z * c;
-    GRID_STRIDE(i, n)
+    // one thread per 8 channels of a fine voxel (c is a multiple of 8): 16-byte
+    // loads and stores, the voxel's coordinates decoded once per 8 channels
+    const int X = 2 * d.x, Y = 2 * d.y, Z = 2 * d.z, cg = c >> 3;
+    const long long n = (long long)d.B * X * Y * Z * cg;
+    GRID_STRIDE(t, n)
     {
-        const int ch = (int)(i % c);
-        long long v = i / c;
+        const int g = (int)(t % cg);
+        long long v = t / cg;
+        const long long vf = v;
         const int x = (int)(v % X);
         v /= X;
         const int y = (int)(v % Y);
@@ -478,7 +645,18 @@ __global__ void k_up2_add(const float *h, const bf16 *skip, bf16 *out, Dims d, i
         const int z = (int)(v % Z);
         const int b = (int)(v / Z);
         const long long src = (((long long)b * d.z + z / 2) * d.y + y / 2) * d.x + x / 2;
-        out[i] = __float2bfloat16(h[src * c + ch] + __bfloat162float(skip[i]));
+        const float4 *hp = reinterpret_cast<const float4 *>(h + src * c + 8 * g);
+        const float4 h0 = hp[0], h1 = hp[1];
+        const uint4 sk = *reinterpret_cast<const uint4 *>(skip + vf * c + 8 * g);
+        const __nv_bfloat162 *s2 = reinterpret_cast<const __nv_bfloat162 *>(&sk);
+        const float hv[8] = {h0.x, h0.y, h0.z, h0.w, h1.x, h1.y, h1.z, h1.w};
+        __nv_bfloat162 o[4];
+#pragma unroll
+        for (int e = 0; e < 4; ++e) {
+            const float2 f = __bfloat1622float2(s2[e]);
+            o[e] = __floats2bfloat162_rn(hv[2 * e] + f.x, hv[2 * e + 1] + f.y);
+        }
+        *reinterpret_cast<uint4 *>(out + vf * c + 8 * g) = *reinterpret_cast<const uint4 *>(o);
     }
 }
 
@@ -641,11 +819,37 @@ static void conv_umma(const Geo &g, const bf16 *in, const bf16 *w, const float *
     k_conv_umma<N, OB><<<(rows + 127) / 128, 128, sm, s>>>(g, in, w, bias, addend, out, relu, rows);
 }
 
-// tcgen05: the 5th-generation tensor-core kernel above; otherwise mma.sync
+template <int N>
+static void conv3_direct(const Geo &g, const bf16 *in, const bf16 *w, const float *bias, bf16 *out, int relu,
+                         cudaStream_t s)
+{
+    static int attr_bytes = 0;
+    const size_t sm = direct_smem(g.cin, N);
+    if ((int)sm > attr_bytes) {
+        // a failure here surfaces as the launch's error
+        if (cudaFuncSetAttribute(k_conv3_direct<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm) ==
+            cudaSuccess)
+            attr_bytes = (int)sm;
+    }
+    const long long tiles = (long long)((g.Wo + 7) / 8) * ((g.Ho + 15) / 16);
+    k_conv3_direct<N><<<(unsigned)(tiles * g.Do * g.nb), 128, sm, s>>>(g, in, w, bias, out, relu);
+}
+
+// tcgen05: the 5th-generation tensor-core kernels above (the direct kernel for
+// 3x3x3 stride-1 forward convolutions with BF16 output, the gathering kernel
+// otherwise); else mma.sync
 template <bool OB>
 static void conv_gemm(const Geo &g, const bf16 *in, const bf16 *w, const float *bias, const float *addend, void *out,
                       int relu, int rows, cudaStream_t s, bool tcgen05)
 {
+    // the direct kernel wins where a dz plane's weights are small (measured at
+    // 128^3: 16->32 0.29 ms vs 0.49 gathering, 32->32 0.77 vs 0.95; at 48->48
+    // and 64->64 the 135-216 KB of staging leave one CTA per SM and it loses)
+    if (tcgen05 && OB && g.mode == 0 && g.taps == 27 && g.stride == 1 && !addend && bias && g.cout == 32 &&
+        g.cin <= 32) {
+        conv3_direct<32>(g, in, w, bias, reinterpret_cast<bf16 *>(out), relu, s);
+        return;
+    }
     if (tcgen05) {
         switch (g.cout) {
         case 16: conv_umma<16, OB>(g, in, w, bias, addend, out, relu, rows, s); return;
@@ -762,6 +966,7 @@ Geo fwd_geo(const qmin_warmnet_ctx *n, const Layer &L)
     g.taps = L.taps;
     g.stride = L.stride;
     g.mode = 0;
+    g.nb = n->B;
     return g;
 }
 
@@ -823,6 +1028,7 @@ void layer_backward(qmin_warmnet_ctx *n, int i, const float *gout, const bf16 *a
     d.taps = L.taps;
     d.stride = L.stride;
     d.mode = L.stride == 2 ? 1 : 0;
+    d.nb = n->B;
     const int flip = (L.stride == 1 && L.taps == 27) ? 1 : 0;
     k_dgrad_weights<<<grid1((long long)L.cout * L.cin * L.taps), 256, 0, s>>>(n->pb + L.woff, n->wd, L.cout, L.cin,
                                                                               L.taps, flip);
@@ -1023,13 +1229,13 @@ int qmin_warmnet_forward(qmin_warmnet n)
     run_layer(n, 2, n->act[1], nullptr);
     run_layer(n, 3, n->act[2], nullptr);
     run_layer(n, 4, n->act[3], n->pre[4]);
-    k_up2_add<<<grid1(rows_at(n, 2) * 64), 256, 0, s>>>(n->pre[4], n->act[2], n->act[4], dims_at(n, 3), 64);
+    k_up2_add<<<grid1(rows_at(n, 2) * 8), 256, 0, s>>>(n->pre[4], n->act[2], n->act[4], dims_at(n, 3), 64);
     run_layer(n, 5, n->act[4], nullptr);
     run_layer(n, 6, n->act[5], n->pre[6]);
-    k_up2_add<<<grid1(rows_at(n, 1) * 48), 256, 0, s>>>(n->pre[6], n->act[1], n->act[6], dims_at(n, 2), 48);
+    k_up2_add<<<grid1(rows_at(n, 1) * 6), 256, 0, s>>>(n->pre[6], n->act[1], n->act[6], dims_at(n, 2), 48);
     run_layer(n, 7, n->act[6], nullptr);
     run_layer(n, 8, n->act[7], n->pre[8]);
-    k_up2_add<<<grid1(rows_at(n, 0) * 32), 256, 0, s>>>(n->pre[8], n->act[0], n->act[8], dims_at(n, 1), 32);
+    k_up2_add<<<grid1(rows_at(n, 0) * 4), 256, 0, s>>>(n->pre[8], n->act[0], n->act[8], dims_at(n, 1), 32);
     run_layer(n, 9, n->act[8], nullptr);
     run_layer(n, 10, n->act[9], n->y);
     return check_launch(n, "qmin_warmnet_forward", 14);
