@@ -711,8 +711,11 @@ def main():
     ap.add_argument("--no-configs", action="store_true", help="skip the c1 and c3 runs")
     ap.add_argument("--lattice", type=int, default=200, help="cube side (profiling of smaller cases)")
     ap.add_argument("--forms", default="both", choices=["both", "fp64", "fp32"])
-    ap.add_argument("--workload", default="c2", choices=["c2", "c5", "warmnet"],
-                    help="c5: the 400^3 multi-sphere E-field case; warmnet: the warm-start net's forward pass")
+    ap.add_argument("--workload", default="c2", choices=["c2", "c3", "c5", "warmnet"],
+                    help="c3: the batched uneven solves alone; c5: the 400^3 multi-sphere E-field case; "
+                         "warmnet: the warm-start net's forward pass")
+    ap.add_argument("--c3-solves", type=int, default=512, help="c3: number of solves (profiling of smaller cases)")
+    ap.add_argument("--c3-max-iterations", type=int, default=30000)
     ap.add_argument("--c5-max-iterations", type=int, default=20000)
     ap.add_argument("--c4-test", type=int, default=64, help="c4 test solves for the warm-start protocol (0: skip)")
     # a fixed FIRE strategy instead of the autotuner's choice (for profiling runs, where the
@@ -733,6 +736,11 @@ def main():
     if args.workload == "warmnet":
         if rank == 0:
             print(json.dumps(run_warmnet(args)))
+        return 0
+    if args.workload == "c3":
+        if rank == 0:
+            import __graft_entry__ as ge
+            print(json.dumps(run_c3(ge.load_package(), args.c3_solves, args.c3_max_iterations)))
         return 0
 
     if args.impl == "reference":

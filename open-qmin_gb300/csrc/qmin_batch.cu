@@ -75,22 +75,36 @@ template <class T> __global__ void __launch_bounds__(kBlock) k_b_pred(BatchArgs<
     for (int c = blockIdx.x; c < B.nchunks; c += gridDim.x) {
         const ChunkDesc ch = B.chunks[c];
         const FireDev &fd = fds[ch.solve];
-        if (!fd.active) continue;
+        if (!fd.active) continue;  // uniform per block
+        // the deferred mix folded into the Verlet coefficients, as k_fire_pred does:
+        // v' = cvv v + cvf f, q' = q + cqv v + cqf f; formed in FP64 by one lane per warp
+        double cf[4] = {0.0, 0.0, 0.0, 0.0};
+        if ((threadIdx.x & 31) == 0) {
+            const double dt = fd.dt, hdt = 0.5 * dt, hdt2 = 0.5 * dt * dt;
+            double mv = 1.0, mf = 0.0;
+            if (fd.pending) {
+                mv = fd.reset ? 0.0 : 1.0 - fd.mixA;
+                mf = fd.reset ? 0.0 : fd.mixA * fd.mixS;
+            }
+            cf[0] = mv;
+            cf[1] = mf + hdt;
+            cf[2] = dt * mv;
+            cf[3] = dt * mf + hdt2;
+        }
+#pragma unroll
+        for (int k = 0; k < 4; ++k) cf[k] = __shfl_sync(0xffffffffu, cf[k], 0);
+        const T cvv = T(cf[0]), cvf = T(cf[1]), cqv = T(cf[2]), cqf = T(cf[3]);
         const SolveDesc sd = B.solves[ch.solve];
         const int li = ch.start + threadIdx.x;
         if (li >= sd.Lx * sd.Ly * sd.Lz) continue;
         const int i = sd.off + li;
-        const T dt = T(fd.dt), hdt2 = T(0.5 * fd.dt * fd.dt), hdt = T(0.5) * T(fd.dt);
-        const T ma = T(1.0 - fd.mixA), mb = T(fd.mixA * fd.mixS);
 #pragma unroll
         for (int k = 0; k < 5; ++k) {
             const long long j = (long long)k * B.L.P + i;
-            T v = B.L.V[j];
+            const T v = B.L.V[j];
             const T f = B.L.F[j];
-            if (fd.pending) v = fd.reset ? T(0) : ma * v + mb * f;
-            const T disp = dt * v + hdt2 * f;
-            B.L.V[j] = v + hdt * f;
-            B.L.Q[j] += disp;
+            B.L.Q[j] += cqv * v + cqf * f;
+            B.L.V[j] = cvv * v + cvf * f;
         }
     }
 }
@@ -119,8 +133,9 @@ template <class T> __global__ void __launch_bounds__(kBlock) k_b_derivs(BatchArg
     }
 }
 
-// force (KICK = 0) or force + half kick + per-chunk FIRE reductions (KICK = 1)
-template <class T, int KICK, int CAP>
+// force (KICK = 0) or force + half kick + per-chunk FIRE reductions (KICK = 1);
+// ONE_CONST: the one-constant form only (a batch whose parameters are one-constant)
+template <class T, int KICK, int CAP, bool ONE_CONST = false>
 __global__ void __launch_bounds__(kBlock, CAP + 1) k_b_force(BatchArgs<T> B, const FireDev *fds, double *partials)
 {
     for (int c = blockIdx.x; c < B.nchunks; c += gridDim.x) {
@@ -128,12 +143,14 @@ __global__ void __launch_bounds__(kBlock, CAP + 1) k_b_force(BatchArgs<T> B, con
         if (KICK && !fds[ch.solve].active) continue;  // uniform per block
         const SolveDesc sd = B.solves[ch.solve];
         const int li = ch.start + threadIdx.x;
-        double acc[3] = {0.0, 0.0, 0.0};
+        // the site's three dot products in the site precision (FP32 warp sums for
+        // the FP32 form, FP64 across warps and chunks)
+        T acc[3] = {T(0), T(0), T(0)};
         if (li < sd.Lx * sd.Ly * sd.Lz) {
             BatchAcc<T> a(B.L, sd, li);
             const int t = B.L.types[a.i];
             T f[5];
-            site_force_core(B.L, a, t, f);
+            site_force_core<T, BatchAcc<T>, false, false, ONE_CONST>(B.L, a, t, f);
             const long long P = B.L.P;
             if (KICK) {
                 const T hdt = T(0.5) * T(fds[ch.solve].dt);
@@ -143,19 +160,26 @@ __global__ void __launch_bounds__(kBlock, CAP + 1) k_b_force(BatchArgs<T> B, con
                     v[k] = B.L.V[k * P + a.i] + hdt * f[k];
                     B.L.V[k * P + a.i] = v[k];
                 }
-                acc[0] = (double)dot_qt(f, f);
-                acc[1] = (double)dot_qt(v, v);
-                acc[2] = (double)dot_qt(f, v);
+                acc[0] = dot_qt(f, f);
+                acc[1] = dot_qt(v, v);
+                acc[2] = dot_qt(f, v);
             }
 #pragma unroll
             for (int k = 0; k < 5; ++k) B.L.F[k * P + a.i] = f[k];
         }
         if (KICK) {
-            block_sum<3>(acc);
+            double sum[3];
+            if constexpr (sizeof(T) == 4) {
+                block_sum_f32<3>(acc, sum);
+            } else {
+#pragma unroll
+                for (int k = 0; k < 3; ++k) sum[k] = acc[k];
+                block_sum_smem<3>(sum);
+            }
             if (threadIdx.x == 0) {
-                partials[3 * c + 0] = acc[0];
-                partials[3 * c + 1] = acc[1];
-                partials[3 * c + 2] = acc[2];
+                partials[3 * c + 0] = sum[0];
+                partials[3 * c + 1] = sum[1];
+                partials[3 * c + 2] = sum[2];
             }
         }
     }
@@ -318,6 +342,13 @@ template <class T> static int launch_b_force(const BatchArgs<T> &B, const FireDe
     if (B.L.multi) {
         k_b_derivs<T><<<g, kBlock, 0, s>>>(B, kick ? fds : nullptr);
         ++n;
+    }
+    if (!B.L.multi) {
+        if (!kick) k_b_force<T, 0, 0, true><<<g, kBlock, 0, s>>>(B, fds, partials);
+        else if (cap == 2) k_b_force<T, 1, 2, true><<<g, kBlock, 0, s>>>(B, fds, partials);
+        else if (cap == 1) k_b_force<T, 1, 1, true><<<g, kBlock, 0, s>>>(B, fds, partials);
+        else k_b_force<T, 1, 0, true><<<g, kBlock, 0, s>>>(B, fds, partials);
+        return n + 1;
     }
     if (!kick) k_b_force<T, 0, 0><<<g, kBlock, 0, s>>>(B, fds, partials);
     else if (cap == 2) k_b_force<T, 1, 2><<<g, kBlock, 0, s>>>(B, fds, partials);

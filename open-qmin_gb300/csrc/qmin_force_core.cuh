@@ -90,6 +90,60 @@ __device__ __forceinline__ void block_sum(double (&v)[NV])
     __syncthreads();
 }
 
+// the same for FP32 per-thread values: each warp sums its 32 values in FP32
+// (terms that are themselves FP32-rounded), the warps' sums are added in FP64;
+// result valid in thread 0 of `out`
+template <int NV, int NT = kBlock>
+__device__ __forceinline__ void block_sum_f32(float (&v)[NV], double (&out)[NV])
+{
+    __shared__ double shf[NV][NT / 32];
+#pragma unroll
+    for (int k = 0; k < NV; ++k)
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v[k] += __shfl_down_sync(0xffffffffu, v[k], o);
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    if (lane == 0)
+#pragma unroll
+        for (int k = 0; k < NV; ++k) shf[k][w] = (double)v[k];
+    __syncthreads();
+    if (w == 0) {
+#pragma unroll
+        for (int k = 0; k < NV; ++k) {
+            out[k] = lane < NT / 32 ? shf[k][lane] : 0.0;
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) out[k] += __shfl_down_sync(0xffffffffu, out[k], o);
+        }
+    }
+    __syncthreads();
+}
+
+// block-wide sum of NV doubles through shared memory: warp 0 adds eight
+// consecutive threads' values per lane, then shuffles; about a third of the
+// FP64 additions of block_sum (which adds in every lane at every shuffle
+// level), for kernels that reduce once per few sites; result in thread 0
+template <int NV, int NT = kBlock>
+__device__ __forceinline__ void block_sum_smem(double (&v)[NV])
+{
+    static_assert(NT == 256, "eight values per lane of warp 0");
+    __shared__ double shs[NV][NT];
+#pragma unroll
+    for (int k = 0; k < NV; ++k) shs[k][threadIdx.x] = v[k];
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        const int lane = threadIdx.x;
+#pragma unroll
+        for (int k = 0; k < NV; ++k) {
+            double a = shs[k][8 * lane];
+#pragma unroll
+            for (int e = 1; e < 8; ++e) a += shs[k][8 * lane + e];
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) a += __shfl_down_sync(0xffffffffu, a, o);
+            v[k] = a;
+        }
+    }
+    __syncthreads();
+}
+
 // deterministic sum of partials[NV * nparts] by one block; result in thread 0
 template <int NV>
 __device__ __forceinline__ void sum_partials(const double *partials, int nparts, double (&v)[NV])
@@ -134,7 +188,10 @@ __device__ __forceinline__ T deriv2_rule(int t, int td, int tu, T qd, T q, T qu)
 // BND_LINES evaluates the boundary L2-L4 forms as straight-line code per case
 // (merged coefficients L.cbd) instead of walking the sparse tables; it needs
 // L.cbd and costs code size, so only the listed-site kernel takes it
-template <class T, class A, bool WITH_L6 = false, bool BND_LINES = false>
+// ONE_CONST compiles the one-constant form only (the caller guarantees
+// !L.multi), which keeps the multi-constant forms' registers out of kernels
+// that run one-constant lattices
+template <class T, class A, bool WITH_L6 = false, bool BND_LINES = false, bool ONE_CONST = false>
 __device__ __forceinline__ void site_force_core(const Lat<T> &L, const A &acc, int t, T *f, const T *hs = nullptr)
 {
     if (t > 0) {
@@ -162,7 +219,7 @@ __device__ __forceinline__ void site_force_core(const Lat<T> &L, const A &acc, i
 
     T sp[5] = {T(0), T(0), T(0), T(0), T(0)};
     // multi-constant bulk sites carry L1 inside the combined linear form below
-    if (!L.multi || (boundary && L.L1 != T(0))) {
+    if (ONE_CONST || !L.multi || (boundary && L.L1 != T(0))) {
         // lcForce::bulkL1Force / boundaryL1Force (lcForces.h:26-63)
         T s1[5];
         if (!boundary) {
@@ -188,7 +245,7 @@ __device__ __forceinline__ void site_force_core(const Lat<T> &L, const A &acc, i
 #pragma unroll
         for (int k = 0; k < 5; ++k) sp[k] += s1[k];
     }
-    if (L.multi) {
+    if (!ONE_CONST && L.multi) {
         if (!boundary) {
             // bulk L1/L2/L3/L4 forms, straight-line over their union pattern
             T s2[5];
