@@ -833,6 +833,8 @@ static int settle_pingpong(qmin_ctx *h, int executed)
 // after the force + kick timings (whose forces equal the ones already resident).
 template <class T> static int tune_fire(qmin_ctx *h, const Lat<T> &L)
 {
+    // a strategy restored from a checkpoint that this handle cannot launch is tuned afresh
+    if (h->path == 3 && h->split_cap == kSplitTma && !h->tmap_ok) h->path = -1;
     if (h->path >= 0 && h->tuned_version == h->version && h->tuned_mode == h->fire_mode &&
         h->tuned_variant == h->fire_variant)
         return QMIN_OK;
