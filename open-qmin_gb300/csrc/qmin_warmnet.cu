@@ -370,48 +370,53 @@ __global__ void __launch_bounds__(128) k_conv_umma(Geo g, const bf16 *__restrict
 
 // ---- direct 3x3x3 stride-1 convolution on tcgen05 (no per-tap gather)
 //
-// A CTA computes an 8 (x) x 16 (y) x 1 (z) tile of output voxels = 128 GEMM
-// rows, row r = (x0 + r % 8, y0 + r / 8).  It stages the input halo (10 x 18
-// x 3 voxels, zero outside the volume) once, in the layout
-// [cin/8][3][18][10][8 channels]: 8 consecutive x voxels of one 8-channel
-// group form a canonical 8-row x 16-byte core matrix, and for tap (dx, dy,
-// dz) the A operand is that staged tile seen from (dx, dy, dz): the start
-// address moves by the tap, the stride (M) byte offset is one halo row (160
-// bytes, the next output y) and the leading (K) byte offset one 8-channel
-// group (3 * 18 * 160 bytes).  The weights of the 9 taps of one dz plane are
-// staged per stage ([tap][cout][cin] in the canonical layout), two buffers;
-// one thread issues 27 * cin/16 tcgen05.mma into tensor memory.  Every wait is
-// bounded and reports through g_conv_err; the CTA always frees its tensor memory.
-static size_t direct_smem(int cin, int n)
+// A CTA computes 8 (x) x 16 (y) output voxels = 128 GEMM rows, row r = (x0 +
+// r % 8, y0 + r / 8), for each of ZT consecutive output planes.  8 consecutive
+// x voxels of one 8-channel group of a staged input halo plane form a
+// canonical 8-row x 16-byte core matrix, so for tap (dx, dy, dz) the A operand
+// is the staged plane z - 1 + dz seen from (dx, dy): the start address moves
+// by the tap, the stride (M) byte offset is one halo row (160 bytes, the next
+// output y) and the leading (K) byte offset one 8-channel group (180 * 16
+// bytes).  The 27 taps' weights stay resident in shared memory for the whole
+// column, the input halo planes (18 x 10 voxels, zero outside the volume) pass
+// through a ring of four slots ([cin/8][18][10][8 channels] each), and two
+// tensor-memory accumulators alternate: the MMAs of plane p run while the
+// epilogue of plane p - 1 reads the other accumulator and the halo plane z + 2
+// is loaded into the slot that the MMAs of plane p - 1 have finished reading.
+// Every wait is bounded and reports through g_conv_err; the CTA always frees
+// its tensor memory.
+static size_t direct_z_smem(int cin, int n)
 {
-    const size_t need = (size_t)540 * cin * 2 + 2 * (size_t)9 * n * cin * 2 + 64;
-    const int per_sm = 512 / umma_cols(n);
+    const size_t need = (size_t)27 * n * cin * 2 + (size_t)4 * 180 * cin * 2 + 64;
+    const int per_sm = 512 / umma_cols(2 * n);
     const size_t floor_bytes = (size_t)(232448 / per_sm) - 1024 + 1;
     return std::max(need, std::min<size_t>(floor_bytes, 232448 - 1024));
 }
 
 template <int N>
-__global__ void __launch_bounds__(128) k_conv3_direct(Geo g, const bf16 *__restrict__ in, const bf16 *__restrict__ w,
-                                                      const float *__restrict__ bias, bf16 *__restrict__ out, int relu)
+__global__ void __launch_bounds__(128) k_conv3_direct_z(Geo g, const bf16 *__restrict__ in,
+                                                        const bf16 *__restrict__ w, const float *__restrict__ bias,
+                                                        bf16 *__restrict__ out, int relu, int zt)
 {
-    static_assert(N % 16 == 0 && N >= 16 && N <= 256, "tcgen05 M=128 needs N a multiple of 16 in [16, 256]");
-    constexpr int COLS = N <= 32 ? 32 : (N <= 64 ? 64 : (N <= 128 ? 128 : 256));
+    static_assert(N % 16 == 0 && N >= 16 && 2 * N <= 256, "two M=128 accumulators of N columns");
+    constexpr int COLS = 2 * N <= 32 ? 32 : (2 * N <= 64 ? 64 : (2 * N <= 128 ? 128 : 256));
     extern __shared__ __align__(128) unsigned char smem_raw[];
     const int cin = g.cin, kc8 = cin >> 3, K = 27 * cin;
-    const int W = g.Wo, H = g.Ho, D = g.Do;  // stride 1: the input grid is the output grid
-    const size_t tile_bytes = (size_t)540 * cin * 2, wstage_bytes = (size_t)9 * N * cin * 2;
-    unsigned char *tile = smem_raw;
-    unsigned char *wbuf[2] = {smem_raw + tile_bytes, smem_raw + tile_bytes + wstage_bytes};
-    uint64_t *bar = reinterpret_cast<uint64_t *>(smem_raw + tile_bytes + 2 * wstage_bytes);
+    const int W = g.Wo, H = g.Ho, D = g.Do;
+    const size_t w_bytes = (size_t)27 * N * cin * 2, slot_bytes = (size_t)180 * cin * 2;
+    unsigned char *wts = smem_raw;
+    unsigned char *ring = smem_raw + w_bytes;
+    uint64_t *bar = reinterpret_cast<uint64_t *>(ring + 4 * slot_bytes);
     uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(bar + 2);
     const int tid = threadIdx.x, warp = tid >> 5;
-    const int tx = (W + 7) >> 3, ty = (H + 15) >> 4;
+    const int tx = (W + 7) >> 3, ty = (H + 15) >> 4, tz = (D + zt - 1) / zt;
     int bidx = blockIdx.x;
     const int x0 = (bidx % tx) * 8;
     bidx /= tx;
     const int y0 = (bidx % ty) * 16;
     bidx /= ty;
-    const int z = bidx % D, b = bidx / D;
+    const int z0 = (bidx % tz) * zt, b = bidx / tz;
+    const int nz = min(zt, D - z0);
     if (*(volatile int *)&g_conv_err) return;
 
     if (warp == 0) {
@@ -425,75 +430,54 @@ __global__ void __launch_bounds__(128) k_conv3_direct(Geo g, const bf16 *__restr
         asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(s_addr(&bar[1])) : "memory");
         asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
     }
-    // the input halo: (hx, hy, hz) -> input (x0 - 1 + hx, y0 - 1 + hy, z - 1 + hz)
-    for (int e = tid; e < 540 * kc8; e += 128) {
-        const int vox = e / kc8, k8 = e - vox * kc8;
-        const int hx = vox % 10, hy = (vox / 10) % 18, hz = vox / 180;
-        const int ix = x0 - 1 + hx, iy = y0 - 1 + hy, iz = z - 1 + hz;
-        uint4 v = make_uint4(0, 0, 0, 0);
-        if (ix >= 0 && iy >= 0 && iz >= 0 && ix < W && iy < H && iz < D)
-            v = *reinterpret_cast<const uint4 *>(in + ((((size_t)b * D + iz) * H + iy) * W + ix) * cin + k8 * 8);
-        *reinterpret_cast<uint4 *>(tile + (((size_t)(k8 * 3 + hz) * 18 + hy) * 10 + hx) * 16) = v;
+    // all 27 taps' weights, [tap][co][cin] with each tap's [co][cin] in the canonical layout
+    for (int e = tid; e < 27 * N * kc8; e += 128) {
+        const int tap = e / (N * kc8), rem = e - tap * N * kc8, co = rem / kc8, k8 = rem - co * kc8;
+        const uint4 v = *reinterpret_cast<const uint4 *>(w + (size_t)co * K + (size_t)tap * cin + k8 * 8);
+        *reinterpret_cast<uint4 *>(wts + (size_t)tap * N * cin * 2 + ((size_t)(co >> 3) * kc8 + k8) * 128 +
+                                   (co & 7) * 16) = v;
     }
-    auto load_weights = [&](int dz, unsigned char *dst) {
-        // taps dz*9 .. dz*9+8, [tap][co][cin] with each tap's [co][cin] in the canonical layout
-        for (int e = tid; e < 9 * N * kc8; e += 128) {
-            const int t9 = e / (N * kc8), rem = e - t9 * N * kc8, co = rem / kc8, k8 = rem - co * kc8;
-            const int tap = dz * 9 + t9;
-            const uint4 v = *reinterpret_cast<const uint4 *>(w + (size_t)co * K + (size_t)tap * cin + k8 * 8);
-            *reinterpret_cast<uint4 *>(dst + (size_t)t9 * N * cin * 2 + ((size_t)(co >> 3) * kc8 + k8) * 128 +
-                                       (co & 7) * 16) = v;
+    auto slot_of = [&](int iz) { return ((iz - z0 + 1) & 3); };  // iz >= z0 - 1
+    // input plane iz (zero outside the volume) into its ring slot
+    auto load_plane = [&](int iz) {
+        unsigned char *dst = ring + (size_t)slot_of(iz) * slot_bytes;
+        const bool zin = iz >= 0 && iz < D;
+        for (int e = tid; e < 180 * kc8; e += 128) {
+            const int vox = e / kc8, k8 = e - vox * kc8;
+            const int hx = vox % 10, hy = vox / 10;
+            const int ix = x0 - 1 + hx, iy = y0 - 1 + hy;
+            uint4 v = make_uint4(0, 0, 0, 0);
+            if (zin && ix >= 0 && iy >= 0 && ix < W && iy < H)
+                v = *reinterpret_cast<const uint4 *>(in + ((((size_t)b * D + iz) * H + iy) * W + ix) * cin + k8 * 8);
+            *reinterpret_cast<uint4 *>(dst + ((size_t)k8 * 180 + hy * 10 + hx) * 16) = v;
         }
     };
-    auto issue = [&](int dz, const unsigned char *wb, int b_idx) {
+    auto issue = [&](int z, int acc_idx) {
         asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
-        const unsigned st = s_addr(tile), sw = s_addr(wb);
-        const unsigned lbo_a = 3u * 18u * 160u, sbo_a = 160u, sbo_b = (unsigned)kc8 * 128u;
-        for (int t9 = 0; t9 < 9; ++t9) {
-            const int dy = t9 / 3, dx = t9 % 3;
+        const unsigned sw = s_addr(wts), sbo_b = (unsigned)kc8 * 128u;
+        const uint32_t dst = *tmem_slot + (uint32_t)(acc_idx * N);
+        for (int tap = 0; tap < 27; ++tap) {
+            const int dz = tap / 9, dy = (tap / 3) % 3, dx = tap % 3;
+            const unsigned sa = s_addr(ring + (size_t)slot_of(z - 1 + dz) * slot_bytes);
             for (int kk = 0; kk < (cin >> 4); ++kk) {
-                const unsigned a0 = st + ((unsigned)((2 * kk * 3 + dz) * 18 + dy) * 160u) + (unsigned)dx * 16u;
-                const unsigned b0 = sw + (unsigned)t9 * (unsigned)(N * cin * 2) + (unsigned)kk * 256u;
-                const uint64_t da = umma_desc(a0, lbo_a, sbo_a), db = umma_desc(b0, 128, sbo_b);
-                const unsigned acc = (dz > 0 || t9 > 0 || kk > 0) ? 1u : 0u;
+                const unsigned a0 = sa + ((unsigned)(2 * kk * 180 + dy * 10 + dx) * 16u);
+                const unsigned b0 = sw + (unsigned)tap * (unsigned)(N * cin * 2) + (unsigned)kk * 256u;
+                const uint64_t da = umma_desc(a0, 2880, 160), db = umma_desc(b0, 128, sbo_b);
+                const unsigned acc = (tap > 0 || kk > 0) ? 1u : 0u;
                 asm volatile(
                     "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
-                    " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(*tmem_slot),
+                    " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(dst),
                     "l"(da), "l"(db), "r"(umma_idesc(N)), "r"(acc)
                     : "memory");
             }
         }
         asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(
-                         s_addr(&bar[b_idx]))
+                         s_addr(&bar[acc_idx]))
                      : "memory");
     };
-    load_weights(0, wbuf[0]);
-    asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
-    asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
-    __syncthreads();
-    asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
-    const uint32_t tmem = *tmem_slot;
-    if (tid == 0) issue(0, wbuf[0], 0);
-    load_weights(1, wbuf[1]);
-    asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
-    __syncthreads();
-    if (tid == 0) issue(1, wbuf[1], 1);
-    // wbuf[0] is free once the dz = 0 MMAs have completed
-    bool ok = mbar_wait_bounded(s_addr(&bar[0]), 0u);
-    if (!__syncthreads_or(!ok)) {
-        load_weights(2, wbuf[0]);
-        asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
-        __syncthreads();
-        if (tid == 0) issue(2, wbuf[0], 0);
-        // the second commit to bar[0] covers every MMA of this CTA
-        ok = mbar_wait_bounded(s_addr(&bar[0]), 1u);
-        ok = !__syncthreads_or(!ok);
-    } else {
-        ok = false;
-    }
-    if (ok) {
+    auto epilogue = [&](int z, int acc_idx, uint32_t tmem) {
         asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
-        const uint32_t taddr = tmem + ((uint32_t)(warp * 32) << 16);
+        const uint32_t taddr = tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(acc_idx * N);
         const int ox = x0 + (tid & 7), oy = y0 + (tid >> 3);
         const bool inside = ox < W && oy < H;
         bf16 *o = out + ((((size_t)b * D + z) * H + oy) * W + ox) * N;
@@ -506,7 +490,7 @@ __global__ void __launch_bounds__(128) k_conv3_direct(Geo g, const bf16 *__restr
                          : "r"(taddr + c0));
             asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
             if (inside) {
-                __nv_bfloat162 h[4];
+                __nv_bfloat162 hh[4];
 #pragma unroll
                 for (int e = 0; e < 4; ++e) {
                     float v0 = __uint_as_float(r[2 * e]) + bias[c0 + 2 * e];
@@ -515,12 +499,45 @@ __global__ void __launch_bounds__(128) k_conv3_direct(Geo g, const bf16 *__restr
                         v0 = fmaxf(v0, 0.f);
                         v1 = fmaxf(v1, 0.f);
                     }
-                    h[e] = __floats2bfloat162_rn(v0, v1);
+                    hh[e] = __floats2bfloat162_rn(v0, v1);
                 }
-                *reinterpret_cast<uint4 *>(o + c0) = *reinterpret_cast<const uint4 *>(h);
+                *reinterpret_cast<uint4 *>(o + c0) = *reinterpret_cast<const uint4 *>(hh);
             }
         }
-    } else if (tid == 0) {
+    };
+    load_plane(z0 - 1);
+    load_plane(z0);
+    load_plane(z0 + 1);
+    asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+    asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+    const uint32_t tmem = *tmem_slot;
+    bool ok = true;
+    for (int p = 0; p < nz; ++p) {
+        const int z = z0 + p;
+        if (tid == 0) issue(z, p & 1);
+        if (p >= 1) {
+            // the MMAs of plane p - 1: done with their accumulator and with slot z - 2
+            const bool w_ok = mbar_wait_bounded(s_addr(&bar[(p - 1) & 1]), (unsigned)((p - 1) >> 1) & 1u);
+            if (__syncthreads_or(!w_ok)) {
+                ok = false;
+                break;
+            }
+            epilogue(z - 1, (p - 1) & 1, tmem);
+        }
+        if (p + 1 < nz) load_plane(z + 2);
+        asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+        asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+        __syncthreads();
+    }
+    if (ok) {
+        const int last = nz - 1;
+        const bool w_ok = mbar_wait_bounded(s_addr(&bar[last & 1]), (unsigned)(last >> 1) & 1u);
+        ok = !__syncthreads_or(!w_ok);
+        if (ok) epilogue(z0 + last, last & 1, tmem);
+    }
+    if (!ok && tid == 0) {
         // a wait gave up: let the MMAs in flight finish (bounded) before the buffers go away
         for (int k = 0; k < 2; ++k) mbar_wait_bounded(s_addr(&bar[k]), 0u), mbar_wait_bounded(s_addr(&bar[k]), 1u);
         atomicExch(&g_conv_err, 1);
@@ -820,19 +837,20 @@ static void conv_umma(const Geo &g, const bf16 *in, const bf16 *w, const float *
 }
 
 template <int N>
-static void conv3_direct(const Geo &g, const bf16 *in, const bf16 *w, const float *bias, bf16 *out, int relu,
-                         cudaStream_t s)
+static void conv3_direct_z(const Geo &g, const bf16 *in, const bf16 *w, const float *bias, bf16 *out, int relu,
+                           cudaStream_t s)
 {
     static int attr_bytes = 0;
-    const size_t sm = direct_smem(g.cin, N);
+    const size_t sm = direct_z_smem(g.cin, N);
     if ((int)sm > attr_bytes) {
         // a failure here surfaces as the launch's error
-        if (cudaFuncSetAttribute(k_conv3_direct<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm) ==
+        if (cudaFuncSetAttribute(k_conv3_direct_z<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm) ==
             cudaSuccess)
             attr_bytes = (int)sm;
     }
-    const long long tiles = (long long)((g.Wo + 7) / 8) * ((g.Ho + 15) / 16);
-    k_conv3_direct<N><<<(unsigned)(tiles * g.Do * g.nb), 128, sm, s>>>(g, in, w, bias, out, relu);
+    const int zt = std::min(g.Do, 16);
+    const long long tiles = (long long)((g.Wo + 7) / 8) * ((g.Ho + 15) / 16) * ((g.Do + zt - 1) / zt) * g.nb;
+    k_conv3_direct_z<N><<<(unsigned)tiles, 128, sm, s>>>(g, in, w, bias, out, relu, zt);
 }
 
 // tcgen05: the 5th-generation tensor-core kernels above (the direct kernel for
@@ -845,10 +863,16 @@ static void conv_gemm(const Geo &g, const bf16 *in, const bf16 *w, const float *
     // the direct kernel wins where a dz plane's weights are small (measured at
     // 128^3: 16->32 0.29 ms vs 0.49 gathering, 32->32 0.77 vs 0.95; at 48->48
     // and 64->64 the 135-216 KB of staging leave one CTA per SM and it loses)
-    if (tcgen05 && OB && g.mode == 0 && g.taps == 27 && g.stride == 1 && !addend && bias && g.cout == 32 &&
-        g.cin <= 32) {
-        conv3_direct<32>(g, in, w, bias, reinterpret_cast<bf16 *>(out), relu, s);
-        return;
+    if (tcgen05 && OB && g.mode == 0 && g.taps == 27 && g.stride == 1 && !addend && bias &&
+        direct_z_smem(g.cin, g.cout) <= 232448 - 1024) {
+        if (g.cout == 32) {
+            conv3_direct_z<32>(g, in, w, bias, reinterpret_cast<bf16 *>(out), relu, s);
+            return;
+        }
+        if (g.cout == 48) {
+            conv3_direct_z<48>(g, in, w, bias, reinterpret_cast<bf16 *>(out), relu, s);
+            return;
+        }
     }
     if (tcgen05) {
         switch (g.cout) {
