@@ -39,6 +39,9 @@ template <class T> struct BatchArgs {
     const SolveDesc *solves;
     const ChunkDesc *chunks;
     int nchunks;
+    // multi-constant: site classes (0 deep bulk, 1 other LC site, 2 object) and
+    // the sites whose derivative planes the class-1 forms read
+    const uint8_t *cls, *needd;
 };
 
 // accessor for a site of a packed solve: neighbours wrap inside that solve's box
@@ -118,6 +121,7 @@ template <class T> __global__ void __launch_bounds__(kBlock) k_b_derivs(BatchArg
         const SolveDesc sd = B.solves[ch.solve];
         const int li = ch.start + threadIdx.x;
         if (li >= sd.Lx * sd.Ly * sd.Lz) continue;
+        if (B.needd && !B.needd[sd.off + li]) continue;
         BatchAcc<T> a(B.L, sd, li);
         const int t = B.L.types[a.i];
         const long long P = B.L.P;
@@ -147,25 +151,30 @@ __global__ void __launch_bounds__(kBlock, CAP + 1) k_b_force(BatchArgs<T> B, con
         // the FP32 form, FP64 across warps and chunks)
         T acc[3] = {T(0), T(0), T(0)};
         if (li < sd.Lx * sd.Ly * sd.Lz) {
-            BatchAcc<T> a(B.L, sd, li);
-            const int t = B.L.types[a.i];
+            const int gi = sd.off + li;
             T f[5];
-            site_force_core<T, BatchAcc<T>, false, false, ONE_CONST>(B.L, a, t, f);
+            if (!ONE_CONST && B.cls && B.cls[gi] == 0) {
+                // deep bulk site: the 25-point form over Q, no derivative planes
+                deep_force_box(B.L, sd.off, sd.Lx, sd.Ly, sd.Lz, li, (long long)gi, f);
+            } else {
+                BatchAcc<T> a(B.L, sd, li);
+                site_force_core<T, BatchAcc<T>, false, !ONE_CONST, ONE_CONST>(B.L, a, B.L.types[gi], f);
+            }
             const long long P = B.L.P;
             if (KICK) {
                 const T hdt = T(0.5) * T(fds[ch.solve].dt);
                 T v[5];
 #pragma unroll
                 for (int k = 0; k < 5; ++k) {
-                    v[k] = B.L.V[k * P + a.i] + hdt * f[k];
-                    B.L.V[k * P + a.i] = v[k];
+                    v[k] = B.L.V[k * P + gi] + hdt * f[k];
+                    B.L.V[k * P + gi] = v[k];
                 }
                 acc[0] = dot_qt(f, f);
                 acc[1] = dot_qt(v, v);
                 acc[2] = dot_qt(f, v);
             }
 #pragma unroll
-            for (int k = 0; k < 5; ++k) B.L.F[k * P + a.i] = f[k];
+            for (int k = 0; k < 5; ++k) B.L.F[k * P + gi] = f[k];
         }
         if (KICK) {
             double sum[3];
@@ -299,6 +308,8 @@ struct qmin_batch_ctx {
     ChunkDesc *chunks = nullptr;
     void *Q = nullptr, *V = nullptr, *F = nullptr, *D = nullptr, *objs = nullptr;
     int8_t *types = nullptr;
+    uint8_t *cls = nullptr, *needd = nullptr;  // per packed site (multi-constant split of the force)
+    void *cbd = nullptr;                       // merged boundary coefficients (multi-constant)
     double *partials = nullptr, *stage = nullptr;
     int32_t *stage_t = nullptr;
     FireDev *fds = nullptr;
@@ -326,6 +337,9 @@ template <class T> static BatchArgs<T> batch_args(qmin_batch_ctx *b)
     B.L.types = b->types;
     B.L.objs = (const ObjDev<T> *)b->objs;
     fill_lat_params(B.L, b->params, b->metric_mode);
+    B.L.cbd = (const T *)b->cbd;
+    B.cls = b->params.multi_constant ? b->cls : nullptr;
+    B.needd = b->params.multi_constant ? b->needd : nullptr;
     B.solves = b->solves;
     B.chunks = b->chunks;
     B.nchunks = b->nchunks;
@@ -419,7 +433,8 @@ int qmin_batch_create(int nsolves, const int32_t *dims, int precision, int metri
               cudaMalloc(&b->stage, sizeof(double) * 5 * (size_t)b->maxN) == cudaSuccess &&
               cudaMalloc(&b->stage_t, sizeof(int32_t) * (size_t)b->maxN) == cudaSuccess &&
               cudaMalloc(&b->fds, sizeof(FireDev) * nsolves) == cudaSuccess &&
-              cudaMalloc(&b->any, sizeof(int)) == cudaSuccess && cudaMallocHost(&b->any_h, sizeof(int)) == cudaSuccess;
+              cudaMalloc(&b->any, sizeof(int)) == cudaSuccess && cudaMallocHost(&b->any_h, sizeof(int)) == cudaSuccess &&
+              cudaMalloc(&b->cls, (size_t)b->P) == cudaSuccess && cudaMalloc(&b->needd, (size_t)b->P) == cudaSuccess;
     if (!ok) {
         cudaGetLastError();
         qmin_batch_destroy(b);
@@ -429,6 +444,8 @@ int qmin_batch_create(int nsolves, const int32_t *dims, int precision, int metri
     cudaMemsetAsync(b->V, 0, 5 * plane, b->stream);
     cudaMemsetAsync(b->F, 0, 5 * plane, b->stream);
     cudaMemsetAsync(b->types, 0, (size_t)b->P, b->stream);
+    cudaMemsetAsync(b->cls, 2, (size_t)b->P, b->stream);    // nothing deep until a solve is set
+    cudaMemsetAsync(b->needd, 1, (size_t)b->P, b->stream);  // every derivative until then
     cudaMemsetAsync(b->objs, 0, sizeof(ObjDev<double>) * kObjPerSolve * nsolves, b->stream);
     cudaMemcpyAsync(b->solves, b->solves_h.data(), sizeof(SolveDesc) * nsolves, cudaMemcpyHostToDevice, b->stream);
     cudaMemcpyAsync(b->chunks, b->chunks_h.data(), sizeof(ChunkDesc) * b->nchunks, cudaMemcpyHostToDevice, b->stream);
@@ -446,7 +463,7 @@ int qmin_batch_destroy(qmin_batch b)
     if (b->stream) cudaStreamSynchronize(b->stream);
     if (b->graph) cudaGraphExecDestroy(b->graph);
     void *bufs[] = {b->Q, b->V, b->F, b->D, b->objs, b->types, b->partials, b->stage, b->stage_t, b->fds, b->any,
-                    b->solves, b->chunks};
+                    b->solves, b->chunks, b->cls, b->needd, b->cbd};
     for (void *p : bufs)
         if (p) cudaFree(p);
     if (b->any_h) cudaFreeHost(b->any_h);
@@ -467,6 +484,26 @@ int qmin_batch_set_params(qmin_batch b, const qmin_ldg_params *p)
             return bfail(QMIN_ENOMEM, "qmin_batch_set_params: derivative planes allocation failed");
         }
         BCK(cudaMemsetAsync(b->D, 0, 15 * (size_t)b->P * b->esz, b->stream));
+    }
+    if (p->multi_constant) {
+        // the merged boundary coefficients of the straight-line boundary forms
+        const size_t n = (size_t)QMIN_BND_CASES * 5 * QMIN_BND_W;
+        if (!b->cbd && cudaMalloc(&b->cbd, n * b->esz) != cudaSuccess) {
+            cudaGetLastError();
+            b->cbd = nullptr;
+            return bfail(QMIN_ENOMEM, "qmin_batch_set_params: boundary coefficient allocation failed");
+        }
+        if (b->prec == QMIN_FP64) {
+            std::vector<double> c(n);
+            fill_boundary_coeffs(*p, c.data());
+            BCK(cudaMemcpyAsync(b->cbd, c.data(), n * sizeof(double), cudaMemcpyHostToDevice, b->stream));
+            BCK(cudaStreamSynchronize(b->stream));
+        } else {
+            std::vector<float> c(n);
+            fill_boundary_coeffs(*p, c.data());
+            BCK(cudaMemcpyAsync(b->cbd, c.data(), n * sizeof(float), cudaMemcpyHostToDevice, b->stream));
+            BCK(cudaStreamSynchronize(b->stream));
+        }
     }
     b->have_params = true;
     if (b->graph) {
@@ -492,6 +529,37 @@ int qmin_batch_set_solve(qmin_batch b, int s, const double *Q, const int32_t *ty
         if (types[i] <= 0) ++nT;
     }
     b->ntotal_h[s] = nT;
+    {
+        // site classes of the split force (deep bulk: type 0 with six type-0
+        // neighbours; 1: other LC sites; 2: objects) and the sites whose
+        // derivative planes the class-1 forms read, with this solve's periodic wrap
+        std::vector<uint8_t> cls((size_t)n), need((size_t)n, 0);
+        auto nb = [&](int i, int k) {
+            const int x = i % sd.Lx, r = i / sd.Lx, y = r % sd.Ly, z = r / sd.Ly;
+            switch (k) {
+            case 0: return (x == 0 ? sd.Lx - 1 : x - 1) + sd.Lx * (y + sd.Ly * z);
+            case 1: return (x == sd.Lx - 1 ? 0 : x + 1) + sd.Lx * (y + sd.Ly * z);
+            case 2: return x + sd.Lx * ((y == 0 ? sd.Ly - 1 : y - 1) + sd.Ly * z);
+            case 3: return x + sd.Lx * ((y == sd.Ly - 1 ? 0 : y + 1) + sd.Ly * z);
+            case 4: return x + sd.Lx * (y + sd.Ly * (z == 0 ? sd.Lz - 1 : z - 1));
+            default: return x + sd.Lx * (y + sd.Ly * (z == sd.Lz - 1 ? 0 : z + 1));
+            }
+        };
+        for (int i = 0; i < n; ++i) {
+            if (types[i] > 0) {
+                cls[i] = 2;
+                continue;
+            }
+            bool deep = types[i] == 0;
+            for (int k = 0; k < 6 && deep; ++k) deep = types[nb(i, k)] == 0;
+            cls[i] = deep ? 0 : 1;
+            if (!deep)
+                for (int k = 0; k < 6; ++k) need[nb(i, k)] = 1;
+        }
+        BCK(cudaMemcpyAsync(b->cls + sd.off, cls.data(), (size_t)n, cudaMemcpyHostToDevice, b->stream));
+        BCK(cudaMemcpyAsync(b->needd + sd.off, need.data(), (size_t)n, cudaMemcpyHostToDevice, b->stream));
+        BCK(cudaStreamSynchronize(b->stream));
+    }
     BCK(cudaMemcpyAsync(b->stage, Q, sizeof(double) * 5 * (size_t)n, cudaMemcpyHostToDevice, b->stream));
     BCK(cudaMemcpyAsync(b->stage_t, types, sizeof(int32_t) * (size_t)n, cudaMemcpyHostToDevice, b->stream));
     if (b->prec == QMIN_FP64)

@@ -364,6 +364,65 @@ template <class T> __device__ __forceinline__ const T *site_field(const Lat<T> &
     return h;
 }
 
+// periodic wrap of a coordinate at most two steps outside [0, m), m >= 2
+__device__ __forceinline__ int wrap_near(int v, int m) { return v < 0 ? v + m : (v >= m ? v - m : v); }
+
+// Force at Q of a deep bulk site (type 0 with six type-0 neighbours, so every
+// neighbour derivative the bulk forms read is a central difference) through
+// the combined L1-L4 form over Q on the 25-point stencil.  The site is li =
+// x + Lx (y + Ly z) of a periodic Lx x Ly x Lz box whose planes start at
+// element `base` (0 for a lattice, the solve's offset in a batch); i is its
+// index in the planes.  M is applied as the reference does for type-0 sites
+// (twice in CPU mode, the fields between the two).
+template <class T>
+__device__ __forceinline__ void deep_force_box(const Lat<T> &L, long long base, int Lx, int Ly, int Lz, int li,
+                                               long long i, T *f)
+{
+    const int x = li % Lx, r = li / Lx, y = r % Ly, z = r / Ly;
+    const int sxy = Lx * Ly;
+    int xi[5], yo[5], zo[5];
+#pragma unroll
+    for (int d = 0; d < 5; ++d) {
+        xi[d] = wrap_near(x + d - 2, Lx);
+        yo[d] = Lx * wrap_near(y + d - 2, Ly);
+        zo[d] = sxy * wrap_near(z + d - 2, Lz);
+    }
+    const T *Q = L.Q + base;
+    const long long P = L.P;
+#define QQ(dx, dy, dz, c) ld(Q + (long long)(c) * P + (xi[(dx) + 2] + yo[(dy) + 2] + zo[(dz) + 2]))
+    T q[5];
+#pragma unroll
+    for (int k = 0; k < 5; ++k) q[k] = QQ(0, 0, 0, k);
+    T force[5];
+    phase_force(L.a, L.b, L.c, q, force);
+    T s2[5];
+    if (L.L4 == T(0)) {
+        QMIN_BULK_Q25_NO_L4(L.cq, s2);
+    } else {
+        QMIN_BULK_Q25(L.cq, s2);
+    }
+#undef QQ
+#pragma unroll
+    for (int k = 0; k < 5; ++k) f[k] = force[k] - s2[k];
+    if (L.metric_mode == 0) metric(f);
+    if (L.efield)
+#pragma unroll
+        for (int k = 0; k < 5; ++k) f[k] -= L.fE[k];
+    if (L.hfield)
+#pragma unroll
+        for (int k = 0; k < 5; ++k) f[k] -= L.fH[k];
+    T h[3];
+    if (const T *hs = site_field(L, i, h)) {
+        const T hx = hs[0], hy = hs[1], hz = hs[2], fp = L.hvp;
+        f[0] -= T(-0.5) * fp * (hx * hx - hz * hz);
+        f[1] -= -fp * hx * hy;
+        f[2] -= -fp * hx * hz;
+        f[3] -= T(-0.5) * fp * (hy * hy - hz * hz);
+        f[4] -= -fp * hy * hz;
+    }
+    metric(f);
+}
+
 // accessor over the global SoA planes; neighbour derivatives from the D planes.
 // It copies the few pointers it needs: holding a reference to the kernel's
 // parameter block would force that block into local memory.

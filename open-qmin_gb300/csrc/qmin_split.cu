@@ -18,57 +18,11 @@ namespace qmin {
 
 namespace {
 
-// periodic wrap of a coordinate at most two steps outside [0, m), m >= 2
-__device__ __forceinline__ int wrap_near(int v, int m) { return v < 0 ? v + m : (v >= m ? v - m : v); }
-
-// force at the predicted Q of a deep bulk site; M applied as the reference does
-// for type-0 sites (twice in CPU mode, the fields between the two)
+// force at the predicted Q of a deep bulk site of the lattice
 template <class T>
 __device__ __forceinline__ void deep_force(const Lat<T> &L, int i, T *f)
 {
-    const int x = i % L.Lx, r = i / L.Lx, y = r % L.Ly, z = r / L.Ly;
-    const int sxy = L.Lx * L.Ly;
-    int xi[5], yo[5], zo[5];
-#pragma unroll
-    for (int d = 0; d < 5; ++d) {
-        xi[d] = wrap_near(x + d - 2, L.Lx);
-        yo[d] = L.Lx * wrap_near(y + d - 2, L.Ly);
-        zo[d] = sxy * wrap_near(z + d - 2, L.Lz);
-    }
-    const T *Q = L.Q;
-    const long long P = L.P;
-#define QQ(dx, dy, dz, c) ld(Q + (long long)(c) * P + (xi[(dx) + 2] + yo[(dy) + 2] + zo[(dz) + 2]))
-    T q[5];
-#pragma unroll
-    for (int k = 0; k < 5; ++k) q[k] = QQ(0, 0, 0, k);
-    T force[5];
-    phase_force(L.a, L.b, L.c, q, force);
-    T s2[5];
-    if (L.L4 == T(0)) {
-        QMIN_BULK_Q25_NO_L4(L.cq, s2);
-    } else {
-        QMIN_BULK_Q25(L.cq, s2);
-    }
-#undef QQ
-#pragma unroll
-    for (int k = 0; k < 5; ++k) f[k] = force[k] - s2[k];
-    if (L.metric_mode == 0) metric(f);
-    if (L.efield)
-#pragma unroll
-        for (int k = 0; k < 5; ++k) f[k] -= L.fE[k];
-    if (L.hfield)
-#pragma unroll
-        for (int k = 0; k < 5; ++k) f[k] -= L.fH[k];
-    T h[3];
-    if (const T *hs = site_field(L, i, h)) {
-        const T hx = hs[0], hy = hs[1], hz = hs[2], fp = L.hvp;
-        f[0] -= T(-0.5) * fp * (hx * hx - hz * hz);
-        f[1] -= -fp * hx * hy;
-        f[2] -= -fp * hx * hz;
-        f[3] -= T(-0.5) * fp * (hy * hy - hz * hz);
-        f[4] -= -fp * hy * hz;
-    }
-    metric(f);
+    deep_force_box(L, 0, L.Lx, L.Ly, L.Lz, i, (long long)i, f);
 }
 
 template <class T>
