@@ -404,6 +404,10 @@ __device__ __forceinline__ void deep_force_box(const Lat<T> &L, long long base, 
 #undef QQ
 #pragma unroll
     for (int k = 0; k < 5; ++k) f[k] = force[k] - s2[k];
+    if (L.metric_mode == 0 && !L.efield && !L.hfield && !L.Hv) {
+        metric2(f);
+        return;
+    }
     if (L.metric_mode == 0) metric(f);
     if (L.efield)
 #pragma unroll

@@ -173,6 +173,10 @@ __device__ __forceinline__ void deep_force_finish(const Lat<T> &L, const T *q, c
     phase_force(L.a, L.b, L.c, q, force);
 #pragma unroll
     for (int k = 0; k < 5; ++k) f[k] = force[k] - s2[k];
+    if (L.metric_mode == 0 && !L.efield && !L.hfield && !L.Hv) {
+        metric2(f);
+        return;
+    }
     if (L.metric_mode == 0) metric(f);
     if (L.efield)
 #pragma unroll
