@@ -6,6 +6,7 @@
 // they implement.
 #pragma once
 #include <cuda_runtime.h>
+#include <math.h>
 #include <stdint.h>
 
 namespace qmin {
@@ -32,6 +33,36 @@ __device__ __forceinline__ void phase_force(T a, T b, T c, const T *q, T *f)
                      T(6) * q1 * q2 - T(6) * q0 * q4};
 #pragma unroll
     for (int k = 0; k < 5; ++k) f[k] = -(g * d2[k]) - b * d3[k];
+}
+
+// f = phase force - e for a site with distortion (or other) term e, in the
+// fewest FP64 operations: the constant factors of dTrQ2 and dTrQ3 folded into
+// 2 (a + 4 c s) and 3 b, 6 b (loop-invariant), e entering the FMA chains.
+//   f0 = -2 g u0 + 3 b X0 - e0,  u0 = 2 q0 + q3,  X0 = -q1^2 + q3^2 + q4^2 + 2 q0 q3
+//   f1 = -4 g q1 - 6 b X1 - e1,  X1 = q0 q1 + q1 q3 + q2 q4
+//   f2 = -4 g q2 - 6 b X2 - e2,  X2 = q1 q4 - q2 q3
+//   f3 = -2 g u3 + 3 b X3 - e3,  u3 = q0 + 2 q3,  X3 = q0^2 - q1^2 + q2^2 + 2 q0 q3
+//   f4 = -4 g q4 - 6 b X4 - e4,  X4 = q1 q2 - q0 q4
+template <class T>
+__device__ __forceinline__ void phase_force_sub(T a, T b, T c, const T *q, const T *e, T *f)
+{
+    const T q0 = q[0], q1 = q[1], q2 = q[2], q3 = q[3], q4 = q[4];
+    // s = q0^2 + q1^2 + q2^2 + q3^2 + q4^2 + q0 q3
+    const T s = fma(q0, q0 + q3, fma(q1, q1, fma(q2, q2, fma(q3, q3, q4 * q4))));
+    const T g2 = fma(T(8) * c, s, T(2) * a), g4 = g2 + g2;
+    const T b3 = T(3) * b, b6 = T(6) * b;
+    const T u0 = fma(T(2), q0, q3), u3 = fma(T(2), q3, q0);
+    const T w = fma(q0 + q0, q3, -(q1 * q1));  // 2 q0 q3 - q1^2
+    const T X0 = fma(q3, q3, fma(q4, q4, w));
+    const T X1 = fma(q0, q1, fma(q1, q3, q2 * q4));
+    const T X2 = fma(q1, q4, -(q2 * q3));
+    const T X3 = fma(q0, q0, fma(q2, q2, w));
+    const T X4 = fma(q1, q2, -(q0 * q4));
+    f[0] = fma(b3, X0, fma(-g2, u0, -e[0]));
+    f[1] = fma(-b6, X1, fma(-g4, q1, -e[1]));
+    f[2] = fma(-b6, X2, fma(-g4, q2, -e[2]));
+    f[3] = fma(b3, X3, fma(-g2, u3, -e[3]));
+    f[4] = fma(-b6, X4, fma(-g4, q4, -e[4]));
 }
 
 // lcForce::bulkL1Force cross terms (lcForces.h:26-37): S0 += S0+S3, S3 += S0+S3, S1,S2,S4 *= 2

@@ -207,9 +207,6 @@ __device__ __forceinline__ void site_force_core(const Lat<T> &L, const A &acc, i
 #pragma unroll
         for (int k = 0; k < 5; ++k) nq[s][k] = acc.nq(s, k);
 
-    T force[5];
-    phase_force(L.a, L.b, L.c, q, force);
-
     const bool boundary = (t == -1);  // type -2 uses the bulk forms (DT:241-279)
     int mask = 0;                     // which neighbours are objects
     if (t < 0) {
@@ -322,8 +319,7 @@ __device__ __forceinline__ void site_force_core(const Lat<T> &L, const A &acc, i
             }
         }
     }
-#pragma unroll
-    for (int k = 0; k < 5; ++k) f[k] = force[k] - sp[k];
+    phase_force_sub(L.a, L.b, L.c, q, sp, f);
 
     if (L.metric_mode == 0 && t == 0) metric(f);
     if (t < 0 && mask) {
@@ -393,8 +389,6 @@ __device__ __forceinline__ void deep_force_box(const Lat<T> &L, long long base, 
     T q[5];
 #pragma unroll
     for (int k = 0; k < 5; ++k) q[k] = QQ(0, 0, 0, k);
-    T force[5];
-    phase_force(L.a, L.b, L.c, q, force);
     T s2[5];
     if (L.L4 == T(0)) {
         QMIN_BULK_Q25_NO_L4(L.cq, s2);
@@ -402,8 +396,7 @@ __device__ __forceinline__ void deep_force_box(const Lat<T> &L, long long base, 
         QMIN_BULK_Q25(L.cq, s2);
     }
 #undef QQ
-#pragma unroll
-    for (int k = 0; k < 5; ++k) f[k] = force[k] - s2[k];
+    phase_force_sub(L.a, L.b, L.c, q, s2, f);
     if (L.metric_mode == 0 && !L.efield && !L.hfield && !L.Hv) {
         metric2(f);
         return;

@@ -169,10 +169,7 @@ template <int TX> __device__ __forceinline__ void tile_site(int t, int &lx, int 
 template <class T>
 __device__ __forceinline__ void deep_force_finish(const Lat<T> &L, const T *q, const T *s2, long long i, T *f)
 {
-    T force[5];
-    phase_force(L.a, L.b, L.c, q, force);
-#pragma unroll
-    for (int k = 0; k < 5; ++k) f[k] = force[k] - s2[k];
+    phase_force_sub(L.a, L.b, L.c, q, s2, f);
     if (L.metric_mode == 0 && !L.efield && !L.hfield && !L.Hv) {
         metric2(f);
         return;
