@@ -104,6 +104,17 @@ __device__ __forceinline__ T dot_qt(const T *x, const T *y)
     return s + x[0] * y[3];
 }
 
+// acc += (F.F, v.v, F.v) in the QT metric, accumulated inside the FMA chains
+// (x.y = x0 (y0 + y3) + x1 y1 + x2 y2 + x3 y3 + x4 y4, the y0 + y3 of v shared)
+template <class T>
+__device__ __forceinline__ void dot3_acc(const T *f, const T *v, T *acc)
+{
+    const T fs = f[0] + f[3], vs = v[0] + v[3];
+    acc[0] = fma(f[0], fs, fma(f[1], f[1], fma(f[2], f[2], fma(f[3], f[3], fma(f[4], f[4], acc[0])))));
+    acc[1] = fma(v[0], vs, fma(v[1], v[1], fma(v[2], v[2], fma(v[3], v[3], fma(v[4], v[4], acc[1])))));
+    acc[2] = fma(f[0], vs, fma(f[1], v[1], fma(f[2], v[2], fma(f[3], v[3], fma(f[4], v[4], acc[2])))));
+}
+
 template <class T>
 __device__ __forceinline__ T tr_q2(const T *q)
 {

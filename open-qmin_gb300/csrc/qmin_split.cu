@@ -35,9 +35,13 @@ __device__ __forceinline__ void kick_and_sum(const Lat<T> &L, long long i, T hdt
         L.F[k * L.P + i] = f[k];
         L.V[k * L.P + i] = v[k];
     }
-    acc[0] += (double)dot_qt(f, f);
-    acc[1] += (double)dot_qt(v, v);
-    acc[2] += (double)dot_qt(f, v);
+    if constexpr (sizeof(T) == 8) {
+        dot3_acc(f, v, acc);
+    } else {
+        acc[0] += (double)dot_qt(f, f);
+        acc[1] += (double)dot_qt(v, v);
+        acc[2] += (double)dot_qt(f, v);
+    }
 }
 
 int list_grid(int n) { return std::max(1, std::min((n + kBlock - 1) / kBlock, 152 * 4)); }
