@@ -154,9 +154,15 @@ def lib():
     return _lib
 
 
-def _check(code):
+def _check(code, iterations=None, force_max=None):
+    """Raise QminError for a non-zero status; a minimiser's error carries the
+    iterations it completed and the last forceMax (the C entry points write
+    both before reporting a non-finite force norm)."""
     if code != QMIN_OK:
-        raise QminError(code, lib().qmin_last_error_string().decode())
+        err = QminError(code, lib().qmin_last_error_string().decode())
+        err.iterations = iterations.value if iterations is not None else None
+        err.forceMax = force_max.value if force_max is not None else None
+        raise err
 
 
 def _dp(a):
@@ -304,19 +310,19 @@ class Lattice:
     def adam_run(self, max_iterations, dt=1e-4, beta1=0.9, beta2=0.99, eps=1e-8, force_cutoff=1e-12, reset=True):
         it, fm = C.c_int(), C.c_double()
         _check(lib().qmin_adam_run(self._h, beta1, beta2, eps, dt, force_cutoff, int(max_iterations), int(reset),
-                                   C.byref(it), C.byref(fm)))
+                                   C.byref(it), C.byref(fm)), it, fm)
         return dict(iterations=it.value, forceMax=fm.value)
 
     def nesterov_run(self, max_iterations, dt=1e-4, mu=0.01, force_cutoff=1e-12, reset=True):
         it, fm = C.c_int(), C.c_double()
         _check(lib().qmin_nesterov_run(self._h, dt, mu, force_cutoff, int(max_iterations), int(reset), C.byref(it),
-                                       C.byref(fm)))
+                                       C.byref(fm)), it, fm)
         return dict(iterations=it.value, forceMax=fm.value)
 
     def lbfgs_run(self, max_iterations, eta=1e-4, m=5, force_cutoff=1e-12, reset=True):
         it, fm = C.c_int(), C.c_double()
         _check(lib().qmin_lbfgs_run(self._h, int(m), eta, force_cutoff, int(max_iterations), int(reset), C.byref(it),
-                                    C.byref(fm)))
+                                    C.byref(fm)), it, fm)
         return dict(iterations=it.value, forceMax=fm.value)
 
     def get_types(self):
@@ -367,7 +373,7 @@ class Lattice:
     def gd_run(self, max_iterations, dt=0.01, force_cutoff=1e-7, reset=True):
         its, fm = C.c_int(), C.c_double()
         _check(lib().qmin_gd_run(self._h, dt, force_cutoff, int(max_iterations), int(bool(reset)), C.byref(its),
-                                 C.byref(fm)))
+                                 C.byref(fm)), its, fm)
         return dict(iterations=its.value, forceMax=fm.value)
 
     def set_fire_kernel(self, mode):

@@ -1271,9 +1271,9 @@ template <class T> static int lbfgs_impl(qmin_ctx *h, int m, double eta, int max
 {
     Lat<T> L = make_lat<T>(h);
     if (h->iter_h->iterations == 0) {
-        // LoLBFGSStepCPU step 1 (energyMinimizerLoLBFGS.cpp:110-116)
+        // LoLBFGSStepCPU step 1 (energyMinimizerLoLBFGS.cpp:110-116): p = forces at Q,
+        // which the iteration's first pass reads from F
         h->launches += launch_force<T>(L, h->grid, h->stream);
-        h->launches += launch_lbfgs_first<T>(L, (T *)h->lbp, h->iter, h->stream);
     }
     const double args[4] = {(double)m, eta, 0, 0};
     int r = capture_chunk(h, 3, args, [&]() {

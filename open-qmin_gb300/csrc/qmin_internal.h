@@ -118,10 +118,11 @@ template <class T> int launch_gd_move(const Lat<T> &L, IterDev *it, double dt, c
 template <class T> int launch_ff_dot(const Lat<T> &L, IterDev *it, double *partials, int grid, cudaStream_t s);
 int launch_norm_control(IterDev *it, const double *partials, int nparts, int adam, double beta1, double beta2,
                         cudaStream_t s);
+// one L-BFGS iteration; p enters as L.F (the forces at Q), so the forces
+// must be current when the first iteration starts
 template <class T>
 int launch_lbfgs_iteration(const Lat<T> &L, T *p, T *sbase, T *ybase, IterDev *it, int m, double eta,
                            double *partials, int grid, cudaStream_t s);
-template <class T> int launch_lbfgs_first(const Lat<T> &L, T *p, IterDev *it, cudaStream_t s);
 
 int reduction_grid(int N);
 

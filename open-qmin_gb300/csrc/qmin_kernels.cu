@@ -628,147 +628,228 @@ __global__ void __launch_bounds__(kBlock) k_norm_control(IterDev *it, const doub
 }
 
 // ------------------------------------------------------------------ L-BFGS
-// energyMinimizerLoLBFGS::LoLBFGSStepCPU (energyMinimizerLoLBFGS.cpp:105-193).
-// Pair slot t of the two-loop recursion is computed on the device from the
-// iteration counter, so one captured iteration serves every iteration.
-// lb[0..m) = s.y per ii, lb[16..16+m) = alpha per ii, lb[32] = step-3 factor,
-// lb[33] = step-4 factor.
+// energyMinimizerLoLBFGS::LoLBFGSStepCPU (energyMinimizerLoLBFGS.cpp:105-193)
+// as 2m + 1 streaming passes around the force.  Each pass applies one vector
+// update of the two-loop recursion and forms the dot product that the next
+// update's coefficient needs, so a vector is read once per use:
+//   step 2, ii = 0 .. m-2:  p += -alpha_ii y_ii;  dot s_(ii+1).p
+//   ii = m-1 with step 3:   p += -alpha_(m-1) y_(m-1);  p += (sy_0 / y_0.y_0) y_0;
+//                           dot y_(m-1).p (step 4's first beta)
+//   step 4, ii = m-1 .. 1:  p += (alpha_ii - beta_ii) s_ii;  dot y_(ii-1).p
+//   ii = 0 with the step:   p += (alpha_0 - beta_0) s_0;  s_cur = eta p;
+//                           y_cur = F;  Q += s_cur
+//   after the force:        y_cur += -F;  dots F.F, s_cur.y_cur, y_cur.y_cur, s_cur.F
+// The vector updates are the reference's, element by element.  A stored
+// pair's s.y and y.y never change, so they are formed once, in the pass after
+// the force, and kept per slot; alpha_0 of the next iteration (s_0.p / s_0.y_0
+// with p the new forces, the reference's unscaledStep = returnForces()) comes
+// from the same pass, and the first pass of an iteration reads p from F.
+// Pair ii sits in slot (cur - ii - 1 + m) % m, cur = iterations % m.
+// lb[0..16): s.y per slot; lb[16..32): y.y per slot; lb[32..48): alpha per ii;
+// lb[48]: alpha_ii - beta_ii of the pending step-4 update.
 __device__ __forceinline__ int lb_slot(const IterDev *it, int m, int ii)
 {
     const int cur = it->iterations % m;
     return (cur - ii - 1 + m) % m;
 }
 
-template <class T>
-__global__ void __launch_bounds__(kBlock) k_lb_dot(const IterDev *__restrict__ it, int op, int ii, int m,
-                                                   const T *p, const T *sb, const T *yb, long long n5, double *partials)
-{
-    if (!it->active) return;
-    const int t = lb_slot(it, m, ii);
-    const int last = (it->iterations % m - 1 + m) % m;
-    const T *s = sb + t * n5, *y = yb + t * n5;
-    double acc[2] = {0.0, 0.0};
-    for (long long j = blockIdx.x * (long long)kBlock + threadIdx.x; j < n5; j += (long long)gridDim.x * kBlock) {
-        if (op == 0) {
-            acc[0] += (double)(s[j] * y[j]);
-            acc[1] += (double)(s[j] * p[j]);
-        } else if (op == 1) {
-            const T yl = yb[last * n5 + j];
-            acc[0] += (double)(yl * yl);
-        } else if (op == 2) {
-            acc[0] += (double)(y[j] * p[j]);
-        } else {
-            acc[0] += (double)(p[j] * p[j]);
-        }
-    }
-    block_sum<2>(acc);
-    if (threadIdx.x == 0) {
-        partials[2 * blockIdx.x] = acc[0];
-        partials[2 * blockIdx.x + 1] = acc[1];
-    }
-}
+template <class T> struct LbVec;
+template <> struct LbVec<float> {
+    using V = float4;
+};
+template <> struct LbVec<double> {
+    using V = double2;
+};
 
-__global__ void __launch_bounds__(kBlock) k_lb_scalar(IterDev *it, int op, int ii, const double *partials,
-                                                      int nparts)
+// a . b over one 16-byte vector, summed in the element type (FP32: four
+// products, one FP64 addition per two vectors in the caller)
+__device__ __forceinline__ float vdot(const float4 &a, const float4 &b)
 {
-    if (!it->active) return;
-    double v[2];
-    sum_partials<2>(partials, nparts, v);
-    if (threadIdx.x != 0) return;
-    double *lb = it->lb;
-    if (op == 0) {
-        lb[ii] = v[0];
-        lb[16 + ii] = 0;
-        if (v[0] != 0) lb[16 + ii] = v[1] / v[0];
-    } else if (op == 1) {
-        lb[32] = v[0] != 0 ? lb[0] / v[0] : 0.0;
-        lb[34] = v[0] != 0 ? 1.0 : 0.0;
-    } else if (op == 2) {
-        lb[33] = 0.0;
-        if (lb[ii] != 0) lb[33] = lb[16 + ii] - v[0] / lb[ii];
-    } else {
-        it->forceMax = sqrt(v[0]) / (double)it->ndof;
-        it->iterations += 1;
-        if (!isfinite(v[0])) {
-            it->status = 1;
-            it->active = 0;
-            return;
-        }
-        it->active = (it->iterations < it->max_iters && it->forceMax > it->fcut) ? 1 : 0;
-    }
+    return a.x * b.x + a.y * b.y + a.z * b.z + a.w * b.w;
 }
-
-// op 0: p += -alpha[ii] y_t;  op 1: p += (sy0 / y.y) y_last (if y.y != 0);
-// op 2: p += (alpha[ii] - beta) s_t (if s.y != 0)
-template <class T>
-__global__ void __launch_bounds__(kBlock) k_lb_axpy(const IterDev *__restrict__ it, int op, int ii, int m, T *p,
-                                                    const T *sb, const T *yb, long long n5)
+__device__ __forceinline__ double vdot(const double2 &a, const double2 &b) { return a.x * b.x + a.y * b.y; }
+// x + c y lane by lane (host_dVec_plusEqual_dVec), c x, x + y
+__device__ __forceinline__ float4 vaxpy(const float4 &x, float c, const float4 &y)
 {
-    if (!it->active) return;
-    const int t = lb_slot(it, m, ii);
-    const int last = (it->iterations % m - 1 + m) % m;
-    const double *lb = it->lb;
-    const T *x;
-    T a;
-    if (op == 0) {
-        x = yb + t * n5;
-        a = T(-lb[16 + ii]);
-    } else if (op == 1) {
-        if (lb[34] == 0.0) return;
-        x = yb + last * n5;
-        a = T(lb[32]);
-    } else {
-        if (lb[ii] == 0) return;
-        x = sb + t * n5;
-        a = T(lb[33]);
-    }
-    for (long long j = blockIdx.x * (long long)kBlock + threadIdx.x; j < n5; j += (long long)gridDim.x * kBlock)
-        p[j] = p[j] + a * x[j];
+    return make_float4(x.x + c * y.x, x.y + c * y.y, x.z + c * y.z, x.w + c * y.w);
 }
-
-// s_cur = eta p; y_cur = F (old forces); Q += s_cur
-template <class T>
-__global__ void __launch_bounds__(kBlock) k_lb_update(const IterDev *__restrict__ it, int m, T eta, const T *p,
-                                                      T *sb, T *yb, const T *F, T *Q, long long n5)
+__device__ __forceinline__ double2 vaxpy(const double2 &x, double c, const double2 &y)
 {
-    if (!it->active) return;
-    const int cur = it->iterations % m;
-    T *s = sb + cur * n5, *y = yb + cur * n5;
-    for (long long j = blockIdx.x * (long long)kBlock + threadIdx.x; j < n5; j += (long long)gridDim.x * kBlock) {
-        const T sv = eta * p[j];
-        s[j] = sv;
-        y[j] = F[j];
-        Q[j] += sv;
-    }
+    return make_double2(x.x + c * y.x, x.y + c * y.y);
 }
+__device__ __forceinline__ float4 vscale(float c, const float4 &x)
+{
+    return make_float4(c * x.x, c * x.y, c * x.z, c * x.w);
+}
+__device__ __forceinline__ double2 vscale(double c, const double2 &x) { return make_double2(c * x.x, c * x.y); }
+__device__ __forceinline__ float4 vadd(const float4 &x, const float4 &y)
+{
+    return make_float4(x.x + y.x, x.y + y.y, x.z + y.z, x.w + y.w);
+}
+__device__ __forceinline__ double2 vadd(const double2 &x, const double2 &y) { return make_double2(x.x + y.x, x.y + y.y); }
 
-// p = F (new forces); y_cur += -1 * p; partial p.p
-template <class T>
-__global__ void __launch_bounds__(kBlock) k_lb_post(const IterDev *__restrict__ it, int m, T *p, T *yb, const T *F,
+// KIND 0: step 2 at ii < m - 1;  KIND 1: step 2 at ii = m - 1 with step 3;
+// KIND 2: step 4 at ii >= 1.  p_in is F in an iteration's first pass.  Two
+// 16-byte vectors per thread per trip; the dot's block partial in partials[b].
+template <class T, int KIND>
+__global__ void __launch_bounds__(kBlock) k_lb_pass(const IterDev *__restrict__ it, int ii, int m, const T *p_in,
+                                                    T *p, const T *__restrict__ sb, const T *__restrict__ yb,
                                                     long long n5, double *partials)
 {
     if (!it->active) return;
-    const int cur = it->iterations % m;
-    T *y = yb + cur * n5;
-    double acc[2] = {0.0, 0.0};
-    for (long long j = blockIdx.x * (long long)kBlock + threadIdx.x; j < n5; j += (long long)gridDim.x * kBlock) {
-        const T f = F[j];
-        p[j] = f;
-        y[j] = y[j] + T(-1.0) * f;
-        acc[0] += (double)(f * f);
+    using V = typename LbVec<T>::V;
+    const double *lb = it->lb;
+    const long long n = n5 / (16 / sizeof(T));
+    const V *x, *z = nullptr, *w = nullptr;
+    T c, cw = T(0);
+    bool upd = true;
+    if (KIND == 0 || KIND == 1) {
+        x = reinterpret_cast<const V *>(yb + lb_slot(it, m, ii) * n5);
+        c = T(-lb[32 + ii]);
+        if (KIND == 0) {
+            z = reinterpret_cast<const V *>(sb + lb_slot(it, m, ii + 1) * n5);
+        } else {
+            const int t0 = lb_slot(it, m, 0);
+            if (lb[16 + t0] != 0) {
+                w = reinterpret_cast<const V *>(yb + t0 * n5);
+                cw = T(lb[t0] / lb[16 + t0]);
+            }
+        }
+    } else {
+        const int t = lb_slot(it, m, ii);
+        x = reinterpret_cast<const V *>(sb + t * n5);
+        c = T(lb[48]);
+        upd = lb[t] != 0;
+        z = reinterpret_cast<const V *>(yb + lb_slot(it, m, ii - 1) * n5);
     }
-    block_sum<2>(acc);
-    if (threadIdx.x == 0) {
-        partials[2 * blockIdx.x] = acc[0];
-        partials[2 * blockIdx.x + 1] = 0.0;
+    const V *pi = reinterpret_cast<const V *>(p_in);
+    V *po = reinterpret_cast<V *>(p);
+    const bool store = upd || p_in != p;
+    const long long stride = (long long)gridDim.x * kBlock;
+    double acc[1] = {0.0};
+    for (long long j0 = blockIdx.x * (long long)kBlock + threadIdx.x; j0 < n; j0 += 2 * stride) {
+        T part = T(0);
+#pragma unroll
+        for (int u = 0; u < 2; ++u) {
+            const long long j = j0 + u * stride;
+            if (j < n) {
+                V v = pi[j];
+                V xv;
+                if (upd) {
+                    xv = x[j];
+                    v = vaxpy(v, c, xv);
+                }
+                if (KIND == 1 && w) v = vaxpy(v, cw, w[j]);
+                if (store) po[j] = v;
+                part += vdot(KIND == 1 ? xv : z[j], v);
+            }
+        }
+        acc[0] += (double)part;
+    }
+    block_sum<1>(acc);
+    if (threadIdx.x == 0) partials[blockIdx.x] = acc[0];
+}
+
+// step 4 at ii = 0 and the step: p_f = p + (alpha_0 - beta_0) s_0,
+// s_cur = eta p_f, y_cur = F (the old forces), Q += s_cur
+template <class T>
+__global__ void __launch_bounds__(kBlock) k_lb_step(const IterDev *__restrict__ it, int m, T eta, const T *p,
+                                                    T *sb, T *yb, const T *F, T *Q, long long n5)
+{
+    if (!it->active) return;
+    using V = typename LbVec<T>::V;
+    const double *lb = it->lb;
+    const long long n = n5 / (16 / sizeof(T));
+    const int t0 = lb_slot(it, m, 0), cur = it->iterations % m;
+    const bool upd = lb[t0] != 0;
+    const T c = T(lb[48]);
+    const V *p4 = reinterpret_cast<const V *>(p), *s0 = reinterpret_cast<const V *>(sb + t0 * n5);
+    const V *F4 = reinterpret_cast<const V *>(F);
+    V *sc = reinterpret_cast<V *>(sb + cur * n5), *yc = reinterpret_cast<V *>(yb + cur * n5);
+    V *Q4 = reinterpret_cast<V *>(Q);
+    for (long long j = blockIdx.x * (long long)kBlock + threadIdx.x; j < n; j += (long long)gridDim.x * kBlock) {
+        V v = p4[j];
+        if (upd) v = vaxpy(v, c, s0[j]);
+        const V sv = vscale(eta, v);
+        sc[j] = sv;
+        yc[j] = F4[j];
+        Q4[j] = vadd(Q4[j], sv);
     }
 }
 
+// y_cur += -F (F the new forces); dots F.F, s_cur.y_cur, y_cur.y_cur, s_cur.F
 template <class T>
-__global__ void k_copy(T *dst, const T *src, long long n)
+__global__ void __launch_bounds__(kBlock) k_lb_post(const IterDev *__restrict__ it, int m, const T *__restrict__ sb,
+                                                    T *yb, const T *__restrict__ F, long long n5, double *partials)
 {
-    for (long long j = blockIdx.x * (long long)blockDim.x + threadIdx.x; j < n; j += (long long)gridDim.x * blockDim.x)
-        dst[j] = src[j];
+    if (!it->active) return;
+    using V = typename LbVec<T>::V;
+    const long long n = n5 / (16 / sizeof(T));
+    const int cur = it->iterations % m;
+    const V *s = reinterpret_cast<const V *>(sb + cur * n5), *F4 = reinterpret_cast<const V *>(F);
+    V *y = reinterpret_cast<V *>(yb + cur * n5);
+    const long long stride = (long long)gridDim.x * kBlock;
+    double acc[4] = {0.0, 0.0, 0.0, 0.0};
+    for (long long j0 = blockIdx.x * (long long)kBlock + threadIdx.x; j0 < n; j0 += 2 * stride) {
+        T part[4] = {T(0), T(0), T(0), T(0)};
+#pragma unroll
+        for (int u = 0; u < 2; ++u) {
+            const long long j = j0 + u * stride;
+            if (j < n) {
+                const V f = F4[j], sv = s[j];
+                const V yv = vaxpy(y[j], T(-1), f);
+                y[j] = yv;
+                part[0] += vdot(f, f);
+                part[1] += vdot(sv, yv);
+                part[2] += vdot(yv, yv);
+                part[3] += vdot(sv, f);
+            }
+        }
+#pragma unroll
+        for (int k = 0; k < 4; ++k) acc[k] += (double)part[k];
+    }
+    block_sum<4>(acc);
+    if (threadIdx.x == 0)
+#pragma unroll
+        for (int k = 0; k < 4; ++k) partials[4 * blockIdx.x + k] = acc[k];
+}
+
+// op 0: alpha_ii = s_ii.p / s_ii.y_ii (0 when s.y = 0);
+// op 1: lb[48] = alpha_ii - y_ii.p / s_ii.y_ii (unused when s.y = 0)
+__global__ void __launch_bounds__(kBlock) k_lb_coef(IterDev *it, int op, int ii, int m, const double *partials,
+                                                    int nparts)
+{
+    if (!it->active) return;
+    double v[1];
+    sum_partials<1>(partials, nparts, v);
+    if (threadIdx.x != 0) return;
+    double *lb = it->lb;
+    const double sy = lb[lb_slot(it, m, ii)];
+    if (op == 0) lb[32 + ii] = sy != 0 ? v[0] / sy : 0.0;
+    else lb[48] = sy != 0 ? lb[32 + ii] - v[0] / sy : 0.0;
+}
+
+// after the post pass: forceMax = sqrt(F.F) / N, the iteration count and the
+// stopping test; the new pair's s.y and y.y and the next iteration's alpha_0
+__global__ void __launch_bounds__(kBlock) k_lb_close(IterDev *it, int m, const double *partials, int nparts)
+{
+    if (!it->active) return;
+    double v[4];
+    sum_partials<4>(partials, nparts, v);
+    if (threadIdx.x != 0) return;
+    double *lb = it->lb;
+    const int cur = it->iterations % m;
+    lb[cur] = v[1];
+    lb[16 + cur] = v[2];
+    lb[32] = v[1] != 0 ? v[3] / v[1] : 0.0;
+    it->forceMax = sqrt(v[0]) / (double)it->ndof;
+    it->iterations += 1;
+    if (!isfinite(v[0])) {
+        it->status = 1;
+        it->active = 0;
+        return;
+    }
+    it->active = (it->iterations < it->max_iters && it->forceMax > it->fcut) ? 1 : 0;
 }
 
 // ---------------------------------------------------------------- launchers
@@ -892,40 +973,31 @@ int launch_norm_control(IterDev *it, const double *partials, int nparts, int ada
     k_norm_control<<<1, kBlock, 0, s>>>(it, partials, nparts, adam, beta1, beta2);
     return 1;
 }
-template <class T> int launch_lbfgs_first(const Lat<T> &L, T *p, IterDev *it, cudaStream_t s)
-{
-    (void)it;
-    k_copy<T><<<elem_grid(5 * L.P), kBlock, 0, s>>>(p, L.F, 5 * L.P);
-    return 1;
-}
 template <class T>
 int launch_lbfgs_iteration(const Lat<T> &L, T *p, T *sb, T *yb, IterDev *it, int m, double eta, double *partials,
                            int grid, cudaStream_t s)
 {
     const long long n5 = 5 * L.P;
     int n = 0;
-    for (int ii = 0; ii < m; ++ii) {
-        k_lb_dot<T><<<grid, kBlock, 0, s>>>(it, 0, ii, m, p, sb, yb, n5, partials);
-        k_lb_scalar<<<1, kBlock, 0, s>>>(it, 0, ii, partials, grid);
-        k_lb_axpy<T><<<elem_grid(n5), kBlock, 0, s>>>(it, 0, ii, m, p, sb, yb, n5);
-        n += 3;
+    for (int ii = 0; ii < m - 1; ++ii) {
+        k_lb_pass<T, 0><<<grid, kBlock, 0, s>>>(it, ii, m, ii == 0 ? L.F : p, p, sb, yb, n5, partials);
+        k_lb_coef<<<1, kBlock, 0, s>>>(it, 0, ii + 1, m, partials, grid);
+        n += 2;
     }
-    k_lb_dot<T><<<grid, kBlock, 0, s>>>(it, 1, 0, m, p, sb, yb, n5, partials);
-    k_lb_scalar<<<1, kBlock, 0, s>>>(it, 1, 0, partials, grid);
-    k_lb_axpy<T><<<elem_grid(n5), kBlock, 0, s>>>(it, 1, 0, m, p, sb, yb, n5);
-    n += 3;
-    for (int ii = m - 1; ii >= 0; --ii) {
-        k_lb_dot<T><<<grid, kBlock, 0, s>>>(it, 2, ii, m, p, sb, yb, n5, partials);
-        k_lb_scalar<<<1, kBlock, 0, s>>>(it, 2, ii, partials, grid);
-        k_lb_axpy<T><<<elem_grid(n5), kBlock, 0, s>>>(it, 2, ii, m, p, sb, yb, n5);
-        n += 3;
+    k_lb_pass<T, 1><<<grid, kBlock, 0, s>>>(it, m - 1, m, m == 1 ? L.F : p, p, sb, yb, n5, partials);
+    k_lb_coef<<<1, kBlock, 0, s>>>(it, 1, m - 1, m, partials, grid);
+    n += 2;
+    for (int ii = m - 1; ii >= 1; --ii) {
+        k_lb_pass<T, 2><<<grid, kBlock, 0, s>>>(it, ii, m, p, p, sb, yb, n5, partials);
+        k_lb_coef<<<1, kBlock, 0, s>>>(it, 1, ii - 1, m, partials, grid);
+        n += 2;
     }
-    k_lb_update<T><<<elem_grid(n5), kBlock, 0, s>>>(it, m, T(eta), p, sb, yb, L.F, L.Q, n5);
+    k_lb_step<T><<<elem_grid(n5 / (16 / sizeof(T))), kBlock, 0, s>>>(it, m, T(eta), p, sb, yb, L.F, L.Q, n5);
     n += 1;
     // forces at the moved Q (no FIRE state: a force-only launch)
     n += launch_force(L, grid, s);
-    k_lb_post<T><<<grid, kBlock, 0, s>>>(it, m, p, yb, L.F, n5, partials);
-    k_lb_scalar<<<1, kBlock, 0, s>>>(it, 3, 0, partials, grid);
+    k_lb_post<T><<<grid, kBlock, 0, s>>>(it, m, sb, yb, L.F, n5, partials);
+    k_lb_close<<<1, kBlock, 0, s>>>(it, m, partials, grid);
     return n + 2;
 }
 
@@ -959,7 +1031,6 @@ int launch_energy_full(const Lat<T> &L, double *partials, int grid, double *out5
                                          cudaStream_t);                                   \
     template int launch_gd_move<T>(const Lat<T> &, IterDev *, double, cudaStream_t);                                 \
     template int launch_ff_dot<T>(const Lat<T> &, IterDev *, double *, int, cudaStream_t);                          \
-    template int launch_lbfgs_first<T>(const Lat<T> &, T *, IterDev *, cudaStream_t);                              \
     template int launch_lbfgs_iteration<T>(const Lat<T> &, T *, T *, T *, IterDev *, int, double, double *, int,   \
                                            cudaStream_t);                                                          \
     template int launch_energy_full<T>(const Lat<T> &, double *, int, double *, const double *, double, double,    \

@@ -116,6 +116,38 @@ def test_other_minimisers_fp64(qmin, oracle, name):
     assert rel_err(Q, g["qfinal"]) <= TOL_TRAJ
 
 
+@pytest.mark.parametrize("name", ["l123_walls_sphere_fire", "l1234_planar_fields_fire"])
+@pytest.mark.parametrize("m", [1, 2, 5])
+def test_lbfgs_multi_constant(qmin, oracle, name, m):
+    """L-BFGS through the multi-constant split force kernels and the fused
+    two-loop passes: FP64 follows the oracle's L-BFGS to 1e-9 after 40
+    iterations; 15 + 25 iterations (the second call resuming) give the
+    40-iteration run bit for bit; the FP32 form stays within 1e-4 of the
+    oracle in forceMax and Q."""
+    g = load(name)
+    cfg = parse_args(g["args"])
+    eta, n = 5e-4, 40
+    s = oracle_system(oracle, cfg)
+    lat = gpu_lattice(qmin, s, qmin.FP64)
+    lat32 = gpu_lattice(qmin, s, qmin.FP32)
+    lat_resumed = gpu_lattice(qmin, s, qmin.FP64)
+    ro = s.lbfgs(n, eta=eta, m=m)  # moves s.Q to the oracle's end state
+    r = lat.lbfgs_run(n, eta=eta, m=m)
+    assert r["iterations"] == ro["iterations"] == n
+    assert abs(r["forceMax"] - ro["forceMax"]) <= TOL_TRAJ * ro["forceMax"]
+    Q = lat.get_state(Q=True)[0]
+    assert rel_err(Q, s.Q) <= TOL_TRAJ
+    r1 = lat_resumed.lbfgs_run(15, eta=eta, m=m)
+    assert r1["iterations"] == 15
+    r2 = lat_resumed.lbfgs_run(n, eta=eta, m=m, reset=False)
+    assert r2 == r
+    np.testing.assert_array_equal(lat_resumed.get_state(Q=True)[0], Q)
+    r32 = lat32.lbfgs_run(n, eta=eta, m=m)
+    assert r32["iterations"] == n
+    assert abs(r32["forceMax"] - ro["forceMax"]) <= 1e-4 * ro["forceMax"]
+    assert rel_err(lat32.get_state(Q=True)[0], s.Q) <= 1e-4
+
+
 def test_c1_50cube_fire100(qmin, oracle):
     """openQmin -i 100 -l 50 --L1 2.32 end state (reference pin)."""
     g = load("c1_50cube_fire100")
