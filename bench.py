@@ -43,9 +43,9 @@ KERNEL_NAMES = ["fire_predictor", "first_derivatives", "force_kick_reduce", "fir
 FUSED_BYTES = {8: 241, 4: 121}
 
 
-# FP64 instructions per deep bulk site of the split force + kick (150 DFMA, 29 DMUL,
-# 12 DADD counted by ncu; 121 of them the 25-point form)
-FP64_OPS_PER_DEEP_SITE = 191
+# FP64 instructions per deep bulk site of the split force + kick (135 DFMA, 15.2 DMUL,
+# 22.7 DADD counted by ncu; 106 of them the 25-point form over shared sums)
+FP64_OPS_PER_DEEP_SITE = 173
 
 
 def kernel_roofline(lat, esz, N, peak, peak_kind, tag):
