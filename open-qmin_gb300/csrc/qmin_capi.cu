@@ -157,13 +157,17 @@ template <class T> void fill_lat_params(Lat<T> &L, const qmin_ldg_params &p, int
             L.cb[k * QMIN_BULK_W + n] = T(c);
         }
     // the kernels take the shared-sum form (its own coefficient layout) when L4
-    // is zero in the site precision
+    // is zero in the site precision; FP32 keeps the term-by-term form beside it
     const auto &q25k = L.L4 == T(0) ? qmin_q25c_k : qmin_q25_k;
     for (int k = 0; k < 5; ++k)
         for (int n = 0; n < QMIN_Q25_W; ++n) {
-            double c = 0.0;  // k L / 8 per stencil value or shared sum
-            for (int t = 0; t < 4; ++t) c += Lt[t] * (double)q25k[t][k][n] * 0.125;
+            double c = 0.0, cp = 0.0;  // k L / 8 per stencil value or shared sum
+            for (int t = 0; t < 4; ++t) {
+                c += Lt[t] * (double)q25k[t][k][n] * 0.125;
+                cp += Lt[t] * (double)qmin_q25_k[t][k][n] * 0.125;
+            }
             L.cq[k * QMIN_Q25_W + n] = T(c);
+            if constexpr (sizeof(T) == 4) L.cqp[k * QMIN_Q25_W + n] = T(cp);
         }
 }
 template void fill_lat_params<double>(Lat<double> &, const qmin_ldg_params &, int);

@@ -391,7 +391,12 @@ __device__ __forceinline__ void deep_force_box(const Lat<T> &L, long long base, 
     for (int k = 0; k < 5; ++k) q[k] = QQ(0, 0, 0, k);
     T s2[5];
     if (L.L4 == T(0)) {
-        QMIN_BULK_Q25_NO_L4(L.cq, s2);
+        // FP32 (latency-bound) term by term; FP64 (bound by the FP64 pipe) over shared sums
+        if constexpr (sizeof(T) == 4) {
+            QMIN_BULK_Q25_NO_L4_PLAIN(L.cqp, s2);
+        } else {
+            QMIN_BULK_Q25_NO_L4(L.cq, s2);
+        }
     } else {
         QMIN_BULK_Q25(L.cq, s2);
     }

@@ -48,7 +48,9 @@ template <class T> struct Lat {
     T hvp;              // its dchi * mu0
     int metric_mode, multi, efield, hfield;
     T cb[5 * QMIN_BULK_W];  // combined bulk multi-constant coefficients
-    T cq[5 * QMIN_Q25_W];   // the same form over Q on the 25-point stencil (deep bulk sites)
+    T cq[5 * QMIN_Q25_W];   // the same form over Q on the 25-point stencil (deep bulk sites;
+                            // without L4 over shared sums of stencil values)
+    T cqp[sizeof(T) == 4 ? 5 * QMIN_Q25_W : 1];  // FP32: the 25-point form term by term
     const T *cbd;           // merged boundary L2-L4 coefficients [27][5][QMIN_BND_W] in device memory, or null
     SplitLists split;       // deep / listed site classes and lists (all null when not built)
 };

@@ -16,7 +16,9 @@ enter several components' sums with coefficients in a fixed ratio (1, -1, 2,
 -2, 1/2 or -1/2 for every elastic constant), their combination is formed once
 and weighted once per component (greedy pairing, most reuse first).  On
 GB300 the FP64 deep-site force is bound by the FP64 pipe, and this takes the
-stencil from 121 to 106 FP64 operations per site.  The rewritten form is
+stencil from 121 to 106 FP64 operations per site.  The plain L4-free form
+(one term per stencil value) stays beside it: the batched FP32 kernel, bound
+by latency rather than by an arithmetic pipe, runs faster with it.  The rewritten form is
 checked term by term against the plain one before it is written.
 
     python3 oracle/ref/gen_q25_form.py           # write the header
@@ -81,7 +83,7 @@ def main():
              " * the 25-point stencil: s[c] = sum_m cq[c * QMIN_Q25_W + m] * QQ(dx, dy, dz, comp),",
              " * cq = sum_t L_t k_t / 8 with the terms ordered L2, L3, L4, L1 (qmin_q25_k).",
              " * Without L4: the same sums over shared combinations of stencil values,",
-             " * cq from qmin_q25c_k. */", "#pragma once",
+             " * cq from qmin_q25c_k (QMIN_BULK_Q25_NO_L4), or term by term (_PLAIN). */", "#pragma once",
              f"#define QMIN_Q25_W {width}"]
     lines.append("static const int qmin_q25_n[5] = {" + ",".join(str(len(f)) for f in forms) + "};")
     lines.append("static const int qmin_q25_k[4][5][QMIN_Q25_W] = " + table(forms, width) + ";")
@@ -97,6 +99,13 @@ def main():
                      + (f"{abs(r)!r} * " if abs(r) != 1 else "") + f"{operand(b)}; \\")
     for c, f in enumerate(cforms):
         terms = [f"(cq)[{c * width + m}] * {operand(key)}" for m, (key, _) in enumerate(f)]
+        lines.append(f"    (s)[{c}] = " + " + ".join(terms) + "; \\")
+    lines.append("    do {} while (0)")
+    # the plain L4-free form, one term per stencil value (qmin_q25_k layout)
+    lines.append("#define QMIN_BULK_Q25_NO_L4_PLAIN(cq, s) \\")
+    for c, f in enumerate(forms):
+        terms = [f"(cq)[{c * width + m}] * QQ({o[0]},{o[1]},{o[2]},{cc})" for m, ((o, cc), v) in enumerate(f)
+                 if v[0] or v[1] or v[3]]
         lines.append(f"    (s)[{c}] = " + " + ".join(terms) + "; \\")
     lines.append("    do {} while (0)")
     lines.append("")
