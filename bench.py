@@ -178,6 +178,24 @@ def traffic_from_profiles(kernel, precision_tag):
     return None
 
 
+def max_over_ranks(ms, device="cuda"):
+    """The job's time: the slowest rank's (every rank's timed region is closed
+    by a barrier); the value itself when no process group is running."""
+    import torch
+    dist = torch.distributed
+    if not (dist.is_available() and dist.is_initialized()) or dist.get_world_size() == 1:
+        return ms
+    t = torch.tensor([ms], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_value(world, sites, steps, ms):
+    """Whole-job site-steps/s: every replica advances its own lattice of
+    `sites` sites by `steps` FIRE iterations within the job's time."""
+    return world * sites * steps / (ms / 1e3)
+
+
 def run_ours(args, rank, world):
     import torch
     import __graft_entry__ as ge
@@ -230,11 +248,8 @@ def run_ours(args, rank, world):
     # ---- device-resident FP64 run (the headline)
     lat, r, ms, launches, clocks = timed_fire(q.FP64)
     ms_all = [ms]
-    if dist:
-        t = torch.tensor([ms], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
-    value = world * N * K / (ms / 1e3)
+    ms = max_over_ranks(ms)
+    value = job_value(world, N, K, ms)
 
     # ---- roofline of the dominant kernel (direct launches, CUDA events per kernel)
     import ctypes as C
@@ -295,15 +310,11 @@ def run_e2e(q, consts, g, K, W, barrier, dist):
     torch.cuda.synchronize()
     wall_e2e = time.perf_counter() - t0
     barrier()
-    ms_e2e = max(e0.elapsed_time(e1), wall_e2e * 1e3)
-    if dist:
-        t = torch.tensor([ms_e2e], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms_e2e = float(t.item())
+    ms_e2e = max_over_ranks(max(e0.elapsed_time(e1), wall_e2e * 1e3))
     h2d = N * 5 * 8 + N * 4
     d2h = N * 5 * 8
     world = int(os.environ.get("WORLD_SIZE", 1))
-    e2e = {"value": world * N * K / (ms_e2e / 1e3), "unit": "site-steps/s", "h2d_bytes_per_step": h2d / K,
+    e2e = {"value": job_value(world, N, K, ms_e2e), "unit": "site-steps/s", "h2d_bytes_per_step": h2d / K,
            "d2h_bytes_per_step": d2h / K,
            "note": "per job: upload Q0 (AoS f64) + int32 types, K FIRE iterations, download final Q; bytes amortised over K"}
     lat.close()
