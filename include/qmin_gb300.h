@@ -192,7 +192,12 @@ int qmin_adam_run(qmin_handle h, double beta1, double beta2, double eps, double 
 int qmin_nesterov_run(qmin_handle h, double dt, double mu, double force_cutoff, int max_iterations, int reset,
                       int *iterations, double *force_max);
 /* energyMinimizerLoLBFGS::setLoLBFGSParameters + minimize
- * (energyMinimizerLoLBFGS.h:29-44, .cpp:195-226); history reset when reset != 0 */
+ * (energyMinimizerLoLBFGS.h:29-44, .cpp:195-226); history reset when reset != 0.
+ * Each iteration starts its two-loop recursion from the resident forces (the
+ * reference's unscaledStep, which equals them after every iteration), so a
+ * call with reset = 0 after the state or forces were changed by another call
+ * continues from the forces now resident.  *iterations and *force_max are
+ * written before QMIN_ENONFINITE is returned. */
 int qmin_lbfgs_run(qmin_handle h, int m, double eta, double force_cutoff, int max_iterations, int reset,
                    int *iterations, double *force_max);
 
