@@ -108,6 +108,28 @@ def test_checkpoint_exact_resume(qmin, oracle, tmp_path, prec):
     assert fresh.energy()[0] == lat.energy()[0]
 
 
+@pytest.mark.parametrize("prec", [0, 1])
+def test_checkpoint_exact_resume_lbfgs(qmin, oracle, tmp_path, prec):
+    """A checkpoint taken between two L-BFGS calls carries the pair history,
+    the kept pair products and the forces the next iteration starts from: the
+    resumed run equals the uninterrupted one bit for bit."""
+    g = load("l123_walls_sphere_fire")
+    s = oracle_system(oracle, parse_args(g["args"]))
+    lat = gpu_lattice(qmin, s, prec)
+    lat.lbfgs_run(12, eta=5e-4)
+    lat.checkpoint_save(str(tmp_path / "ck.bin"))
+    r_a = lat.lbfgs_run(30, eta=5e-4, reset=False)
+    a = lat.get_state(Q=True, F=True)
+    fresh = qmin.Lattice(s.L, prec)
+    fresh.checkpoint_load(str(tmp_path / "ck.bin"))
+    r_b = fresh.lbfgs_run(30, eta=5e-4, reset=False)
+    b = fresh.get_state(Q=True, F=True)
+    assert r_a == r_b and r_a["iterations"] == 30
+    for x, y in zip(a, b):
+        if x is not None:
+            np.testing.assert_array_equal(x, y)
+
+
 def test_checkpoint_rejects_other_lattice(qmin, tmp_path):
     lat = qmin.Lattice((8, 8, 8))
     lat.set_params(-1.0, -12.3, 10.1, 2.32)
