@@ -80,10 +80,10 @@ template <class T> __global__ void __launch_bounds__(kBlock) k_b_pred(BatchArgs<
         const FireDev &fd = fds[ch.solve];
         if (!fd.active) continue;  // uniform per block
         // the deferred mix folded into the Verlet coefficients, as k_fire_pred does:
-        // v' = cvv v + cvf f, q' = q + cqv v + cqf f; formed in FP64 by one lane per warp
-        double cf[4] = {0.0, 0.0, 0.0, 0.0};
+        // v' = cvv v + cvf f, q' = q + dt v'; formed in FP64 by one lane per warp
+        double cf[3] = {0.0, 0.0, 0.0};
         if ((threadIdx.x & 31) == 0) {
-            const double dt = fd.dt, hdt = 0.5 * dt, hdt2 = 0.5 * dt * dt;
+            const double dt = fd.dt, hdt = 0.5 * dt;
             double mv = 1.0, mf = 0.0;
             if (fd.pending) {
                 mv = fd.reset ? 0.0 : 1.0 - fd.mixA;
@@ -91,12 +91,11 @@ template <class T> __global__ void __launch_bounds__(kBlock) k_b_pred(BatchArgs<
             }
             cf[0] = mv;
             cf[1] = mf + hdt;
-            cf[2] = dt * mv;
-            cf[3] = dt * mf + hdt2;
+            cf[2] = dt;
         }
 #pragma unroll
-        for (int k = 0; k < 4; ++k) cf[k] = __shfl_sync(0xffffffffu, cf[k], 0);
-        const T cvv = T(cf[0]), cvf = T(cf[1]), cqv = T(cf[2]), cqf = T(cf[3]);
+        for (int k = 0; k < 3; ++k) cf[k] = __shfl_sync(0xffffffffu, cf[k], 0);
+        const T cvv = T(cf[0]), cvf = T(cf[1]), tdt = T(cf[2]);
         const SolveDesc sd = B.solves[ch.solve];
         const int li = ch.start + threadIdx.x;
         if (li >= sd.Lx * sd.Ly * sd.Lz) continue;
@@ -104,10 +103,9 @@ template <class T> __global__ void __launch_bounds__(kBlock) k_b_pred(BatchArgs<
 #pragma unroll
         for (int k = 0; k < 5; ++k) {
             const long long j = (long long)k * B.L.P + i;
-            const T v = B.L.V[j];
-            const T f = B.L.F[j];
-            B.L.Q[j] += cqv * v + cqf * f;
-            B.L.V[j] = cvv * v + cvf * f;
+            const T vn = cvv * B.L.V[j] + cvf * B.L.F[j];
+            B.L.V[j] = vn;
+            B.L.Q[j] += tdt * vn;
         }
     }
 }

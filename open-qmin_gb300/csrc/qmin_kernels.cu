@@ -85,19 +85,20 @@ template <class T>
 __global__ void __launch_bounds__(kBlock) k_fire_pred(Lat<T> L, const FireDev *__restrict__ fd)
 {
     if (!fd->active) return;
-    // With the mix ve = ma v + mb f folded into the Verlet step's coefficients
+    // With the mix ve = mv v + mf f folded into the Verlet step's coefficients
     // (scalars formed in FP64 once per launch):
-    //   v' = cvv v + cvf f,   q' = q + cqv v + cqf f
-    // four FP64 operations per element instead of five (the FP64 pipe bounds
-    // this kernel on GB300 about as much as HBM does); the same quantities as
-    // ve, q + dt ve + dt^2/2 f, ve + dt/2 f up to rounding.
-    const double dt = fd->dt, hdt = 0.5 * dt, hdt2 = 0.5 * dt * dt;
+    //   v' = cvv v + cvf f,   q' = q + dt v'
+    // since dt v' = dt ve + dt^2/2 f is the step d: three FP64 operations per
+    // element instead of five (the FP64 pipe bounds this kernel on GB300 about
+    // as much as HBM does); the same quantities as q + dt ve + dt^2/2 f and
+    // ve + dt/2 f up to rounding.
+    const double dt = fd->dt, hdt = 0.5 * dt;
     double mv = 1.0, mf = 0.0;  // ve = mv v + mf f
     if (fd->pending) {
         mv = fd->reset ? 0.0 : 1.0 - fd->mixA;
         mf = fd->reset ? 0.0 : fd->mixA * fd->mixS;
     }
-    const T cvv = T(mv), cvf = T(mf + hdt), cqv = T(dt * mv), cqf = T(dt * mf + hdt2);
+    const T cvv = T(mv), cvf = T(mf + hdt), tdt = T(dt);
     // 16-byte vectors: 5 * P is a multiple of 32 elements and the planes are 256-byte aligned
     using V4 = typename std::conditional<sizeof(T) == 8, double2, float4>::type;
     constexpr int W = 16 / sizeof(T);
@@ -111,9 +112,9 @@ __global__ void __launch_bounds__(kBlock) k_fire_pred(Lat<T> L, const FireDev *_
         const T *f = reinterpret_cast<const T *>(&ff);
 #pragma unroll
         for (int e = 0; e < W; ++e) {
-            const T ve = v[e];
-            q[e] += cqv * ve + cqf * f[e];
-            v[e] = cvv * ve + cvf * f[e];
+            const T vn = cvv * v[e] + cvf * f[e];
+            v[e] = vn;
+            q[e] += tdt * vn;
         }
         Vv4[j] = vv;
         Q4[j] = qq;
