@@ -66,7 +66,7 @@ def kernel_roofline(lat, esz, N, peak, peak_kind, tag):
     dom = int(np.argmax(kms))
     achieved = nbytes[dom] * N / (kms[dom] / 1e3) / 1e9
     out = {"bound": "hbm", "kernel": names[dom], "achieved": achieved, "peak": peak, "unit": "GB/s",
-           "frac": achieved / peak, "peak_source": peak_kind, "traffic": traffic_from_profiles(names[dom], tag),
+           "frac": achieved / peak, "peak_source": peak_kind, "traffic": dram_traffic(names[dom], tag, N),
            "kernel_ms": {n: float(x) for n, x in zip(names, kms) if x > 0},
            "algorithmic_bytes_per_site": nbytes[dom], "sites_per_launch": N}
     out["autotuned"] = tuning
@@ -163,19 +163,25 @@ def make_lattice(q, consts, g, precision):
     return lat
 
 
-def traffic_from_profiles(kernel, precision_tag):
-    """DRAM bytes per launch recorded in profiles/ by the ncu capture, if present."""
-    p = os.path.join(ROOT, "profiles", "dram_traffic.md")
-    if not os.path.exists(p):
-        return None
-    for line in open(p):
-        parts = [x.strip() for x in line.strip().strip("|").split("|")]
-        if len(parts) >= 4 and parts[0] == kernel and parts[1] == precision_tag:
-            try:
-                return float(parts[3])
-            except ValueError:
-                return None
-    return None
+# DRAM bytes per launch of each force + kick strategy on the 200^3 workload:
+# dram__bytes_read.sum + dram__bytes_write.sum from ncu (--clock-control none).
+# The split kernels were captured on the full 200^3 launch (one-pass metrics);
+# the older strategies on a 128^3 case, scaled by the number of sites (their
+# traffic grows in proportion to the sites they process).
+DRAM_BYTES_PER_LAUNCH = {
+    ("force_kick_split", "f64"): 1715513856.0,   # 214.4 B/site (161 algorithmic)
+    ("force_kick_split", "f32"): 648814080.0,    # 81.1 B/site (81 algorithmic)
+    ("force_kick_reduce", "f64"): 2872800000.0,  # 359.1 B/site
+    ("force_kick_tiled", "f32"): 1082400000.0,   # 135.3 B/site
+    ("force_kick_reduce", "f32"): 1124800000.0,  # 140.6 B/site
+}
+
+
+def dram_traffic(kernel, precision_tag, sites=8000000):
+    """DRAM bytes per launch measured by ncu for this kernel at 200^3, scaled to
+    `sites`; None for a kernel without a capture."""
+    v = DRAM_BYTES_PER_LAUNCH.get((kernel, precision_tag))
+    return None if v is None else v * sites / 8000000.0
 
 
 def max_over_ranks(ms, device="cuda"):
@@ -268,9 +274,8 @@ def run_ours(args, rank, world):
         peak_ops = 304 * mhz * 1e6 / 1e9
         roofline["fp64_pipe"] = {"ops_per_site": FP64_OPS_PER_DEEP_SITE, "achieved": achieved, "peak": peak_ops,
                                  "unit": "G FP64 instructions/s", "frac": achieved / peak_ops,
-                                 "source": "ncu dfma + dmul + dadd per deep site "
-                                           "(profiles/k_force_kick_deep_fp64_128cube.md); every site counted at "
-                                           "the deep-site figure"}
+                                 "source": "ncu dfma + dmul + dadd per deep site of the FP64 deep-site kernel "
+                                           "(128^3 capture); every site counted at the deep-site figure"}
     fire_state = {"forceMax": r["forceMax"], "iterations": r["iterations"]}
     lat.close()
     if args.forms == "fp64":
@@ -285,40 +290,69 @@ def run_ours(args, rank, world):
 
 
 def run_e2e(q, consts, g, K, W, barrier, dist):
+    """End to end through the C ABI from pinned host memory.  The timed region
+    starts from nothing on the device: a fresh handle (qmin_create, the force
+    parameters and objects), the upload of Q0 and the site types, the site
+    classes and lists built from the types, the FIRE strategy's autotuning and
+    graph capture, K FIRE iterations and the download of the final Q, then
+    qmin_destroy.  The same job on a handle that already holds this geometry
+    (lists, tuned strategy and graphs kept) is reported beside it."""
     import torch
-    import torch as _t
     N = g.Q.shape[0]
-    Qh = _t.from_numpy(g.Q).pin_memory()
-    Th = _t.from_numpy(g.types).pin_memory()
-    Qout = _t.empty_like(Qh).pin_memory()
-    lat = make_lattice(q, consts, g, q.FP64)
+    Qh = torch.from_numpy(g.Q).pin_memory()
+    Th = torch.from_numpy(g.types).pin_memory()
+    Qout = torch.empty_like(Qh).pin_memory()
     stream = torch.cuda.Stream()
+
+    def job(lat=None):
+        fresh = lat is None
+        if fresh:
+            lat = make_lattice(q, consts, g, q.FP64)
+            q._check(q.lib().qmin_set_stream(lat._h, stream.cuda_stream))
+        lat.set_state_ptr(Qh.data_ptr(), Th.data_ptr())
+        lat.fire_init(dt=WORKLOAD["dt"])
+        r = lat.fire_run(K)
+        lat.get_state_ptr(Qout.data_ptr(), None, None)
+        if fresh:
+            lat.close()
+        return r
+
+    job()                        # library and kernels loaded, allocator warm
+    torch.cuda.synchronize()
+    barrier()
+    t0 = time.perf_counter()
+    r = job()
+    torch.cuda.synchronize()
+    wall_fresh = time.perf_counter() - t0
+    barrier()
+    ms_fresh = max_over_ranks(wall_fresh * 1e3)
+    # the same job on a handle that already holds the geometry
+    lat = make_lattice(q, consts, g, q.FP64)
     q._check(q.lib().qmin_set_stream(lat._h, stream.cuda_stream))
-    lat.set_state_ptr(Qh.data_ptr(), Th.data_ptr())
-    lat.fire_init(dt=WORKLOAD["dt"])
+    job(lat)
     lat.fire_run(W)
     torch.cuda.synchronize()
     barrier()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     t0 = time.perf_counter()
     e0.record(stream)
-    lat.set_state_ptr(Qh.data_ptr(), Th.data_ptr())
-    lat.fire_init(dt=WORKLOAD["dt"])
-    lat.fire_run(K)
-    lat.get_state_ptr(Qout.data_ptr(), None, None)
+    job(lat)
     e1.record(stream)
     torch.cuda.synchronize()
-    wall_e2e = time.perf_counter() - t0
+    wall_warm = time.perf_counter() - t0
     barrier()
-    ms_e2e = max_over_ranks(max(e0.elapsed_time(e1), wall_e2e * 1e3))
+    lat.close()
+    ms_warm = max_over_ranks(max(e0.elapsed_time(e1), wall_warm * 1e3))
     h2d = N * 5 * 8 + N * 4
     d2h = N * 5 * 8
     world = int(os.environ.get("WORLD_SIZE", 1))
-    e2e = {"value": job_value(world, N, K, ms_e2e), "unit": "site-steps/s", "h2d_bytes_per_step": h2d / K,
-           "d2h_bytes_per_step": d2h / K,
-           "note": "per job: upload Q0 (AoS f64) + int32 types, K FIRE iterations, download final Q; bytes amortised over K"}
-    lat.close()
-    return e2e
+    return {"value": job_value(world, N, K, ms_fresh), "unit": "site-steps/s", "h2d_bytes_per_step": h2d / K,
+            "d2h_bytes_per_step": d2h / K, "job_ms": ms_fresh, "iterations": r["iterations"],
+            "warm_handle_value": job_value(world, N, K, ms_warm), "warm_handle_job_ms": ms_warm,
+            "setup_ms": ms_fresh - ms_warm,
+            "note": "per job, wall clock: fresh handle, upload Q0 (AoS f64) + int32 types, site lists, autotuning "
+                    "and graph capture, K FIRE iterations, download final Q, destroy; bytes amortised over K. "
+                    "warm_handle_*: the same job on a handle already holding this geometry"}
 
 
 def finish(q, args, rank, world, consts, g, N, K, W, timed_fire, value, ms, launches, clocks, roofline, fire_state,
@@ -330,7 +364,16 @@ def finish(q, args, rank, world, consts, g, N, K, W, timed_fire, value, ms, laun
             "note": "FP32 state and stencils, FP64 reductions; its error against FP64 is reported at convergence "
                     "in time_to_converge (FIRE trajectories of the two precisions decorrelate step by step)"}
     fp32["roofline"] = kernel_roofline(lat32, 4, N, peak, "measured", "f32")
+    fp32["roofline"]["iteration_achieved_gbs_at_121B"] = 121 * N / (ms32 / K / 1e3) / 1e9
     lat32.close()
+    # the FP32 form's figures as scalars of the headline roofline object too
+    roofline["fp32_form_site_steps_per_s"] = fp32["value"]
+    roofline["fp32_form_ms_per_step"] = fp32["ms_per_step"]
+    roofline["fp32_kernel"] = fp32["roofline"]["kernel"]
+    roofline["fp32_kernel_achieved_gbs"] = fp32["roofline"]["achieved"]
+    roofline["fp32_kernel_frac"] = fp32["roofline"]["frac"]
+    roofline["fp32_iteration_achieved_gbs_at_121B"] = fp32["roofline"]["iteration_achieved_gbs_at_121B"]
+    roofline["fp32_iteration_frac_at_121B"] = fp32["roofline"]["iteration_achieved_gbs_at_121B"] / peak
 
     ttc = None
     if not args.no_configs:
@@ -557,7 +600,8 @@ def run_c4(q, ntest=64):
 def cpu_baseline(sample_iters=2, threads=1):
     """The oracle (CPU restatement of the reference's CPU path) on a bounded
     sample of the same workload: `sample_iters` FIRE iterations of the 200^3
-    lattice, timed with wall clock around the FIRE loop."""
+    lattice, timed with wall clock around the FIRE loop.  Returns the baseline
+    record, the oracle's FIRE result and its final Q."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import qmin_oracle as qo
     qo.build()
@@ -575,7 +619,24 @@ def cpu_baseline(sample_iters=2, threads=1):
     value = s.N * sample_iters / dt
     return {"value": value, "unit": "site-steps/s", "cores": used, "kind": "port",
             "sample": f"{sample_iters} FIRE iterations (+1 entry force evaluation) of the 200^3 workload, "
-                      f"{used} thread(s); oracle = C restatement of the reference CPU path"}, r
+                      f"{used} thread(s); oracle = C restatement of the reference CPU path"}, r, s.Q
+
+
+def c2_parity(q, iters, oracle_result, oracle_Q):
+    """The headline workload's FP64 FIRE run on the GPU (autotuned strategy)
+    after the same `iters` iterations as the oracle's sample: relative error of
+    forceMax, and normwise relative error of Q."""
+    consts, g = build_workload_host(q)
+    lat = make_lattice(q, consts, g, q.FP64)
+    lat.set_state(g.Q, g.types)
+    lat.fire_init(dt=WORKLOAD["dt"])
+    r = lat.fire_run(iters)
+    Q = lat.get_state()[0]
+    lat.close()
+    fo = oracle_result["forceMax"]
+    return {"parity_iterations": r["iterations"], "parity_forceMax_gpu": r["forceMax"], "parity_forceMax_oracle": fo,
+            "parity_forceMax_rel_err": abs(r["forceMax"] - fo) / fo,
+            "parity_Q_rel_err": float(np.abs(Q - oracle_Q).max() / np.abs(oracle_Q).max())}
 
 
 def run_reference(args):
@@ -780,7 +841,9 @@ def main():
     out = run_ours(args, rank, world)
     if rank == 0:
         if not args.no_cpu_baseline and args.forms == "both":
-            out["cpu_baseline"], _ = cpu_baseline(args.cpu_sample_iters)
+            out["cpu_baseline"], r_or, q_or = cpu_baseline(args.cpu_sample_iters)
+            import __graft_entry__ as ge
+            out["cpu_baseline"].update(c2_parity(ge.load_package(), args.cpu_sample_iters, r_or, q_or))
         print(json.dumps(out))
     if world > 1:
         import torch

@@ -120,6 +120,11 @@ int qmin_get_types(qmin_handle h, int32_t *types);
 /* overwrite Q only, keeping types, velocities and minimiser state (writing
  * through simpleModel::returnPositions, as multirankSimulation::loadState does) */
 int qmin_set_positions(qmin_handle h, const double *Q, int layout);
+/* overwrite the velocities (writing through simpleModel::returnVelocities,
+ * simpleModel.h:67): a caller whose own model holds the velocities between
+ * minimize() calls (the reference keeps them in the model) restores them
+ * after qmin_set_state and qmin_fire_init, which both zero them */
+int qmin_set_velocities(qmin_handle h, const double *V, int layout);
 /* qTensorLatticeModel::computeDefectMeasures (qTensorLatticeModel.cpp:95-133):
  * kind 0 largest eigenvalue of Q, 1 det Q, 2 (tr Q^2)^3 - 54 (det Q)^2, on
  * sites with type <= 0; object sites get 0.  out: host, N doubles. */
@@ -182,6 +187,19 @@ int qmin_fire_init(qmin_handle h, const qmin_fire_params *p);
  * setMaximumIterations(max_iterations); velocity Verlet + FIRE on the GPU,
  * graph-captured, no host synchronisation inside a chunk of iterations. */
 int qmin_fire_run(qmin_handle h, int max_iterations, qmin_fire_result *res);
+/* The FIRE updater's state that persists between minimize() calls in the
+ * reference: updater::iterations and energyMinimizerFIRE's forceMax, alpha,
+ * deltaT, deltaTMin, Power and NSinceNegativePower (energyMinimizerFIRE.h:66-94). */
+typedef struct {
+    int iterations;
+    double force_max, alpha, dt, dt_min, power;
+    int n_since;
+} qmin_fire_state;
+/* A caller that keeps those members in its own updater object (a subclass of
+ * energyMinimizerFIRE) restores them after qmin_fire_init; the next
+ * qmin_fire_run continues from them as minimize() does.  Requires
+ * qmin_fire_init first. */
+int qmin_fire_set_state(qmin_handle h, const qmin_fire_state *st);
 /* energyMinimizerAdam::setAdamParameters + minimize (energyMinimizerAdam.h:20-31,
  * energyMinimizerAdam.cpp:56-76); moments reset when reset != 0 */
 int qmin_adam_run(qmin_handle h, double beta1, double beta2, double eps, double dt, double force_cutoff,
@@ -264,16 +282,22 @@ int qmin_fire_tuning(qmin_handle h, int *path, int *variant, int *tile_x, int *t
 /* Energy of a Q field held in the caller's own device memory, for callers
  * that cannot call cudaMalloc (their device memory is owned by a pool
  * allocator of their own, or is fully committed).  Allocates nothing: its
- * scratch is a static device array of about 1.6 MB that every GPU loading
- * this library holds until exit.  FP64 only.
+ * scratch is a static device array of about 1.6 MB inside this library.  FP64 only.
  *   Q_dev:       device, SoA double planes Q_dev[k * plane_stride + i], k = 0..4
- *   types_dev:   device, int8 site types (same meaning as qmin_set_state's)
+ *   types_dev:   device, int8 site types (same meaning as qmin_set_state's);
+ *                an object type j must satisfy j <= nobj: a site next to an
+ *                object past nobj makes the anchoring energy and E NaN
  *   out_dev:     device, 6 doubles: E / NActive, then the phase, distortion,
  *                anchoring, E-field and H-field totals (as qmin_energy)
  *   objs:        host array of nobj objects; stream: cudaStream_t or NULL
  * Results match qmin_energy on the same state.  Returns QMIN_EINVAL for a
- * lattice larger than QMIN_NOALLOC_MAX_SITES sites.  The first call on each
- * device looks up the scratch address; make it before any stream capture.
+ * lattice larger than QMIN_NOALLOC_MAX_SITES sites.
+ * CUDA loads this library's device code and the scratch array lazily by
+ * default, so the first call on a device is what places them there (they stay
+ * until the process exits): a caller that later commits all of its device
+ * memory makes one call on each device before doing so (any small lattice),
+ * or runs with CUDA_MODULE_LOADING=EAGER.  That first call also looks up the
+ * scratch address; make it before any stream capture.
  * All calls share the scratch: calls that overlap on the GPU race, so
  * serialise them.  The result is ready when the stream reaches it.
  * No counterpart in the reference (an addition for allocation-free callers). */

@@ -82,6 +82,12 @@ class FireResult(C.Structure):
                 ("power", C.c_double), ("n_since", C.c_int)]
 
 
+class FireState(C.Structure):
+    """qmin_fire_state: the FIRE updater's members that persist between minimize() calls."""
+    _fields_ = [("iterations", C.c_int), ("force_max", C.c_double), ("alpha", C.c_double), ("dt", C.c_double),
+                ("dt_min", C.c_double), ("power", C.c_double), ("n_since", C.c_int)]
+
+
 _lib = None
 
 
@@ -107,6 +113,7 @@ def lib():
             "qmin_lbfgs_run": [h, C.c_int, C.c_double, C.c_double, C.c_int, C.c_int, ip, dp],
             "qmin_gd_run": [h, C.c_double, C.c_double, C.c_int, C.c_int, ip, dp],
             "qmin_get_sides": [h, ip, ip, ip], "qmin_get_types": [h, vp], "qmin_set_positions": [h, vp, C.c_int],
+            "qmin_set_velocities": [h, vp, C.c_int], "qmin_fire_set_state": [h, C.POINTER(FireState)],
             "qmin_defect_measures": [h, C.c_int, vp], "qmin_object_forces": [h, vp, C.c_int, ip],
             "qmin_set_field_map": [h, vp, C.c_double, C.c_double, C.c_double],
             "qmin_load_field_map": [h, C.c_char_p, C.c_double, C.c_double, C.c_double],
@@ -306,6 +313,15 @@ class Lattice:
         _check(lib().qmin_fire_run(self._h, int(max_iterations), C.byref(r)))
         return dict(iterations=r.iterations, forceMax=r.force_max, alpha=r.alpha, dt=r.dt, power=r.power,
                     nsince=r.n_since)
+
+    def set_velocities(self, V, layout=LAYOUT_AOS):
+        V = np.ascontiguousarray(V, dtype=np.float64)
+        _check(lib().qmin_set_velocities(self._h, V.ctypes.data, layout))
+
+    def fire_set_state(self, iterations, force_max, alpha, dt, dt_min, power, n_since):
+        """Restore the FIRE scalars an updater object keeps between minimize() calls."""
+        st = FireState(int(iterations), force_max, alpha, dt, dt_min, power, int(n_since))
+        _check(lib().qmin_fire_set_state(self._h, C.byref(st)))
 
     def adam_run(self, max_iterations, dt=1e-4, beta1=0.9, beta2=0.99, eps=1e-8, force_cutoff=1e-12, reset=True):
         it, fm = C.c_int(), C.c_double()

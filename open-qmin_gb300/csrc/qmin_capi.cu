@@ -642,6 +642,23 @@ int qmin_set_positions(qmin_handle h, const double *Q, int layout)
     return QMIN_OK;
 }
 
+int qmin_set_velocities(qmin_handle h, const double *V, int layout)
+{
+    if (!h || !V) return fail(QMIN_EINVAL, "qmin_set_velocities: null argument");
+    if (layout != QMIN_LAYOUT_AOS && layout != QMIN_LAYOUT_SOA)
+        return fail(QMIN_EINVAL, "qmin_set_velocities: bad layout");
+    if (!h->have_state) return fail(QMIN_ESTATE, "qmin_set_velocities: qmin_set_state has not been called");
+    int r = ensure_stage(h);
+    if (r) return r;
+    CK(cudaMemcpyAsync(h->stage, V, sizeof(double) * 5 * (size_t)h->N, cudaMemcpyHostToDevice, h->stream));
+    if (h->prec == QMIN_FP64)
+        h->launches += launch_aos_to_soa<double>(h->stage, (double *)h->V, h->N, h->P, layout, h->stream);
+    else
+        h->launches += launch_aos_to_soa<float>(h->stage, (float *)h->V, h->N, h->P, layout, h->stream);
+    CK(cudaStreamSynchronize(h->stream));
+    return QMIN_OK;
+}
+
 int qmin_defect_measures(qmin_handle h, int kind, double *out)
 {
     if (!h || !out) return fail(QMIN_EINVAL, "qmin_defect_measures: null argument");
@@ -787,6 +804,31 @@ int qmin_fire_init(qmin_handle h, const qmin_fire_params *p)
     if (h->have_state) CK(cudaMemsetAsync(h->V, 0, 5 * (size_t)h->P * h->esz, h->stream));
     CK(cudaStreamSynchronize(h->stream));
     h->fire_ready = true;
+    return QMIN_OK;
+}
+
+int qmin_fire_set_state(qmin_handle h, const qmin_fire_state *st)
+{
+    if (!h || !st) return fail(QMIN_EINVAL, "qmin_fire_set_state: null argument");
+    if (!h->fire_ready) return fail(QMIN_ESTATE, "qmin_fire_set_state: qmin_fire_init has not been called");
+    if (st->iterations < 0 || st->n_since < 0 || !(st->dt > 0) || !(st->dt_min >= 0))
+        return fail(QMIN_EINVAL, "qmin_fire_set_state: negative counter, dt <= 0 or dt_min < 0");
+    FireDev *f = h->fire_h;
+    CK(cudaMemcpyAsync(f, h->fire, sizeof(FireDev), cudaMemcpyDeviceToHost, h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+    // the updater's persistent members between minimize() calls
+    // (energyMinimizerFIRE.h:66-94): no velocity mix is pending between calls
+    f->iterations = st->iterations;
+    f->forceMax = st->force_max;
+    f->alpha = st->alpha;
+    f->dt = st->dt;
+    f->dtmin = st->dt_min;
+    f->power = st->power;
+    f->nsince = st->n_since;
+    f->pending = 0;
+    f->reset = 0;
+    CK(cudaMemcpyAsync(h->fire, f, sizeof(FireDev), cudaMemcpyHostToDevice, h->stream));
+    CK(cudaStreamSynchronize(h->stream));
     return QMIN_OK;
 }
 

@@ -9,18 +9,26 @@
 // per-block partial sums of the reduction, the object table and the site
 // count) sits in one file-scope static device array below.
 //
-// That array is allocated once per GPU when the library is loaded and is held
-// until the process exits.  All calls share it, so calls that overlap on the
-// GPU (two streams, two host threads, or a call made while a previous call's
-// kernels still run on another stream) race on it and give wrong results:
-// serialise them.  Every scratch slot a call reads is first written by the
-// same call, so nothing needs clearing between calls.
+// When that array exists: CUDA loads a library's device code and its static
+// device arrays lazily by default (CUDA_MODULE_LOADING=LAZY), so the array
+// (about 1.6 MB) and the kernels this call launches are placed on a device by
+// the first call made on it, and stay there until the process exits.  A caller
+// that will later commit all of its device memory makes one call on each
+// device first (any small lattice), or runs with CUDA_MODULE_LOADING=EAGER.
+//
+// All calls share the array, so calls that overlap on the GPU (two streams,
+// two host threads, or a call made while a previous call's kernels still run
+// on another stream) race on it and give wrong results: serialise them.  Every
+// scratch slot a call reads is first written by the same call (the object
+// table is rewritten in full, the slots past nobj with a NaN sentinel), so
+// nothing needs clearing between calls.
 //
 // The first call on each device looks up the array's device address with
 // cudaGetSymbolAddress (with that device current) and caches it; make that
 // first call before any stream capture.
 #include <cuda_runtime.h>
 
+#include <cstring>
 #include <mutex>
 #include <string>
 
@@ -35,7 +43,7 @@ constexpr int kMaxBlocks = QMIN_NOALLOC_MAX_SITES / kBlock;  // one reduction bl
 constexpr int kPartials = 5 * kMaxBlocks;                    // energy partials (doubles)
 constexpr int kCounts = kMaxBlocks;                          // active-site counts per block (doubles)
 constexpr int kSums = 8;                                     // summed energy components
-constexpr int kObjDoubles = 3 * 128;                         // object table, 127 ObjDev<double> entries
+constexpr int kObjDoubles = 3 * 128;                         // object table, 128 ObjDev<double> slots
 constexpr int kScratchDoubles = kPartials + kCounts + kSums + kObjDoubles;
 
 static_assert(sizeof(ObjDev<double>) == 24, "object record layout");
@@ -46,10 +54,31 @@ static __device__ __align__(256) double g_noalloc_scratch[kScratchDoubles];
 std::mutex g_addr_mutex;
 double *g_addr[64] = {};  // cached device address of g_noalloc_scratch per device ordinal
 
+// The whole object table as a kernel argument (128 x 24 B): the table reaches
+// the scratch without a host-to-device copy from a host buffer.
+struct ObjTable {
+    ObjDev<double> o[128];
+};
+
 int noalloc_fail(int code, const std::string &m)
 {
     qmin::g_last_error = m;  // reported by qmin_last_error_string
     return code;
+}
+
+// Writes all 128 slots: the caller's nobj objects, then a sentinel whose
+// anchoring energy is NaN, so a site type naming an object past nobj (which
+// this entry point cannot see on the host: the types are in device memory)
+// turns the anchoring energy and the total into NaN instead of reading a slot
+// left by an earlier call.
+__global__ void k_noalloc_objects(ObjTable t, int nobj, ObjDev<double> *dst)
+{
+    const int k = threadIdx.x;
+    if (k < 128) {
+        ObjDev<double> o = t.o[k];
+        if (k >= nobj) o = {0, __longlong_as_double(0x7ff8000000000000LL), __longlong_as_double(0x7ff8000000000000LL)};
+        dst[k] = o;
+    }
 }
 
 __global__ void __launch_bounds__(kBlock) k_count_active(const int8_t *types, int N, double *counts)
@@ -104,8 +133,11 @@ int qmin_energy_noalloc(const qmin_lattice_desc *desc, const qmin_ldg_params *p,
 
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);
-    if (e != cudaSuccess || dev < 0 || dev >= 64)
+    if (e != cudaSuccess)
         return noalloc_fail(QMIN_ECUDA, std::string("qmin_energy_noalloc: cudaGetDevice: ") + cudaGetErrorString(e));
+    if (dev < 0 || dev >= 64)
+        return noalloc_fail(QMIN_EINVAL, "qmin_energy_noalloc: device ordinal " + std::to_string(dev) +
+                                             " not supported (ordinals 0..63)");
     double *base = nullptr;
     {
         std::lock_guard<std::mutex> lock(g_addr_mutex);
@@ -127,14 +159,11 @@ int qmin_energy_noalloc(const qmin_lattice_desc *desc, const qmin_ldg_params *p,
     ObjDev<double> *dobjs = reinterpret_cast<ObjDev<double> *>(sums + kSums);
     cudaStream_t s = (cudaStream_t)stream;
 
-    // object table into the scratch (pageable source: the copy is staged before return)
-    ObjDev<double> host_objs[128];
-    for (int k = 0; k < nobj; ++k) host_objs[k] = {objs[k].kind, objs[k].W, objs[k].S0};
-    if (nobj > 0) {
-        e = cudaMemcpyAsync(dobjs, host_objs, sizeof(ObjDev<double>) * nobj, cudaMemcpyHostToDevice, s);
-        if (e != cudaSuccess)
-            return noalloc_fail(QMIN_ECUDA, std::string("qmin_energy_noalloc: object copy: ") + cudaGetErrorString(e));
-    }
+    // object table into the scratch, as a kernel argument
+    ObjTable tbl;
+    memset(&tbl, 0, sizeof tbl);
+    for (int k = 0; k < nobj; ++k) tbl.o[k] = {objs[k].kind, objs[k].W, objs[k].S0};
+    k_noalloc_objects<<<1, 128, 0, s>>>(tbl, nobj, dobjs);
 
     Lat<double> L;
     memset(&L, 0, sizeof L);

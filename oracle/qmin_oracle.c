@@ -752,6 +752,14 @@ static void site_energies(const qo_params *p, const double *Q, const int *types,
     }
 }
 
+/* The per-site energy densities that qo_energy sums (5 per site: phase,
+ * distortion, anchoring, E field, H field; zero on object sites), for checks
+ * that sum them in another order than the reference's sequential loop. */
+void qo_energy_densities(const qo_params *p, const double *Q, const int *types, const qo_object *objs, double *e)
+{
+    site_energies(p, Q, types, objs, e);
+}
+
 double qo_energy(const qo_params *p, const double *Q, const int *types, const qo_object *objs, double comps[5])
 {
     size_t N = (size_t)p->Lx * p->Ly * p->Lz;

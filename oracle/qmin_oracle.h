@@ -61,6 +61,7 @@ int qo_count_active(int N, const int *types);
 
 /* force and energy */
 void qo_force(const qo_params *p, const double *Q, const int *types, const qo_object *objs, double *F);
+void qo_energy_densities(const qo_params *p, const double *Q, const int *types, const qo_object *objs, double *e);
 double qo_energy(const qo_params *p, const double *Q, const int *types, const qo_object *objs, double comps[5]);
 
 /* minimisers; each returns the number of iterations it performed */

@@ -67,6 +67,8 @@ def lib():
         L.qo_force.argtypes = [C.POINTER(Params), dp, ip, C.POINTER(Object), dp]
         L.qo_energy.argtypes = [C.POINTER(Params), dp, ip, C.POINTER(Object), dp]
         L.qo_energy.restype = C.c_double
+        L.qo_energy_densities.argtypes = [C.POINTER(Params), dp, ip, C.POINTER(Object), dp]
+        L.qo_energy_densities.restype = None
         L.qo_fire_init.argtypes = [C.POINTER(FireParams), C.POINTER(FireState)]
         L.qo_fire.argtypes = [C.POINTER(Params), dp, dp, dp, ip, C.POINTER(Object), C.POINTER(FireParams), C.c_int,
                               C.POINTER(FireState), dp]
@@ -195,6 +197,23 @@ class System:
         comps = np.zeros(5)
         e = lib().qo_energy(C.byref(self.p), _dp(Q), _ip(self.types), self.objs, _dp(comps))
         return e / self.n_active(), comps
+
+    def energy_densities(self, Q=None):
+        """Per-site energy densities (N, 5): phase, distortion, anchoring, E, H."""
+        Q = self.Q if Q is None else np.ascontiguousarray(Q, dtype=np.float64)
+        e = np.zeros((self.N, 5))
+        lib().qo_energy_densities(C.byref(self.p), _dp(Q), _ip(self.types), self.objs, _dp(e))
+        return e
+
+    def energy_exact_sum(self, Q=None):
+        """(E / NActive, components[5]) with every component summed exactly
+        rounded (math.fsum) instead of the reference's sequential loop: the
+        check for lattices whose sequential FP64 sum carries more rounding
+        error than the 1e-12 parity tolerance (millions of sites)."""
+        import math
+        e = self.energy_densities(Q)
+        comps = np.array([math.fsum(e[:, k]) for k in range(5)])
+        return math.fsum(comps) / self.n_active(), comps
 
     def fire(self, iters, dt=5e-4, fcut=1e-12, trace=False, V=None):
         """CLI FIRE parameters (openQmin.cpp:256-258). Updates self.Q in place."""

@@ -21,7 +21,7 @@ object; down wins)}.  The bulk form equals case 0.  Every coefficient is a
 multiple of L/4 and is stored as an integer k with value k*L/4.
 
 Run from the repository root (needs the reference tree):
-    make -C oracle/ref REF=/root/reference && python3 oracle/ref/gen_distortion_tables.py
+    make -C oracle/ref && python3 oracle/ref/gen_distortion_tables.py
 """
 import collections
 import os

@@ -17,7 +17,7 @@ multiple of 1/2, stored here as the integer k = 2B.  This script writes:
   boundary cases as packed sparse tables.
 
 Run from the repository root (needs the reference tree):
-    make -C oracle/ref REF=/root/reference && python3 oracle/ref/gen_l6_tables.py
+    make -C oracle/ref && python3 oracle/ref/gen_l6_tables.py
 """
 import collections
 import os

@@ -6,7 +6,7 @@ the reference tree by oracle/ref/Makefile) on a set of small seeded cases and
 stores its dumps as compressed .npz files.  Needs the reference tree, so it
 runs only where that tree is mounted:
 
-    make -C oracle/ref REF=/root/reference -j8 && python3 tests/golden/make_golden.py
+    make -C oracle/ref -j8 && python3 tests/golden/make_golden.py
 
 Each case records: the arguments, the initial Q and site types, the force at
 Q0 (CPU-path semantics), the energy at Q0 (E/NActive and its five
