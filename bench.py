@@ -39,8 +39,10 @@ WORKLOAD = dict(L=(200, 200, 200), seed=13371, Ls=(2.32, 1.0, 0.5), W=5.3, walls
 #  control: scalars only
 KERNEL_BYTES = {8: [200, 161, 161, 0], 4: [100, 81, 81, 0]}
 KERNEL_NAMES = ["fire_predictor", "first_derivatives", "force_kick_reduce", "fire_control"]
-# the fused tiled iteration: read Q, V, F, types; write Q, V, F (halo re-reads excluded)
+# the fused iteration: read Q, V, F, types; write Q, V, F (halo re-reads excluded)
 FUSED_BYTES = {8: 241, 4: 121}
+# split variants from this index on fuse the predictor into the deep-site kernel
+SPLIT_FUSED_FIRST = 7
 
 
 # FP64 instructions per deep bulk site of the split force + kick (135 DFMA, 15.2 DMUL,
@@ -59,6 +61,12 @@ def kernel_roofline(lat, esz, N, peak, peak_kind, tag):
         nbytes[2] = FUSED_BYTES[esz]
     elif tuning["path"] == "tiled":
         names[2] = "force_kick_tiled"
+    elif tuning["path"] == "split" and tuning["variant"] >= SPLIT_FUSED_FIRST:
+        # predictor fused into the deep-site kernel (one buffer set in, the other out);
+        # the listed sites' derivative planes and force + kick counted with it
+        names[1] = "first_derivatives_listed"
+        names[2] = "fire_fused_split"
+        nbytes[2] = FUSED_BYTES[esz]
     elif tuning["path"] == "split":
         # deep bulk sites over Q (no derivative planes) + the listed sites; derivative planes only at the list
         names[1] = "first_derivatives_listed"

@@ -410,14 +410,15 @@ class Lattice:
 
     def fire_tuning(self):
         path, var, tx, ty, zc = C.c_int(), C.c_int(), C.c_int(), C.c_int(), C.c_int()
-        ms = (C.c_double * 24)()
+        ms = (C.c_double * 29)()
         _check(lib().qmin_fire_tuning(self._h, C.byref(path), C.byref(var), C.byref(tx), C.byref(ty), C.byref(zc),
                                       ms))
         names = (["separate_1blk", "separate_2blk", "separate_3blk"]
                  + [f"fused_{a}x{b}_z{v}" for a, b in ((32, 8), (32, 16), (64, 8), (32, 4)) for v in (0, 1)]
                  + [f"tiled_{a}x{b}_z{v}" for a, b in ((32, 8), (32, 4), (16, 16)) for v in (0, 1)]
                  + ["split_1blk", "split_2blk", "split_smem_32x8", "split_smem_16x16", "split_pair_32x8_z8",
-                    "split_pair_32x8_zfit", "split_pair_tma_32x8"])
+                    "split_pair_32x8_zfit", "split_pair_tma_32x8", "split_fused_32x8_z16", "split_fused_32x8_zfit",
+                    "split_fused_32x4_z16", "split_fused_cp_32x8", "split_fused_cp_32x4"])
         return dict(path=["separate", "fused", "tiled", "split"][path.value], variant=var.value, tile=(tx.value, ty.value),
                     zc=zc.value, candidates_ms={n: m for n, m in zip(names, ms) if m >= 0})
 

@@ -41,9 +41,13 @@ static const int kSepVariants = 3;  // separate-kernel force + kick with 1, 2, 3
 // deep-site kernel: 1 or 2 blocks per SM, shared-memory 32x8 or 16x16, and
 // (FP32 only) two sites per thread on 32x8 tiles, z chunks of 8 planes or about
 // two waves of columns, the latter also with TMA staging of interior tiles
-static const int kSplitVariants = 7;
+static const int kSplitVariants = 12;
 static const int kSplitTma = 6;
 static const int kSplitFp32First = 4;
+// variants 7-11: the predictor fused into the deep-site kernel (ping-pong state
+// sets, the listed sites' predicted Q formed on the fly), both precisions
+static const int kSplitFusedFirst = 7;
+static bool split_fused(int cap) { return cap >= kSplitFusedFirst; }
 static const int kTuneCandidates = kSepVariants + 2 * kFusedConfigs + 2 * kTiledConfigs + kSplitVariants;
 static_assert(kTuneCandidates == QMIN_TUNE_CANDIDATES, "tuning candidate count");
 
@@ -944,7 +948,7 @@ template <class T> static int tune_fire(qmin_ctx *h, const Lat<T> &L)
         if (try_split) {
             const SplitLists sl = split_lists(h);
             const float t_dl = timed([&]() { return launch_split_derivs<T>(L, sl, h->fire, h->stream); }, kNoBudget);
-            for (int cap = 0; cap < kSplitVariants; ++cap) {
+            for (int cap = 0; cap < kSplitFusedFirst; ++cap) {
                 if (pinned_out(cap) || (sizeof(T) == 8 && cap >= kSplitFp32First)) continue;
                 if (cap == kSplitTma && !h->tmap_ok) continue;
                 int np = 0;
@@ -1010,6 +1014,29 @@ template <class T> static int tune_fire(qmin_ctx *h, const Lat<T> &L)
             }
         }
         CK(cudaMemcpyAsync(h->V, h->V2, bytes, cudaMemcpyDeviceToDevice, h->stream));
+    }
+    // the fused split variants: the whole iteration but the control, writing only
+    // the second buffer set, the derivative planes and the partials (timed after
+    // the velocities above are restored from the second set)
+    for (int cap = kSplitFusedFirst; try_split && cap < kSplitVariants; ++cap) {
+        if (pinned_out(cap)) continue;
+        const SplitLists sl = split_lists(h);
+        const float ms = timed(
+            [&]() {
+                const int nd = launch_split_fused_deep<T>(L, (T *)h->Q2, (T *)h->V2, (T *)h->F2, sl, h->fire,
+                                                          h->partials, cap - kSplitFusedFirst, h->stream);
+                int nl = 0;
+                return 1 + launch_split_fused_list<T>(L, (T *)h->V2, (T *)h->F2, sl, h->fire,
+                                                      h->partials + 3 * std::max(nd, 0), h->stream, &nl);
+            },
+            budget_for(0.f));
+        if (cudaGetLastError() != cudaSuccess) continue;
+        h->tune_ms[kSepVariants + 2 * kFusedConfigs + 2 * kTiledConfigs + cap] = ms;
+        if (ms < best) {
+            best = ms;
+            h->path = 3;
+            h->split_cap = cap;
+        }
     }
     // the fused kernel writes only the second buffer set and the partials
     for (int cfg = 0; try_fused && cfg < kFusedConfigs; ++cfg) {
@@ -1079,6 +1106,25 @@ template <class T> static int fire_impl(qmin_ctx *h, int max_iterations)
             n = launch_fire_pred<T>(L, h->fire, h->stream);
             n += launch_force_kick<T>(L, h->fire, h->partials, h->grid, h->stream, h->sep_cap);
             n += launch_fire_control(h->fire, h->partials, h->grid, h->stream);
+        } else if (h->path == 3 && split_fused(h->split_cap)) {
+            // predictor fused into the deep-site kernel: one buffer set in, the
+            // other out; the listed sites on the side stream form their predicted
+            // Q from the input set
+            const SplitLists sl = split_lists(h);
+            const Lat<T> &Lin = parity == 0 ? L : LB;
+            T *Qo = (T *)(parity == 0 ? h->Q2 : h->Q), *Vo = (T *)(parity == 0 ? h->V2 : h->V),
+              *Fo = (T *)(parity == 0 ? h->F2 : h->F);
+            parity ^= 1;
+            cudaEventRecord(h->ev_fork, h->stream);
+            cudaStreamWaitEvent(h->aux, h->ev_fork, 0);
+            const int nd = launch_split_fused_deep<T>(Lin, Qo, Vo, Fo, sl, h->fire, h->partials,
+                                                      h->split_cap - kSplitFusedFirst, h->stream);
+            n = 1;
+            int nl = 0;
+            n += launch_split_fused_list<T>(Lin, Vo, Fo, sl, h->fire, h->partials + 3 * nd, h->aux, &nl);
+            cudaEventRecord(h->ev_join, h->aux);
+            cudaStreamWaitEvent(h->stream, h->ev_join, 0);
+            n += launch_fire_control(h->fire, h->partials, nd + nl, h->stream);
         } else if (h->path == 3) {
             // the listed sites (derivative planes, then force + kick) on the
             // high-priority side stream, beside the deep-site kernel
@@ -1117,7 +1163,9 @@ template <class T> static int fire_impl(qmin_ctx *h, int max_iterations)
     int remaining = std::max(max_iterations - it0, 1);
     r = run_chunks(h, 0, h->fire, h->fire_h, (remaining + kChunk - 1) / kChunk + 1);
     if (r) return r;
-    if (h->path == 1 && (r = settle_pingpong(h, h->fire_h->iterations - it0))) return r;
+    if ((h->path == 1 || (h->path == 3 && split_fused(h->split_cap))) &&
+        (r = settle_pingpong(h, h->fire_h->iterations - it0)))
+        return r;
     if (h->path == 3 && h->split_cap == kSplitTma && h->dev_err) {
         int e = 0;
         CK(cudaMemcpyAsync(&e, h->dev_err, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
@@ -1378,7 +1426,8 @@ template <class T> static int fire_profile_impl(qmin_ctx *h, int iterations, dou
     cudaEvent_t ev[5];
     for (auto &e : ev) CK(cudaEventCreate(&e));
     double acc[4] = {0, 0, 0, 0};
-    const bool fused = h->path == 1, tiled = h->path == 2, split = h->path == 3;
+    const bool sfused = h->path == 3 && split_fused(h->split_cap);
+    const bool fused = h->path == 1, tiled = h->path == 2, split = h->path == 3 && !sfused;
     const SplitLists sl = split_lists(h);
     Lat<T> LB = L;
     LB.Q = (T *)h->Q2;
@@ -1386,13 +1435,24 @@ template <class T> static int fire_profile_impl(qmin_ctx *h, int iterations, dou
     LB.F = (T *)h->F2;
     for (int it = 0; it < iterations; ++it) {
         CK(cudaEventRecord(ev[0], h->stream));
-        if (!fused) h->launches += launch_fire_pred<T>(L, h->fire, h->stream);
+        if (!fused && !sfused) h->launches += launch_fire_pred<T>(L, h->fire, h->stream);
         CK(cudaEventRecord(ev[1], h->stream));
         if (split) h->launches += launch_split_derivs<T>(L, sl, h->fire, h->stream);
-        else if (!fused && L.multi) h->launches += launch_derivs<T>(L, h->stream);
+        else if (!fused && !sfused && L.multi) h->launches += launch_derivs<T>(L, h->stream);
         CK(cudaEventRecord(ev[2], h->stream));
         int nparts = h->grid;
-        if (split) {
+        if (sfused) {
+            // deep sites and listed sites in sequence (the graph runs the latter beside the former)
+            const Lat<T> &Lin = (it & 1) == 0 ? L : LB;
+            T *Qo = (T *)((it & 1) == 0 ? h->Q2 : h->Q), *Vo = (T *)((it & 1) == 0 ? h->V2 : h->V),
+              *Fo = (T *)((it & 1) == 0 ? h->F2 : h->F);
+            const int nd = launch_split_fused_deep<T>(Lin, Qo, Vo, Fo, sl, h->fire, h->partials,
+                                                      h->split_cap - kSplitFusedFirst, h->stream);
+            int nl = 0;
+            h->launches += 1 + launch_split_fused_list<T>(Lin, Vo, Fo, sl, h->fire, h->partials + 3 * nd, h->stream,
+                                                          &nl);
+            nparts = nd + nl;
+        } else if (split) {
             h->launches += launch_split_force_kick<T>(L, sl, h->fire, h->partials, h->grid, h->split_cap, h->stream,
                                                       &nparts);
         } else if (tiled) {
@@ -1418,7 +1478,7 @@ template <class T> static int fire_profile_impl(qmin_ctx *h, int iterations, dou
         }
     }
     for (int k = 0; k < 4; ++k) ms[k] = iterations > 0 ? acc[k] / iterations : 0.0;
-    if (fused && (r = settle_pingpong(h, iterations))) return r;
+    if ((fused || sfused) && (r = settle_pingpong(h, iterations))) return r;
     h->launches += launch_fire_finish<T>(L, h->fire, h->stream);
     for (auto &e : ev) cudaEventDestroy(e);
     CK(cudaMemcpyAsync(h->fire_h, h->fire, sizeof(FireDev), cudaMemcpyDeviceToHost, h->stream));
@@ -1473,7 +1533,8 @@ int qmin_set_fire_variant(qmin_handle h, int variant)
                                                          : 0;
         if (n == 0) return fail(QMIN_EINVAL, "qmin_set_fire_variant: pin a strategy with qmin_set_fire_kernel first");
         if (variant >= n) return fail(QMIN_EINVAL, "qmin_set_fire_variant: no such variant of this strategy");
-        if (h->fire_mode == QMIN_FIRE_SPLIT && variant >= kSplitFp32First && h->prec != QMIN_FP32)
+        if (h->fire_mode == QMIN_FIRE_SPLIT && variant >= kSplitFp32First && !split_fused(variant) &&
+            h->prec != QMIN_FP32)
             return fail(QMIN_EINVAL, "qmin_set_fire_variant: the two-sites-per-thread kernels are FP32 only");
         if (h->fire_mode == QMIN_FIRE_SPLIT && variant == kSplitTma && !ensure_tmap(h))
             return fail(QMIN_EINVAL, "qmin_set_fire_variant: TMA staging needs an x extent that is a multiple of 4 "

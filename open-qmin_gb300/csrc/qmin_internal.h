@@ -156,6 +156,16 @@ int launch_split_force_kick(const Lat<T> &L, const SplitLists &sl, FireDev *fd, 
 template <class T>
 int launch_split_deep(const Lat<T> &L, const SplitLists &sl, FireDev *fd, double *partials, int grid, int cap,
                       cudaStream_t s);
+// fused split iteration (predictor inside): the deep sites from the input set
+// Lin into the output set (Qo, Vo, Fo; returns the block count, -1 for an
+// unknown variant), and the listed sites (derivative planes of the predicted
+// Q, force + kick into Vo, Fo; returns the launch count, *nblocks its partials)
+template <class T>
+int launch_split_fused_deep(const Lat<T> &Lin, T *Qo, T *Vo, T *Fo, const SplitLists &sl, FireDev *fd,
+                            double *partials, int variant, cudaStream_t s);
+template <class T>
+int launch_split_fused_list(const Lat<T> &Lin, T *Vo, T *Fo, const SplitLists &sl, FireDev *fd, double *partials,
+                            cudaStream_t s, int *nblocks);
 template <class T>
 int launch_split_list(const Lat<T> &L, const SplitLists &sl, FireDev *fd, double *partials, cudaStream_t s);
 

@@ -733,6 +733,432 @@ __global__ void __launch_bounds__(TX / 2 * TY, MINB)
     }
 }
 
+// ------------------------------------------------ fused predictor + force + kick
+// One launch per FIRE iteration for the deep bulk sites, the velocity-Verlet
+// predictor included: a block owns a TX x TY column of the lattice and walks
+// zc planes.  For each plane it loads raw Q, V, F of the tile plus a one-site
+// halo (every deep site's combined L1-L4 form reads only the 19 sites within
+// one step along an axis or a face diagonal: the two-step axis terms of the
+// 25-point form all have zero coefficients), applies the predictor (the
+// deferred FIRE mix and the Verlet step, k_fire_pred's arithmetic) and keeps
+// the predicted Q in a ring of four planes in shared memory; the force of the
+// plane below then reads planes z-1, z, z+1 of the ring.  Each thread owns one
+// site of the tile; threads 0 .. NH-1 also own one halo position.  Input is
+// one buffer set (L.Q, L.V, L.F), output the other (Qo, Vo, Fo): predicted Q
+// of every site of the tile, V and F of the deep sites (object sites:
+// V = F = 0; listed sites: k_force_kick_list_pred).
+template <class T> struct PredCoef {
+    T cvv, cvf, tdt;
+};
+
+// the predictor's coefficients (as k_fire_pred: ve = mv v + mf f folded into the
+// Verlet step, v' = cvv v + cvf f, q' = q + dt v')
+template <class T> __device__ __forceinline__ PredCoef<T> pred_coef(const FireDev *fd)
+{
+    const double dt = fd->dt, hdt = 0.5 * dt;
+    double mv = 1.0, mf = 0.0;
+    if (fd->pending) {
+        mv = fd->reset ? 0.0 : 1.0 - fd->mixA;
+        mf = fd->reset ? 0.0 : fd->mixA * fd->mixS;
+    }
+    return PredCoef<T>{T(mv), T(mf + hdt), T(dt)};
+}
+
+// predicted velocity and Q of one component: explicit FMAs, so that every
+// kernel that recomputes a site's prediction gets the same bits
+template <class T> __device__ __forceinline__ T pred_v(const PredCoef<T> &c, T v, T f)
+{
+    return fma(c.cvf, f, c.cvv * v);
+}
+template <class T> __device__ __forceinline__ T pred_q(const PredCoef<T> &c, T q, T vn) { return fma(c.tdt, vn, q); }
+
+template <int TX, int TY> __host__ __device__ constexpr int fused_halo_count() { return 2 * (TX + 2) + 2 * TY; }
+
+// position of halo entry t (< fused_halo_count) in the (TX + 2) x (TY + 2) staged plane
+template <int TX, int TY> __device__ __forceinline__ void fused_halo_pos(int t, int &rx, int &ry)
+{
+    constexpr int SX = TX + 2, SY = TY + 2;
+    if (t < SX) {
+        rx = t;
+        ry = 0;
+    } else if (t < 2 * SX) {
+        rx = t - SX;
+        ry = SY - 1;
+    } else if (t < 2 * SX + TY) {
+        rx = 0;
+        ry = 1 + (t - 2 * SX);
+    } else {
+        rx = SX - 1;
+        ry = 1 + (t - 2 * SX - TY);
+    }
+}
+
+// force of the owned site of plane z from the ring, kick, writes to the output
+// set, FIRE sums: shared by the two staging schemes
+template <class T, int TS, int SX, class Acc>
+__device__ __forceinline__ void fused_site_out(const Lat<T> &L, const T *sQ, const int (&sl)[3], int po, long long i,
+                                               uint8_t c, const T (&vn)[5], T hdt, T *Qo, T *Vo, T *Fo, Acc *sacc)
+{
+    const long long P = L.P;
+    const T *s0 = sQ + sl[1];
+    if (c == 0) {
+        int sb[5];
+        sb[0] = sb[4] = 0;  // the two-step planes carry no terms
+        sb[1] = sl[0] + po;
+        sb[2] = sl[1] + po;
+        sb[3] = sl[2] + po;
+        T f[5], v[5];
+        deep_force_tile<T, TS, SX>(L, sQ, sb, i, f);
+#pragma unroll
+        for (int k = 0; k < 5; ++k) {
+            v[k] = vn[k] + hdt * f[k];
+            Qo[k * P + i] = s0[k * TS + po];
+            Vo[k * P + i] = v[k];
+            Fo[k * P + i] = f[k];
+        }
+        sacc[0] += (Acc)dot_qt(f, f);
+        sacc[1] += (Acc)dot_qt(v, v);
+        sacc[2] += (Acc)dot_qt(f, v);
+    } else {
+#pragma unroll
+        for (int k = 0; k < 5; ++k) Qo[k * P + i] = s0[k * TS + po];
+        if (c == 2)
+#pragma unroll
+            for (int k = 0; k < 5; ++k) {
+                Vo[k * P + i] = T(0);
+                Fo[k * P + i] = T(0);
+            }
+    }
+}
+
+template <class T, int TX, int TY> constexpr size_t fused_deep_smem()
+{
+    return (size_t)4 * 5 * (TX + 2) * (TY + 2) * sizeof(T);
+}
+
+// raw planes prefetched into registers one plane ahead
+template <class T, int TX, int TY, int MINB>
+__global__ void __launch_bounds__(TX *TY, MINB)
+    k_fire_deep_fused(Lat<T> L, T *__restrict__ Qo, T *__restrict__ Vo, T *__restrict__ Fo,
+                      const uint8_t *__restrict__ cls, const FireDev *__restrict__ fd, double *partials, int zc)
+{
+    constexpr int NT = TX * TY, SX = TX + 2, SY = TY + 2, TS = SX * SY, NH = fused_halo_count<TX, TY>();
+    static_assert(NH <= NT, "every halo position needs a thread");
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    T *sQ = reinterpret_cast<T *>(smem_raw);  // [4][5][TS]: predicted Q of planes z-1 .. z+2
+    if (!fd->active) return;
+    const PredCoef<T> pc = pred_coef<T>(fd);
+    const T hdt = T(0.5) * T(fd->dt);
+    const int ntx = (L.Lx + TX - 1) / TX;
+    const int gx0 = (blockIdx.x % ntx) * TX, gy0 = (blockIdx.x / ntx) * TY;
+    const int zs = blockIdx.y * zc, ze = min(L.Lz, zs + zc);
+    const long long P = L.P;
+    const int sxy = L.Lx * L.Ly;
+    const int t = threadIdx.x, lx = t % TX, ly = t / TX;
+    const int po = (ly + 1) * SX + (lx + 1);
+    const int gxo = gx0 + lx, gyo = gy0 + ly;
+    const bool own_in = gxo < L.Lx && gyo < L.Ly;
+    // a tile that overhangs the lattice still stages the wrapped sites: its
+    // positions past the edge are the halo of the last column or row
+    const int colo = wrap_any(gxo, L.Lx) + L.Lx * wrap_any(gyo, L.Ly);
+    int ph = 0, colh = 0;
+    if (t < NH) {
+        int rx, ry;
+        fused_halo_pos<TX, TY>(t, rx, ry);
+        ph = ry * SX + rx;
+        colh = wrap_any(gx0 + rx - 1, L.Lx) + L.Lx * wrap_any(gy0 + ry - 1, L.Ly);
+    }
+    auto slot = [&](int z) { return ((z - zs + 1) & 3) * 5 * TS; };
+    T ro[15], rh[15];
+    uint8_t c_next = 1;
+    auto load = [&](int z) {
+        const long long base = (long long)sxy * wrap_any(z, L.Lz);
+        const long long io = base + colo;
+#pragma unroll
+        for (int k = 0; k < 5; ++k) {
+            ro[k] = ld(L.Q + k * P + io);
+            ro[5 + k] = ld(L.V + k * P + io);
+            ro[10 + k] = ld(L.F + k * P + io);
+        }
+        if (t < NH) {
+            const long long ih = base + colh;
+#pragma unroll
+            for (int k = 0; k < 5; ++k) {
+                rh[k] = ld(L.Q + k * P + ih);
+                rh[5 + k] = ld(L.V + k * P + ih);
+                rh[10 + k] = ld(L.F + k * P + ih);
+            }
+        }
+        c_next = (own_in && z >= zs && z < ze) ? cls[io] : uint8_t(1);
+    };
+    auto predict = [&](int z, T(&vn)[5]) {
+        T *s = sQ + slot(z);
+#pragma unroll
+        for (int k = 0; k < 5; ++k) {
+            vn[k] = pred_v(pc, ro[5 + k], ro[10 + k]);
+            s[k * TS + po] = pred_q(pc, ro[k], vn[k]);
+        }
+        if (t < NH)
+#pragma unroll
+            for (int k = 0; k < 5; ++k) s[k * TS + ph] = pred_q(pc, rh[k], pred_v(pc, rh[5 + k], rh[10 + k]));
+    };
+    using Acc = typename std::conditional<sizeof(T) == 4, float, double>::type;
+    Acc sacc[3] = {Acc(0), Acc(0), Acc(0)};
+    if (zs < L.Lz) {
+        T vn_cur[5], vn_nxt[5];
+        load(zs - 1);
+        predict(zs - 1, vn_cur);
+        load(zs);
+        uint8_t c_cur = c_next;
+        predict(zs, vn_cur);
+        load(zs + 1);
+        for (int z = zs; z < ze; ++z) {
+            const uint8_t c_here = c_cur;
+            c_cur = c_next;
+            predict(z + 1, vn_nxt);
+            if (z + 2 <= ze) load(z + 2);
+            __syncthreads();
+            if (own_in) {
+                const int sl[3] = {slot(z - 1), slot(z), slot(z + 1)};
+                fused_site_out<T, TS, SX, Acc>(L, sQ, sl, po, (long long)sxy * z + colo, c_here, vn_cur, hdt, Qo,
+                                               Vo, Fo, sacc);
+            }
+#pragma unroll
+            for (int k = 0; k < 5; ++k) vn_cur[k] = vn_nxt[k];
+        }
+    }
+    double acc[3] = {(double)sacc[0], (double)sacc[1], (double)sacc[2]};
+    block_sum<3, NT>(acc);
+    if (threadIdx.x == 0) {
+        const int b = blockIdx.y * gridDim.x + blockIdx.x;
+#pragma unroll
+        for (int k = 0; k < 3; ++k) partials[3 * b + k] = acc[k];
+    }
+}
+
+// The same iteration with the raw Q, V, F of each plane copied into shared
+// memory by cp.async two planes ahead (a ring of three raw planes) instead of
+// prefetched into registers one plane ahead: each thread copies and then reads
+// back only its own positions (its site and, for threads 0 .. NH-1, one halo
+// position), so the raw ring needs no barrier of its own.
+template <class T, int TX, int TY> constexpr size_t fused_deep_cp_smem()
+{
+    return (size_t)(4 * 5 + 3 * 15) * (TX + 2) * (TY + 2) * sizeof(T);
+}
+
+template <class T, int TX, int TY, int MINB>
+__global__ void __launch_bounds__(TX *TY, MINB)
+    k_fire_deep_fused_cp(Lat<T> L, T *__restrict__ Qo, T *__restrict__ Vo, T *__restrict__ Fo,
+                         const uint8_t *__restrict__ cls, const FireDev *__restrict__ fd, double *partials, int zc)
+{
+    constexpr int NT = TX * TY, SX = TX + 2, SY = TY + 2, TS = SX * SY, NH = fused_halo_count<TX, TY>();
+    static_assert(NH <= NT, "every halo position needs a thread");
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    T *sQ = reinterpret_cast<T *>(smem_raw);  // [4][5][TS]: predicted Q of planes z-1 .. z+2
+    T *sR = sQ + 4 * 5 * TS;                   // [3][15][TS]: raw Q, V, F of planes z+1 .. z+3
+    if (!fd->active) return;
+    const PredCoef<T> pc = pred_coef<T>(fd);
+    const T hdt = T(0.5) * T(fd->dt);
+    const int ntx = (L.Lx + TX - 1) / TX;
+    const int gx0 = (blockIdx.x % ntx) * TX, gy0 = (blockIdx.x / ntx) * TY;
+    const int zs = blockIdx.y * zc, ze = min(L.Lz, zs + zc);
+    const long long P = L.P;
+    const int sxy = L.Lx * L.Ly;
+    const int t = threadIdx.x, lx = t % TX, ly = t / TX;
+    const int po = (ly + 1) * SX + (lx + 1);
+    const int gxo = gx0 + lx, gyo = gy0 + ly;
+    const bool own_in = gxo < L.Lx && gyo < L.Ly;
+    const int colo = wrap_any(gxo, L.Lx) + L.Lx * wrap_any(gyo, L.Ly);
+    int ph = 0, colh = 0;
+    if (t < NH) {
+        int rx, ry;
+        fused_halo_pos<TX, TY>(t, rx, ry);
+        ph = ry * SX + rx;
+        colh = wrap_any(gx0 + rx - 1, L.Lx) + L.Lx * wrap_any(gy0 + ry - 1, L.Ly);
+    }
+    auto slot = [&](int z) { return ((z - zs + 1) & 3) * 5 * TS; };
+    auto rslot = [&](int z) { return ((z - zs + 1) % 3) * 15 * TS; };
+    // one commit group per plane (an empty group past the chunk's upper halo plane)
+    auto issue = [&](int z) {
+        if (z <= ze) {
+            const long long base = (long long)sxy * wrap_any(z, L.Lz);
+            T *r = sR + rslot(z);
+            const long long io = base + colo;
+#pragma unroll
+            for (int k = 0; k < 5; ++k) {
+                cp_async_q(r + k * TS + po, L.Q + k * P + io);
+                cp_async_q(r + (5 + k) * TS + po, L.V + k * P + io);
+                cp_async_q(r + (10 + k) * TS + po, L.F + k * P + io);
+            }
+            if (t < NH) {
+                const long long ih = base + colh;
+#pragma unroll
+                for (int k = 0; k < 5; ++k) {
+                    cp_async_q(r + k * TS + ph, L.Q + k * P + ih);
+                    cp_async_q(r + (5 + k) * TS + ph, L.V + k * P + ih);
+                    cp_async_q(r + (10 + k) * TS + ph, L.F + k * P + ih);
+                }
+            }
+        }
+        asm volatile("cp.async.commit_group;\n" ::: "memory");
+    };
+    auto predict = [&](int z, T(&vn)[5]) {
+        T *s = sQ + slot(z);
+        const T *r = sR + rslot(z);
+#pragma unroll
+        for (int k = 0; k < 5; ++k) {
+            vn[k] = pred_v(pc, r[(5 + k) * TS + po], r[(10 + k) * TS + po]);
+            s[k * TS + po] = pred_q(pc, r[k * TS + po], vn[k]);
+        }
+        if (t < NH)
+#pragma unroll
+            for (int k = 0; k < 5; ++k)
+                s[k * TS + ph] = pred_q(pc, r[k * TS + ph], pred_v(pc, r[(5 + k) * TS + ph], r[(10 + k) * TS + ph]));
+    };
+    auto cls_at = [&](int z) -> uint8_t {
+        return (own_in && z >= zs && z < ze) ? cls[(long long)sxy * z + colo] : uint8_t(1);
+    };
+    using Acc = typename std::conditional<sizeof(T) == 4, float, double>::type;
+    Acc sacc[3] = {Acc(0), Acc(0), Acc(0)};
+    if (zs < L.Lz) {
+        T vn_cur[5], vn_nxt[5];
+        issue(zs - 1);
+        issue(zs);
+        issue(zs + 1);
+        asm volatile("cp.async.wait_group 2;\n" ::: "memory");
+        predict(zs - 1, vn_cur);
+        issue(zs + 2);  // into the raw slot of plane zs - 1, just consumed
+        asm volatile("cp.async.wait_group 2;\n" ::: "memory");
+        predict(zs, vn_cur);
+        uint8_t c_cur = cls_at(zs), c_nxt = cls_at(zs + 1);
+        for (int z = zs; z < ze; ++z) {
+            issue(z + 3);  // into the raw slot of plane z, which this thread has consumed
+            asm volatile("cp.async.wait_group 2;\n" ::: "memory");  // plane z + 1 has landed
+            predict(z + 1, vn_nxt);
+            const uint8_t c_here = c_cur;
+            c_cur = c_nxt;
+            c_nxt = cls_at(z + 2);
+            __syncthreads();
+            if (own_in) {
+                const int sl[3] = {slot(z - 1), slot(z), slot(z + 1)};
+                fused_site_out<T, TS, SX, Acc>(L, sQ, sl, po, (long long)sxy * z + colo, c_here, vn_cur, hdt, Qo,
+                                               Vo, Fo, sacc);
+            }
+#pragma unroll
+            for (int k = 0; k < 5; ++k) vn_cur[k] = vn_nxt[k];
+        }
+        asm volatile("cp.async.wait_group 0;\n" ::: "memory");
+    }
+    double acc[3] = {(double)sacc[0], (double)sacc[1], (double)sacc[2]};
+    block_sum<3, NT>(acc);
+    if (threadIdx.x == 0) {
+        const int b = blockIdx.y * gridDim.x + blockIdx.x;
+#pragma unroll
+        for (int k = 0; k < 3; ++k) partials[3 * b + k] = acc[k];
+    }
+}
+
+// Q at the predicted step, formed on the fly from the input buffer set
+template <class T>
+__device__ __forceinline__ T pred_q_at(const Lat<T> &L, const PredCoef<T> &c, long long j, int k)
+{
+    const long long o = (long long)k * L.P + j;
+    return pred_q(c, ld(L.Q + o), pred_v(c, ld(L.V + o), ld(L.F + o)));
+}
+
+// twice the first derivatives (k_derivs' rules) of the predicted Q at the listed
+// sites' neighbours, formed from the input buffer set
+template <class T>
+__global__ void __launch_bounds__(kBlock)
+    k_derivs_list_pred(Lat<T> L, const int *__restrict__ list, int n, const FireDev *__restrict__ fd)
+{
+    if (!fd->active) return;
+    const PredCoef<T> pc = pred_coef<T>(fd);
+    const long long P = L.P;
+    for (int e = blockIdx.x * kBlock + threadIdx.x; e < n; e += gridDim.x * kBlock) {
+        const int i = list[e];
+        const int t = L.types[i];
+        const Nb b = neighbours(L, i);
+        T q[5];
+#pragma unroll
+        for (int k = 0; k < 5; ++k) q[k] = pred_q_at(L, pc, i, k);
+#pragma unroll
+        for (int ax = 0; ax < 3; ++ax) {
+            const int dn = b.n[2 * ax], up = b.n[2 * ax + 1];
+            const int td = t < 0 ? L.types[dn] : 0, tu = t < 0 ? L.types[up] : 0;
+#pragma unroll
+            for (int k = 0; k < 5; ++k)
+                L.D[(5 * ax + k) * P + i] =
+                    deriv2_rule(t, td, tu, pred_q_at(L, pc, dn, k), q[k], pred_q_at(L, pc, up, k));
+        }
+    }
+}
+
+// accessor over the predicted Q of the input buffer set; neighbour derivatives
+// from the D planes k_derivs_list_pred wrote
+template <class T> struct PredAcc {
+    const T *Q, *V, *F, *D;
+    const int8_t *types;
+    const ObjDev<T> *objs;
+    long long P;
+    int i;
+    Nb b;
+    PredCoef<T> c;
+    __device__ __forceinline__ PredAcc(const Lat<T> &L, int i_, const PredCoef<T> &c_)
+        : Q(L.Q), V(L.V), F(L.F), D(L.D), types(L.types), objs(L.objs), P(L.P), i(i_), b(neighbours(L, i_)), c(c_)
+    {
+    }
+    __device__ __forceinline__ T at(long long j, int k) const
+    {
+        const long long o = (long long)k * P + j;
+        return pred_q(c, ld(Q + o), pred_v(c, ld(V + o), ld(F + o)));
+    }
+    __device__ __forceinline__ ObjDev<T> obj(int t) const { return objs[t - 1]; }
+    __device__ __forceinline__ int tn(int s) const { return types[b.n[s]]; }
+    __device__ __forceinline__ T q(int k) const { return at(i, k); }
+    __device__ __forceinline__ T nq(int s, int k) const { return at(b.n[s], k); }
+    __device__ __forceinline__ T dn(int s, int d) const { return ld(D + (long long)d * P + b.n[s]); }
+};
+
+// the listed LC sites' force at the predicted Q and kick, from the input buffer
+// set into the output set's V and F (their predicted Q: the fused deep kernel)
+template <class T>
+__global__ void __launch_bounds__(kBlock)
+    k_force_kick_list_pred(Lat<T> L, T *__restrict__ Vo, T *__restrict__ Fo, const int *__restrict__ list, int n,
+                           const FireDev *__restrict__ fd, double *partials)
+{
+    if (!fd->active) return;
+    const PredCoef<T> pc = pred_coef<T>(fd);
+    const T hdt = T(0.5) * T(fd->dt);
+    const long long P = L.P;
+    double acc[3] = {0.0, 0.0, 0.0};
+    for (int e = blockIdx.x * kBlock + threadIdx.x; e < n; e += gridDim.x * kBlock) {
+        const int i = list[e];
+        const int t = L.types[i];
+        PredAcc<T> a(L, i, pc);
+        T f[5], h[3], v[5];
+        site_force_core<T, PredAcc<T>, false, true>(L, a, t, f, site_field(L, i, h));
+#pragma unroll
+        for (int k = 0; k < 5; ++k) {
+            const long long o = (long long)k * P + i;
+            v[k] = pred_v(pc, ld(L.V + o), ld(L.F + o)) + hdt * f[k];
+            Fo[o] = f[k];
+            Vo[o] = v[k];
+        }
+        if constexpr (sizeof(T) == 8) {
+            dot3_acc(f, v, acc);
+        } else {
+            acc[0] += (double)dot_qt(f, f);
+            acc[1] += (double)dot_qt(v, v);
+            acc[2] += (double)dot_qt(f, v);
+        }
+    }
+    block_sum<3>(acc);
+    if (threadIdx.x == 0)
+#pragma unroll
+        for (int k = 0; k < 3; ++k) partials[3 * blockIdx.x + k] = acc[k];
+}
+
 // shared-memory deep kernel over TX x TY columns of kDeepZc planes (more when
 // the grid would not fit the partials buffer); returns its block count
 template <class T, int TX, int TY>
@@ -802,6 +1228,102 @@ static int launch_deep_pair_tma(const Lat<float> &L, const SplitLists &sl, FireD
     k_force_kick_deep_pair_tma<TX, TY, MINB, KICK>
         <<<dim3(ntiles, nz), TX / 2 * TY, sm, s>>>(L, *sl.tmap_q, sl.cls, fd, partials, zc, sl.err);
     return ntiles * nz;
+}
+
+// grid of the fused deep kernels over TX x TY columns; zc > 0: z chunks of zc
+// planes, zc = 0: chunks long enough that the grid is about two waves of
+// MINB blocks on each of the 152 SMs
+static inline void fused_grid(int Lx, int Ly, int Lz, int TX, int TY, int MINB, int zc, int &ntiles, int &zc_out,
+                              int &nz)
+{
+    ntiles = ((Lx + TX - 1) / TX) * ((Ly + TY - 1) / TY);
+    if (zc <= 0) {
+        const long long nzt = std::max(1LL, 2LL * 152 * MINB / ntiles);
+        zc = (int)((Lz + nzt - 1) / nzt);
+    }
+    zc = std::max(1, std::min(zc, Lz));
+    while ((long long)ntiles * ((Lz + zc - 1) / zc) > kMaxFusedBlocks - 1024) ++zc;
+    zc_out = zc;
+    nz = (Lz + zc - 1) / zc;
+}
+
+template <class T, int TX, int TY, int MINB>
+static int launch_fused_deep(const Lat<T> &L, T *Qo, T *Vo, T *Fo, const SplitLists &sl, FireDev *fd,
+                             double *partials, int zc, cudaStream_t s)
+{
+    constexpr size_t sm = fused_deep_smem<T, TX, TY>();
+    static bool attr_set = false;
+    if (!attr_set) {
+        // a failure here surfaces as the launch's error
+        attr_set = cudaFuncSetAttribute(k_fire_deep_fused<T, TX, TY, MINB>,
+                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm) == cudaSuccess;
+    }
+    int ntiles, nz;
+    fused_grid(L.Lx, L.Ly, L.Lz, TX, TY, MINB, zc, ntiles, zc, nz);
+    k_fire_deep_fused<T, TX, TY, MINB><<<dim3(ntiles, nz), TX * TY, sm, s>>>(L, Qo, Vo, Fo, sl.cls, fd, partials, zc);
+    return ntiles * nz;
+}
+
+template <class T, int TX, int TY, int MINB>
+static int launch_fused_deep_cp(const Lat<T> &L, T *Qo, T *Vo, T *Fo, const SplitLists &sl, FireDev *fd,
+                                double *partials, int zc, cudaStream_t s)
+{
+    constexpr size_t sm = fused_deep_cp_smem<T, TX, TY>();
+    static bool attr_set = false;
+    if (!attr_set) {
+        // a failure here surfaces as the launch's error
+        attr_set = cudaFuncSetAttribute(k_fire_deep_fused_cp<T, TX, TY, MINB>,
+                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm) == cudaSuccess;
+    }
+    int ntiles, nz;
+    fused_grid(L.Lx, L.Ly, L.Lz, TX, TY, MINB, zc, ntiles, zc, nz);
+    k_fire_deep_fused_cp<T, TX, TY, MINB>
+        <<<dim3(ntiles, nz), TX * TY, sm, s>>>(L, Qo, Vo, Fo, sl.cls, fd, partials, zc);
+    return ntiles * nz;
+}
+
+// Fused split iteration, deep part: variant 0 = 32 x 8 tiles, z chunks of 16;
+// 1 = 32 x 8, about two waves; 2 = 32 x 4, z chunks of 16 (raw planes
+// prefetched into registers; FP32 at 2, 2, 4 blocks per SM, FP64 at 1, 1, 2);
+// 3 = 32 x 8, about two waves, 4 = 32 x 4, about two waves (raw planes
+// copied into shared memory two planes ahead; FP32 at 2 and 4 blocks per SM,
+// FP64 at 1 and 2).  Returns the block count (partials used), -1 for an
+// unknown variant.
+template <class T>
+int launch_split_fused_deep(const Lat<T> &Lin, T *Qo, T *Vo, T *Fo, const SplitLists &sl, FireDev *fd,
+                            double *partials, int variant, cudaStream_t s)
+{
+    constexpr bool f32 = sizeof(T) == 4;
+    switch (variant) {
+    case 0: return launch_fused_deep<T, 32, 8, f32 ? 2 : 1>(Lin, Qo, Vo, Fo, sl, fd, partials, 16, s);
+    case 1: return launch_fused_deep<T, 32, 8, f32 ? 2 : 1>(Lin, Qo, Vo, Fo, sl, fd, partials, 0, s);
+    case 2: return launch_fused_deep<T, 32, 4, f32 ? 4 : 2>(Lin, Qo, Vo, Fo, sl, fd, partials, 16, s);
+    case 3: return launch_fused_deep_cp<T, 32, 8, f32 ? 2 : 1>(Lin, Qo, Vo, Fo, sl, fd, partials, 0, s);
+    case 4: return launch_fused_deep_cp<T, 32, 4, f32 ? 4 : 2>(Lin, Qo, Vo, Fo, sl, fd, partials, 0, s);
+    default: return -1;
+    }
+}
+
+// Fused split iteration, listed part: derivative planes of the predicted Q at
+// the sites the listed forms read, then the listed sites' force + kick into the
+// output set.  Returns its launch count; *nblocks its partials.
+template <class T>
+int launch_split_fused_list(const Lat<T> &Lin, T *Vo, T *Fo, const SplitLists &sl, FireDev *fd, double *partials,
+                            cudaStream_t s, int *nblocks)
+{
+    int n = 0;
+    *nblocks = 0;
+    if (sl.n_derivs > 0) {
+        k_derivs_list_pred<T><<<list_grid(sl.n_derivs), kBlock, 0, s>>>(Lin, sl.derivs, sl.n_derivs, fd);
+        ++n;
+    }
+    if (sl.n_sites > 0) {
+        const int g = list_grid(sl.n_sites);
+        k_force_kick_list_pred<T><<<g, kBlock, 0, s>>>(Lin, Vo, Fo, sl.sites, sl.n_sites, fd, partials);
+        *nblocks = g;
+        ++n;
+    }
+    return n;
 }
 
 template <class T> int launch_split_derivs(const Lat<T> &L, const SplitLists &sl, FireDev *fd, cudaStream_t s)
@@ -881,5 +1403,13 @@ template int launch_split_list<double>(const Lat<double> &, const SplitLists &, 
 template int launch_split_list<float>(const Lat<float> &, const SplitLists &, FireDev *, double *, cudaStream_t);
 template int launch_split_force<double>(const Lat<double> &, int, cudaStream_t);
 template int launch_split_force<float>(const Lat<float> &, int, cudaStream_t);
+template int launch_split_fused_deep<double>(const Lat<double> &, double *, double *, double *, const SplitLists &,
+                                             FireDev *, double *, int, cudaStream_t);
+template int launch_split_fused_deep<float>(const Lat<float> &, float *, float *, float *, const SplitLists &,
+                                            FireDev *, double *, int, cudaStream_t);
+template int launch_split_fused_list<double>(const Lat<double> &, double *, double *, const SplitLists &, FireDev *,
+                                             double *, cudaStream_t, int *);
+template int launch_split_fused_list<float>(const Lat<float> &, float *, float *, const SplitLists &, FireDev *,
+                                            double *, cudaStream_t, int *);
 
 }  // namespace qmin

@@ -250,7 +250,7 @@ def test_fused_matches_separate_kernels(qmin, oracle, L, prec, other):
 
 @pytest.mark.parametrize("L", [(16, 9, 7), (40, 33, 21), (65, 17, 30), (104, 30, 20)])
 @pytest.mark.parametrize("prec", [0, 1])
-@pytest.mark.parametrize("variant", [0, 1, 2, 3, 4, 5, 6])
+@pytest.mark.parametrize("variant", [0, 1, 2, 3, 4, 5, 6, 7, 8, 9, 10, 11])
 def test_split_variants_match_separate(qmin, oracle, L, prec, variant):
     """Each pinned deep-site kernel of the split force + kick (0, 1: global
     memory at 1 or 2 blocks per SM; 2, 3: shared-memory tiles of 32 x 8 and
@@ -258,14 +258,19 @@ def test_split_variants_match_separate(qmin, oracle, L, prec, variant):
     narrower than a tile; 4, 5, FP32 only: two x-adjacent sites per thread,
     the second past the edge of an odd Lx; 6, FP32 only: the same with the
     interior tiles' planes staged by TMA, which the 104 x 30 x 20 lattice has
-    beside its periodic edge tiles) tracks the separate kernels, with an L4
-    term and an external field: FP64 to 1e-12 after 7 iterations, FP32 to
-    1e-5."""
+    beside its periodic edge tiles; 7-11: the predictor fused into the
+    deep-site kernel with ping-pong state sets and a one-site halo of raw
+    planes, in registers (7, 8: 32 x 8 tiles with z chunks of 16 or about two
+    waves; 9: 32 x 4) or in shared memory two planes ahead (10: 32 x 8; 11:
+    32 x 4), the listed sites forming their predicted Q on the fly; an odd
+    iteration count leaves the state in the second set, which the run copies
+    back) tracks the separate kernels, with an L4 term and an external field:
+    FP64 to 1e-12 after 7 iterations, FP32 to 1e-5."""
     cfg = parse_args([f"L={L[0]},{L[1]},{L[2]}", "seed=13", "Ls=2.32,1.0,0.5,0.3,0", "wall=2,0,h,5.3",
                       f"sphere={L[0] / 2},{L[1] / 2},{L[2] / 2},{min(L) / 4},p,2.0", "H=0.1,0.2,0.3,0.5,1.0,0.2"])
     s = oracle_system(oracle, cfg)
     tma_ok = L[0] % 4 == 0 and L[0] >= 40 and L[1] >= 12
-    if (variant >= 4 and prec == 0) or (variant == 6 and not tma_ok):
+    if (4 <= variant <= 6 and prec == 0) or (variant == 6 and not tma_ok):
         lat = gpu_lattice(qmin, s, prec)
         lat.set_fire_kernel(4)
         with pytest.raises(qmin.QminError):
@@ -284,7 +289,9 @@ def test_split_variants_match_separate(qmin, oracle, L, prec, variant):
     assert t["path"] == "split" and t["variant"] == variant
     assert list(t["candidates_ms"]) == [["split_1blk", "split_2blk", "split_smem_32x8", "split_smem_16x16",
                                          "split_pair_32x8_z8", "split_pair_32x8_zfit",
-                                         "split_pair_tma_32x8"][variant]]
+                                         "split_pair_tma_32x8", "split_fused_32x8_z16", "split_fused_32x8_zfit",
+                                         "split_fused_32x4_z16", "split_fused_cp_32x8",
+                                         "split_fused_cp_32x4"][variant]]
     tol = 1e-12 if prec == 0 else 1e-5
     assert res[0][0]["iterations"] == res[1][0]["iterations"] == 7
     assert abs(res[0][0]["forceMax"] - res[1][0]["forceMax"]) <= tol * res[0][0]["forceMax"]
@@ -301,14 +308,16 @@ def test_fire_variant_pin_errors(qmin, oracle):
         lat.set_fire_variant(0)  # FIRE_AUTO
     lat.set_fire_kernel(4)
     with pytest.raises(qmin.QminError):
-        lat.set_fire_variant(7)
+        lat.set_fire_variant(12)
+    with pytest.raises(qmin.QminError):
+        lat.set_fire_variant(5)  # FP32 only
     with pytest.raises(qmin.QminError):
         lat.set_fire_variant(-2)
     lat.set_fire_variant(3)
     lat.set_fire_variant(-1)
     lat.fire_init()
     lat.fire_run(2)
-    assert len(lat.fire_tuning()["candidates_ms"]) == 4
+    assert len(lat.fire_tuning()["candidates_ms"]) == 9  # FP64: 4 split kernels + 5 fused
 
 
 @pytest.mark.parametrize("Ls", ["2.32,0,0,0,0", "2.32,1.0,0.5,0,0"])
