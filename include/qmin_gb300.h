@@ -249,7 +249,7 @@ int qmin_fire_profile(qmin_handle h, int iterations, double kernel_ms[4], int *f
 /* (kernel_ms[2] is the staged force + kick when path 2 runs; *fused is 1 only for path 1) */
 /* Pin one variant of the strategy chosen with qmin_set_fire_kernel (its index
  * among that strategy's candidates in qmin_fire_tuning's ms[]: 0-2 separate,
- * 0-3 fused, 0-2 staged, 0-11 split with 4-6 FP32 only), or -1 to let the autotuner pick (the
+ * 0-3 fused, 0-2 staged, 0-11 split with 4-6 and 10-11 FP32 only), or -1 to let the autotuner pick (the
  * default; qmin_set_fire_kernel resets it).  QMIN_EINVAL for an index the
  * strategy does not have or when no strategy is pinned.  No reference
  * counterpart (execution strategy). */
@@ -272,8 +272,9 @@ int qmin_set_fire_variant(qmin_handle h, int variant);
  * and writes the other, staging raw Q, V, F of each plane with a one-site
  * halo: raw planes prefetched into registers one plane ahead on 32 x 8 tiles
  * with z chunks of 16 planes (7) or about two waves (8), on 32 x 4 tiles
- * (9), or copied into shared memory by cp.async two planes ahead on 32 x 8
- * (10) or 32 x 4 (11) tiles; the listed sites form their predicted Q on the
+ * (9), or copied into shared memory cooperatively by 16-byte row chunks two
+ * planes ahead on 32 x 8 (10) or 32 x 4 (11) tiles, FP32 with an x extent
+ * that is a multiple of 4; the listed sites form their predicted Q on the
  * fly); -1 = not run.
  * No reference counterpart (the reference's kernelTuner scans block sizes,
  * src/utilities/kernelTuner.cpp:5-125). */

@@ -117,6 +117,17 @@ struct qmin_ctx {
     double tune_ms[kTuneCandidates] = {};
 };
 
+// whether this handle can run split variant cap: 4-6 FP32 only (6 also needs the
+// tensor map), 7-11 need 32-bit component offsets (5 P < 2^31), 10-11 FP32 with
+// an x extent that is a multiple of 4
+static bool split_variant_ok(const qmin_ctx *h, int cap)
+{
+    if (cap >= kSplitFp32First && !split_fused(cap) && h->prec != QMIN_FP32) return false;
+    if (split_fused(cap) && 5LL * h->P >= (1LL << 31)) return false;
+    if (cap >= kSplitFusedFirst + 3 && (h->prec != QMIN_FP32 || h->Lx % 4 != 0)) return false;
+    return true;
+}
+
 static const int kChunk = 32;  // iterations per captured graph
 
 namespace qmin {
@@ -1019,7 +1030,7 @@ template <class T> static int tune_fire(qmin_ctx *h, const Lat<T> &L)
     // the second buffer set, the derivative planes and the partials (timed after
     // the velocities above are restored from the second set)
     for (int cap = kSplitFusedFirst; try_split && cap < kSplitVariants; ++cap) {
-        if (pinned_out(cap)) continue;
+        if (pinned_out(cap) || !split_variant_ok(h, cap)) continue;
         const SplitLists sl = split_lists(h);
         const float ms = timed(
             [&]() {
@@ -1533,9 +1544,10 @@ int qmin_set_fire_variant(qmin_handle h, int variant)
                                                          : 0;
         if (n == 0) return fail(QMIN_EINVAL, "qmin_set_fire_variant: pin a strategy with qmin_set_fire_kernel first");
         if (variant >= n) return fail(QMIN_EINVAL, "qmin_set_fire_variant: no such variant of this strategy");
-        if (h->fire_mode == QMIN_FIRE_SPLIT && variant >= kSplitFp32First && !split_fused(variant) &&
-            h->prec != QMIN_FP32)
-            return fail(QMIN_EINVAL, "qmin_set_fire_variant: the two-sites-per-thread kernels are FP32 only");
+        if (h->fire_mode == QMIN_FIRE_SPLIT && !split_variant_ok(h, variant))
+            return fail(QMIN_EINVAL, "qmin_set_fire_variant: this split variant needs the FP32 form (4-6, 10-11), "
+                                     "an x extent that is a multiple of 4 (10-11) and at most 2^31 / 5 sites "
+                                     "per plane set (7-11)");
         if (h->fire_mode == QMIN_FIRE_SPLIT && variant == kSplitTma && !ensure_tmap(h))
             return fail(QMIN_EINVAL, "qmin_set_fire_variant: TMA staging needs an x extent that is a multiple of 4 "
                                      "and at least 40 (and a driver that encodes tensor maps)");

@@ -774,59 +774,115 @@ template <class T> __device__ __forceinline__ T pred_q(const PredCoef<T> &c, T q
 
 template <int TX, int TY> __host__ __device__ constexpr int fused_halo_count() { return 2 * (TX + 2) + 2 * TY; }
 
-// position of halo entry t (< fused_halo_count) in the (TX + 2) x (TY + 2) staged plane
-template <int TX, int TY> __device__ __forceinline__ void fused_halo_pos(int t, int &rx, int &ry)
+// position of halo entry h (< fused_halo_count) in the (TX + 2) x (TY + 2) staged plane
+template <int TX, int TY> __device__ __forceinline__ void fused_halo_pos(int h, int &rx, int &ry)
 {
     constexpr int SX = TX + 2, SY = TY + 2;
-    if (t < SX) {
-        rx = t;
+    if (h < SX) {
+        rx = h;
         ry = 0;
-    } else if (t < 2 * SX) {
-        rx = t - SX;
+    } else if (h < 2 * SX) {
+        rx = h - SX;
         ry = SY - 1;
-    } else if (t < 2 * SX + TY) {
+    } else if (h < 2 * SX + TY) {
         rx = 0;
-        ry = 1 + (t - 2 * SX);
+        ry = 1 + (h - 2 * SX);
     } else {
         rx = SX - 1;
-        ry = 1 + (t - 2 * SX - TY);
+        ry = 1 + (h - 2 * SX - TY);
     }
 }
 
-// force of the owned site of plane z from the ring, kick, writes to the output
-// set, FIRE sums: shared by the two staging schemes
-template <class T, int TS, int SX, class Acc>
-__device__ __forceinline__ void fused_site_out(const Lat<T> &L, const T *sQ, const int (&sl)[3], int po, long long i,
-                                               uint8_t c, const T (&vn)[5], T hdt, T *Qo, T *Vo, T *Fo, Acc *sacc)
+// the halo entry of thread t, or -1: entries go to the first threads of the
+// block, so that they occupy as few warps as possible (a warp issues its halo
+// loads and predictor once whatever number of its lanes take part)
+template <int TX, int TY> __device__ __forceinline__ int fused_halo_entry(int t)
 {
-    const long long P = L.P;
-    const T *s0 = sQ + sl[1];
+    return t < fused_halo_count<TX, TY>() ? t : -1;
+}
+
+// the fused kernels' per-thread staging geometry: the owned site's position in
+// the staged plane and its (wrapped) column, the halo position and column
+template <int TX, int TY> struct FusedPos {
+    int po, colo, ph, colh;
+    bool own_in, has_h;
+    template <class T> __device__ __forceinline__ FusedPos(const Lat<T> &L, int gx0, int gy0, int t)
+    {
+        constexpr int SX = TX + 2;
+        const int lx = t % TX, ly = t / TX;
+        po = (ly + 1) * SX + (lx + 1);
+        const int gxo = gx0 + lx, gyo = gy0 + ly;
+        own_in = gxo < L.Lx && gyo < L.Ly;
+        // a tile that overhangs the lattice still stages the wrapped sites: its
+        // positions past the edge are the halo of the last column or row
+        colo = wrap_any(gxo, L.Lx) + L.Lx * wrap_any(gyo, L.Ly);
+        const int h = fused_halo_entry<TX, TY>(t);
+        has_h = h >= 0;
+        ph = 0;
+        colh = 0;
+        if (has_h) {
+            int rx, ry;
+            fused_halo_pos<TX, TY>(h, rx, ry);
+            ph = ry * SX + rx;
+            colh = wrap_any(gx0 + rx - 1, L.Lx) + L.Lx * wrap_any(gy0 + ry - 1, L.Ly);
+        }
+    }
+};
+
+// force of a deep bulk site from the predicted-Q ring, its own column (planes
+// z-1, z, z+1) from registers
+template <class T, int TS, int SX>
+__device__ __forceinline__ void deep_force_ring(const Lat<T> &L, const T *sQ, const int (&sb)[3],
+                                                const T (&qc)[3][5], long long i, T *f)
+{
+    // one pointer per plane, every stencil offset a compile-time displacement from it
+    const T *r0 = sQ + sb[0], *r1 = sQ + sb[1], *r2 = sQ + sb[2];
+#define QQ(dx, dy, dz, c)                                                                     \
+    (((dx) == 0 && (dy) == 0) ? qc[(dz) + 1][c]                                               \
+                              : ((dz) < 0 ? r0 : (dz) == 0 ? r1 : r2)[(c) * TS + (dy) * SX + (dx)])
+    T s2[5];
+    if (L.L4 == T(0)) {
+        QMIN_BULK_Q25_NO_L4(L.cq, s2);
+    } else {
+        QMIN_BULK_Q25(L.cq, s2);
+    }
+#undef QQ
+    deep_force_finish(L, qc[1], s2, i, f);
+}
+
+// the owned site of plane z: force from the ring, kick, writes to the output
+// set (32-bit component offsets from the site's address), FIRE sums
+template <class T, int TS, int SX, class Acc>
+__device__ __forceinline__ void fused_site_out(const Lat<T> &L, const T *sQ, const int (&sb)[3],
+                                               const T (&qc)[3][5], unsigned Pu, unsigned i, uint8_t c,
+                                               const T (&vn)[5], T hdt, T *Qo, T *Vo, T *Fo, Acc *sacc)
+{
+    // component k of site i at (X + k P)[i]: the plane bases are the same for every
+    // thread, the site index a 32-bit offset (the launcher requires 5 P < 2^31)
+    auto qo = [&](int k) -> T & { return (Qo + (size_t)k * Pu)[i]; };
+    auto vo = [&](int k) -> T & { return (Vo + (size_t)k * Pu)[i]; };
+    auto fo = [&](int k) -> T & { return (Fo + (size_t)k * Pu)[i]; };
     if (c == 0) {
-        int sb[5];
-        sb[0] = sb[4] = 0;  // the two-step planes carry no terms
-        sb[1] = sl[0] + po;
-        sb[2] = sl[1] + po;
-        sb[3] = sl[2] + po;
         T f[5], v[5];
-        deep_force_tile<T, TS, SX>(L, sQ, sb, i, f);
+        deep_force_ring<T, TS, SX>(L, sQ, sb, qc, i, f);
 #pragma unroll
         for (int k = 0; k < 5; ++k) {
             v[k] = vn[k] + hdt * f[k];
-            Qo[k * P + i] = s0[k * TS + po];
-            Vo[k * P + i] = v[k];
-            Fo[k * P + i] = f[k];
+            qo(k) = qc[1][k];
+            vo(k) = v[k];
+            fo(k) = f[k];
         }
         sacc[0] += (Acc)dot_qt(f, f);
         sacc[1] += (Acc)dot_qt(v, v);
         sacc[2] += (Acc)dot_qt(f, v);
     } else {
 #pragma unroll
-        for (int k = 0; k < 5; ++k) Qo[k * P + i] = s0[k * TS + po];
+        for (int k = 0; k < 5; ++k) qo(k) = qc[1][k];
         if (c == 2)
 #pragma unroll
             for (int k = 0; k < 5; ++k) {
-                Vo[k * P + i] = T(0);
-                Fo[k * P + i] = T(0);
+                vo(k) = T(0);
+                fo(k) = T(0);
             }
     }
 }
@@ -836,14 +892,14 @@ template <class T, int TX, int TY> constexpr size_t fused_deep_smem()
     return (size_t)4 * 5 * (TX + 2) * (TY + 2) * sizeof(T);
 }
 
-// raw planes prefetched into registers one plane ahead
+// raw planes prefetched into registers one plane ahead.  Component offsets are
+// 32-bit (the launcher requires 5 P < 2^31).
 template <class T, int TX, int TY, int MINB>
 __global__ void __launch_bounds__(TX *TY, MINB)
     k_fire_deep_fused(Lat<T> L, T *__restrict__ Qo, T *__restrict__ Vo, T *__restrict__ Fo,
                       const uint8_t *__restrict__ cls, const FireDev *__restrict__ fd, double *partials, int zc)
 {
-    constexpr int NT = TX * TY, SX = TX + 2, SY = TY + 2, TS = SX * SY, NH = fused_halo_count<TX, TY>();
-    static_assert(NH <= NT, "every halo position needs a thread");
+    constexpr int NT = TX * TY, SX = TX + 2, SY = TY + 2, TS = SX * SY;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     T *sQ = reinterpret_cast<T *>(smem_raw);  // [4][5][TS]: predicted Q of planes z-1 .. z+2
     if (!fd->active) return;
@@ -852,76 +908,72 @@ __global__ void __launch_bounds__(TX *TY, MINB)
     const int ntx = (L.Lx + TX - 1) / TX;
     const int gx0 = (blockIdx.x % ntx) * TX, gy0 = (blockIdx.x / ntx) * TY;
     const int zs = blockIdx.y * zc, ze = min(L.Lz, zs + zc);
-    const long long P = L.P;
+    const unsigned Pu = (unsigned)L.P;
     const int sxy = L.Lx * L.Ly;
-    const int t = threadIdx.x, lx = t % TX, ly = t / TX;
-    const int po = (ly + 1) * SX + (lx + 1);
-    const int gxo = gx0 + lx, gyo = gy0 + ly;
-    const bool own_in = gxo < L.Lx && gyo < L.Ly;
-    // a tile that overhangs the lattice still stages the wrapped sites: its
-    // positions past the edge are the halo of the last column or row
-    const int colo = wrap_any(gxo, L.Lx) + L.Lx * wrap_any(gyo, L.Ly);
-    int ph = 0, colh = 0;
-    if (t < NH) {
-        int rx, ry;
-        fused_halo_pos<TX, TY>(t, rx, ry);
-        ph = ry * SX + rx;
-        colh = wrap_any(gx0 + rx - 1, L.Lx) + L.Lx * wrap_any(gy0 + ry - 1, L.Ly);
-    }
+    const FusedPos<TX, TY> fp(L, gx0, gy0, threadIdx.x);
     auto slot = [&](int z) { return ((z - zs + 1) & 3) * 5 * TS; };
     T ro[15], rh[15];
     uint8_t c_next = 1;
+    // component k of site j at (X + k P)[j]: plane bases shared by every thread,
+    // 32-bit site offsets
     auto load = [&](int z) {
-        const long long base = (long long)sxy * wrap_any(z, L.Lz);
-        const long long io = base + colo;
+        const unsigned base = (unsigned)(sxy * wrap_near(z, L.Lz));
+        const unsigned io = base + fp.colo;
 #pragma unroll
         for (int k = 0; k < 5; ++k) {
-            ro[k] = ld(L.Q + k * P + io);
-            ro[5 + k] = ld(L.V + k * P + io);
-            ro[10 + k] = ld(L.F + k * P + io);
+            ro[k] = ld(L.Q + (size_t)k * Pu + io);
+            ro[5 + k] = ld(L.V + (size_t)k * Pu + io);
+            ro[10 + k] = ld(L.F + (size_t)k * Pu + io);
         }
-        if (t < NH) {
-            const long long ih = base + colh;
+        if (fp.has_h) {
+            const unsigned ih = base + fp.colh;
 #pragma unroll
             for (int k = 0; k < 5; ++k) {
-                rh[k] = ld(L.Q + k * P + ih);
-                rh[5 + k] = ld(L.V + k * P + ih);
-                rh[10 + k] = ld(L.F + k * P + ih);
+                rh[k] = ld(L.Q + (size_t)k * Pu + ih);
+                rh[5 + k] = ld(L.V + (size_t)k * Pu + ih);
+                rh[10 + k] = ld(L.F + (size_t)k * Pu + ih);
             }
         }
-        c_next = (own_in && z >= zs && z < ze) ? cls[io] : uint8_t(1);
+        c_next = (fp.own_in && z >= zs && z < ze) ? cls[io] : uint8_t(1);
     };
-    auto predict = [&](int z, T(&vn)[5]) {
+    // predicted Q of plane z into the ring; the owned site's predicted velocity and Q
+    auto predict = [&](int z, T(&vn)[5], T(&qn)[5]) {
         T *s = sQ + slot(z);
 #pragma unroll
         for (int k = 0; k < 5; ++k) {
             vn[k] = pred_v(pc, ro[5 + k], ro[10 + k]);
-            s[k * TS + po] = pred_q(pc, ro[k], vn[k]);
+            qn[k] = pred_q(pc, ro[k], vn[k]);
+            s[k * TS + fp.po] = qn[k];
         }
-        if (t < NH)
+        if (fp.has_h)
 #pragma unroll
-            for (int k = 0; k < 5; ++k) s[k * TS + ph] = pred_q(pc, rh[k], pred_v(pc, rh[5 + k], rh[10 + k]));
+            for (int k = 0; k < 5; ++k) s[k * TS + fp.ph] = pred_q(pc, rh[k], pred_v(pc, rh[5 + k], rh[10 + k]));
     };
     using Acc = typename std::conditional<sizeof(T) == 4, float, double>::type;
     Acc sacc[3] = {Acc(0), Acc(0), Acc(0)};
     if (zs < L.Lz) {
-        T vn_cur[5], vn_nxt[5];
+        T vn_cur[5], vn_nxt[5], qc[3][5];
         load(zs - 1);
-        predict(zs - 1, vn_cur);
+        predict(zs - 1, vn_cur, qc[1]);
         load(zs);
         uint8_t c_cur = c_next;
-        predict(zs, vn_cur);
+        predict(zs, vn_cur, qc[2]);
         load(zs + 1);
         for (int z = zs; z < ze; ++z) {
             const uint8_t c_here = c_cur;
             c_cur = c_next;
-            predict(z + 1, vn_nxt);
+#pragma unroll
+            for (int k = 0; k < 5; ++k) {
+                qc[0][k] = qc[1][k];
+                qc[1][k] = qc[2][k];
+            }
+            predict(z + 1, vn_nxt, qc[2]);
             if (z + 2 <= ze) load(z + 2);
             __syncthreads();
-            if (own_in) {
-                const int sl[3] = {slot(z - 1), slot(z), slot(z + 1)};
-                fused_site_out<T, TS, SX, Acc>(L, sQ, sl, po, (long long)sxy * z + colo, c_here, vn_cur, hdt, Qo,
-                                               Vo, Fo, sacc);
+            if (fp.own_in) {
+                const int sb[3] = {slot(z - 1) + fp.po, slot(z) + fp.po, slot(z + 1) + fp.po};
+                fused_site_out<T, TS, SX, Acc>(L, sQ, sb, qc, Pu, (unsigned)(sxy * z + fp.colo), c_here, vn_cur,
+                                               hdt, Qo, Vo, Fo, sacc);
             }
 #pragma unroll
             for (int k = 0; k < 5; ++k) vn_cur[k] = vn_nxt[k];
@@ -936,14 +988,20 @@ __global__ void __launch_bounds__(TX *TY, MINB)
     }
 }
 
-// The same iteration with the raw Q, V, F of each plane copied into shared
-// memory by cp.async two planes ahead (a ring of three raw planes) instead of
-// prefetched into registers one plane ahead: each thread copies and then reads
-// back only its own positions (its site and, for threads 0 .. NH-1, one halo
-// position), so the raw ring needs no barrier of its own.
+// The same iteration with the raw Q, V, F of each plane staged cooperatively:
+// every component row of the tile plus halo is copied as a 40-float segment
+// (x = gx0 - 4 .. gx0 + 35) by 16-byte cp.async, two planes ahead, into a
+// ring of three raw planes, wrapping across the periodic faces chunk by chunk
+// (needs Lx % 4 == 0, so that every chunk is 16-byte aligned and a wrapped
+// chunk stays one).  Each step then predicts plane z + 2 and computes the
+// force of plane z after one barrier: the predicted-Q ring holds planes
+// z - 1 .. z + 2.  The owned site's predicted velocity and Q of the planes in
+// flight stay in registers.
+template <int TY> constexpr int fused_v_rows() { return TY + 2; }
+constexpr int kFusedVRow = 40;  // floats per staged row segment
 template <class T, int TX, int TY> constexpr size_t fused_deep_cp_smem()
 {
-    return (size_t)(4 * 5 + 3 * 15) * (TX + 2) * (TY + 2) * sizeof(T);
+    return (size_t)4 * 5 * (TX + 2) * (TY + 2) * sizeof(T) + (size_t)3 * 15 * (TY + 2) * kFusedVRow * sizeof(T);
 }
 
 template <class T, int TX, int TY, int MINB>
@@ -951,101 +1009,115 @@ __global__ void __launch_bounds__(TX *TY, MINB)
     k_fire_deep_fused_cp(Lat<T> L, T *__restrict__ Qo, T *__restrict__ Vo, T *__restrict__ Fo,
                          const uint8_t *__restrict__ cls, const FireDev *__restrict__ fd, double *partials, int zc)
 {
-    constexpr int NT = TX * TY, SX = TX + 2, SY = TY + 2, TS = SX * SY, NH = fused_halo_count<TX, TY>();
-    static_assert(NH <= NT, "every halo position needs a thread");
+    static_assert(sizeof(T) == 4 && TX == 32, "16-byte row chunks of the 32-wide FP32 tile");
+    constexpr int NT = TX * TY, SX = TX + 2, SY = TY + 2, TS = SX * SY;
+    constexpr int RW = kFusedVRow, RC = RW / 4;           // row floats, 16-byte chunks per row
+    constexpr int RPLANE = 15 * SY * RW;                  // floats per raw plane: [15][SY][RW]
+    constexpr int NCH = 15 * SY * RC;                     // chunks per raw plane
+    constexpr int CPT = (NCH + NT - 1) / NT;              // chunks per thread
     extern __shared__ __align__(16) unsigned char smem_raw[];
     T *sQ = reinterpret_cast<T *>(smem_raw);  // [4][5][TS]: predicted Q of planes z-1 .. z+2
-    T *sR = sQ + 4 * 5 * TS;                   // [3][15][TS]: raw Q, V, F of planes z+1 .. z+3
+    T *sR = sQ + 4 * 5 * TS;                   // [3][15][SY][RW]: raw Q, V, F of planes in flight
     if (!fd->active) return;
     const PredCoef<T> pc = pred_coef<T>(fd);
     const T hdt = T(0.5) * T(fd->dt);
     const int ntx = (L.Lx + TX - 1) / TX;
     const int gx0 = (blockIdx.x % ntx) * TX, gy0 = (blockIdx.x / ntx) * TY;
     const int zs = blockIdx.y * zc, ze = min(L.Lz, zs + zc);
-    const long long P = L.P;
+    const unsigned Pu = (unsigned)L.P;
     const int sxy = L.Lx * L.Ly;
-    const int t = threadIdx.x, lx = t % TX, ly = t / TX;
-    const int po = (ly + 1) * SX + (lx + 1);
-    const int gxo = gx0 + lx, gyo = gy0 + ly;
-    const bool own_in = gxo < L.Lx && gyo < L.Ly;
-    const int colo = wrap_any(gxo, L.Lx) + L.Lx * wrap_any(gyo, L.Ly);
-    int ph = 0, colh = 0;
-    if (t < NH) {
-        int rx, ry;
-        fused_halo_pos<TX, TY>(t, rx, ry);
-        ph = ry * SX + rx;
-        colh = wrap_any(gx0 + rx - 1, L.Lx) + L.Lx * wrap_any(gy0 + ry - 1, L.Ly);
+    const FusedPos<TX, TY> fp(L, gx0, gy0, threadIdx.x);
+    // raw staging position of a staged-plane position (rx, ry): row ry, column rx + 3
+    auto raw_of = [&](int p) { return (p / SX) * RW + (p % SX) + 3; };
+    const int ro_own = raw_of(fp.po), ro_h = raw_of(fp.ph);
+    // this thread's chunks: field, component, row, chunk -> source offset within the
+    // field's planes (without the z plane) and destination within a raw plane
+    unsigned coff[CPT];
+    int cfield[CPT], cdst[CPT];
+#pragma unroll
+    for (int j = 0; j < CPT; ++j) {
+        const int c = threadIdx.x + j * NT;
+        cfield[j] = -1;
+        if (c < NCH) {
+            const int ch = c % RC, row = (c / RC) % SY, fk = c / (RC * SY);  // fk = 5 field + component
+            const int x = wrap_any(gx0 - 4 + 4 * ch, L.Lx), y = wrap_any(gy0 - 1 + row, L.Ly);
+            cfield[j] = fk / 5;
+            coff[j] = (unsigned)(fk % 5) * Pu + (unsigned)(x + L.Lx * y);
+            cdst[j] = (fk * SY + row) * RW + 4 * ch;
+        }
     }
+    auto rslot = [&](int z) { return sR + ((z - zs + 1) % 3) * RPLANE; };
     auto slot = [&](int z) { return ((z - zs + 1) & 3) * 5 * TS; };
-    auto rslot = [&](int z) { return ((z - zs + 1) % 3) * 15 * TS; };
-    // one commit group per plane (an empty group past the chunk's upper halo plane)
+    // one commit group per plane (an empty one past the chunk's upper halo plane)
     auto issue = [&](int z) {
         if (z <= ze) {
-            const long long base = (long long)sxy * wrap_any(z, L.Lz);
-            T *r = sR + rslot(z);
-            const long long io = base + colo;
+            const unsigned zoff = (unsigned)(sxy * wrap_near(z, L.Lz));
+            T *r = rslot(z);
 #pragma unroll
-            for (int k = 0; k < 5; ++k) {
-                cp_async_q(r + k * TS + po, L.Q + k * P + io);
-                cp_async_q(r + (5 + k) * TS + po, L.V + k * P + io);
-                cp_async_q(r + (10 + k) * TS + po, L.F + k * P + io);
-            }
-            if (t < NH) {
-                const long long ih = base + colh;
-#pragma unroll
-                for (int k = 0; k < 5; ++k) {
-                    cp_async_q(r + k * TS + ph, L.Q + k * P + ih);
-                    cp_async_q(r + (5 + k) * TS + ph, L.V + k * P + ih);
-                    cp_async_q(r + (10 + k) * TS + ph, L.F + k * P + ih);
-                }
+            for (int j = 0; j < CPT; ++j) {
+                if (cfield[j] < 0) continue;
+                const T *src = (cfield[j] == 0 ? L.Q : cfield[j] == 1 ? L.V : L.F) + (coff[j] + zoff);
+                const unsigned sa = (unsigned)__cvta_generic_to_shared(r + cdst[j]);
+                asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(sa), "l"(src) : "memory");
             }
         }
         asm volatile("cp.async.commit_group;\n" ::: "memory");
     };
-    auto predict = [&](int z, T(&vn)[5]) {
+    auto predict = [&](int z, T(&vn)[5], T(&qn)[5]) {
         T *s = sQ + slot(z);
-        const T *r = sR + rslot(z);
+        const T *r = rslot(z);
 #pragma unroll
         for (int k = 0; k < 5; ++k) {
-            vn[k] = pred_v(pc, r[(5 + k) * TS + po], r[(10 + k) * TS + po]);
-            s[k * TS + po] = pred_q(pc, r[k * TS + po], vn[k]);
+            vn[k] = pred_v(pc, r[((5 + k) * SY) * RW + ro_own], r[((10 + k) * SY) * RW + ro_own]);
+            qn[k] = pred_q(pc, r[(k * SY) * RW + ro_own], vn[k]);
+            s[k * TS + fp.po] = qn[k];
         }
-        if (t < NH)
+        if (fp.has_h)
 #pragma unroll
             for (int k = 0; k < 5; ++k)
-                s[k * TS + ph] = pred_q(pc, r[k * TS + ph], pred_v(pc, r[(5 + k) * TS + ph], r[(10 + k) * TS + ph]));
+                s[k * TS + fp.ph] = pred_q(pc, r[(k * SY) * RW + ro_h],
+                                           pred_v(pc, r[((5 + k) * SY) * RW + ro_h], r[((10 + k) * SY) * RW + ro_h]));
     };
     auto cls_at = [&](int z) -> uint8_t {
-        return (own_in && z >= zs && z < ze) ? cls[(long long)sxy * z + colo] : uint8_t(1);
+        return (fp.own_in && z >= zs && z < ze) ? cls[(unsigned)(sxy * z + fp.colo)] : uint8_t(1);
     };
-    using Acc = typename std::conditional<sizeof(T) == 4, float, double>::type;
-    Acc sacc[3] = {Acc(0), Acc(0), Acc(0)};
+    using Acc = float;
+    Acc sacc[3] = {0.f, 0.f, 0.f};
     if (zs < L.Lz) {
-        T vn_cur[5], vn_nxt[5];
+        // prologue: planes zs-1 .. zs+1 predicted; zs+2 and zs+3 in flight
+        T vn0[5], vn1[5], vn2[5], qc[3][5], qn[5];
         issue(zs - 1);
         issue(zs);
         issue(zs + 1);
-        asm volatile("cp.async.wait_group 2;\n" ::: "memory");
-        predict(zs - 1, vn_cur);
-        issue(zs + 2);  // into the raw slot of plane zs - 1, just consumed
-        asm volatile("cp.async.wait_group 2;\n" ::: "memory");
-        predict(zs, vn_cur);
-        uint8_t c_cur = cls_at(zs), c_nxt = cls_at(zs + 1);
+        asm volatile("cp.async.wait_group 0;\n" ::: "memory");
+        __syncthreads();
+        predict(zs - 1, vn0, qc[0]);
+        predict(zs, vn0, qc[1]);
+        predict(zs + 1, vn1, qc[2]);
+        __syncthreads();
+        issue(zs + 2);
+        issue(zs + 3);
+        uint8_t c_cur = cls_at(zs);
         for (int z = zs; z < ze; ++z) {
-            issue(z + 3);  // into the raw slot of plane z, which this thread has consumed
-            asm volatile("cp.async.wait_group 2;\n" ::: "memory");  // plane z + 1 has landed
-            predict(z + 1, vn_nxt);
             const uint8_t c_here = c_cur;
-            c_cur = c_nxt;
-            c_nxt = cls_at(z + 2);
-            __syncthreads();
-            if (own_in) {
-                const int sl[3] = {slot(z - 1), slot(z), slot(z + 1)};
-                fused_site_out<T, TS, SX, Acc>(L, sQ, sl, po, (long long)sxy * z + colo, c_here, vn_cur, hdt, Qo,
-                                               Vo, Fo, sacc);
+            c_cur = cls_at(z + 1);
+            asm volatile("cp.async.wait_group 1;\n" ::: "memory");  // this thread's copies of plane z + 2
+            __syncthreads();  // every copy of plane z + 2; plane z + 1's raw slot and plane z - 2's ring slot free
+            issue(z + 4);     // into the raw slot of plane z + 1
+            if (z + 2 <= ze) predict(z + 2, vn2, qn);
+            if (fp.own_in) {
+                const int sb[3] = {slot(z - 1) + fp.po, slot(z) + fp.po, slot(z + 1) + fp.po};
+                fused_site_out<T, TS, SX, Acc>(L, sQ, sb, qc, Pu, (unsigned)(sxy * z + fp.colo), c_here, vn0,
+                                               hdt, Qo, Vo, Fo, sacc);
             }
 #pragma unroll
-            for (int k = 0; k < 5; ++k) vn_cur[k] = vn_nxt[k];
+            for (int k = 0; k < 5; ++k) {
+                vn0[k] = vn1[k];
+                vn1[k] = vn2[k];
+                qc[0][k] = qc[1][k];
+                qc[1][k] = qc[2][k];
+                qc[2][k] = qn[k];
+            }
         }
         asm volatile("cp.async.wait_group 0;\n" ::: "memory");
     }
@@ -1286,20 +1358,29 @@ static int launch_fused_deep_cp(const Lat<T> &L, T *Qo, T *Vo, T *Fo, const Spli
 // 1 = 32 x 8, about two waves; 2 = 32 x 4, z chunks of 16 (raw planes
 // prefetched into registers; FP32 at 2, 2, 4 blocks per SM, FP64 at 1, 1, 2);
 // 3 = 32 x 8, about two waves, 4 = 32 x 4, about two waves (raw planes
-// copied into shared memory two planes ahead; FP32 at 2 and 4 blocks per SM,
-// FP64 at 1 and 2).  Returns the block count (partials used), -1 for an
-// unknown variant.
+// copied into shared memory by 16-byte row chunks two planes ahead; FP32 with
+// Lx % 4 == 0 only, at 2 and 4 blocks per SM).  Returns the block count
+// (partials used), -1 for a variant this lattice or precision does not have.
 template <class T>
 int launch_split_fused_deep(const Lat<T> &Lin, T *Qo, T *Vo, T *Fo, const SplitLists &sl, FireDev *fd,
                             double *partials, int variant, cudaStream_t s)
 {
     constexpr bool f32 = sizeof(T) == 4;
+    if (5 * Lin.P >= (1LL << 31)) return -1;  // the kernels' component offsets are 32-bit
     switch (variant) {
     case 0: return launch_fused_deep<T, 32, 8, f32 ? 2 : 1>(Lin, Qo, Vo, Fo, sl, fd, partials, 16, s);
     case 1: return launch_fused_deep<T, 32, 8, f32 ? 2 : 1>(Lin, Qo, Vo, Fo, sl, fd, partials, 0, s);
     case 2: return launch_fused_deep<T, 32, 4, f32 ? 4 : 2>(Lin, Qo, Vo, Fo, sl, fd, partials, 16, s);
-    case 3: return launch_fused_deep_cp<T, 32, 8, f32 ? 2 : 1>(Lin, Qo, Vo, Fo, sl, fd, partials, 0, s);
-    case 4: return launch_fused_deep_cp<T, 32, 4, f32 ? 4 : 2>(Lin, Qo, Vo, Fo, sl, fd, partials, 0, s);
+    case 3:
+    case 4:
+        // 16-byte row chunks: FP32 with Lx a multiple of 4 only
+        if constexpr (f32) {
+            if (Lin.Lx % 4 != 0) return -1;
+            if (variant == 3) return launch_fused_deep_cp<T, 32, 8, 2>(Lin, Qo, Vo, Fo, sl, fd, partials, 0, s);
+            return launch_fused_deep_cp<T, 32, 4, 4>(Lin, Qo, Vo, Fo, sl, fd, partials, 0, s);
+        } else {
+            return -1;
+        }
     default: return -1;
     }
 }

@@ -261,8 +261,9 @@ def test_split_variants_match_separate(qmin, oracle, L, prec, variant):
     beside its periodic edge tiles; 7-11: the predictor fused into the
     deep-site kernel with ping-pong state sets and a one-site halo of raw
     planes, in registers (7, 8: 32 x 8 tiles with z chunks of 16 or about two
-    waves; 9: 32 x 4) or in shared memory two planes ahead (10: 32 x 8; 11:
-    32 x 4), the listed sites forming their predicted Q on the fly; an odd
+    waves; 9: 32 x 4) or copied into shared memory by 16-byte row chunks two
+    planes ahead (10: 32 x 8; 11: 32 x 4; FP32 with Lx % 4 == 0), the listed
+    sites forming their predicted Q on the fly; an odd
     iteration count leaves the state in the second set, which the run copies
     back) tracks the separate kernels, with an L4 term and an external field:
     FP64 to 1e-12 after 7 iterations, FP32 to 1e-5."""
@@ -270,7 +271,8 @@ def test_split_variants_match_separate(qmin, oracle, L, prec, variant):
                       f"sphere={L[0] / 2},{L[1] / 2},{L[2] / 2},{min(L) / 4},p,2.0", "H=0.1,0.2,0.3,0.5,1.0,0.2"])
     s = oracle_system(oracle, cfg)
     tma_ok = L[0] % 4 == 0 and L[0] >= 40 and L[1] >= 12
-    if (4 <= variant <= 6 and prec == 0) or (variant == 6 and not tma_ok):
+    if (4 <= variant <= 6 and prec == 0) or (variant == 6 and not tma_ok) or \
+            (variant >= 10 and (prec == 0 or L[0] % 4 != 0)):
         lat = gpu_lattice(qmin, s, prec)
         lat.set_fire_kernel(4)
         with pytest.raises(qmin.QminError):
@@ -317,7 +319,7 @@ def test_fire_variant_pin_errors(qmin, oracle):
     lat.set_fire_variant(-1)
     lat.fire_init()
     lat.fire_run(2)
-    assert len(lat.fire_tuning()["candidates_ms"]) == 9  # FP64: 4 split kernels + 5 fused
+    assert len(lat.fire_tuning()["candidates_ms"]) == 7  # FP64: 4 split kernels + 3 fused
 
 
 @pytest.mark.parametrize("Ls", ["2.32,0,0,0,0", "2.32,1.0,0.5,0,0"])
