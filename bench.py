@@ -301,10 +301,13 @@ def run_e2e(q, consts, g, K, W, barrier, dist):
     """End to end through the C ABI from pinned host memory.  The timed region
     starts from nothing on the device: a fresh handle (qmin_create, the force
     parameters and objects), the upload of Q0 and the site types, the site
-    classes and lists built from the types, the FIRE strategy's autotuning and
+    classes and lists built from the types, the FIRE strategy's choice and
     graph capture, K FIRE iterations and the download of the final Q, then
-    qmin_destroy.  The same job on a handle that already holds this geometry
-    (lists, tuned strategy and graphs kept) is reported beside it."""
+    qmin_destroy.  `value` is such a job in a process that has met this
+    problem before (the autotuner's choice is kept per process); `cold_*` the
+    same job after qmin_tuning_cache_clear, the autotuner timing its
+    candidates inside the job; `warm_handle_*` the job on a handle that
+    already holds this geometry (lists, tuned strategy and graphs kept)."""
     import torch
     N = g.Q.shape[0]
     Qh = torch.from_numpy(g.Q).pin_memory()
@@ -325,15 +328,20 @@ def run_e2e(q, consts, g, K, W, barrier, dist):
             lat.close()
         return r
 
+    def timed_fresh_job():
+        torch.cuda.synchronize()
+        barrier()
+        t0 = time.perf_counter()
+        r = job()
+        torch.cuda.synchronize()
+        wall = time.perf_counter() - t0
+        barrier()
+        return r, max_over_ranks(wall * 1e3)
+
     job()                        # library and kernels loaded, allocator warm
-    torch.cuda.synchronize()
-    barrier()
-    t0 = time.perf_counter()
-    r = job()
-    torch.cuda.synchronize()
-    wall_fresh = time.perf_counter() - t0
-    barrier()
-    ms_fresh = max_over_ranks(wall_fresh * 1e3)
+    q.lib().qmin_tuning_cache_clear()
+    _, ms_cold = timed_fresh_job()
+    r, ms_fresh = timed_fresh_job()
     # the same job on a handle that already holds the geometry
     lat = make_lattice(q, consts, g, q.FP64)
     q._check(q.lib().qmin_set_stream(lat._h, stream.cuda_stream))
@@ -356,11 +364,13 @@ def run_e2e(q, consts, g, K, W, barrier, dist):
     world = int(os.environ.get("WORLD_SIZE", 1))
     return {"value": job_value(world, N, K, ms_fresh), "unit": "site-steps/s", "h2d_bytes_per_step": h2d / K,
             "d2h_bytes_per_step": d2h / K, "job_ms": ms_fresh, "iterations": r["iterations"],
+            "cold_value": job_value(world, N, K, ms_cold), "cold_job_ms": ms_cold,
             "warm_handle_value": job_value(world, N, K, ms_warm), "warm_handle_job_ms": ms_warm,
-            "setup_ms": ms_fresh - ms_warm,
-            "note": "per job, wall clock: fresh handle, upload Q0 (AoS f64) + int32 types, site lists, autotuning "
-                    "and graph capture, K FIRE iterations, download final Q, destroy; bytes amortised over K. "
-                    "warm_handle_*: the same job on a handle already holding this geometry"}
+            "setup_ms": ms_fresh - ms_warm, "cold_setup_ms": ms_cold - ms_warm,
+            "note": "per job, wall clock: fresh handle, upload Q0 (AoS f64) + int32 types, site lists, strategy "
+                    "choice and graph capture, K FIRE iterations, download final Q, destroy; bytes amortised over "
+                    "K. value: the process has tuned this problem before; cold_*: after qmin_tuning_cache_clear; "
+                    "warm_handle_*: a handle already holding this geometry"}
 
 
 def finish(q, args, rank, world, consts, g, N, K, W, timed_fire, value, ms, launches, clocks, roofline, fire_state,

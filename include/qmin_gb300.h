@@ -279,6 +279,13 @@ int qmin_set_fire_variant(qmin_handle h, int variant);
  * No reference counterpart (the reference's kernelTuner scans block sizes,
  * src/utilities/kernelTuner.cpp:5-125). */
 #define QMIN_TUNE_CANDIDATES 29
+/* The autotuner's choices are kept for the life of the process: a handle whose
+ * problem the process has already tuned (same sides, precision, metric, force
+ * form, field terms, strategy request and site-class counts) takes the stored
+ * choice on its first run instead of timing the candidates again.  This call
+ * forgets every stored choice (the next first run of each problem tunes
+ * afresh).  No reference counterpart (execution strategy). */
+int qmin_tuning_cache_clear(void);
 int qmin_fire_tuning(qmin_handle h, int *path, int *variant, int *tile_x, int *tile_y, int *zc,
                      double ms[QMIN_TUNE_CANDIDATES]);
 

@@ -155,6 +155,8 @@ def lib():
             fn = getattr(L, name)
             fn.argtypes = args
             fn.restype = C.c_int
+        L.qmin_tuning_cache_clear.argtypes = []
+        L.qmin_tuning_cache_clear.restype = C.c_int
         L.qmin_last_error_string.restype = C.c_char_p
         L.qmin_last_error_string.argtypes = []
         _lib = L

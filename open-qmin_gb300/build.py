@@ -44,7 +44,8 @@ def build(verbose=False, force=False):
     headers = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".h", ".cuh"))]
     headers.append(os.path.join(HERE, "..", "include", "qmin_gb300.h"))
     units = ["qmin_kernels.cu", "qmin_fused.cu", "qmin_capi.cu", "qmin_batch.cu", "qmin_host_setup.cpp",
-             "qmin_noalloc.cu", "qmin_warmnet.cu", "qmin_tiled.cu", "qmin_io.cpp", "qmin_split.cu"]
+             "qmin_noalloc.cu", "qmin_warmnet.cu", "qmin_tiled.cu", "qmin_io.cpp", "qmin_split.cu",
+             "qmin_geometry.cu"]
     objs, jobs = [], []
     for u in units:
         src = os.path.join(CSRC, u)

@@ -9,6 +9,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -71,7 +72,10 @@ struct qmin_ctx {
     void *objs = nullptr;
     int nobj = 0;
     std::vector<qmin_object> objs_host;
-    std::vector<int8_t> types_host;  // site types of the last qmin_set_state (split lists built from them)
+    // site-type scan and split-list building on the device (qmin_geometry.cu)
+    void *geo_scratch = nullptr;
+    size_t geo_scratch_bytes = 0;
+    int *scan_part = nullptr, *scan_out = nullptr;
     double *partials = nullptr;
     int grid = 1;
     double *stage = nullptr;
@@ -112,7 +116,7 @@ struct qmin_ctx {
     // sites and the sites whose derivative planes they read
     uint8_t *split_cls = nullptr;
     int *split_sites = nullptr, *split_derivs = nullptr;
-    int n_split_sites = 0, n_split_derivs = 0;
+    int n_split_sites = 0, n_split_derivs = 0, split_sites_cap = 0, split_derivs_cap = 0;
     // separate (register caps), fused (cfg, z extent), staged force + kick (cfg, z extent)
     double tune_ms[kTuneCandidates] = {};
 };
@@ -272,7 +276,8 @@ static void free_ctx(qmin_ctx *h)
         if (h->graph[g]) cudaGraphExecDestroy(h->graph[g]);
     void *bufs[] = {h->Q, h->V, h->F, h->D, h->types, h->objs, h->partials, h->stage, h->stage_t, h->fire, h->iter,
                     h->out5, h->M, h->S, h->alt, h->lbp, h->lbs, h->lby, h->Q2, h->V2, h->F2, h->hvar,
-                    h->split_cls, h->split_sites, h->split_derivs, h->cbd, h->dev_err};
+                    h->split_cls, h->split_sites, h->split_derivs, h->cbd, h->dev_err, h->geo_scratch,
+                    h->scan_part, h->scan_out};
     for (void *b : bufs)
         if (b) cudaFree(b);
     if (h->fire_h) cudaFreeHost(h->fire_h);
@@ -456,68 +461,52 @@ static int ensure_stage(qmin_ctx *h)
     return QMIN_OK;
 }
 
-// classes and index lists of the split force + kick, from host site types
-static int build_split_lists(qmin_ctx *h, const int8_t *t8)
+// classes and index lists of the split force + kick, built on the device from
+// the device site types (h->types)
+static int build_split_lists(qmin_ctx *h)
 {
-    const int Lx = h->Lx, Ly = h->Ly, Lz = h->Lz, N = h->N;
-    std::vector<uint8_t> cls((size_t)N);
-    std::vector<int> sites, derivs;
-    std::vector<char> need((size_t)N, 0);
-    auto nb = [&](int i, int s) {
-        const int x = i % Lx, r = i / Lx, y = r % Ly, z = r / Ly;
-        switch (s) {
-        case 0: return (x == 0 ? Lx - 1 : x - 1) + Lx * (y + Ly * z);
-        case 1: return (x == Lx - 1 ? 0 : x + 1) + Lx * (y + Ly * z);
-        case 2: return x + Lx * ((y == 0 ? Ly - 1 : y - 1) + Ly * z);
-        case 3: return x + Lx * ((y == Ly - 1 ? 0 : y + 1) + Ly * z);
-        case 4: return x + Lx * (y + Ly * (z == 0 ? Lz - 1 : z - 1));
-        default: return x + Lx * (y + Ly * (z == Lz - 1 ? 0 : z + 1));
-        }
-    };
-    for (int i = 0; i < N; ++i) {
-        if (t8[i] > 0) {
-            cls[i] = 2;
-            continue;
-        }
-        bool deep = t8[i] == 0;
-        for (int s = 0; s < 6 && deep; ++s) deep = t8[nb(i, s)] == 0;
-        cls[i] = deep ? 0 : 1;
-        if (!deep) {
-            sites.push_back(i);
-            for (int s = 0; s < 6; ++s) need[nb(i, s)] = 1;
-        }
+    const size_t need = split_scratch_bytes(h->N);
+    if (!h->split_cls && cudaMalloc(&h->split_cls, (size_t)h->N) != cudaSuccess) {
+        cudaGetLastError();
+        return fail(QMIN_ENOMEM, "split site classes: allocation failed");
     }
-    for (int i = 0; i < N; ++i)
-        if (need[i]) derivs.push_back(i);
-    // listed sites grouped by form (bulk-like first, then each boundary case),
-    // so that the warps of the listed-site kernel take one branch
-    auto form_of = [&](int i) {
-        if (t8[i] != -1) return 0;
-        int xx = 0, yy = 0, zz = 0;  // lcForce::getBoundaryCase: the down neighbour wins
-        if (t8[nb(i, 1)] > 0) xx = 1;
-        if (t8[nb(i, 0)] > 0) xx = 2;
-        if (t8[nb(i, 3)] > 0) yy = 1;
-        if (t8[nb(i, 2)] > 0) yy = 2;
-        if (t8[nb(i, 5)] > 0) zz = 1;
-        if (t8[nb(i, 4)] > 0) zz = 2;
-        return 1 + xx + 3 * yy + 9 * zz;
-    };
-    std::stable_sort(sites.begin(), sites.end(), [&](int a, int b) { return form_of(a) < form_of(b); });
-    auto upload = [&](void **dst, const void *src, size_t bytes) -> bool {
-        if (*dst) cudaFree(*dst);
-        *dst = nullptr;
-        if (bytes == 0) return true;
-        return cudaMalloc(dst, bytes) == cudaSuccess &&
-               cudaMemcpy(*dst, src, bytes, cudaMemcpyHostToDevice) == cudaSuccess;
-    };
-    if (!upload((void **)&h->split_cls, cls.data(), cls.size()) ||
-        !upload((void **)&h->split_sites, sites.data(), sites.size() * sizeof(int)) ||
-        !upload((void **)&h->split_derivs, derivs.data(), derivs.size() * sizeof(int))) {
+    if (h->geo_scratch_bytes < need) {
+        if (h->geo_scratch) cudaFree(h->geo_scratch);
+        h->geo_scratch = nullptr;
+        h->geo_scratch_bytes = 0;
+        if (cudaMalloc(&h->geo_scratch, need) != cudaSuccess) {
+            cudaGetLastError();
+            return fail(QMIN_ENOMEM, "split site lists: scratch allocation failed");
+        }
+        h->geo_scratch_bytes = need;
+    }
+    int totals[32];
+    const int n = build_split_lists_dev(h->types, h->Lx, h->Ly, h->Lz, h->split_cls, h->geo_scratch, totals,
+                                        &h->split_sites, &h->split_sites_cap, &h->n_split_sites, &h->split_derivs,
+                                        &h->split_derivs_cap, &h->n_split_derivs, h->stream);
+    if (n == -2) {
         cudaGetLastError();
         return fail(QMIN_ENOMEM, "split site lists: allocation failed");
     }
-    h->n_split_sites = (int)sites.size();
-    h->n_split_derivs = (int)derivs.size();
+    if (n < 0) return fail(QMIN_ECUDA, std::string("split site lists: ") + cudaGetErrorString(cudaGetLastError()));
+    h->launches += n;
+    return QMIN_OK;
+}
+
+// min / max type, count of types <= 0 and sites changed from the device types
+// (when `compare`), of int32 (t32) or int8 (t8) types on the device
+static int scan_device_types(qmin_ctx *h, const int32_t *t32, const int8_t *t8, bool compare, int out[4])
+{
+    if (!h->scan_part && (cudaMalloc(&h->scan_part, sizeof(int) * 4 * 152 * 4) != cudaSuccess ||
+                          cudaMalloc(&h->scan_out, sizeof(int) * 4) != cudaSuccess)) {
+        cudaGetLastError();
+        return fail(QMIN_ENOMEM, "site-type scan: allocation failed");
+    }
+    const int r = t32 ? scan_types<int32_t>(t32, compare ? h->types : nullptr, h->N, h->scan_part, h->scan_out, out,
+                                            h->stream)
+                      : scan_types<int8_t>(t8, nullptr, h->N, h->scan_part, h->scan_out, out, h->stream);
+    if (r < 0) return fail(QMIN_ECUDA, std::string("site-type scan: ") + cudaGetErrorString(cudaGetLastError()));
+    h->launches += r;
     return QMIN_OK;
 }
 
@@ -533,18 +522,15 @@ int qmin_set_state(qmin_handle h, const double *Q, const int32_t *types, int lay
     if (layout != QMIN_LAYOUT_AOS && layout != QMIN_LAYOUT_SOA) return fail(QMIN_EINVAL, "qmin_set_state: bad layout");
     int r = ensure_stage(h);
     if (r) return r;
-    long long nT = 0;
-    int mx = 0;
-    for (int i = 0; i < h->N; ++i) {
-        int t = types[i];
-        if (t < -2 || t > 127) return fail(QMIN_EINVAL, "qmin_set_state: site type out of range [-2, 127]");
-        if (t <= 0) ++nT;
-        mx = std::max(mx, t);
-    }
-    h->nTotal = nT;
-    h->max_type = mx;
     CK(cudaMemcpyAsync(h->stage, Q, sizeof(double) * 5 * (size_t)h->N, cudaMemcpyHostToDevice, h->stream));
     CK(cudaMemcpyAsync(h->stage_t, types, sizeof(int32_t) * (size_t)h->N, cudaMemcpyHostToDevice, h->stream));
+    // the types are checked on the device before any resident state changes
+    int sc[4];
+    if ((r = scan_device_types(h, h->stage_t, nullptr, h->have_state, sc))) return r;
+    if (sc[0] < -2 || sc[1] > 127) return fail(QMIN_EINVAL, "qmin_set_state: site type out of range [-2, 127]");
+    h->nTotal = sc[2];
+    h->max_type = std::max(0, sc[1]);
+    const bool same_geometry = h->have_state && sc[3] == 0;
     if (h->prec == QMIN_FP64)
         h->launches += launch_aos_to_soa<double>(h->stage, (double *)h->Q, h->N, h->P, layout, h->stream);
     else
@@ -553,16 +539,14 @@ int qmin_set_state(qmin_handle h, const double *Q, const int32_t *types, int lay
     CK(cudaMemsetAsync(h->V, 0, 5 * (size_t)h->P * h->esz, h->stream));
     CK(cudaMemsetAsync(h->F, 0, 5 * (size_t)h->P * h->esz, h->stream));
     CK(cudaGetLastError());
-    std::vector<int8_t> t8((size_t)h->N);
-    for (int i = 0; i < h->N; ++i) t8[i] = (int8_t)types[i];
-    CK(cudaStreamSynchronize(h->stream));
-    if (h->have_state && t8 == h->types_host) {
-        // same geometry: the split lists, the tuned strategy and the captured
-        // graphs (which hold buffer pointers, not contents) stay valid
+    if (same_geometry) {
+        // the split lists, the tuned strategy and the captured graphs (which
+        // hold buffer pointers, not contents) stay valid
+        CK(cudaStreamSynchronize(h->stream));
         return QMIN_OK;
     }
-    if ((r = build_split_lists(h, t8.data()))) return r;
-    h->types_host.swap(t8);
+    if ((r = build_split_lists(h))) return r;
+    CK(cudaStreamSynchronize(h->stream));
     invalidate_graphs(h);
     h->have_state = true;
     return QMIN_OK;
@@ -885,6 +869,44 @@ static int settle_pingpong(qmin_ctx *h, int executed)
     return QMIN_OK;
 }
 
+// The autotuner's choices, kept for the life of the process: a handle that
+// meets a problem the process has already tuned (same sides, precision,
+// metric, force form, strategy request and site-class counts) takes the
+// stored choice instead of timing every candidate again.
+struct TuneKey {
+    int Lx, Ly, Lz, prec, metric, multi, l6, l4, fields, mode, variant, tmap;
+    long long nTotal, n_sites, n_derivs;
+    bool operator==(const TuneKey &o) const { return memcmp(this, &o, sizeof(TuneKey)) == 0; }
+};
+struct TuneChoice {
+    int path, sep_cap, fused_cfg, fused_zc, fused_nblocks, tiled_cfg, tiled_zc, tiled_nblocks, split_cap;
+    double ms[kTuneCandidates];
+};
+static std::mutex g_tune_mutex;
+static std::vector<std::pair<TuneKey, TuneChoice>> g_tune_cache;
+
+static TuneKey tune_key(const qmin_ctx *h)
+{
+    TuneKey k;
+    memset(&k, 0, sizeof k);  // padding included: the key is compared bytewise
+    k.Lx = h->Lx;
+    k.Ly = h->Ly;
+    k.Lz = h->Lz;
+    k.prec = h->prec;
+    k.metric = h->metric_mode;
+    k.multi = h->params.multi_constant;
+    k.l6 = h->params.L6 != 0;
+    k.l4 = h->params.L4 != 0;
+    k.fields = (h->params.efield ? 1 : 0) | (h->params.hfield ? 2 : 0) | (h->hvar_on ? 4 : 0);
+    k.mode = h->fire_mode;
+    k.variant = h->fire_variant;
+    k.tmap = h->tmap_ok;
+    k.nTotal = h->nTotal;
+    k.n_sites = h->n_split_sites;
+    k.n_derivs = h->n_split_derivs;
+    return k;
+}
+
 // Autotuner for the FIRE iteration: times the candidate strategies on the live
 // lattice with CUDA events and keeps the fastest.  Candidates: the split force
 // + kick (deep-site kernel variants), the separate kernels (predictor,
@@ -906,6 +928,28 @@ template <class T> static int tune_fire(qmin_ctx *h, const Lat<T> &L)
     auto pinned_out = [&](int v) { return h->fire_variant >= 0 && v != h->fire_variant; };
     int r = ensure_pingpong(h);
     if (r) return r;
+    const TuneKey key = tune_key(h);
+    {
+        std::lock_guard<std::mutex> lock(g_tune_mutex);
+        for (const auto &e : g_tune_cache)
+            if (e.first == key) {
+                const TuneChoice &c = e.second;
+                h->path = c.path;
+                h->sep_cap = c.sep_cap;
+                h->fused_cfg = c.fused_cfg;
+                h->fused_zc = c.fused_zc;
+                h->fused_nblocks = c.fused_nblocks;
+                h->tiled_cfg = c.tiled_cfg;
+                h->tiled_zc = c.tiled_zc;
+                h->tiled_nblocks = c.tiled_nblocks;
+                h->split_cap = c.split_cap;
+                memcpy(h->tune_ms, c.ms, sizeof c.ms);
+                h->tuned_version = h->version;
+                h->tuned_mode = h->fire_mode;
+                h->tuned_variant = h->fire_variant;
+                return QMIN_OK;
+            }
+    }
     cudaEvent_t e0, e1;
     CK(cudaEventCreate(&e0));
     CK(cudaEventCreate(&e1));
@@ -933,7 +977,7 @@ template <class T> static int tune_fire(qmin_ctx *h, const Lat<T> &L)
     const float kNoBudget = 1e30f;
     const int H = L.multi ? 2 : 1;
     float best = kNoBudget;
-    auto budget_for = [&](float fixed) { return best < kNoBudget ? 2.f * best - fixed : kNoBudget; };
+    auto budget_for = [&](float fixed) { return best < kNoBudget ? 1.25f * best - fixed : kNoBudget; };
     for (int k = 0; k < kTuneCandidates; ++k) h->tune_ms[k] = -1;
     Lat<T> LB = L;
     LB.Q = (T *)h->Q2;
@@ -1086,6 +1130,13 @@ template <class T> static int tune_fire(qmin_ctx *h, const Lat<T> &L)
     cudaEventDestroy(e1);
     CK(cudaGetLastError());
     if (h->path < 0) return fail(QMIN_ECUDA, "FIRE autotuner: no strategy could be launched");
+    {
+        TuneChoice c{h->path, h->sep_cap, h->fused_cfg, h->fused_zc, h->fused_nblocks, h->tiled_cfg, h->tiled_zc,
+                     h->tiled_nblocks, h->split_cap, {}};
+        memcpy(c.ms, h->tune_ms, sizeof c.ms);
+        std::lock_guard<std::mutex> lock(g_tune_mutex);
+        g_tune_cache.emplace_back(key, c);
+    }
     h->tuned_version = h->version;
     h->tuned_mode = h->fire_mode;
     h->tuned_variant = h->fire_variant;
@@ -1557,6 +1608,13 @@ int qmin_set_fire_variant(qmin_handle h, int variant)
     return QMIN_OK;
 }
 
+int qmin_tuning_cache_clear(void)
+{
+    std::lock_guard<std::mutex> lock(g_tune_mutex);
+    g_tune_cache.clear();
+    return QMIN_OK;
+}
+
 int qmin_fire_tuning(qmin_handle h, int *path, int *variant, int *tile_x, int *tile_y, int *zc, double *ms)
 {
     if (!h) return fail(QMIN_EINVAL, "qmin_fire_tuning: null handle");
@@ -1715,19 +1773,13 @@ int qmin_checkpoint_load(qmin_handle h, const char *path)
     }
     fclose(f);
     if (!ok) return fail(QMIN_EINVAL, "qmin_checkpoint_load: truncated or unreadable checkpoint");
-    // site counts from the restored types
-    std::vector<int8_t> t8((size_t)h->N);
-    CK(cudaMemcpy(t8.data(), h->types, (size_t)h->N, cudaMemcpyDeviceToHost));
-    long long nT = 0;
-    int mx = 0;
-    for (int i = 0; i < h->N; ++i) {
-        nT += t8[i] <= 0;
-        mx = std::max(mx, (int)t8[i]);
-    }
-    h->nTotal = nT;
-    h->max_type = mx;
-    if (int rr = build_split_lists(h, t8.data())) return rr;
-    h->types_host = t8;
+    // site counts and split lists from the restored types
+    int sc[4];
+    if (int rr = scan_device_types(h, nullptr, h->types, false, sc)) return rr;
+    h->nTotal = sc[2];
+    h->max_type = std::max(0, sc[1]);
+    if (int rr = build_split_lists(h)) return rr;
+    CK(cudaStreamSynchronize(h->stream));
     h->have_state = true;
     h->fire_ready = hd.fire_ready != 0;
     CK(cudaMemcpy(h->fire_h, h->fire, sizeof(FireDev), cudaMemcpyDeviceToHost));

@@ -160,6 +160,18 @@ int launch_split_deep(const Lat<T> &L, const SplitLists &sl, FireDev *fd, double
 // Lin into the output set (Qo, Vo, Fo; returns the block count, -1 for an
 // unknown variant), and the listed sites (derivative planes of the predicted
 // Q, force + kick into Vo, Fo; returns the launch count, *nblocks its partials)
+// site types on the device (qmin_geometry.cu): min, max, count of types <= 0 and
+// count of sites that differ from old8 (when given) into out_host[0..3] (the
+// call synchronises the stream; part: 4 * 608 ints, out_dev: 4 ints)
+template <class TT>
+int scan_types(const TT *t, const int8_t *old8, int N, int *part, int *out_dev, int *out_host, cudaStream_t s);
+// the split path's classes and lists from the device types (qmin_geometry.cu):
+// cls (N bytes) written, *sites / *derivs grown as needed, host_totals: 29 ints;
+// scratch of split_scratch_bytes(N).  Returns the launch count, < 0 on failure.
+size_t split_scratch_bytes(int N);
+int build_split_lists_dev(const int8_t *t8, int Lx, int Ly, int Lz, uint8_t *cls, void *scratch, int *host_totals,
+                          int **sites, int *sites_cap, int *n_sites, int **derivs, int *derivs_cap, int *n_derivs,
+                          cudaStream_t s);
 template <class T>
 int launch_split_fused_deep(const Lat<T> &Lin, T *Qo, T *Vo, T *Fo, const SplitLists &sl, FireDev *fd,
                             double *partials, int variant, cudaStream_t s);

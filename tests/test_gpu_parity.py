@@ -354,3 +354,25 @@ def test_l6_batch_rejected(qmin):
     b = qmin.Batch([(8, 8, 8)])
     with pytest.raises(qmin.QminError):
         b.set_params(-1.0, -12.3, 10.1, 2.32, 1.0, 0.5, L6=0.8)
+
+
+def test_tuning_choice_kept_per_process(qmin, oracle):
+    """A second handle on the same problem takes the autotuner's stored choice
+    (the same per-candidate times, not re-measured); after
+    qmin_tuning_cache_clear a new handle times the candidates afresh.  The
+    trajectories agree whatever the choice."""
+    cfg = parse_args(["L=24,20,18", "seed=3", "Ls=2.32,1.0,0.5,0,0", "wall=2,0,h,5.3", "sphere=12,10,9,3.5,h,5.3"])
+    s = oracle_system(oracle, cfg)
+    runs = []
+    for clear in (False, False, True):
+        if clear:
+            assert qmin.lib().qmin_tuning_cache_clear() == qmin.QMIN_OK
+        lat = gpu_lattice(qmin, s, 1)
+        lat.fire_init()
+        r = lat.fire_run(6)
+        runs.append((lat.fire_tuning(), r))
+        lat.close()
+    assert runs[1][0] == runs[0][0]
+    assert runs[2][0]["candidates_ms"] != runs[0][0]["candidates_ms"]
+    for t, r in runs:
+        assert abs(r["forceMax"] - runs[0][1]["forceMax"]) <= 1e-5 * runs[0][1]["forceMax"]
