@@ -482,7 +482,8 @@ def run_c3(q, nsolves=512, max_iterations=30000):
         diverged = [int(k) for k in np.nonzero(~np.isfinite(fm))[0]]
         out[tag] = {"time_to_converge_s": dt, "converged": conv.value, "diverged_solves": diverged,
                     "status": int(rc), "iterations_mean": float(its.mean()), "iterations_max": int(its.max()),
-                    "site_steps_per_s": float((sizes * its).sum() / dt), "gpu_launches": b.launches() - l0}
+                    "site_steps_per_s": float((sizes * its).sum() / dt), "gpu_launches": b.launches() - l0,
+                    "chunk_shape": b.tuning()}
         b.close()
     out["note"] = ("diverged solves follow the reference's own FIRE schedule into overflow (checked against the "
                    "oracle in tests/test_gpu_batch.py)")

@@ -31,6 +31,7 @@ extern "C" {
 #define QMIN_ESTATE 4      /* call out of order (e.g. force before set_state) */
 #define QMIN_ENONFINITE 5  /* a reduction produced NaN/Inf (state left as computed) */
 #define QMIN_ENODEVICE 6   /* no CUDA device / extension not usable */
+#define QMIN_ETIMEOUT 7    /* a bounded device-side wait gave up (the run stopped; see the entry point) */
 
 /* precision of the resident state and stencil arithmetic */
 #define QMIN_FP64 0        /* every operation in FP64 (oracle-parity form) */
@@ -321,13 +322,15 @@ int qmin_energy_noalloc(const qmin_lattice_desc *desc, const qmin_ldg_params *p,
                         void *stream);
 
 /* ---- batched solves (many independent lattices of uneven sizes) ---- */
-/* A batch packs nsolves independent lattices (dims[3*s .. 3*s+2] = Lx, Ly, Lz)
- * into one device state and minimises them together: each solve follows
- * energyMinimizerFIRE::minimize on its own lattice (its own FIRE scalars,
- * stopping rule and iteration count), one launch per kernel per iteration
- * covers every still-active solve, converged solves retire.  All solves share
- * the force parameters; each has up to 16 objects.  No reference counterpart
- * for the batching itself (the reference minimises one lattice per process). */
+/* A batch packs nsolves (at most 16384) independent lattices (dims[3*s ..
+ * 3*s+2] = Lx, Ly, Lz) into one device state and minimises them together:
+ * each solve follows energyMinimizerFIRE::minimize on its own lattice (its own
+ * FIRE scalars, stopping rule and iteration count), converged solves retire.
+ * qmin_batch_fire_run runs all iterations of all solves in one persistent
+ * cooperative launch (grid barriers between the phases of an iteration).  All
+ * solves share the force parameters; each has up to 16 objects.  No reference
+ * counterpart for the batching itself (the reference minimises one lattice per
+ * process). */
 typedef struct qmin_batch_ctx *qmin_batch;
 int qmin_batch_create(int nsolves, const int32_t *dims, int precision, int metric_mode, qmin_batch *out);
 int qmin_batch_destroy(qmin_batch b);
@@ -340,8 +343,24 @@ int qmin_batch_get_solve(qmin_batch b, int s, double *Q, double *F);
 /* FIRE parameters for every solve (energyMinimizerFIRE::setFIREParameters) */
 int qmin_batch_fire_init(qmin_batch b, const qmin_fire_params *p);
 /* minimise every solve; per-solve iteration counts and forceMax (arrays of
- * nsolves, may be NULL) and the number of solves with forceMax <= cutoff */
+ * nsolves, may be NULL) and the number of solves with forceMax <= cutoff.
+ * QMIN_ETIMEOUT when a grid barrier of the persistent loop waited longer than
+ * its limit (qmin_batch_set_barrier_limit): every solve still running then
+ * has QMIN_ETIMEOUT in its status and stops, with the state of an unfinished
+ * iteration; set those solves again before the next run. */
 int qmin_batch_fire_run(qmin_batch b, int max_iterations, int *iterations, double *force_max, int *converged);
+/* polls a block makes at one grid barrier before the run gives up (0: the
+ * default, about a second).  No reference counterpart. */
+int qmin_batch_set_barrier_limit(qmin_batch b, long long spins);
+/* the chunk shape the tuner chose (-1 before the first run; 0: 256
+ * consecutive sites, 1-4: tiles of 32x8x1, 16x16x1, 16x4x4, 8x8x4 sites, as
+ * tile[3]) and the force + kick time of each shape in ms (-1: not timed).
+ * No reference counterpart (execution strategy). */
+int qmin_batch_tuning(qmin_batch b, int *shape, int tile[3], double ms[5]);
+/* pin the chunk shape (0-4 as in qmin_batch_tuning) or hand it back to the
+ * tuner (-1, the default); takes effect at the next run.  Every shape gives
+ * the same results to rounding.  No reference counterpart. */
+int qmin_batch_set_chunk_shape(qmin_batch b, int shape);
 int qmin_batch_kernel_launches(qmin_batch b, long long *count);
 
 /* ---- learned warm start ----

@@ -21,7 +21,7 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "_build", "libqmin_gb300.so")
 
-QMIN_OK, QMIN_EINVAL, QMIN_ECUDA, QMIN_ENOMEM, QMIN_ESTATE, QMIN_ENONFINITE, QMIN_ENODEVICE = range(7)
+QMIN_OK, QMIN_EINVAL, QMIN_ECUDA, QMIN_ENOMEM, QMIN_ESTATE, QMIN_ENONFINITE, QMIN_ENODEVICE, QMIN_ETIMEOUT = range(8)
 FP64, FP32 = 0, 1
 METRIC_CPU, METRIC_SINGLE = 0, 1
 LAYOUT_AOS, LAYOUT_SOA = 0, 1
@@ -131,6 +131,9 @@ def lib():
             "qmin_batch_fire_init": [h, C.POINTER(FireParams)],
             "qmin_batch_fire_run": [h, C.c_int, ip, dp, ip],
             "qmin_batch_kernel_launches": [h, C.POINTER(C.c_longlong)],
+            "qmin_batch_set_barrier_limit": [h, C.c_longlong],
+            "qmin_batch_tuning": [h, ip, ip, dp],
+            "qmin_batch_set_chunk_shape": [h, C.c_int],
             "qmin_fire_profile": [h, C.c_int, dp, ip],
             "qmin_fire_tuning": [h, ip, ip, ip, ip, ip, dp],
             "qmin_warmnet_create": [C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.POINTER(C.c_void_p)],
@@ -497,6 +500,21 @@ class Batch:
         conv = C.c_int()
         _check(lib().qmin_batch_fire_run(self._h, int(max_iterations), _ip(its), _dp(fm), C.byref(conv)))
         return dict(iterations=its, forceMax=fm, converged=conv.value)
+
+    def set_chunk_shape(self, shape):
+        """0: 256 consecutive sites; 1-4: tiles of 32x8x1, 16x16x1, 16x4x4, 8x8x4; -1: tuned."""
+        _check(lib().qmin_batch_set_chunk_shape(self._h, int(shape)))
+
+    def set_barrier_limit(self, spins):
+        _check(lib().qmin_batch_set_barrier_limit(self._h, int(spins)))
+
+    def tuning(self):
+        shape = C.c_int()
+        tile = (C.c_int * 3)()
+        ms = (C.c_double * 5)()
+        _check(lib().qmin_batch_tuning(self._h, C.byref(shape), tile, ms))
+        names = ["linear_256", "tile_32x8x1", "tile_16x16x1", "tile_16x4x4", "tile_8x8x4"]
+        return dict(shape=shape.value, tile=tuple(tile), candidates_ms={n: m for n, m in zip(names, ms) if m >= 0})
 
     def launches(self):
         n = C.c_longlong()

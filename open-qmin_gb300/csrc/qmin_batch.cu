@@ -1,13 +1,15 @@
 // Batched minimisation: many independent lattices of uneven sizes minimised
 // together.  Every solve is an independent energyMinimizerFIRE::minimize
 // (energyMinimizerFIRE.cpp:151-170) on its own lattice; the batch packs all of
-// them into one set of SoA planes and runs each FIRE iteration for all active
-// solves in one launch per kernel, over a work list of 256-site chunks that
-// never straddle two solves.  Per-solve FIRE scalars live on the device; a
-// solve that converged or ran out of iterations retires (its chunks return at
-// once) while the others continue.  The step loop is a captured CUDA graph of
-// a fixed number of iterations; the host reads one "any solve still active"
-// word per graph replay.
+// them into one set of SoA planes, cut into chunks of 256 sites that never
+// straddle two solves (256 consecutive sites, or tiles of the solve's box; the
+// tuner picks the shape by timing the force + kick).  qmin_batch_fire_run runs
+// every iteration of every solve in one persistent cooperative launch: per
+// iteration the predictor, the force + half kick + per-chunk FIRE sums and the
+// per-solve FIRE control, separated by bounded grid barriers.  Per-solve FIRE
+// scalars live on the device; a solve that converged or ran out of iterations
+// retires, and the phases then cover only the chunks of the solves still
+// active.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -31,7 +33,7 @@ struct SolveDesc {
 
 struct ChunkDesc {
     int solve;
-    int start;  // solve-local site index of the chunk's first site
+    int start;  // solve-local index of the chunk's first site (a tile's lowest corner)
 };
 
 template <class T> struct BatchArgs {
@@ -39,10 +41,45 @@ template <class T> struct BatchArgs {
     const SolveDesc *solves;
     const ChunkDesc *chunks;
     int nchunks;
+    // chunk shape: tx = 0: 256 consecutive sites of the solve; else a tx x ty x tz
+    // tile of its box (tx ty tz = 256, powers of two: lx = log2 tx, lxy = log2 tx ty)
+    // cut where it overhangs the box
+    int tx, ty, tz, lx, lxy;
     // multi-constant: site classes (0 deep bulk, 1 other LC site, 2 object) and
     // the sites whose derivative planes the class-1 forms read
     const uint8_t *cls, *needd;
 };
+
+// solve-local site (index li, coordinates x y z) of thread t in chunk ch,
+// false where the chunk's tile overhangs the solve's box
+template <class T>
+__device__ __forceinline__ bool chunk_site(const BatchArgs<T> &B, const SolveDesc &sd, const ChunkDesc &ch, int t,
+                                           int &li, int &x, int &y, int &z)
+{
+    if (B.tx == 0) {
+        li = ch.start + t;
+        if (li >= sd.Lx * sd.Ly * sd.Lz) return false;
+        x = li % sd.Lx;
+        const int r = li / sd.Lx;
+        y = r % sd.Ly;
+        z = r / sd.Ly;
+        return true;
+    }
+    const int x0 = ch.start % sd.Lx, r = ch.start / sd.Lx, y0 = r % sd.Ly, z0 = r / sd.Ly;
+    x = x0 + (t & (B.tx - 1));
+    y = y0 + ((t >> B.lx) & (B.ty - 1));
+    z = z0 + (t >> B.lxy);
+    if (x >= sd.Lx || y >= sd.Ly || z >= sd.Lz) return false;
+    li = x + sd.Lx * (y + sd.Ly * z);
+    return true;
+}
+template <class T>
+__device__ __forceinline__ bool chunk_site(const BatchArgs<T> &B, const SolveDesc &sd, const ChunkDesc &ch, int t,
+                                           int &li)
+{
+    int x, y, z;
+    return chunk_site(B, sd, ch, t, li, x, y, z);
+}
 
 // accessor for a site of a packed solve: neighbours wrap inside that solve's box
 template <class T> struct BatchAcc {
@@ -54,9 +91,12 @@ template <class T> struct BatchAcc {
     int i;
     int nb[6];
     __device__ __forceinline__ BatchAcc(const Lat<T> &L, const SolveDesc &sd, int li)
+        : BatchAcc(L, sd, li, li % sd.Lx, (li / sd.Lx) % sd.Ly, li / (sd.Lx * sd.Ly))
+    {
+    }
+    __device__ __forceinline__ BatchAcc(const Lat<T> &L, const SolveDesc &sd, int li, int x, int y, int z)
         : Q(L.Q), D(L.D), types(L.types), objs(L.objs + sd.obj_base), P(L.P), i(sd.off + li)
     {
-        const int x = li % sd.Lx, r = li / sd.Lx, y = r % sd.Ly, z = r / sd.Ly;
         const int sx = sd.Lx, sy = sd.Lx * sd.Ly;
         nb[0] = i + (x == 0 ? sd.Lx - 1 : -1);
         nb[1] = i + (x == sd.Lx - 1 ? -(sd.Lx - 1) : 1);
@@ -72,145 +112,142 @@ template <class T> struct BatchAcc {
     __device__ __forceinline__ ObjDev<T> obj(int t) const { return objs[t - 1]; }
 };
 
-// ---------------------------------------------------------------- kernels
-template <class T> __global__ void __launch_bounds__(kBlock) k_b_pred(BatchArgs<T> B, const FireDev *fds)
+constexpr int kBatchWarps = kBlock / 32;  // warp partial sums per chunk
+
+// ----------------------------------------------------- per-chunk phases
+// The deferred mix folded into the Verlet coefficients, as k_fire_pred does:
+// v' = cvv v + cvf f, q' = q + dt v' (chunk c of an active solve)
+template <class T> __device__ __forceinline__ void b_pred_chunk(const BatchArgs<T> &B, const FireDev *fds, int c)
 {
-    for (int c = blockIdx.x; c < B.nchunks; c += gridDim.x) {
-        const ChunkDesc ch = B.chunks[c];
-        const FireDev &fd = fds[ch.solve];
-        if (!fd.active) continue;  // uniform per block
-        // the deferred mix folded into the Verlet coefficients, as k_fire_pred does:
-        // v' = cvv v + cvf f, q' = q + dt v'; formed in FP64 by one lane per warp
-        double cf[3] = {0.0, 0.0, 0.0};
-        if ((threadIdx.x & 31) == 0) {
-            const double dt = fd.dt, hdt = 0.5 * dt;
-            double mv = 1.0, mf = 0.0;
-            if (fd.pending) {
-                mv = fd.reset ? 0.0 : 1.0 - fd.mixA;
-                mf = fd.reset ? 0.0 : fd.mixA * fd.mixS;
-            }
-            cf[0] = mv;
-            cf[1] = mf + hdt;
-            cf[2] = dt;
+    const ChunkDesc ch = B.chunks[c];
+    const FireDev &fd = fds[ch.solve];
+    if (!fd.active) return;  // uniform per block
+    // formed in FP64 by one lane per warp
+    double cf[3] = {0.0, 0.0, 0.0};
+    if ((threadIdx.x & 31) == 0) {
+        const double dt = fd.dt, hdt = 0.5 * dt;
+        double mv = 1.0, mf = 0.0;
+        if (fd.pending) {
+            mv = fd.reset ? 0.0 : 1.0 - fd.mixA;
+            mf = fd.reset ? 0.0 : fd.mixA * fd.mixS;
         }
+        cf[0] = mv;
+        cf[1] = mf + hdt;
+        cf[2] = dt;
+    }
 #pragma unroll
-        for (int k = 0; k < 3; ++k) cf[k] = __shfl_sync(0xffffffffu, cf[k], 0);
-        const T cvv = T(cf[0]), cvf = T(cf[1]), tdt = T(cf[2]);
-        const SolveDesc sd = B.solves[ch.solve];
-        const int li = ch.start + threadIdx.x;
-        if (li >= sd.Lx * sd.Ly * sd.Lz) continue;
-        const int i = sd.off + li;
+    for (int k = 0; k < 3; ++k) cf[k] = __shfl_sync(0xffffffffu, cf[k], 0);
+    const T cvv = T(cf[0]), cvf = T(cf[1]), tdt = T(cf[2]);
+    const SolveDesc sd = B.solves[ch.solve];
+    int li;
+    if (!chunk_site(B, sd, ch, threadIdx.x, li)) return;
+    const int i = sd.off + li;
 #pragma unroll
-        for (int k = 0; k < 5; ++k) {
-            const long long j = (long long)k * B.L.P + i;
-            const T vn = cvv * B.L.V[j] + cvf * B.L.F[j];
-            B.L.V[j] = vn;
-            B.L.Q[j] += tdt * vn;
-        }
+    for (int k = 0; k < 5; ++k) {
+        const long long j = (long long)k * B.L.P + i;
+        const T vn = cvv * B.L.V[j] + cvf * B.L.F[j];
+        B.L.V[j] = vn;
+        B.L.Q[j] += tdt * vn;
     }
 }
 
-// twice the first derivatives of every LC site (see qmin_force_core.cuh)
-template <class T> __global__ void __launch_bounds__(kBlock) k_b_derivs(BatchArgs<T> B, const FireDev *fds)
+// twice the first derivatives of the LC sites the class-1 forms read (see qmin_force_core.cuh)
+template <class T> __device__ __forceinline__ void b_derivs_chunk(const BatchArgs<T> &B, const FireDev *fds, int c)
 {
-    for (int c = blockIdx.x; c < B.nchunks; c += gridDim.x) {
-        const ChunkDesc ch = B.chunks[c];
-        if (fds && !fds[ch.solve].active) continue;
-        const SolveDesc sd = B.solves[ch.solve];
-        const int li = ch.start + threadIdx.x;
-        if (li >= sd.Lx * sd.Ly * sd.Lz) continue;
-        if (B.needd && !B.needd[sd.off + li]) continue;
-        BatchAcc<T> a(B.L, sd, li);
-        const int t = B.L.types[a.i];
+    const ChunkDesc ch = B.chunks[c];
+    if (fds && !fds[ch.solve].active) return;
+    const SolveDesc sd = B.solves[ch.solve];
+    int li, x, y, z;
+    if (!chunk_site(B, sd, ch, threadIdx.x, li, x, y, z)) return;
+    if (B.needd && !B.needd[sd.off + li]) return;
+    BatchAcc<T> a(B.L, sd, li, x, y, z);
+    const int t = B.L.types[a.i];
+    const long long P = B.L.P;
+#pragma unroll
+    for (int ax = 0; ax < 3; ++ax) {
+        const int dn = a.nb[2 * ax], up = a.nb[2 * ax + 1];
+        const int td = t < 0 ? B.L.types[dn] : 0, tu = t < 0 ? B.L.types[up] : 0;
+#pragma unroll
+        for (int k = 0; k < 5; ++k)
+            B.L.D[(5 * ax + k) * P + a.i] =
+                deriv2_rule(t, td, tu, ld(B.L.Q + k * P + dn), ld(B.L.Q + k * P + a.i), ld(B.L.Q + k * P + up));
+    }
+}
+
+// force (KICK = 0) or force + half kick + the chunk's FIRE reductions (KICK =
+// 1): each warp's sums of its 32 sites into partials[3 (kWarps c + warp) ..],
+// so that the warps of a block go through their chunks without waiting for
+// one another; ONE_CONST: the one-constant form only
+template <class T, int KICK, bool ONE_CONST>
+__device__ __forceinline__ void b_force_chunk(const BatchArgs<T> &B, const FireDev *fds, double *partials, int c)
+{
+    const ChunkDesc ch = B.chunks[c];
+    if (KICK && !fds[ch.solve].active) return;  // uniform per block
+    const SolveDesc sd = B.solves[ch.solve];
+    int li, x, y, z;
+    const bool in = chunk_site(B, sd, ch, threadIdx.x, li, x, y, z);
+    // the site's three dot products in the site precision (FP32 warp sums for
+    // the FP32 form, FP64 across warps and chunks)
+    T acc[3] = {T(0), T(0), T(0)};
+    if (in) {
+        const int gi = sd.off + li;
+        T f[5];
+        if (!ONE_CONST && B.cls && B.cls[gi] == 0) {
+            // deep bulk site: the 25-point form over Q, no derivative planes
+            deep_force_box(B.L, sd.off, sd.Lx, sd.Ly, sd.Lz, li, (long long)gi, f);
+        } else {
+            BatchAcc<T> a(B.L, sd, li, x, y, z);
+            site_force_core<T, BatchAcc<T>, false, !ONE_CONST, ONE_CONST>(B.L, a, B.L.types[gi], f);
+        }
         const long long P = B.L.P;
-#pragma unroll
-        for (int ax = 0; ax < 3; ++ax) {
-            const int dn = a.nb[2 * ax], up = a.nb[2 * ax + 1];
-            const int td = t < 0 ? B.L.types[dn] : 0, tu = t < 0 ? B.L.types[up] : 0;
-#pragma unroll
-            for (int k = 0; k < 5; ++k)
-                B.L.D[(5 * ax + k) * P + a.i] =
-                    deriv2_rule(t, td, tu, ld(B.L.Q + k * P + dn), ld(B.L.Q + k * P + a.i), ld(B.L.Q + k * P + up));
-        }
-    }
-}
-
-// force (KICK = 0) or force + half kick + per-chunk FIRE reductions (KICK = 1);
-// ONE_CONST: the one-constant form only (a batch whose parameters are one-constant)
-template <class T, int KICK, int CAP, bool ONE_CONST = false>
-__global__ void __launch_bounds__(kBlock, CAP + 1) k_b_force(BatchArgs<T> B, const FireDev *fds, double *partials)
-{
-    for (int c = blockIdx.x; c < B.nchunks; c += gridDim.x) {
-        const ChunkDesc ch = B.chunks[c];
-        if (KICK && !fds[ch.solve].active) continue;  // uniform per block
-        const SolveDesc sd = B.solves[ch.solve];
-        const int li = ch.start + threadIdx.x;
-        // the site's three dot products in the site precision (FP32 warp sums for
-        // the FP32 form, FP64 across warps and chunks)
-        T acc[3] = {T(0), T(0), T(0)};
-        if (li < sd.Lx * sd.Ly * sd.Lz) {
-            const int gi = sd.off + li;
-            T f[5];
-            if (!ONE_CONST && B.cls && B.cls[gi] == 0) {
-                // deep bulk site: the 25-point form over Q, no derivative planes
-                deep_force_box(B.L, sd.off, sd.Lx, sd.Ly, sd.Lz, li, (long long)gi, f);
-            } else {
-                BatchAcc<T> a(B.L, sd, li);
-                site_force_core<T, BatchAcc<T>, false, !ONE_CONST, ONE_CONST>(B.L, a, B.L.types[gi], f);
-            }
-            const long long P = B.L.P;
-            if (KICK) {
-                const T hdt = T(0.5) * T(fds[ch.solve].dt);
-                T v[5];
-#pragma unroll
-                for (int k = 0; k < 5; ++k) {
-                    v[k] = B.L.V[k * P + gi] + hdt * f[k];
-                    B.L.V[k * P + gi] = v[k];
-                }
-                acc[0] = dot_qt(f, f);
-                acc[1] = dot_qt(v, v);
-                acc[2] = dot_qt(f, v);
-            }
-#pragma unroll
-            for (int k = 0; k < 5; ++k) B.L.F[k * P + gi] = f[k];
-        }
         if (KICK) {
-            double sum[3];
-            if constexpr (sizeof(T) == 4) {
-                block_sum_f32<3>(acc, sum);
-            } else {
+            const T hdt = T(0.5) * T(fds[ch.solve].dt);
+            T v[5];
 #pragma unroll
-                for (int k = 0; k < 3; ++k) sum[k] = acc[k];
-                block_sum_smem<3>(sum);
+            for (int k = 0; k < 5; ++k) {
+                v[k] = B.L.V[k * P + gi] + hdt * f[k];
+                B.L.V[k * P + gi] = v[k];
             }
-            if (threadIdx.x == 0) {
-                partials[3 * c + 0] = sum[0];
-                partials[3 * c + 1] = sum[1];
-                partials[3 * c + 2] = sum[2];
-            }
+            acc[0] = dot_qt(f, f);
+            acc[1] = dot_qt(v, v);
+            acc[2] = dot_qt(f, v);
+        }
+#pragma unroll
+        for (int k = 0; k < 5; ++k) B.L.F[k * P + gi] = f[k];
+    }
+    if (KICK) {
+        // the warp's sums in the site precision (32 terms), FP64 from there on
+#pragma unroll
+        for (int k = 0; k < 3; ++k)
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) acc[k] += __shfl_xor_sync(0xffffffffu, acc[k], o);
+        if ((threadIdx.x & 31) == 0) {
+            double *p = partials + 3 * ((long long)kBatchWarps * c + threadIdx.x / 32);
+            p[0] = (double)acc[0];
+            p[1] = (double)acc[1];
+            p[2] = (double)acc[2];
         }
     }
 }
 
-// one warp per solve: deterministic sum of its chunks' partials, then the
+// one warp, solve w: deterministic sum of its chunks' partials, then the
 // fireStepCPU scalar logic (energyMinimizerFIRE.cpp:104-144) and the loop
-// condition of minimize(); raises *any when the solve stays active
-__global__ void k_b_control(FireDev *fds, const SolveDesc *solves, int nsolves, const double *partials, int *any)
+// condition of minimize(); returns (in lane 0) whether the solve retired now
+__device__ __forceinline__ bool b_control_solve(FireDev *fds, const SolveDesc *solves, int w, const double *partials)
 {
-    const int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
-    if (w >= nsolves) return;
+    const int lane = threadIdx.x & 31;
     FireDev *fd = fds + w;
-    if (!fd->active) return;  // uniform per warp
+    if (!fd->active) return false;  // uniform per warp
     const SolveDesc sd = solves[w];
     double v[3] = {0.0, 0.0, 0.0};
-    for (int c = lane; c < sd.nchunks; c += 32)
+    for (int c = lane; c < kBatchWarps * sd.nchunks; c += 32)
 #pragma unroll
-        for (int k = 0; k < 3; ++k) v[k] += partials[3 * (sd.chunk0 + c) + k];
+        for (int k = 0; k < 3; ++k) v[k] += partials[3 * ((long long)kBatchWarps * sd.chunk0 + c) + k];
 #pragma unroll
     for (int k = 0; k < 3; ++k)
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) v[k] += __shfl_down_sync(0xffffffffu, v[k], o);
-    if (lane != 0) return;
+    if (lane != 0) return false;
     const double fn = v[0], vn = v[1], pw = v[2];
     const int it = fd->iterations + 1;
     fd->power = pw;
@@ -238,10 +275,23 @@ __global__ void k_b_control(FireDev *fds, const SolveDesc *solves, int nsolves, 
     if (!isfinite(fn) || !isfinite(vn) || !isfinite(pw)) {
         fd->status = 1;
         fd->active = 0;
-        return;
+        return true;
     }
     fd->active = (it < fd->max_iters && fd->forceMax > fd->fcut) ? 1 : 0;
-    if (fd->active) atomicOr(any, 1);
+    return !fd->active;
+}
+
+// ----------------------------------------------- launch-per-phase kernels
+// (the entry force evaluation of every minimize() call, the tuner's timings)
+template <class T, int KICK, bool ONE_CONST>
+__global__ void __launch_bounds__(kBlock) k_b_force(BatchArgs<T> B, const FireDev *fds, double *partials)
+{
+    for (int c = blockIdx.x; c < B.nchunks; c += gridDim.x) b_force_chunk<T, KICK, ONE_CONST>(B, fds, partials, c);
+}
+
+template <class T> __global__ void __launch_bounds__(kBlock) k_b_derivs(BatchArgs<T> B, const FireDev *fds)
+{
+    for (int c = blockIdx.x; c < B.nchunks; c += gridDim.x) b_derivs_chunk<T>(B, fds, c);
 }
 
 // apply each solve's last deferred velocity mix
@@ -252,8 +302,8 @@ template <class T> __global__ void __launch_bounds__(kBlock) k_b_finish(BatchArg
         const FireDev &fd = fds[ch.solve];
         if (!fd.pending) continue;
         const SolveDesc sd = B.solves[ch.solve];
-        const int li = ch.start + threadIdx.x;
-        if (li >= sd.Lx * sd.Ly * sd.Lz) continue;
+        int li;
+        if (!chunk_site(B, sd, ch, threadIdx.x, li)) continue;
         const T ma = T(1.0 - fd.mixA), mb = T(fd.mixA * fd.mixS);
 #pragma unroll
         for (int k = 0; k < 5; ++k) {
@@ -267,6 +317,134 @@ __global__ void k_b_clear_pending(FireDev *fds, int n)
 {
     const int s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s < n) fds[s].pending = 0;
+}
+
+// ---------------------------------------------------- persistent FIRE loop
+// Run state of one persistent launch: grid barrier (arrival count, generation,
+// abort flag, spin limit) and, per iteration, the number of solves that retired.
+struct BatchRun {
+    unsigned count, gen;
+    int abort;
+    int pad;
+    long long spin_limit;
+    int retired[3];
+    int pad2;
+};
+
+
+// grid-wide barrier between two phases; bounded: a block that has waited
+// spin_limit polls raises the abort flag, and every block leaves at its next
+// barrier once the flag is up.  Returns false on abort.
+__device__ __forceinline__ bool b_grid_sync(BatchRun *run)
+{
+    __shared__ int ok;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        volatile unsigned *vgen = &run->gen;
+        volatile int *vabort = &run->abort;
+        const unsigned g = *vgen;
+        __threadfence();
+        if (atomicAdd(&run->count, 1u) == gridDim.x - 1) {
+            atomicExch(&run->count, 0u);
+            __threadfence();
+            atomicAdd(&run->gen, 1u);
+        } else {
+            long long spins = 0;
+            while (*vgen == g) {
+                if (*vabort) break;
+                if (++spins > run->spin_limit) {
+                    atomicExch(&run->abort, 1);
+                    break;
+                }
+                __nanosleep(64);
+            }
+        }
+        __threadfence();
+        ok = *vabort == 0;
+    }
+    __syncthreads();
+    return ok != 0;
+}
+
+// Every FIRE iteration of every solve in one cooperative launch: predictor,
+// (derivative planes,) force + half kick + per-chunk sums, per-solve control,
+// a grid barrier after each phase.  The work of a phase is the chunks of the
+// active solves: each block holds the same list of active solves and the
+// prefix sums of their chunk counts in shared memory, rebuilt (in solve order)
+// when a solve retires, so retired solves cost nothing.
+constexpr int kMaxBatchSolves = 16384;  // the lists take 8 (nsolves + 1) bytes of shared memory
+
+// (the one-constant forms ask for three blocks per SM, the FP32 multi-constant
+// form for two: the force phase would otherwise hold the registers of fewer)
+template <class T, bool ONE_CONST>
+__global__ void __launch_bounds__(kBlock, ONE_CONST ? 3 : (sizeof(T) == 4 ? 2 : 1))
+    k_b_fire_persistent(BatchArgs<T> B, FireDev *fds, double *partials, int nsolves, BatchRun *run)
+{
+    extern __shared__ int b_lists[];
+    int *act = b_lists;                // active solve ids, in solve order
+    int *pre = b_lists + nsolves + 1;  // prefix sums of their chunk counts
+    __shared__ int n_act;
+    auto rebuild = [&]() {
+        // one warp: ballot over the solves in order
+        if (threadIdx.x < 32) {
+            int n = 0, tot = 0;
+            for (int s0 = 0; s0 < nsolves; s0 += 32) {
+                const int s = s0 + threadIdx.x;
+                const bool a = s < nsolves && fds[s].active;
+                const int nc = a ? B.solves[s].nchunks : 0;
+                const unsigned m = __ballot_sync(0xffffffffu, a);
+                int inc = nc;
+#pragma unroll
+                for (int o = 1; o < 32; o <<= 1) {
+                    const int v = __shfl_up_sync(0xffffffffu, inc, o);
+                    if (threadIdx.x >= o) inc += v;
+                }
+                if (a) {
+                    const int k = n + __popc(m & ((1u << threadIdx.x) - 1u));
+                    act[k] = s;
+                    pre[k] = tot + inc - nc;
+                }
+                n += __popc(m);
+                tot += __shfl_sync(0xffffffffu, inc, 31);
+            }
+            if (threadIdx.x == 0) {
+                n_act = n;
+                pre[n] = tot;
+            }
+        }
+        __syncthreads();
+    };
+    // chunk of work item w: binary search in the prefix sums
+    auto chunk_of = [&](int w) {
+        int lo = 0, hi = n_act - 1;
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (pre[mid] <= w) lo = mid;
+            else hi = mid - 1;
+        }
+        return B.solves[act[lo]].chunk0 + (w - pre[lo]);
+    };
+    rebuild();
+    const int nwarps = gridDim.x * (kBlock / 32);
+    const int gwarp = blockIdx.x * (kBlock / 32) + threadIdx.x / 32;
+    for (int it = 0; n_act > 0; ++it) {
+        if (blockIdx.x == 0 && threadIdx.x == 0) run->retired[it % 3] = 0;
+        const int nw = pre[n_act];
+        for (int w = blockIdx.x; w < nw; w += gridDim.x) b_pred_chunk<T>(B, fds, chunk_of(w));
+        if (!b_grid_sync(run)) return;
+        if (!ONE_CONST && B.L.multi) {
+            for (int w = blockIdx.x; w < nw; w += gridDim.x) b_derivs_chunk<T>(B, fds, chunk_of(w));
+            if (!b_grid_sync(run)) return;
+        }
+        for (int w = blockIdx.x; w < nw; w += gridDim.x) b_force_chunk<T, 1, ONE_CONST>(B, fds, partials, chunk_of(w));
+        if (!b_grid_sync(run)) return;
+        // per-solve control, one warp per active solve (its warps' sums added in order)
+        for (int k = gwarp; k < n_act; k += nwarps)
+            if (b_control_solve(fds, B.solves, act[k], partials) && (threadIdx.x & 31) == 0)
+                atomicAdd(&run->retired[it % 3], 1);
+        if (!b_grid_sync(run)) return;
+        if (*(volatile int *)&run->retired[it % 3] > 0) rebuild();
+    }
 }
 
 }  // namespace qmin
@@ -289,7 +467,10 @@ int bfail(int code, const std::string &m)
     } while (0)
 
 constexpr int kObjPerSolve = 16;
-constexpr int kBatchChunk = 32;  // iterations per captured graph
+// chunk shapes the tuner tries: 256 consecutive sites, then tiles of the box
+constexpr int kShapes = 5;
+constexpr int kShape[kShapes][3] = {{0, 0, 0}, {32, 8, 1}, {16, 16, 1}, {16, 4, 4}, {8, 8, 4}};
+constexpr long long kDefaultSpinLimit = 1LL << 24;  // about a second of polling at one barrier
 
 }  // namespace
 
@@ -312,15 +493,46 @@ struct qmin_batch_ctx {
     int32_t *stage_t = nullptr;
     FireDev *fds = nullptr;
     std::vector<FireDev> fds_h;
-    int *any = nullptr, *any_h = nullptr;
     cudaStream_t stream = nullptr;
     qmin_ldg_params params{};
     bool have_params = false, fire_ready = false;
-    int cap = -1;  // force + kick register cap chosen by the tuner
-    cudaGraphExec_t graph = nullptr;
-    int graph_cap = -1;
+    int shape = -1;  // chunk shape chosen by the tuner (-1: not tuned; chunks laid out as shape 0)
+    int pinned_shape = -1;  // chunk shape the caller pinned (-1: the tuner picks)
+    int layout = 0;  // chunk shape the device chunk list is laid out in
+    double shape_ms[kShapes] = {-1, -1, -1, -1, -1};
+    int max_chunks = 0;  // partials capacity (chunks of the largest layout)
+    BatchRun *run = nullptr;
+    long long spin_limit = kDefaultSpinLimit;
     long long launches = 0;
 };
+
+// chunk list of shape k: every solve's chunks in solve order, tiles in x-fastest order
+static void chunk_layout(int k, std::vector<SolveDesc> &solves, std::vector<ChunkDesc> *chunks)
+{
+    if (chunks) chunks->clear();
+    int c0 = 0;
+    for (size_t s = 0; s < solves.size(); ++s) {
+        SolveDesc &sd = solves[s];
+        const int n = sd.Lx * sd.Ly * sd.Lz;
+        int nc = 0;
+        if (k == 0) {
+            nc = (n + kBlock - 1) / kBlock;
+            if (chunks)
+                for (int c = 0; c < nc; ++c) chunks->push_back({(int)s, c * kBlock});
+        } else {
+            const int tx = kShape[k][0], ty = kShape[k][1], tz = kShape[k][2];
+            for (int z = 0; z < sd.Lz; z += tz)
+                for (int y = 0; y < sd.Ly; y += ty)
+                    for (int x = 0; x < sd.Lx; x += tx) {
+                        if (chunks) chunks->push_back({(int)s, x + sd.Lx * (y + sd.Ly * z)});
+                        ++nc;
+                    }
+        }
+        sd.chunk0 = c0;
+        sd.nchunks = nc;
+        c0 += nc;
+    }
+}
 
 template <class T> static BatchArgs<T> batch_args(qmin_batch_ctx *b)
 {
@@ -341,13 +553,36 @@ template <class T> static BatchArgs<T> batch_args(qmin_batch_ctx *b)
     B.solves = b->solves;
     B.chunks = b->chunks;
     B.nchunks = b->nchunks;
+    B.tx = kShape[b->layout][0];
+    B.ty = kShape[b->layout][1];
+    B.tz = kShape[b->layout][2];
+    if (B.tx > 0) {
+        B.lx = __builtin_ctz(B.tx);
+        B.lxy = __builtin_ctz(B.tx * B.ty);
+    }
     return B;
+}
+
+// lay the device chunk list out in shape k (solve descriptors included)
+static int set_layout(qmin_batch_ctx *b, int k)
+{
+    if (b->layout == k && b->nchunks > 0) return QMIN_OK;
+    chunk_layout(k, b->solves_h, &b->chunks_h);
+    b->nchunks = (int)b->chunks_h.size();
+    b->layout = k;
+    BCK(cudaMemcpyAsync(b->solves, b->solves_h.data(), sizeof(SolveDesc) * b->nsolves, cudaMemcpyHostToDevice,
+                        b->stream));
+    BCK(cudaMemcpyAsync(b->chunks, b->chunks_h.data(), sizeof(ChunkDesc) * b->nchunks, cudaMemcpyHostToDevice,
+                        b->stream));
+    return QMIN_OK;
 }
 
 static int grid_for(int nchunks) { return std::min(nchunks, 152 * 8); }
 
+// forces (kick = 0: every solve, object sites zero) or force + half kick +
+// per-chunk sums of the active solves (kick = 1), launch per phase
 template <class T> static int launch_b_force(const BatchArgs<T> &B, const FireDev *fds, double *partials, int kick,
-                                             int cap, cudaStream_t s)
+                                             cudaStream_t s)
 {
     const int g = grid_for(B.nchunks);
     int n = 0;
@@ -356,27 +591,81 @@ template <class T> static int launch_b_force(const BatchArgs<T> &B, const FireDe
         ++n;
     }
     if (!B.L.multi) {
-        if (!kick) k_b_force<T, 0, 0, true><<<g, kBlock, 0, s>>>(B, fds, partials);
-        else if (cap == 2) k_b_force<T, 1, 2, true><<<g, kBlock, 0, s>>>(B, fds, partials);
-        else if (cap == 1) k_b_force<T, 1, 1, true><<<g, kBlock, 0, s>>>(B, fds, partials);
-        else k_b_force<T, 1, 0, true><<<g, kBlock, 0, s>>>(B, fds, partials);
-        return n + 1;
+        if (kick) k_b_force<T, 1, true><<<g, kBlock, 0, s>>>(B, fds, partials);
+        else k_b_force<T, 0, true><<<g, kBlock, 0, s>>>(B, fds, partials);
+    } else {
+        if (kick) k_b_force<T, 1, false><<<g, kBlock, 0, s>>>(B, fds, partials);
+        else k_b_force<T, 0, false><<<g, kBlock, 0, s>>>(B, fds, partials);
     }
-    if (!kick) k_b_force<T, 0, 0><<<g, kBlock, 0, s>>>(B, fds, partials);
-    else if (cap == 2) k_b_force<T, 1, 2><<<g, kBlock, 0, s>>>(B, fds, partials);
-    else if (cap == 1) k_b_force<T, 1, 1><<<g, kBlock, 0, s>>>(B, fds, partials);
-    else k_b_force<T, 1, 0><<<g, kBlock, 0, s>>>(B, fds, partials);
     return n + 1;
 }
 
-template <class T> static int launch_b_iteration(qmin_batch_ctx *b, const BatchArgs<T> &B, int cap)
+// the chunk shape for the force + kick: each shape's launch timed with CUDA
+// events on the live batch (mean of three after a warm-up), the velocities the
+// kicks change restored afterwards
+template <class T> static int tune_shape(qmin_batch_ctx *b)
 {
-    cudaMemsetAsync(b->any, 0, sizeof(int), b->stream);
-    k_b_pred<T><<<grid_for(B.nchunks), kBlock, 0, b->stream>>>(B, b->fds);
-    int n = 1 + launch_b_force<T>(B, b->fds, b->partials, 1, cap, b->stream);
-    k_b_control<<<(b->nsolves * 32 + 255) / 256, 256, 0, b->stream>>>(b->fds, b->solves, b->nsolves, b->partials,
-                                                                        b->any);
-    return n + 1;
+    cudaEvent_t e0, e1;
+    BCK(cudaEventCreate(&e0));
+    BCK(cudaEventCreate(&e1));
+    void *vb = nullptr;
+    const size_t bytes = 5 * (size_t)b->P * b->esz;
+    if (cudaMalloc(&vb, bytes) != cudaSuccess) {
+        cudaGetLastError();
+        return bfail(QMIN_ENOMEM, "batch tuner: scratch allocation failed");
+    }
+    BCK(cudaMemcpyAsync(vb, b->V, bytes, cudaMemcpyDeviceToDevice, b->stream));
+    float best = 1e30f;
+    int best_k = 0;
+    for (int k = 0; k < kShapes; ++k) {
+        int r = set_layout(b, k);
+        if (r) return r;
+        BatchArgs<T> B = batch_args<T>(b);
+        b->launches += launch_b_force<T>(B, b->fds, b->partials, 1, b->stream);
+        cudaEventRecord(e0, b->stream);
+        for (int rep = 0; rep < 3; ++rep) b->launches += launch_b_force<T>(B, b->fds, b->partials, 1, b->stream);
+        cudaEventRecord(e1, b->stream);
+        cudaEventSynchronize(e1);
+        float ms = 0;
+        cudaEventElapsedTime(&ms, e0, e1);
+        b->shape_ms[k] = ms / 3;
+        if (ms < best) {
+            best = ms;
+            best_k = k;
+        }
+    }
+    BCK(cudaMemcpyAsync(b->V, vb, bytes, cudaMemcpyDeviceToDevice, b->stream));
+    BCK(cudaStreamSynchronize(b->stream));
+    cudaFree(vb);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    b->shape = best_k;
+    return set_layout(b, best_k);
+}
+
+// the persistent FIRE loop as one cooperative launch of as many blocks as can
+// be resident together
+template <class T, bool ONE_CONST> static int launch_persistent(qmin_batch_ctx *b, const BatchArgs<T> &B)
+{
+    const size_t smem = sizeof(int) * 2 * ((size_t)b->nsolves + 1);
+    auto kern = k_b_fire_persistent<T, ONE_CONST>;
+    if (smem > 48 * 1024 &&
+        cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+        return bfail(QMIN_ECUDA, "batch: shared memory for the active-solve lists");
+    int per_sm = 0, nsm = 0, dev = 0;
+    BCK(cudaGetDevice(&dev));
+    BCK(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+    BCK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kBlock, smem));
+    if (per_sm < 1) return bfail(QMIN_ECUDA, "batch: the persistent kernel does not fit on an SM");
+    const int grid = per_sm * nsm;
+    BatchArgs<T> a = B;
+    FireDev *fds = b->fds;
+    double *partials = b->partials;
+    int ns = b->nsolves;
+    BatchRun *run = b->run;
+    void *args[] = {&a, &fds, &partials, &ns, &run};
+    BCK(cudaLaunchCooperativeKernel((const void *)kern, dim3(grid), dim3(kBlock), args, smem, b->stream));
+    return QMIN_OK;
 }
 
 // The API functions below take C linkage from their declarations in qmin_gb300.h.
@@ -384,6 +673,7 @@ template <class T> static int launch_b_iteration(qmin_batch_ctx *b, const BatchA
 int qmin_batch_create(int nsolves, const int32_t *dims, int precision, int metric_mode, qmin_batch *out)
 {
     if (!out || !dims || nsolves < 1) return bfail(QMIN_EINVAL, "qmin_batch_create: bad argument");
+    if (nsolves > kMaxBatchSolves) return bfail(QMIN_EINVAL, "qmin_batch_create: at most 16384 solves per batch");
     if (precision != QMIN_FP64 && precision != QMIN_FP32) return bfail(QMIN_EINVAL, "qmin_batch_create: precision");
     if (metric_mode != QMIN_METRIC_CPU && metric_mode != QMIN_METRIC_SINGLE)
         return bfail(QMIN_EINVAL, "qmin_batch_create: metric_mode");
@@ -406,8 +696,7 @@ int qmin_batch_create(int nsolves, const int32_t *dims, int precision, int metri
             return bfail(QMIN_EINVAL, "qmin_batch_create: every lattice side must be >= 3");
         }
         const int n = Lx * Ly * Lz;
-        SolveDesc sd{Lx, Ly, Lz, (int)off, (int)b->chunks_h.size(), (n + kBlock - 1) / kBlock, s * kObjPerSolve, 0};
-        for (int c = 0; c < sd.nchunks; ++c) b->chunks_h.push_back({s, c * kBlock});
+        SolveDesc sd{Lx, Ly, Lz, (int)off, 0, 0, s * kObjPerSolve, 0};
         b->solves_h.push_back(sd);
         b->maxN = std::max(b->maxN, n);
         off += n;
@@ -418,6 +707,11 @@ int qmin_batch_create(int nsolves, const int32_t *dims, int precision, int metri
     }
     b->N = (int)off;
     b->P = (off + 31) / 32 * 32;
+    for (int k = kShapes - 1; k >= 0; --k) {
+        chunk_layout(k, b->solves_h, nullptr);
+        b->max_chunks = std::max(b->max_chunks, b->solves_h.back().chunk0 + b->solves_h.back().nchunks);
+    }
+    chunk_layout(0, b->solves_h, &b->chunks_h);
     b->nchunks = (int)b->chunks_h.size();
     b->ntotal_h.assign(nsolves, 0);
     const size_t plane = (size_t)b->P * b->esz;
@@ -426,12 +720,12 @@ int qmin_batch_create(int nsolves, const int32_t *dims, int precision, int metri
               cudaMalloc(&b->F, 5 * plane) == cudaSuccess && cudaMalloc(&b->types, (size_t)b->P) == cudaSuccess &&
               cudaMalloc(&b->objs, sizeof(ObjDev<double>) * kObjPerSolve * nsolves) == cudaSuccess &&
               cudaMalloc(&b->solves, sizeof(SolveDesc) * nsolves) == cudaSuccess &&
-              cudaMalloc(&b->chunks, sizeof(ChunkDesc) * b->nchunks) == cudaSuccess &&
-              cudaMalloc(&b->partials, sizeof(double) * 3 * b->nchunks) == cudaSuccess &&
+              cudaMalloc(&b->chunks, sizeof(ChunkDesc) * b->max_chunks) == cudaSuccess &&
+              cudaMalloc(&b->partials, sizeof(double) * 3 * kBatchWarps * (size_t)b->max_chunks) == cudaSuccess &&
+              cudaMalloc(&b->run, sizeof(BatchRun)) == cudaSuccess &&
               cudaMalloc(&b->stage, sizeof(double) * 5 * (size_t)b->maxN) == cudaSuccess &&
               cudaMalloc(&b->stage_t, sizeof(int32_t) * (size_t)b->maxN) == cudaSuccess &&
               cudaMalloc(&b->fds, sizeof(FireDev) * nsolves) == cudaSuccess &&
-              cudaMalloc(&b->any, sizeof(int)) == cudaSuccess && cudaMallocHost(&b->any_h, sizeof(int)) == cudaSuccess &&
               cudaMalloc(&b->cls, (size_t)b->P) == cudaSuccess && cudaMalloc(&b->needd, (size_t)b->P) == cudaSuccess;
     if (!ok) {
         cudaGetLastError();
@@ -459,12 +753,10 @@ int qmin_batch_destroy(qmin_batch b)
 {
     if (!b) return bfail(QMIN_EINVAL, "qmin_batch_destroy: null handle");
     if (b->stream) cudaStreamSynchronize(b->stream);
-    if (b->graph) cudaGraphExecDestroy(b->graph);
-    void *bufs[] = {b->Q, b->V, b->F, b->D, b->objs, b->types, b->partials, b->stage, b->stage_t, b->fds, b->any,
-                    b->solves, b->chunks, b->cls, b->needd, b->cbd};
+    void *bufs[] = {b->Q, b->V, b->F, b->D, b->objs, b->types, b->partials, b->stage, b->stage_t, b->fds,
+                    b->solves, b->chunks, b->cls, b->needd, b->cbd, b->run};
     for (void *p : bufs)
         if (p) cudaFree(p);
-    if (b->any_h) cudaFreeHost(b->any_h);
     if (b->stream) cudaStreamDestroy(b->stream);
     delete b;
     return QMIN_OK;
@@ -504,11 +796,7 @@ int qmin_batch_set_params(qmin_batch b, const qmin_ldg_params *p)
         }
     }
     b->have_params = true;
-    if (b->graph) {
-        cudaGraphExecDestroy(b->graph);
-        b->graph = nullptr;
-    }
-    b->cap = -1;
+    b->shape = -1;  // the chunk shape is tuned afresh for the new force form
     return QMIN_OK;
 }
 
@@ -631,66 +919,25 @@ int qmin_batch_fire_init(qmin_batch b, const qmin_fire_params *p)
     return QMIN_OK;
 }
 
-template <class T> static int batch_fire_impl(qmin_batch_ctx *b, int max_iterations)
+template <class T> static int batch_fire_impl(qmin_batch_ctx *b, bool *timed_out)
 {
-    BatchArgs<T> B = batch_args<T>(b);
     // every solve's minimize() starts with its forces (energyMinimizerFIRE.cpp:157)
-    b->launches += launch_b_force<T>(B, b->fds, b->partials, 0, 0, b->stream);
-    if (b->cap < 0) {
-        // autotune the force + kick register cap on the live batch (velocities restored)
-        cudaEvent_t e0, e1;
-        BCK(cudaEventCreate(&e0));
-        BCK(cudaEventCreate(&e1));
-        void *vb = nullptr;
-        const size_t bytes = 5 * (size_t)b->P * b->esz;
-        if (cudaMalloc(&vb, bytes) != cudaSuccess) {
-            cudaGetLastError();
-            return bfail(QMIN_ENOMEM, "batch tuner: scratch allocation failed");
-        }
-        BCK(cudaMemcpyAsync(vb, b->V, bytes, cudaMemcpyDeviceToDevice, b->stream));
-        float best = 1e30f;
-        for (int cap = 0; cap < 3; ++cap) {
-            launch_b_force<T>(B, b->fds, b->partials, 1, cap, b->stream);
-            cudaEventRecord(e0, b->stream);
-            for (int r = 0; r < 3; ++r) launch_b_force<T>(B, b->fds, b->partials, 1, cap, b->stream);
-            cudaEventRecord(e1, b->stream);
-            cudaEventSynchronize(e1);
-            float ms = 0;
-            cudaEventElapsedTime(&ms, e0, e1);
-            if (ms < best) {
-                best = ms;
-                b->cap = cap;
-            }
-        }
-        BCK(cudaMemcpyAsync(b->V, vb, bytes, cudaMemcpyDeviceToDevice, b->stream));
-        BCK(cudaStreamSynchronize(b->stream));
-        cudaFree(vb);
-        cudaEventDestroy(e0);
-        cudaEventDestroy(e1);
-        b->launches += 12;
+    b->launches += launch_b_force<T>(batch_args<T>(b), b->fds, b->partials, 0, b->stream);
+    if (b->shape < 0) {
+        int r = b->pinned_shape >= 0 ? (b->shape = b->pinned_shape, set_layout(b, b->pinned_shape)) : tune_shape<T>(b);
+        if (r) return r;
     }
-    if (!b->graph || b->graph_cap != b->cap) {
-        if (b->graph) cudaGraphExecDestroy(b->graph);
-        b->graph = nullptr;
-        cudaGraph_t g = nullptr;
-        BCK(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
-        for (int k = 0; k < kBatchChunk; ++k) launch_b_iteration<T>(b, B, b->cap);
-        cudaError_t e = cudaStreamEndCapture(b->stream, &g);
-        if (e != cudaSuccess) return bfail(QMIN_ECUDA, std::string("batch graph capture: ") + cudaGetErrorString(e));
-        e = cudaGraphInstantiate(&b->graph, g, 0);
-        cudaGraphDestroy(g);
-        if (e != cudaSuccess) return bfail(QMIN_ECUDA, std::string("batch graph: ") + cudaGetErrorString(e));
-        b->graph_cap = b->cap;
-    }
-    const int per_iter = 3 + (B.L.multi ? 1 : 0);
-    const int max_chunks = max_iterations / kBatchChunk + 2;
-    for (int c = 0; c < max_chunks; ++c) {
-        BCK(cudaGraphLaunch(b->graph, b->stream));
-        b->launches += (long long)kBatchChunk * per_iter;
-        BCK(cudaMemcpyAsync(b->any_h, b->any, sizeof(int), cudaMemcpyDeviceToHost, b->stream));
-        BCK(cudaStreamSynchronize(b->stream));
-        if (!*b->any_h) break;
-    }
+    BatchRun run;
+    memset(&run, 0, sizeof run);
+    run.spin_limit = b->spin_limit;
+    BCK(cudaMemcpyAsync(b->run, &run, sizeof run, cudaMemcpyHostToDevice, b->stream));
+    const BatchArgs<T> B = batch_args<T>(b);
+    int r = B.L.multi ? launch_persistent<T, false>(b, B) : launch_persistent<T, true>(b, B);
+    if (r) return r;
+    b->launches += 1;
+    BCK(cudaMemcpyAsync(&run, b->run, sizeof run, cudaMemcpyDeviceToHost, b->stream));
+    BCK(cudaStreamSynchronize(b->stream));
+    *timed_out = run.abort != 0;
     k_b_finish<T><<<grid_for(b->nchunks), kBlock, 0, b->stream>>>(B, b->fds);
     k_b_clear_pending<<<(b->nsolves + 255) / 256, 256, 0, b->stream>>>(b->fds, b->nsolves);
     b->launches += 2;
@@ -713,10 +960,29 @@ int qmin_batch_fire_run(qmin_batch b, int max_iterations, int *iterations, doubl
         f.nTotal = b->ntotal_h[s];
     }
     BCK(cudaMemcpyAsync(b->fds, b->fds_h.data(), sizeof(FireDev) * b->nsolves, cudaMemcpyHostToDevice, b->stream));
-    int r = b->prec == QMIN_FP64 ? batch_fire_impl<double>(b, max_iterations) : batch_fire_impl<float>(b, max_iterations);
+    bool timed_out = false;
+    int r = b->prec == QMIN_FP64 ? batch_fire_impl<double>(b, &timed_out) : batch_fire_impl<float>(b, &timed_out);
     if (r) return r;
     BCK(cudaMemcpyAsync(b->fds_h.data(), b->fds, sizeof(FireDev) * b->nsolves, cudaMemcpyDeviceToHost, b->stream));
     BCK(cudaStreamSynchronize(b->stream));
+    if (timed_out) {
+        // every solve still active records the timeout in its status word and stops
+        for (int s = 0; s < b->nsolves; ++s) {
+            FireDev &f = b->fds_h[s];
+            if (f.active) {
+                f.status = QMIN_ETIMEOUT;
+                f.active = 0;
+            }
+            if (iterations) iterations[s] = f.iterations;
+            if (force_max) force_max[s] = f.forceMax;
+        }
+        BCK(cudaMemcpyAsync(b->fds, b->fds_h.data(), sizeof(FireDev) * b->nsolves, cudaMemcpyHostToDevice,
+                            b->stream));
+        BCK(cudaStreamSynchronize(b->stream));
+        return bfail(QMIN_ETIMEOUT, "qmin_batch_fire_run: a grid barrier of the persistent FIRE loop gave up "
+                                    "(solves still running are marked; their state is that of an unfinished "
+                                    "iteration: set them again before another run)");
+    }
     int conv = 0, bad = 0;
     for (int s = 0; s < b->nsolves; ++s) {
         const FireDev &f = b->fds_h[s];
@@ -727,6 +993,32 @@ int qmin_batch_fire_run(qmin_batch b, int max_iterations, int *iterations, doubl
     }
     if (converged) *converged = conv;
     if (bad) return bfail(QMIN_ENONFINITE, "qmin_batch_fire_run: a solve produced a non-finite force norm");
+    return QMIN_OK;
+}
+
+int qmin_batch_set_barrier_limit(qmin_batch b, long long spins)
+{
+    if (!b || spins < 0) return bfail(QMIN_EINVAL, "qmin_batch_set_barrier_limit: bad argument");
+    b->spin_limit = spins == 0 ? kDefaultSpinLimit : spins;
+    return QMIN_OK;
+}
+
+int qmin_batch_set_chunk_shape(qmin_batch b, int shape)
+{
+    if (!b || shape < -1 || shape >= kShapes) return bfail(QMIN_EINVAL, "qmin_batch_set_chunk_shape: bad argument");
+    b->pinned_shape = shape;
+    b->shape = -1;  // applied (or tuned) at the next run
+    return QMIN_OK;
+}
+
+int qmin_batch_tuning(qmin_batch b, int *shape, int tile[3], double ms[5])
+{
+    if (!b) return bfail(QMIN_EINVAL, "qmin_batch_tuning: null handle");
+    if (shape) *shape = b->shape;
+    if (tile)
+        for (int k = 0; k < 3; ++k) tile[k] = b->shape >= 0 ? kShape[b->shape][k] : 0;
+    if (ms)
+        for (int k = 0; k < kShapes; ++k) ms[k] = b->shape_ms[k];
     return QMIN_OK;
 }
 

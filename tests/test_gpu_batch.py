@@ -127,3 +127,78 @@ def test_batch_reproduces_reference_divergence(qmin, oracle):
     assert rc == qmin.QMIN_ENONFINITE
     assert not np.isfinite(fm[1]) and its[1] == first_bad
     assert np.isfinite(fm[0]) and np.isfinite(fm[2])
+
+
+@pytest.mark.parametrize("shape", [0, 1, 2, 3, 4])
+def test_batch_chunk_shapes_match_each_solve(qmin, oracle, shape):
+    """Every chunk shape of the persistent batch loop (256 consecutive sites;
+    tiles of 32x8x1, 16x16x1, 16x4x4, 8x8x4 sites cut where they overhang a
+    solve's box) follows each solve's oracle run to 1e-9, one-constant and
+    multi-constant (deep sites, walls, planar and homeotropic spheres)."""
+    for cfgs in (_cfgs(), [["L=12,11,10", "seed=5", "Ls=2.32,1.0,0.5,0,0", "wall=2,0,h,5.3", "wall=2,9,h,5.3",
+                            "sphere=6,5.5,4.5,2.6,h,5.3"],
+                           ["L=10,13,9", "seed=8", "Ls=2.32,1.0,0.5,0,0", "wall=0,0,p,1.0",
+                            "sphere=5.2,6.3,4.1,2.4,p,2.0"]]):
+        systems = [oracle_system(oracle, parse_args(c)) for c in cfgs]
+        b = _batch(qmin, systems)
+        b.set_chunk_shape(shape)
+        b.fire_init()
+        r = b.fire_run(20)
+        assert b.tuning()["shape"] == shape
+        for k, s in enumerate(systems):
+            ro = s.fire(20)
+            assert abs(r["forceMax"][k] - ro["forceMax"]) <= 1e-9 * ro["forceMax"]
+            assert rel_err(b.get_solve(k), s.Q) <= 1e-9
+        b.close()
+
+
+def test_batch_one_persistent_launch(qmin):
+    """A run of many uneven solves is a handful of launches (the entry forces,
+    the tuner's timings on the first run, one persistent launch, the final
+    velocity mix), not launches per iteration."""
+    import importlib
+    wl = importlib.import_module("qmin_gb300.workloads")
+    solves = [wl.c3_solve(s) for s in range(24)]
+    b = qmin.Batch([d["L"] for d in solves], qmin.FP32)
+    a, bb, c = solves[0]["consts"]
+    b.set_params(a, bb, c, 2.32)
+    for k, d in enumerate(solves):
+        b.set_solve(k, d["Q"], d["types"], d["objects"])
+    b.fire_init()
+    b.fire_run(5)  # tunes the chunk shape
+    t = b.tuning()
+    assert 0 <= t["shape"] < 5 and len(t["candidates_ms"]) == 5
+    l0 = b.launches()
+    r = b.fire_run(400)
+    assert (r["iterations"] >= 5).all() and r["iterations"].max() > 100
+    assert b.launches() - l0 <= 5
+    b.close()
+
+
+def test_batch_barrier_timeout_then_normal_run(qmin, oracle):
+    """With a grid barrier limit of one poll the persistent loop gives up at
+    its first barrier: the run returns QMIN_ETIMEOUT and marks the solves;
+    set again, the same batch with the default limit follows the oracle."""
+    import ctypes as C
+    systems = [oracle_system(oracle, parse_args(c)) for c in _cfgs()]
+    b = _batch(qmin, systems)
+    b.fire_init()
+    b.set_barrier_limit(1)
+    n = len(systems)
+    its = np.zeros(n, dtype=np.int32)
+    fm = np.zeros(n)
+    conv = C.c_int()
+    rc = qmin.lib().qmin_batch_fire_run(b._h, 30, qmin._ip(its), qmin._dp(fm), C.byref(conv))
+    assert rc == qmin.QMIN_ETIMEOUT
+    assert b"grid barrier" in qmin.lib().qmin_last_error_string()
+    b.set_barrier_limit(0)
+    for k, s in enumerate(systems):
+        b.set_solve(k, s.Q, s.types, [(s.objs[j].kind, s.objs[j].W, s.objs[j].S0) for j in range(s.nobj)])
+    b.fire_init()
+    r = b.fire_run(25)
+    for k, s in enumerate(systems):
+        ro = s.fire(25)
+        assert r["iterations"][k] == ro["iterations"] == 25
+        assert abs(r["forceMax"][k] - ro["forceMax"]) <= 1e-9 * ro["forceMax"]
+        assert rel_err(b.get_solve(k), s.Q) <= 1e-9
+    b.close()
