@@ -600,6 +600,112 @@ def run_warmnet(args):
     return out
 
 
+def run_kernels(args):
+    """One small call of every kernel family, for profilers (ncu -k regex:...):
+    on the c2 geometry at side^3 (--lattice), FP64 with the split force + kick
+    and FP32 with the fused split iteration (pinned, no tuning): FIRE iterations
+    launched one by one, the energy, Adam, Nesterov, L-BFGS, gradient descent,
+    defect measures, the allocation-free energy; a one-constant lattice with a
+    sphere through the separate kernels and the object forces; 64 batched c3
+    solves (persistent launch); the warm-start net's forward, backward and Adam
+    step at 64^3.  Prints the CUDA-event time of each call."""
+    import ctypes as C
+    import importlib
+    import torch
+    import __graft_entry__ as ge
+    q = ge.load_package()
+    wl = importlib.import_module("qmin_gb300.workloads")
+    consts, g = build_workload_host(q)
+    out = {"workload": f"kernel families, {WORKLOAD['L'][0]}^3 c2 geometry", "ms": {}}
+
+    def timed(name, fn):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record()
+        r = fn()
+        e1.record()
+        torch.cuda.synchronize()
+        out["ms"][name] = e0.elapsed_time(e1)
+        return r
+
+    fams = set(args.families.split(","))
+    for prec, tag, variant in ((q.FP64, "fp64", 1), (q.FP32, "fp32", 9)):
+        if tag not in fams:
+            continue
+        lat = make_lattice(q, consts, g, prec)
+        lat.set_fire_kernel(q.FIRE_SPLIT)
+        lat.set_fire_variant(variant)
+        timed(tag + " set_state", lambda: lat.set_state(g.Q, g.types))
+        lat.fire_init(dt=WORKLOAD["dt"])
+        timed(tag + " fire_run 3", lambda: lat.fire_run(3))
+        timed(tag + " fire_profile 2", lambda: lat.fire_profile(2))
+        timed(tag + " energy", lambda: lat.energy())
+        timed(tag + " adam 2", lambda: lat.adam_run(2))
+        timed(tag + " nesterov 2", lambda: lat.nesterov_run(2))
+        timed(tag + " lbfgs 2", lambda: lat.lbfgs_run(2))
+        timed(tag + " gd 2", lambda: lat.gd_run(2))
+        timed(tag + " defects", lambda: lat.defect_measures(0))
+        if prec == q.FP64:
+            n = g.Q.shape[0]
+            Qd = torch.from_numpy(np.ascontiguousarray(g.Q.T)).cuda()
+            td = torch.from_numpy(g.types.astype(np.int8)).cuda()
+            res = torch.zeros(6, dtype=torch.float64, device="cuda")
+            fn = q.lib().qmin_energy_noalloc
+            fn.argtypes = [C.c_void_p] * 3 + [C.c_int, C.c_void_p, C.c_longlong, C.c_void_p, C.c_void_p, C.c_void_p]
+            fn.restype = C.c_int
+            a, b, c, _S0 = consts
+            prm = q.LdgParams()
+            prm.A, prm.B, prm.C, prm.L1, prm.L2, prm.L3 = a, b, c, *WORKLOAD["Ls"]
+            prm.multi_constant = 1
+            objs = g.objects()
+            oa = (q.Object * len(objs))()
+            for k, (kind, W, S0) in enumerate(objs):
+                oa[k].kind, oa[k].W, oa[k].S0 = kind, W, S0
+            desc = q.LatticeDesc(*WORKLOAD["L"], q.FP64, 0)
+            if n <= 8388608:
+                timed("energy_noalloc", lambda: fn(C.byref(desc), C.byref(prm), oa, len(objs), Qd.data_ptr(), n,
+                                                   td.data_ptr(), res.data_ptr(), None))
+        lat.close()
+    s1 = wl.c3_solve(3, 64, 64)
+    a, b, c = s1["consts"]
+    if "onec" in fams:
+        # one-constant lattice with a sphere: separate kernels, object forces
+        lat = q.Lattice(s1["L"], q.FP32)
+        lat.set_params(a, b, c, 2.32)
+        lat.set_objects(s1["objects"])
+        lat.set_state(s1["Q"], s1["types"])
+        lat.set_fire_kernel(q.FIRE_SEPARATE)
+        lat.fire_init()
+        timed("one-constant fire_profile 2", lambda: lat.fire_profile(2))
+        timed("object forces", lambda: lat.object_forces())
+        lat.close()
+    if "batch" in fams:
+        # batched solves
+        solves = [wl.c3_solve(k) for k in range(64)]
+        bt = q.Batch([d["L"] for d in solves], q.FP32)
+        bt.set_params(a, b, c, 2.32)
+        for k, d in enumerate(solves):
+            bt.set_solve(k, d["Q"], d["types"], d["objects"])
+        bt.fire_init()
+        timed("batch fire_run 10", lambda: bt.fire_run(10))
+        bt.close()
+    if "net" not in fams:
+        return out
+    # warm-start net: forward, backward, Adam at 64^3
+    s4 = wl.c4_solve(7)
+    net = q.WarmNet(1, s4["L"], train=True)
+    net.set_params(q.warmnet_init_params(1))
+    qd = torch.from_numpy(np.ascontiguousarray(s4["Q"].T)).cuda()
+    tdv = torch.from_numpy(s4["types"].astype(np.int8)).cuda()
+    net.features(0, qd.data_ptr(), q.FP64, s4["Q"].shape[0], tdv.data_ptr(), s4["objects"])
+    tgt = torch.zeros((1, s4["Q"].shape[0], 5), dtype=torch.float32, device="cuda")
+    timed("net forward", lambda: (net.forward(), net.sync()))
+    timed("net backward", lambda: (net.backward(tgt.data_ptr()), net.sync()))
+    timed("net adam", lambda: (net.adam_step(1e-4), net.sync()))
+    net.close()
+    return out
+
+
 def run_c4(q, ntest=64):
     """The learned warm start on c4 test solves (64^3, seeds 100000..), judged by the protocol."""
     import importlib
@@ -815,9 +921,12 @@ def main():
     ap.add_argument("--no-configs", action="store_true", help="skip the c1 and c3 runs")
     ap.add_argument("--lattice", type=int, default=200, help="cube side (profiling of smaller cases)")
     ap.add_argument("--forms", default="both", choices=["both", "fp64", "fp32"])
-    ap.add_argument("--workload", default="c2", choices=["c2", "c3", "c5", "warmnet"],
+    ap.add_argument("--workload", default="c2", choices=["c2", "c3", "c5", "warmnet", "kernels"],
                     help="c3: the batched uneven solves alone; c5: the 400^3 multi-sphere E-field case; "
-                         "warmnet: the warm-start net's forward pass")
+                         "warmnet: the warm-start net's forward pass; kernels: one small call of every kernel family "
+                         "(for profilers)")
+    ap.add_argument("--families", default="fp64,fp32,onec,batch,net",
+                    help="kernels workload: comma-separated families (fp64, fp32, onec, batch, net)")
     ap.add_argument("--c3-solves", type=int, default=512, help="c3: number of solves (profiling of smaller cases)")
     ap.add_argument("--c3-max-iterations", type=int, default=30000)
     ap.add_argument("--c5-max-iterations", type=int, default=20000)
@@ -840,6 +949,10 @@ def main():
     if args.workload == "warmnet":
         if rank == 0:
             print(json.dumps(run_warmnet(args)))
+        return 0
+    if args.workload == "kernels":
+        if rank == 0:
+            print(json.dumps(run_kernels(args)))
         return 0
     if args.workload == "c3":
         if rank == 0:

@@ -757,7 +757,8 @@ template <class F> static int capture_chunk(qmin_ctx *h, int slot, const double 
     for (int k = 0; k < kChunk; ++k) per = one_iteration();
     cudaError_t e = cudaStreamEndCapture(h->stream, &g);
     if (e != cudaSuccess) return fail(QMIN_ECUDA, std::string("graph capture: ") + cudaGetErrorString(e));
-    e = cudaGraphInstantiate(&h->graph[slot], g, 0);
+    // per-node priorities: the side stream's list kernels carry the greatest one
+    e = cudaGraphInstantiate(&h->graph[slot], g, cudaGraphInstantiateFlagUseNodePriority);
     cudaGraphDestroy(g);
     if (e != cudaSuccess) return fail(QMIN_ECUDA, std::string("graph instantiate: ") + cudaGetErrorString(e));
     h->graph_per_iter[slot] = per;

@@ -150,9 +150,23 @@ __device__ __forceinline__ void sum_partials(const double *partials, int nparts,
 {
 #pragma unroll
     for (int k = 0; k < NV; ++k) v[k] = 0.0;
-    for (int b = threadIdx.x; b < nparts; b += kBlock)
+    // four strides' loads in flight before their adds; each thread still adds
+    // its entries b, b + kBlock, b + 2 kBlock, ... in that order
+    constexpr int U = 4;
+    for (int b0 = threadIdx.x; b0 < nparts; b0 += U * kBlock) {
+        double x[U][NV];
 #pragma unroll
-        for (int k = 0; k < NV; ++k) v[k] += partials[NV * b + k];
+        for (int u = 0; u < U; ++u) {
+            const int b = b0 + u * kBlock;
+#pragma unroll
+            for (int k = 0; k < NV; ++k) x[u][k] = b < nparts ? partials[NV * b + k] : 0.0;
+        }
+#pragma unroll
+        for (int u = 0; u < U; ++u)
+            if (b0 + u * kBlock < nparts)
+#pragma unroll
+                for (int k = 0; k < NV; ++k) v[k] += x[u][k];
+    }
     block_sum<NV>(v);
 }
 

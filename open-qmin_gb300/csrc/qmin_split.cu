@@ -46,6 +46,36 @@ __device__ __forceinline__ void kick_and_sum(const Lat<T> &L, long long i, T hdt
 
 int list_grid(int n) { return std::max(1, std::min((n + kBlock - 1) / kBlock, 152 * 4)); }
 
+// the device's greatest stream priority (the lowest number)
+int high_priority()
+{
+    static int prio = [] {
+        int least = 0, greatest = 0;
+        cudaDeviceGetStreamPriorityRange(&least, &greatest);
+        return greatest;
+    }();
+    return prio;
+}
+
+// A list kernel launched with the greatest priority as a launch attribute: the
+// block scheduler then places its blocks ahead of the deep-site kernel's pending
+// blocks, so that the two overlap.  Graphs keep the attribute on the kernel
+// node (they are instantiated to honour per-node priorities).
+template <class... P, class... A>
+void launch_high(void (*kern)(P...), int grid, cudaStream_t s, A &&...args)
+{
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(grid);
+    cfg.blockDim = dim3(kBlock);
+    cfg.stream = s;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributePriority;
+    at[0].val.priority = high_priority();
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    cudaLaunchKernelEx(&cfg, kern, std::forward<A>(args)...);
+}
+
 }  // namespace
 
 // every deep bulk site (cls == 0); partials[0 .. gridDim.x).  KICK = false:
@@ -1195,7 +1225,7 @@ template <class T> struct PredAcc {
 // the listed LC sites' force at the predicted Q and kick, from the input buffer
 // set into the output set's V and F (their predicted Q: the fused deep kernel)
 template <class T>
-__global__ void __launch_bounds__(kBlock)
+__global__ void __launch_bounds__(kBlock, sizeof(T) == 4 ? 2 : 1)
     k_force_kick_list_pred(Lat<T> L, T *__restrict__ Vo, T *__restrict__ Fo, const int *__restrict__ list, int n,
                            const FireDev *__restrict__ fd, double *partials)
 {
@@ -1395,12 +1425,14 @@ int launch_split_fused_list(const Lat<T> &Lin, T *Vo, T *Fo, const SplitLists &s
     int n = 0;
     *nblocks = 0;
     if (sl.n_derivs > 0) {
-        k_derivs_list_pred<T><<<list_grid(sl.n_derivs), kBlock, 0, s>>>(Lin, sl.derivs, sl.n_derivs, fd);
+        launch_high(k_derivs_list_pred<T>, list_grid(sl.n_derivs), s, Lin, (const int *)sl.derivs, sl.n_derivs,
+                    (const FireDev *)fd);
         ++n;
     }
     if (sl.n_sites > 0) {
         const int g = list_grid(sl.n_sites);
-        k_force_kick_list_pred<T><<<g, kBlock, 0, s>>>(Lin, Vo, Fo, sl.sites, sl.n_sites, fd, partials);
+        launch_high(k_force_kick_list_pred<T>, g, s, Lin, Vo, Fo, (const int *)sl.sites, sl.n_sites, (const FireDev *)fd,
+                    partials);
         *nblocks = g;
         ++n;
     }
@@ -1410,7 +1442,7 @@ int launch_split_fused_list(const Lat<T> &Lin, T *Vo, T *Fo, const SplitLists &s
 template <class T> int launch_split_derivs(const Lat<T> &L, const SplitLists &sl, FireDev *fd, cudaStream_t s)
 {
     if (sl.n_derivs == 0) return 0;
-    k_derivs_list<T><<<list_grid(sl.n_derivs), kBlock, 0, s>>>(L, sl.derivs, sl.n_derivs, fd);
+    launch_high(k_derivs_list<T>, list_grid(sl.n_derivs), s, L, (const int *)sl.derivs, sl.n_derivs, (const FireDev *)fd);
     return 1;
 }
 
@@ -1438,7 +1470,7 @@ int launch_split_list(const Lat<T> &L, const SplitLists &sl, FireDev *fd, double
 {
     if (sl.n_sites <= 0) return 0;
     const int g = list_grid(sl.n_sites);
-    k_force_kick_list<T><<<g, kBlock, 0, s>>>(L, sl.sites, sl.n_sites, fd, partials);
+    launch_high(k_force_kick_list<T>, g, s, L, (const int *)sl.sites, sl.n_sites, (const FireDev *)fd, partials);
     return g;
 }
 
