@@ -327,7 +327,10 @@ int qmin_energy_noalloc(const qmin_lattice_desc *desc, const qmin_ldg_params *p,
  * each solve follows energyMinimizerFIRE::minimize on its own lattice (its own
  * FIRE scalars, stopping rule and iteration count), converged solves retire.
  * qmin_batch_fire_run runs all iterations of all solves in one persistent
- * cooperative launch (grid barriers between the phases of an iteration).  All
+ * cooperative launch (grid barriers between the phases of an iteration; FP32
+ * one-constant batches run the predictor, force and kick as one phase over two
+ * state sets, and the device memory for the second set is allocated on their
+ * first run).  All
  * solves share the force parameters; each has up to 16 objects.  No reference
  * counterpart for the batching itself (the reference minimises one lattice per
  * process). */

@@ -6,7 +6,9 @@
 // tuner picks the shape by timing the force + kick).  qmin_batch_fire_run runs
 // every iteration of every solve in one persistent cooperative launch: per
 // iteration the predictor, the force + half kick + per-chunk FIRE sums and the
-// per-solve FIRE control, separated by bounded grid barriers.  Per-solve FIRE
+// per-solve FIRE control, separated by bounded grid barriers (FP32
+// one-constant batches: predictor, force and kick as one phase from one state
+// set into the other, then the control).  Per-solve FIRE
 // scalars live on the device; a solve that converged or ran out of iterations
 // retires, and the phases then cover only the chunks of the solves still
 // active.
@@ -22,14 +24,28 @@
 
 namespace qmin {
 
-struct SolveDesc {
+struct __align__(16) SolveDesc {
     int Lx, Ly, Lz;
     int off;      // first packed site of this solve
     int chunk0;   // first chunk of this solve
     int nchunks;  // chunks of this solve
     int obj_base; // first object-table entry of this solve
     int pad;
+    unsigned mx, my;  // division multipliers for Lx and Ly (div_magic)
+    int pad2[2];
 };
+
+// multiplier m = ceil(2^32 / d) for udiv (d >= 2; 0 marks d = 1)
+inline unsigned div_magic(unsigned d) { return d < 2 ? 0u : (unsigned)(((1ull << 32) + d - 1) / d); }
+
+// n / d for n < 2^31: the multiply-high estimate is floor(n / d) or one more
+// (m d - 2^32 < d, so the excess n (m d - 2^32) / (d 2^32) stays below 1)
+__device__ __forceinline__ unsigned udiv(unsigned n, unsigned d, unsigned m)
+{
+    if (m == 0) return n;
+    const unsigned q = __umulhi(n, m);
+    return q * d > n ? q - 1 : q;
+}
 
 struct ChunkDesc {
     int solve;
@@ -59,13 +75,16 @@ __device__ __forceinline__ bool chunk_site(const BatchArgs<T> &B, const SolveDes
     if (B.tx == 0) {
         li = ch.start + t;
         if (li >= sd.Lx * sd.Ly * sd.Lz) return false;
-        x = li % sd.Lx;
-        const int r = li / sd.Lx;
-        y = r % sd.Ly;
-        z = r / sd.Ly;
+        const int r = (int)udiv((unsigned)li, (unsigned)sd.Lx, sd.mx);
+        x = li - r * sd.Lx;
+        z = (int)udiv((unsigned)r, (unsigned)sd.Ly, sd.my);
+        y = r - z * sd.Ly;
         return true;
     }
-    const int x0 = ch.start % sd.Lx, r = ch.start / sd.Lx, y0 = r % sd.Ly, z0 = r / sd.Ly;
+    const int r = (int)udiv((unsigned)ch.start, (unsigned)sd.Lx, sd.mx);
+    const int x0 = ch.start - r * sd.Lx;
+    const int z0 = (int)udiv((unsigned)r, (unsigned)sd.Ly, sd.my);
+    const int y0 = r - z0 * sd.Ly;
     x = x0 + (t & (B.tx - 1));
     y = y0 + ((t >> B.lx) & (B.ty - 1));
     z = z0 + (t >> B.lxy);
@@ -113,6 +132,45 @@ template <class T> struct BatchAcc {
 };
 
 constexpr int kBatchWarps = kBlock / 32;  // warp partial sums per chunk
+
+// one set of packed state planes (Q, V, F)
+template <class T> struct BatchSet {
+    T *Q, *V, *F;
+};
+
+// accessor over the predicted Q of a packed solve, formed on the fly from an
+// input state set (one-constant forms: no derivative planes)
+template <class T> struct BatchPredAcc {
+    const T *Q, *V, *F;
+    const int8_t *types;
+    const ObjDev<T> *objs;
+    long long P;
+    int i;
+    int nb[6];
+    PredCoef<T> c;
+    __device__ __forceinline__ BatchPredAcc(const Lat<T> &L, const BatchSet<T> &in, const PredCoef<T> &c_,
+                                            const SolveDesc &sd, int li, int x, int y, int z)
+        : Q(in.Q), V(in.V), F(in.F), types(L.types), objs(L.objs + sd.obj_base), P(L.P), i(sd.off + li), c(c_)
+    {
+        const int sx = sd.Lx, sy = sd.Lx * sd.Ly;
+        nb[0] = i + (x == 0 ? sd.Lx - 1 : -1);
+        nb[1] = i + (x == sd.Lx - 1 ? -(sd.Lx - 1) : 1);
+        nb[2] = i + (y == 0 ? (sd.Ly - 1) * sx : -sx);
+        nb[3] = i + (y == sd.Ly - 1 ? -(sd.Ly - 1) * sx : sx);
+        nb[4] = i + (z == 0 ? (sd.Lz - 1) * sy : -sy);
+        nb[5] = i + (z == sd.Lz - 1 ? -(sd.Lz - 1) * sy : sy);
+    }
+    __device__ __forceinline__ T at(int j, int k) const
+    {
+        const long long o = (long long)k * P + j;
+        return pred_q(c, ld(Q + o), pred_v(c, ld(V + o), ld(F + o)));
+    }
+    __device__ __forceinline__ int tn(int s) const { return types[nb[s]]; }
+    __device__ __forceinline__ T q(int k) const { return at(i, k); }
+    __device__ __forceinline__ T nq(int s, int k) const { return at(nb[s], k); }
+    __device__ __forceinline__ T dn(int, int) const { return T(0); }  // multi-constant forms only
+    __device__ __forceinline__ ObjDev<T> obj(int t) const { return objs[t - 1]; }
+};
 
 // ----------------------------------------------------- per-chunk phases
 // The deferred mix folded into the Verlet coefficients, as k_fire_pred does:
@@ -230,6 +288,69 @@ __device__ __forceinline__ void b_force_chunk(const BatchArgs<T> &B, const FireD
     }
 }
 
+// One fused FIRE iteration of chunk c (one-constant forms): the predicted Q of
+// the site and of its six neighbours formed on the fly from the input set, the
+// force there, the half kick, the output set written (Q', V', F) and each
+// warp's FIRE sums, as b_force_chunk lays them out
+template <class T>
+__device__ __forceinline__ void b_fused_chunk(const BatchArgs<T> &B, const BatchSet<T> &in, const BatchSet<T> &out,
+                                              const FireDev *fds, double *partials, int c)
+{
+    const ChunkDesc ch = B.chunks[c];
+    // coefficients formed in FP64 by one lane per warp
+    double cf[4] = {0.0, 0.0, 0.0, 0.0};
+    if ((threadIdx.x & 31) == 0) {
+        const FireDev &fd = fds[ch.solve];
+        const double dt = fd.dt, hdt = 0.5 * dt;
+        double mv = 1.0, mf = 0.0;
+        if (fd.pending) {
+            mv = fd.reset ? 0.0 : 1.0 - fd.mixA;
+            mf = fd.reset ? 0.0 : fd.mixA * fd.mixS;
+        }
+        cf[0] = mv;
+        cf[1] = mf + hdt;
+        cf[2] = dt;
+        cf[3] = dt;
+    }
+#pragma unroll
+    for (int k = 0; k < 4; ++k) cf[k] = __shfl_sync(0xffffffffu, cf[k], 0);
+    const PredCoef<T> pc{T(cf[0]), T(cf[1]), T(cf[2])};
+    const T hdt = T(0.5) * T(cf[3]);
+    const SolveDesc sd = B.solves[ch.solve];
+    int li, x, y, z;
+    const bool inb = chunk_site(B, sd, ch, threadIdx.x, li, x, y, z);
+    T acc[3] = {T(0), T(0), T(0)};
+    if (inb) {
+        const int gi = sd.off + li;
+        const BatchPredAcc<T> a(B.L, in, pc, sd, li, x, y, z);
+        T f[5], v[5];
+        site_force_core<T, BatchPredAcc<T>, false, false, true>(B.L, a, B.L.types[gi], f);
+        const long long P = B.L.P;
+#pragma unroll
+        for (int k = 0; k < 5; ++k) {
+            const long long o = k * P + gi;
+            const T vp = pred_v(pc, ld(in.V + o), ld(in.F + o));
+            out.Q[o] = pred_q(pc, ld(in.Q + o), vp);
+            v[k] = vp + hdt * f[k];
+            out.V[o] = v[k];
+            out.F[o] = f[k];
+        }
+        acc[0] = dot_qt(f, f);
+        acc[1] = dot_qt(v, v);
+        acc[2] = dot_qt(f, v);
+    }
+#pragma unroll
+    for (int k = 0; k < 3; ++k)
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) acc[k] += __shfl_xor_sync(0xffffffffu, acc[k], o);
+    if ((threadIdx.x & 31) == 0) {
+        double *p = partials + 3 * ((long long)kBatchWarps * c + threadIdx.x / 32);
+        p[0] = (double)acc[0];
+        p[1] = (double)acc[1];
+        p[2] = (double)acc[2];
+    }
+}
+
 // one warp, solve w: deterministic sum of its chunks' partials, then the
 // fireStepCPU scalar logic (energyMinimizerFIRE.cpp:104-144) and the loop
 // condition of minimize(); returns (in lane 0) whether the solve retired now
@@ -240,9 +361,22 @@ __device__ __forceinline__ bool b_control_solve(FireDev *fds, const SolveDesc *s
     if (!fd->active) return false;  // uniform per warp
     const SolveDesc sd = solves[w];
     double v[3] = {0.0, 0.0, 0.0};
-    for (int c = lane; c < kBatchWarps * sd.nchunks; c += 32)
+    // eight strides' loads in flight; each lane adds its entries in index order
+    constexpr int U = 8;
+    const int n = kBatchWarps * sd.nchunks;
+    const double *p = partials + 3LL * kBatchWarps * sd.chunk0;
+    for (int c0 = lane; c0 < n; c0 += 32 * U) {
+        double x[U][3];
 #pragma unroll
-        for (int k = 0; k < 3; ++k) v[k] += partials[3 * ((long long)kBatchWarps * sd.chunk0 + c) + k];
+        for (int u = 0; u < U; ++u)
+#pragma unroll
+            for (int k = 0; k < 3; ++k) x[u][k] = c0 + 32 * u < n ? p[3 * (c0 + 32 * u) + k] : 0.0;
+#pragma unroll
+        for (int u = 0; u < U; ++u)
+            if (c0 + 32 * u < n)
+#pragma unroll
+                for (int k = 0; k < 3; ++k) v[k] += x[u][k];
+    }
 #pragma unroll
     for (int k = 0; k < 3; ++k)
 #pragma unroll
@@ -319,6 +453,27 @@ __global__ void k_b_clear_pending(FireDev *fds, int n)
     if (s < n) fds[s].pending = 0;
 }
 
+// after a fused run: the solves whose last iteration wrote the second state
+// set get their Q, V, F copied back into the first
+template <class T>
+__global__ void __launch_bounds__(kBlock) k_b_settle(BatchArgs<T> B, BatchSet<T> s1, const int *in_second)
+{
+    for (int c = blockIdx.x; c < B.nchunks; c += gridDim.x) {
+        const ChunkDesc ch = B.chunks[c];
+        if (!in_second[ch.solve]) continue;
+        const SolveDesc sd = B.solves[ch.solve];
+        int li;
+        if (!chunk_site(B, sd, ch, threadIdx.x, li)) continue;
+#pragma unroll
+        for (int k = 0; k < 5; ++k) {
+            const long long j = (long long)k * B.L.P + sd.off + li;
+            B.L.Q[j] = s1.Q[j];
+            B.L.V[j] = s1.V[j];
+            B.L.F[j] = s1.F[j];
+        }
+    }
+}
+
 // ---------------------------------------------------- persistent FIRE loop
 // Run state of one persistent launch: grid barrier (arrival count, generation,
 // abort flag, spin limit) and, per iteration, the number of solves that retired.
@@ -376,14 +531,24 @@ constexpr int kMaxBatchSolves = 16384;  // the lists take 8 (nsolves + 1) bytes 
 
 // (the one-constant forms ask for three blocks per SM, the FP32 multi-constant
 // form for two: the force phase would otherwise hold the registers of fewer)
-template <class T, bool ONE_CONST>
+//
+// FUSED (FP32 one-constant forms; in FP64 the neighbours' predictions formed
+// again at every site cost more FP64 FMAs than the separate predictor phase
+// saves): one phase per iteration instead of predictor and force: iteration it reads state set it & 1 (0: B.L's planes, 1: s1) and
+// writes the other, forming the predicted Q of every neighbour on the fly
+// (b_fused_chunk); a solve that retires leaves in_second[solve] = 1 when its
+// final state is in s1 (k_b_settle copies it back)
+template <class T, bool ONE_CONST, bool FUSED = false>
 __global__ void __launch_bounds__(kBlock, ONE_CONST ? 3 : (sizeof(T) == 4 ? 2 : 1))
-    k_b_fire_persistent(BatchArgs<T> B, FireDev *fds, double *partials, int nsolves, BatchRun *run)
+    k_b_fire_persistent(BatchArgs<T> B, BatchSet<T> s1, FireDev *fds, double *partials, int *in_second,
+                        int nsolves, BatchRun *run)
 {
+    static_assert(!FUSED || (ONE_CONST && sizeof(T) == 4), "the fused iteration covers the FP32 one-constant forms");
     extern __shared__ int b_lists[];
     int *act = b_lists;                // active solve ids, in solve order
     int *pre = b_lists + nsolves + 1;  // prefix sums of their chunk counts
     __shared__ int n_act;
+    __shared__ int all_act;  // every solve active: work item w is chunk w
     auto rebuild = [&]() {
         // one warp: ballot over the solves in order
         if (threadIdx.x < 32) {
@@ -409,6 +574,7 @@ __global__ void __launch_bounds__(kBlock, ONE_CONST ? 3 : (sizeof(T) == 4 ? 2 : 
             }
             if (threadIdx.x == 0) {
                 n_act = n;
+                all_act = n == nsolves;
                 pre[n] = tot;
             }
         }
@@ -416,6 +582,7 @@ __global__ void __launch_bounds__(kBlock, ONE_CONST ? 3 : (sizeof(T) == 4 ? 2 : 
     };
     // chunk of work item w: binary search in the prefix sums
     auto chunk_of = [&](int w) {
+        if (all_act) return w;
         int lo = 0, hi = n_act - 1;
         while (lo < hi) {
             const int mid = (lo + hi + 1) >> 1;
@@ -427,21 +594,31 @@ __global__ void __launch_bounds__(kBlock, ONE_CONST ? 3 : (sizeof(T) == 4 ? 2 : 
     rebuild();
     const int nwarps = gridDim.x * (kBlock / 32);
     const int gwarp = blockIdx.x * (kBlock / 32) + threadIdx.x / 32;
+    const BatchSet<T> s0{B.L.Q, B.L.V, B.L.F};
     for (int it = 0; n_act > 0; ++it) {
         if (blockIdx.x == 0 && threadIdx.x == 0) run->retired[it % 3] = 0;
         const int nw = pre[n_act];
-        for (int w = blockIdx.x; w < nw; w += gridDim.x) b_pred_chunk<T>(B, fds, chunk_of(w));
-        if (!b_grid_sync(run)) return;
-        if (!ONE_CONST && B.L.multi) {
-            for (int w = blockIdx.x; w < nw; w += gridDim.x) b_derivs_chunk<T>(B, fds, chunk_of(w));
+        if constexpr (FUSED) {
+            const BatchSet<T> in = (it & 1) ? s1 : s0, out = (it & 1) ? s0 : s1;
+            for (int w = blockIdx.x; w < nw; w += gridDim.x) b_fused_chunk<T>(B, in, out, fds, partials, chunk_of(w));
+            if (!b_grid_sync(run)) return;
+        } else {
+            for (int w = blockIdx.x; w < nw; w += gridDim.x) b_pred_chunk<T>(B, fds, chunk_of(w));
+            if (!b_grid_sync(run)) return;
+            if (!ONE_CONST && B.L.multi) {
+                for (int w = blockIdx.x; w < nw; w += gridDim.x) b_derivs_chunk<T>(B, fds, chunk_of(w));
+                if (!b_grid_sync(run)) return;
+            }
+            for (int w = blockIdx.x; w < nw; w += gridDim.x)
+                b_force_chunk<T, 1, ONE_CONST>(B, fds, partials, chunk_of(w));
             if (!b_grid_sync(run)) return;
         }
-        for (int w = blockIdx.x; w < nw; w += gridDim.x) b_force_chunk<T, 1, ONE_CONST>(B, fds, partials, chunk_of(w));
-        if (!b_grid_sync(run)) return;
         // per-solve control, one warp per active solve (its warps' sums added in order)
         for (int k = gwarp; k < n_act; k += nwarps)
-            if (b_control_solve(fds, B.solves, act[k], partials) && (threadIdx.x & 31) == 0)
+            if (b_control_solve(fds, B.solves, act[k], partials) && (threadIdx.x & 31) == 0) {
                 atomicAdd(&run->retired[it % 3], 1);
+                if (FUSED) in_second[act[k]] = (it & 1) == 0;
+            }
         if (!b_grid_sync(run)) return;
         if (*(volatile int *)&run->retired[it % 3] > 0) rebuild();
     }
@@ -486,6 +663,8 @@ struct qmin_batch_ctx {
     SolveDesc *solves = nullptr;
     ChunkDesc *chunks = nullptr;
     void *Q = nullptr, *V = nullptr, *F = nullptr, *D = nullptr, *objs = nullptr;
+    void *Q2 = nullptr, *V2 = nullptr, *F2 = nullptr;  // second state set of the fused iteration
+    int *in_second = nullptr;                          // per solve: final state in the second set
     int8_t *types = nullptr;
     uint8_t *cls = nullptr, *needd = nullptr;  // per packed site (multi-constant split of the force)
     void *cbd = nullptr;                       // merged boundary coefficients (multi-constant)
@@ -645,10 +824,11 @@ template <class T> static int tune_shape(qmin_batch_ctx *b)
 
 // the persistent FIRE loop as one cooperative launch of as many blocks as can
 // be resident together
-template <class T, bool ONE_CONST> static int launch_persistent(qmin_batch_ctx *b, const BatchArgs<T> &B)
+template <class T, bool ONE_CONST, bool FUSED>
+static int launch_persistent(qmin_batch_ctx *b, const BatchArgs<T> &B)
 {
     const size_t smem = sizeof(int) * 2 * ((size_t)b->nsolves + 1);
-    auto kern = k_b_fire_persistent<T, ONE_CONST>;
+    auto kern = k_b_fire_persistent<T, ONE_CONST, FUSED>;
     if (smem > 48 * 1024 &&
         cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
         return bfail(QMIN_ECUDA, "batch: shared memory for the active-solve lists");
@@ -659,11 +839,13 @@ template <class T, bool ONE_CONST> static int launch_persistent(qmin_batch_ctx *
     if (per_sm < 1) return bfail(QMIN_ECUDA, "batch: the persistent kernel does not fit on an SM");
     const int grid = per_sm * nsm;
     BatchArgs<T> a = B;
+    BatchSet<T> s1{(T *)b->Q2, (T *)b->V2, (T *)b->F2};
     FireDev *fds = b->fds;
     double *partials = b->partials;
+    int *in_second = b->in_second;
     int ns = b->nsolves;
     BatchRun *run = b->run;
-    void *args[] = {&a, &fds, &partials, &ns, &run};
+    void *args[] = {&a, &s1, &fds, &partials, &in_second, &ns, &run};
     BCK(cudaLaunchCooperativeKernel((const void *)kern, dim3(grid), dim3(kBlock), args, smem, b->stream));
     return QMIN_OK;
 }
@@ -696,7 +878,7 @@ int qmin_batch_create(int nsolves, const int32_t *dims, int precision, int metri
             return bfail(QMIN_EINVAL, "qmin_batch_create: every lattice side must be >= 3");
         }
         const int n = Lx * Ly * Lz;
-        SolveDesc sd{Lx, Ly, Lz, (int)off, 0, 0, s * kObjPerSolve, 0};
+        SolveDesc sd{Lx, Ly, Lz, (int)off, 0, 0, s * kObjPerSolve, 0, div_magic(Lx), div_magic(Ly), {0, 0}};
         b->solves_h.push_back(sd);
         b->maxN = std::max(b->maxN, n);
         off += n;
@@ -754,7 +936,7 @@ int qmin_batch_destroy(qmin_batch b)
     if (!b) return bfail(QMIN_EINVAL, "qmin_batch_destroy: null handle");
     if (b->stream) cudaStreamSynchronize(b->stream);
     void *bufs[] = {b->Q, b->V, b->F, b->D, b->objs, b->types, b->partials, b->stage, b->stage_t, b->fds,
-                    b->solves, b->chunks, b->cls, b->needd, b->cbd, b->run};
+                    b->solves, b->chunks, b->cls, b->needd, b->cbd, b->run, b->Q2, b->V2, b->F2, b->in_second};
     for (void *p : bufs)
         if (p) cudaFree(p);
     if (b->stream) cudaStreamDestroy(b->stream);
@@ -932,12 +1114,33 @@ template <class T> static int batch_fire_impl(qmin_batch_ctx *b, bool *timed_out
     run.spin_limit = b->spin_limit;
     BCK(cudaMemcpyAsync(b->run, &run, sizeof run, cudaMemcpyHostToDevice, b->stream));
     const BatchArgs<T> B = batch_args<T>(b);
-    int r = B.L.multi ? launch_persistent<T, false>(b, B) : launch_persistent<T, true>(b, B);
+    const bool fused = !B.L.multi && sizeof(T) == 4;
+    if (fused && !b->Q2) {
+        // the second state set, on the first one-constant run
+        const size_t bytes = 5 * (size_t)b->P * b->esz;
+        if (cudaMalloc(&b->Q2, bytes) != cudaSuccess || cudaMalloc(&b->V2, bytes) != cudaSuccess ||
+            cudaMalloc(&b->F2, bytes) != cudaSuccess ||
+            cudaMalloc(&b->in_second, sizeof(int) * (size_t)b->nsolves) != cudaSuccess) {
+            cudaGetLastError();
+            return bfail(QMIN_ENOMEM, "qmin_batch_fire_run: second state set allocation failed");
+        }
+    }
+    if (fused) BCK(cudaMemsetAsync(b->in_second, 0, sizeof(int) * (size_t)b->nsolves, b->stream));
+    int r;
+    if constexpr (sizeof(T) == 4)
+        r = B.L.multi ? launch_persistent<T, false, false>(b, B) : launch_persistent<T, true, true>(b, B);
+    else
+        r = B.L.multi ? launch_persistent<T, false, false>(b, B) : launch_persistent<T, true, false>(b, B);
     if (r) return r;
     b->launches += 1;
     BCK(cudaMemcpyAsync(&run, b->run, sizeof run, cudaMemcpyDeviceToHost, b->stream));
     BCK(cudaStreamSynchronize(b->stream));
     *timed_out = run.abort != 0;
+    if (fused) {
+        k_b_settle<T><<<grid_for(b->nchunks), kBlock, 0, b->stream>>>(B, BatchSet<T>{(T *)b->Q2, (T *)b->V2,
+                                                                                     (T *)b->F2}, b->in_second);
+        b->launches += 1;
+    }
     k_b_finish<T><<<grid_for(b->nchunks), kBlock, 0, b->stream>>>(B, b->fds);
     k_b_clear_pending<<<(b->nsolves + 255) / 256, 256, 0, b->stream>>>(b->fds, b->nsolves);
     b->launches += 2;

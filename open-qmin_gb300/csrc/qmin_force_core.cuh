@@ -170,6 +170,37 @@ __device__ __forceinline__ void sum_partials(const double *partials, int nparts,
     block_sum<NV>(v);
 }
 
+// ---------------------------------------------------- FIRE predictor
+// Coefficients of the velocity-Verlet predictor with the deferred velocity mix
+// folded in (energyMinimizerFIRE.cpp:104-144 mixes v after the control step;
+// the mix is applied here, at the next predictor): v' = cvv v + cvf f,
+// q' = q + dt v'.  Kernels that form the predicted Q of a neighbour on the fly
+// use pred_v / pred_q, explicit FMAs, so that every kernel gets the same bits.
+template <class T> struct PredCoef {
+    T cvv, cvf, tdt;
+};
+
+// the predictor's coefficients (as k_fire_pred: ve = mv v + mf f folded into the
+// Verlet step, v' = cvv v + cvf f, q' = q + dt v')
+template <class T> __device__ __forceinline__ PredCoef<T> pred_coef(const FireDev *fd)
+{
+    const double dt = fd->dt, hdt = 0.5 * dt;
+    double mv = 1.0, mf = 0.0;
+    if (fd->pending) {
+        mv = fd->reset ? 0.0 : 1.0 - fd->mixA;
+        mf = fd->reset ? 0.0 : fd->mixA * fd->mixS;
+    }
+    return PredCoef<T>{T(mv), T(mf + hdt), T(dt)};
+}
+
+// predicted velocity and Q of one component: explicit FMAs, so that every
+// kernel that recomputes a site's prediction gets the same bits
+template <class T> __device__ __forceinline__ T pred_v(const PredCoef<T> &c, T v, T f)
+{
+    return fma(c.cvf, f, c.cvv * v);
+}
+template <class T> __device__ __forceinline__ T pred_q(const PredCoef<T> &c, T q, T vn) { return fma(c.tdt, vn, q); }
+
 // first derivative of one component along one axis at a site of type t with
 // down/centre/up values and the down/up neighbour types
 // (landauDeGennesLCOtherForces.cpp:50-141): central differences; at type < 0

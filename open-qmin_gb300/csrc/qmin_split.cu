@@ -777,31 +777,6 @@ __global__ void __launch_bounds__(TX / 2 * TY, MINB)
 // one buffer set (L.Q, L.V, L.F), output the other (Qo, Vo, Fo): predicted Q
 // of every site of the tile, V and F of the deep sites (object sites:
 // V = F = 0; listed sites: k_force_kick_list_pred).
-template <class T> struct PredCoef {
-    T cvv, cvf, tdt;
-};
-
-// the predictor's coefficients (as k_fire_pred: ve = mv v + mf f folded into the
-// Verlet step, v' = cvv v + cvf f, q' = q + dt v')
-template <class T> __device__ __forceinline__ PredCoef<T> pred_coef(const FireDev *fd)
-{
-    const double dt = fd->dt, hdt = 0.5 * dt;
-    double mv = 1.0, mf = 0.0;
-    if (fd->pending) {
-        mv = fd->reset ? 0.0 : 1.0 - fd->mixA;
-        mf = fd->reset ? 0.0 : fd->mixA * fd->mixS;
-    }
-    return PredCoef<T>{T(mv), T(mf + hdt), T(dt)};
-}
-
-// predicted velocity and Q of one component: explicit FMAs, so that every
-// kernel that recomputes a site's prediction gets the same bits
-template <class T> __device__ __forceinline__ T pred_v(const PredCoef<T> &c, T v, T f)
-{
-    return fma(c.cvf, f, c.cvv * v);
-}
-template <class T> __device__ __forceinline__ T pred_q(const PredCoef<T> &c, T q, T vn) { return fma(c.tdt, vn, q); }
-
 template <int TX, int TY> __host__ __device__ constexpr int fused_halo_count() { return 2 * (TX + 2) + 2 * TY; }
 
 // position of halo entry h (< fused_halo_count) in the (TX + 2) x (TY + 2) staged plane

@@ -1,6 +1,8 @@
 """Batched minimisation of uneven independent lattices against the oracle,
 solve by solve.  Tolerances: FIRE trajectories 1e-9 relative (FP64),
-FP32 batch within 1e-4 of the FP64 batch in forceMax."""
+FP32 batch within 1e-4 of the FP64 batch in forceMax, and (the fused FP32
+one-constant iteration) within 1e-4 of the oracle's forceMax and 2e-5 of its
+Q."""
 import numpy as np
 import pytest
 
@@ -80,6 +82,44 @@ def test_batch_fp32_tracks_fp64(qmin, oracle):
         b.fire_init()
         res.append(b.fire_run(40)["forceMax"])
     np.testing.assert_allclose(res[1], res[0], rtol=1e-4)
+
+
+def test_batch_fp32_fused_retires_on_either_set(qmin, oracle):
+    """The FP32 one-constant batch runs predictor, force and kick as one phase
+    over two state sets: solves that stop after an odd and after an even
+    number of iterations each come back (copied into the first set where their
+    last iteration wrote the second) at their own oracle iteration, Q within
+    FP32 accuracy of the FP64 oracle."""
+    systems = [oracle_system(oracle, parse_args(c)) for c in _cfgs()]
+    fcut = 0.05
+    b = _batch(qmin, systems, qmin.FP32)
+    b.fire_init(force_cutoff=fcut)
+    r = b.fire_run(400)
+    parities = set()
+    for k, s in enumerate(systems):
+        ro = s.fire(400, fcut=fcut)
+        assert r["iterations"][k] == ro["iterations"], k
+        parities.add(ro["iterations"] % 2)
+        assert abs(r["forceMax"][k] - ro["forceMax"]) <= 1e-4 * ro["forceMax"], k
+        assert rel_err(b.get_solve(k), s.Q) <= 2e-5, k
+    assert parities == {0, 1}, "the cases should stop after odd and after even iteration counts"
+    b.close()
+
+
+def test_batch_fp32_fused_resumes(qmin, oracle):
+    """Two FP32 runs of 7 and 6 iterations (the first ends in the second state
+    set) follow one oracle run of 13."""
+    systems = [oracle_system(oracle, parse_args(c)) for c in _cfgs()]
+    b = _batch(qmin, systems, qmin.FP32)
+    b.fire_init()
+    b.fire_run(7)
+    r = b.fire_run(13)
+    for k, s in enumerate(systems):
+        ro = s.fire(13)
+        assert r["iterations"][k] == 13
+        assert abs(r["forceMax"][k] - ro["forceMax"]) <= 1e-4 * ro["forceMax"], k
+        assert rel_err(b.get_solve(k), s.Q) <= 2e-5, k
+    b.close()
 
 
 def test_c3_generator_and_batch_smoke(qmin):
