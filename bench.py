@@ -635,16 +635,11 @@ def run_kernels(args):
         lat = make_lattice(q, consts, g, prec)
         lat.set_fire_kernel(q.FIRE_SPLIT)
         lat.set_fire_variant(variant)
+        # single launches first, then the iterative runs (graphs of 16 iterations)
         timed(tag + " set_state", lambda: lat.set_state(g.Q, g.types))
-        lat.fire_init(dt=WORKLOAD["dt"])
-        timed(tag + " fire_run 3", lambda: lat.fire_run(3))
-        timed(tag + " fire_profile 2", lambda: lat.fire_profile(2))
         timed(tag + " energy", lambda: lat.energy())
-        timed(tag + " adam 2", lambda: lat.adam_run(2))
-        timed(tag + " nesterov 2", lambda: lat.nesterov_run(2))
-        timed(tag + " lbfgs 2", lambda: lat.lbfgs_run(2))
-        timed(tag + " gd 2", lambda: lat.gd_run(2))
         timed(tag + " defects", lambda: lat.defect_measures(0))
+        timed(tag + " gd 2", lambda: lat.gd_run(2))
         if prec == q.FP64:
             n = g.Q.shape[0]
             Qd = torch.from_numpy(np.ascontiguousarray(g.Q.T)).cuda()
@@ -665,6 +660,12 @@ def run_kernels(args):
             if n <= 8388608:
                 timed("energy_noalloc", lambda: fn(C.byref(desc), C.byref(prm), oa, len(objs), Qd.data_ptr(), n,
                                                    td.data_ptr(), res.data_ptr(), None))
+        lat.fire_init(dt=WORKLOAD["dt"])
+        timed(tag + " fire_run 3", lambda: lat.fire_run(3))
+        timed(tag + " fire_profile 2", lambda: lat.fire_profile(2))
+        timed(tag + " adam 2", lambda: lat.adam_run(2))
+        timed(tag + " nesterov 2", lambda: lat.nesterov_run(2))
+        timed(tag + " lbfgs 2", lambda: lat.lbfgs_run(2))
         lat.close()
     s1 = wl.c3_solve(3, 64, 64)
     a, b, c = s1["consts"]
