@@ -179,6 +179,7 @@ def make_lattice(q, consts, g, precision):
 DRAM_BYTES_PER_LAUNCH = {
     ("force_kick_split", "f64"): 1715513856.0,   # 214.4 B/site (161 algorithmic)
     ("force_kick_split", "f32"): 648814080.0,    # 81.1 B/site (81 algorithmic)
+    ("fire_fused_split", "f32"): 939452544.0,    # 117.4 B/site (121 algorithmic)
     ("force_kick_reduce", "f64"): 2872800000.0,  # 359.1 B/site
     ("force_kick_tiled", "f32"): 1082400000.0,   # 135.3 B/site
     ("force_kick_reduce", "f32"): 1124800000.0,  # 140.6 B/site
@@ -575,7 +576,7 @@ def run_warmnet(args):
         flops += 2 * rows * cout * taps * cin
     out = {"metric": "warm-start net forward", "unit": "TFLOP/s", "sites": L[0] * L[1] * L[2],
            "conv_gflop_per_forward": flops / 1e9, "config": {"workload": f"{L[0]}^3 c2 geometry, batch 1"}}
-    for tc in (True, False):
+    for tc, name in ((1, "tcgen05"), (2, "tcgen05_thread_staged"), (0, "mma_sync")):
         net = q.WarmNet(1, L)
         net.set_params(params)
         net.set_tensor_path(tc)
@@ -593,7 +594,7 @@ def run_warmnet(args):
         e1.record(st)
         net.sync()
         ms = e0.elapsed_time(e1) / args.steps
-        out["tcgen05" if tc else "mma_sync"] = {"ms_per_forward": ms, "tflops": flops / (ms / 1e3) / 1e12}
+        out[name] = {"ms_per_forward": ms, "tflops": flops / (ms / 1e3) / 1e12}
         net.close()
     out["value"] = out["tcgen05"]["tflops"]
     lat.close()

@@ -408,9 +408,12 @@ int qmin_warmnet_write_state(qmin_warmnet n, int sample, void *Q_dev, int precis
                              const int8_t *types_dev);
 int qmin_warmnet_sync(qmin_warmnet n);
 /* Tensor-core instruction family of the convolutions: 1 (default) the
- * 5th-generation tcgen05.mma with tensor-memory accumulators, 0 the mma.sync
- * kernels.  Both compute BF16 x BF16 -> FP32.  No reference counterpart. */
-int qmin_warmnet_set_tensor_path(qmin_warmnet n, int tcgen05);
+ * 5th-generation tcgen05.mma with tensor-memory accumulators, the direct 3^3
+ * kernel's halo planes staged by TMA (cp.async.bulk.tensor) where the grid
+ * holds a 10 x 18 box; 2 the same with the halo planes staged by the threads;
+ * 0 the mma.sync kernels.  All compute BF16 x BF16 -> FP32; paths 1 and 2 give
+ * identical bits.  QMIN_EINVAL for another value.  No reference counterpart. */
+int qmin_warmnet_set_tensor_path(qmin_warmnet n, int path);
 int qmin_warmnet_kernel_launches(qmin_warmnet n, long long *count);
 /* Warm-start a lattice in place: features from its current Q, types and
  * objects, one forward pass, the prediction written into its Q on the sites

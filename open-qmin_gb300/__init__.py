@@ -590,9 +590,12 @@ class WarmNet:
         except Exception:
             pass
 
-    def set_tensor_path(self, tcgen05=True):
-        """Convolutions on tcgen05.mma with tensor-memory accumulators (default) or on mma.sync."""
-        _check(lib().qmin_warmnet_set_tensor_path(self._h, 1 if tcgen05 else 0))
+    def set_tensor_path(self, path=1):
+        """Convolutions on tcgen05.mma with tensor-memory accumulators: 1 (or True,
+        the default) with the direct kernel's halo planes staged by TMA, 2 with
+        them staged by the threads; 0 (or False) on mma.sync."""
+        path = 1 if path is True else (0 if path is False else int(path))
+        _check(lib().qmin_warmnet_set_tensor_path(self._h, path))
 
     def set_stream(self, stream_ptr):
         _check(lib().qmin_warmnet_set_stream(self._h, C.c_void_p(stream_ptr)))

@@ -23,6 +23,7 @@
 // nearest upsampling).
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
+#include <cudaTypedefs.h>
 
 #include <algorithm>
 #include <cmath>
@@ -548,6 +549,218 @@ __global__ void __launch_bounds__(128) k_conv3_direct_z(Geo g, const bf16 *__res
         asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "r"(COLS) : "memory");
 }
 
+// The same column walk with each halo plane staged by the tensor-memory-access
+// unit: one cp.async.bulk.tensor.5d box of 8 channels x 10 x 18 voxels x 1
+// plane per 8-channel group (the box's channel coordinate is a multiple of 8
+// BF16 elements, 16 bytes; the spatial coordinates start one voxel before the
+// tile and may be negative or past the volume, where the box reads zeros,
+// which is the convolution's zero padding in x, y and z).  A group's box lands
+// as [18][10][8 channels], the canonical K-major core-matrix layout the
+// descriptors read, in a slab padded to 2944 bytes so that every box starts on
+// a 128-byte boundary; the leading byte offset of the A descriptor is that
+// slab pitch.  One thread issues the boxes against one mbarrier per ring slot
+// (the expected bytes count the whole box, zero fill included), waits for
+// plane z + 1 before it issues the MMAs of plane z, and reloads a slot only
+// after the MMAs that read it have committed.  All waits are bounded; a wait
+// that gives up leaves the copies and MMAs in flight to land (bounded again)
+// before the CTA frees its tensor memory and reports through g_conv_err.
+constexpr int kTmaSlab = 2944;  // 2880 bytes of box, padded to a multiple of 128
+static size_t direct_z_tma_smem(int cin, int n)
+{
+    const size_t need = (size_t)27 * n * cin * 2 + (size_t)4 * (cin / 8) * kTmaSlab + 128 + 128;
+    const int per_sm = 512 / umma_cols(2 * n);
+    const size_t floor_bytes = (size_t)(232448 / per_sm) - 1024 + 1;
+    return std::max(need, std::min<size_t>(floor_bytes, 232448 - 1024));
+}
+
+namespace {
+__device__ __forceinline__ void tma_box_5d(unsigned dst, const CUtensorMap *map, int c, int x, int y, int z, int b,
+                                           unsigned bar)
+{
+    asm volatile(
+        "cp.async.bulk.tensor.5d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4, %5, "
+        "%6}], [%7];\n" ::"r"(dst),
+        "l"(map), "r"(c), "r"(x), "r"(y), "r"(z), "r"(b), "r"(bar)
+        : "memory");
+}
+}  // namespace
+
+template <int N>
+__global__ void __launch_bounds__(128) k_conv3_direct_z_tma(Geo g, const __grid_constant__ CUtensorMap tmap,
+                                                            const bf16 *__restrict__ w,
+                                                            const float *__restrict__ bias, bf16 *__restrict__ out,
+                                                            int relu, int zt)
+{
+    static_assert(N % 16 == 0 && N >= 16 && 2 * N <= 256, "two M=128 accumulators of N columns");
+    constexpr int COLS = 2 * N <= 32 ? 32 : (2 * N <= 64 ? 64 : (2 * N <= 128 ? 128 : 256));
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    const int cin = g.cin, kc8 = cin >> 3, K = 27 * cin;
+    const int W = g.Wo, H = g.Ho, D = g.Do;
+    const size_t w_bytes = (size_t)27 * N * cin * 2;  // a multiple of 128 (27 * 2 * 16 * 16 divides it)
+    const unsigned slot_bytes = (unsigned)kc8 * kTmaSlab;
+    // the boxes start on 128-byte boundaries: the dynamic area rounded up (128 bytes spare are allocated)
+    unsigned char *base = smem_raw + ((128u - (s_addr(smem_raw) & 127u)) & 127u);
+    unsigned char *wts = base;
+    unsigned char *ring = base + w_bytes;
+    uint64_t *bar = reinterpret_cast<uint64_t *>(ring + 4 * (size_t)slot_bytes);  // [0..1] MMAs, [2..5] ring slots
+    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(bar + 6);
+    const int tid = threadIdx.x, warp = tid >> 5;
+    const int tx = (W + 7) >> 3, ty = (H + 15) >> 4, tz = (D + zt - 1) / zt;
+    int bidx = blockIdx.x;
+    const int x0 = (bidx % tx) * 8;
+    bidx /= tx;
+    const int y0 = (bidx % ty) * 16;
+    bidx /= ty;
+    const int z0 = (bidx % tz) * zt, b = bidx / tz;
+    const int nz = min(zt, D - z0);
+    if (*(volatile int *)&g_conv_err) return;
+
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(s_addr(tmem_slot)),
+                     "r"(COLS)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n" ::: "memory");
+    }
+    if (tid == 0) {
+        for (int k = 0; k < 6; ++k)
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(s_addr(&bar[k])) : "memory");
+        asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+    }
+    auto slot_of = [&](int iz) { return (iz - z0 + 1) & 3; };            // iz >= z0 - 1
+    auto use_of = [&](int iz) { return (unsigned)((iz - z0 + 1) >> 2); };  // how many loads the slot had before
+    // plane iz's boxes into its ring slot (one thread)
+    auto load_plane = [&](int iz) {
+        const int sl = slot_of(iz);
+        const unsigned bs = s_addr(&bar[2 + sl]);
+        asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(bs), "r"(kc8 * 2880u)
+                     : "memory");
+        const unsigned dst = s_addr(ring) + (unsigned)sl * slot_bytes;
+        for (int k8 = 0; k8 < kc8; ++k8) tma_box_5d(dst + (unsigned)k8 * kTmaSlab, &tmap, k8 * 8, x0 - 1, y0 - 1, iz, b, bs);
+    };
+    auto wait_plane = [&](int iz) { return mbar_wait_bounded(s_addr(&bar[2 + slot_of(iz)]), use_of(iz) & 1u); };
+    int issued_hi = z0 - 2;  // the last plane whose boxes were issued
+    __syncthreads();         // the barriers are initialised
+    if (tid == 0) {
+        for (int iz = z0 - 1; iz <= z0 + 1; ++iz) load_plane(iz);
+        issued_hi = z0 + 1;
+    }
+    // all 27 taps' weights, [tap][co][cin] with each tap's [co][cin] in the canonical layout
+    for (int e = tid; e < 27 * N * kc8; e += 128) {
+        const int tap = e / (N * kc8), rem = e - tap * N * kc8, co = rem / kc8, k8 = rem - co * kc8;
+        const uint4 v = *reinterpret_cast<const uint4 *>(w + (size_t)co * K + (size_t)tap * cin + k8 * 8);
+        *reinterpret_cast<uint4 *>(wts + (size_t)tap * N * cin * 2 + ((size_t)(co >> 3) * kc8 + k8) * 128 +
+                                   (co & 7) * 16) = v;
+    }
+    auto issue = [&](int z, int acc_idx) {
+        asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+        const unsigned sw = s_addr(wts), sbo_b = (unsigned)kc8 * 128u;
+        const uint32_t dst = *tmem_slot + (uint32_t)(acc_idx * N);
+        for (int tap = 0; tap < 27; ++tap) {
+            const int dz = tap / 9, dy = (tap / 3) % 3, dx = tap % 3;
+            const unsigned sa = s_addr(ring) + (unsigned)slot_of(z - 1 + dz) * slot_bytes;
+            for (int kk = 0; kk < (cin >> 4); ++kk) {
+                const unsigned a0 = sa + (unsigned)(2 * kk) * kTmaSlab + (unsigned)(dy * 10 + dx) * 16u;
+                const unsigned b0 = sw + (unsigned)tap * (unsigned)(N * cin * 2) + (unsigned)kk * 256u;
+                const uint64_t da = umma_desc(a0, kTmaSlab, 160), db = umma_desc(b0, 128, sbo_b);
+                const unsigned acc = (tap > 0 || kk > 0) ? 1u : 0u;
+                asm volatile(
+                    "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+                    " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(dst),
+                    "l"(da), "l"(db), "r"(umma_idesc(N)), "r"(acc)
+                    : "memory");
+            }
+        }
+        asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(
+                         s_addr(&bar[acc_idx]))
+                     : "memory");
+    };
+    auto epilogue = [&](int z, int acc_idx, uint32_t tmem) {
+        asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+        const uint32_t taddr = tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(acc_idx * N);
+        const int ox = x0 + (tid & 7), oy = y0 + (tid >> 3);
+        const bool inside = ox < W && oy < H;
+        bf16 *o = out + ((((size_t)b * D + z) * H + oy) * W + ox) * N;
+#pragma unroll
+        for (int c0 = 0; c0 < N; c0 += 8) {
+            uint32_t r[8];
+            asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];\n"
+                         : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+                           "=r"(r[7])
+                         : "r"(taddr + c0));
+            asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
+            if (inside) {
+                __nv_bfloat162 hh[4];
+#pragma unroll
+                for (int e = 0; e < 4; ++e) {
+                    float v0 = __uint_as_float(r[2 * e]) + bias[c0 + 2 * e];
+                    float v1 = __uint_as_float(r[2 * e + 1]) + bias[c0 + 2 * e + 1];
+                    if (relu) {
+                        v0 = fmaxf(v0, 0.f);
+                        v1 = fmaxf(v1, 0.f);
+                    }
+                    hh[e] = __floats2bfloat162_rn(v0, v1);
+                }
+                *reinterpret_cast<uint4 *>(o + c0) = *reinterpret_cast<const uint4 *>(hh);
+            }
+        }
+    };
+    // the weights (generic-proxy stores) become visible to the MMAs (async proxy)
+    asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+    asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+    const uint32_t tmem = *tmem_slot;
+    bool ok = true;
+    int committed = 0;  // planes whose MMAs were committed
+    for (int p = 0; p < nz; ++p) {
+        const int z = z0 + p;
+        bool good = true;
+        if (tid == 0) {
+            // planes z - 1 and z were waited for by earlier steps (all three at the first)
+            if (p == 0) good = wait_plane(z - 1) && wait_plane(z);
+            good = good && wait_plane(z + 1);
+            if (good) issue(z, p & 1);
+        }
+        if (__syncthreads_or(!good)) {
+            ok = false;
+            break;
+        }
+        committed = p + 1;
+        if (p >= 1) {
+            // the MMAs of plane p - 1: done with their accumulator and with slot z - 2
+            const bool w_ok = mbar_wait_bounded(s_addr(&bar[(p - 1) & 1]), (unsigned)((p - 1) >> 1) & 1u);
+            if (__syncthreads_or(!w_ok)) {
+                ok = false;
+                break;
+            }
+            epilogue(z - 1, (p - 1) & 1, tmem);
+        }
+        if (tid == 0 && p + 1 < nz) {
+            load_plane(z + 2);
+            issued_hi = z + 2;
+        }
+        asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+        __syncthreads();
+    }
+    if (ok) {
+        const int last = nz - 1;
+        const bool w_ok = mbar_wait_bounded(s_addr(&bar[last & 1]), (unsigned)(last >> 1) & 1u);
+        ok = !__syncthreads_or(!w_ok);
+        if (ok) epilogue(z0 + last, last & 1, tmem);
+    }
+    if (!ok && tid == 0) {
+        // a wait gave up: let the boxes and the MMAs in flight land (bounded) before the buffers go away
+        for (int iz = max(z0 - 1, issued_hi - 3); iz <= issued_hi; ++iz) wait_plane(iz);
+        for (int q = max(0, committed - 2); q < committed; ++q)
+            mbar_wait_bounded(s_addr(&bar[q & 1]), (unsigned)(q >> 1) & 1u);
+        atomicExch(&g_conv_err, 1);
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+    __syncthreads();
+    if (warp == 0)
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "r"(COLS) : "memory");
+}
+
 // dW[co][tap][ci] += sum_v dout[v][co] * in[src(v,tap)][ci] over rows
 // [blockIdx.x * chunk, +chunk): block tile 64 co x 64 ci for one tap, the
 // row dimension staged through shared memory 16 rows at a time; each block
@@ -853,23 +1066,83 @@ static void conv3_direct_z(const Geo &g, const bf16 *in, const bf16 *w, const fl
     k_conv3_direct_z<N><<<(unsigned)tiles, 128, sm, s>>>(g, in, w, bias, out, relu, zt);
 }
 
-// tcgen05: the 5th-generation tensor-core kernels above (the direct kernel for
-// 3x3x3 stride-1 forward convolutions with BF16 output, the gathering kernel
-// otherwise); else mma.sync
+// the driver's tensor-map encoder (fetched at run time: no link-time dependency), or null
+static PFN_cuTensorMapEncodeTiled_v12000 tmap_encoder()
+{
+    static PFN_cuTensorMapEncodeTiled_v12000 fn = [] {
+        void *f = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &f, 12000, cudaEnableDefault, &q) !=
+                cudaSuccess ||
+            q != cudaDriverEntryPointSuccess) {
+            cudaGetLastError();
+            f = nullptr;
+        }
+        return reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(f);
+    }();
+    return fn;
+}
+
+// the TMA-staged direct kernel; false (nothing launched) where its tensor map
+// cannot describe the input: no encoder, an input not 16-byte aligned, or a
+// grid smaller than one halo box (10 x 18)
+template <int N>
+static bool conv3_direct_z_tma(const Geo &g, const bf16 *in, const bf16 *w, const float *bias, bf16 *out, int relu,
+                               cudaStream_t s)
+{
+    auto enc = tmap_encoder();
+    if (!enc || (reinterpret_cast<uintptr_t>(in) & 15) || g.Wi < 10 || g.Hi < 18 || g.cin % 16 != 0) return false;
+    CUtensorMap map;
+    const cuuint64_t es = 2;  // BF16
+    const cuuint64_t dims[5] = {(cuuint64_t)g.cin, (cuuint64_t)g.Wi, (cuuint64_t)g.Hi, (cuuint64_t)g.Di,
+                                (cuuint64_t)g.nb};
+    const cuuint64_t strides[4] = {(cuuint64_t)g.cin * es, (cuuint64_t)g.Wi * g.cin * es,
+                                   (cuuint64_t)g.Hi * g.Wi * g.cin * es, (cuuint64_t)g.Di * g.Hi * g.Wi * g.cin * es};
+    const cuuint32_t box[5] = {8, 10, 18, 1, 1};
+    const cuuint32_t estr[5] = {1, 1, 1, 1, 1};
+    if (enc(&map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 5, const_cast<bf16 *>(in), dims, strides, box, estr,
+            CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+            CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+        return false;
+    static int attr_bytes = 0;
+    const size_t sm = direct_z_tma_smem(g.cin, N);
+    if ((int)sm > attr_bytes) {
+        // a failure here surfaces as the launch's error
+        if (cudaFuncSetAttribute(k_conv3_direct_z_tma<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm) ==
+            cudaSuccess)
+            attr_bytes = (int)sm;
+    }
+    const int zt = std::min(g.Do, 16);
+    const long long tiles = (long long)((g.Wo + 7) / 8) * ((g.Ho + 15) / 16) * ((g.Do + zt - 1) / zt) * g.nb;
+    k_conv3_direct_z_tma<N><<<(unsigned)tiles, 128, sm, s>>>(g, map, w, bias, out, relu, zt);
+    return true;
+}
+
+// path 1 or 2: the 5th-generation tensor-core kernels above (the direct kernel
+// for 3x3x3 stride-1 forward convolutions with BF16 output, its halo planes
+// staged by TMA on path 1 where the tensor map applies, by the threads on path
+// 2; the gathering kernel otherwise); path 0: mma.sync
 template <bool OB>
 static void conv_gemm(const Geo &g, const bf16 *in, const bf16 *w, const float *bias, const float *addend, void *out,
-                      int relu, int rows, cudaStream_t s, bool tcgen05)
+                      int relu, int rows, cudaStream_t s, int path)
 {
+    const bool tcgen05 = path != 0;
     // the direct kernel wins where a dz plane's weights are small (measured at
     // 128^3: 16->32 0.29 ms vs 0.49 gathering, 32->32 0.77 vs 0.95; at 48->48
     // and 64->64 the 135-216 KB of staging leave one CTA per SM and it loses)
     if (tcgen05 && OB && g.mode == 0 && g.taps == 27 && g.stride == 1 && !addend && bias &&
         direct_z_smem(g.cin, g.cout) <= 232448 - 1024) {
         if (g.cout == 32) {
+            if (path == 1 && direct_z_tma_smem(g.cin, 32) <= 232448 - 1024 &&
+                conv3_direct_z_tma<32>(g, in, w, bias, reinterpret_cast<bf16 *>(out), relu, s))
+                return;
             conv3_direct_z<32>(g, in, w, bias, reinterpret_cast<bf16 *>(out), relu, s);
             return;
         }
         if (g.cout == 48) {
+            if (path == 1 && direct_z_tma_smem(g.cin, 48) <= 232448 - 1024 &&
+                conv3_direct_z_tma<48>(g, in, w, bias, reinterpret_cast<bf16 *>(out), relu, s))
+                return;
             conv3_direct_z<48>(g, in, w, bias, reinterpret_cast<bf16 *>(out), relu, s);
             return;
         }
@@ -928,7 +1201,7 @@ struct qmin_warmnet_ctx {
     bool own_stream = false;
     long long adam_t = 0;
     long long launches = 0;
-    bool tcgen05 = true;  // convolutions on tcgen05 (else mma.sync)
+    int path = 1;  // convolutions: 1 tcgen05 (TMA-staged direct kernel), 2 tcgen05 (thread-staged), 0 mma.sync
 };
 
 namespace {
@@ -1009,10 +1282,10 @@ void run_layer(qmin_warmnet_ctx *n, int i, const bf16 *in, float *f32out)
     const Geo g = fwd_geo(n, L);
     const int rows = (int)rows_at(n, out_level(L));
     if (f32out)
-        conv_gemm<false>(g, in, n->pb + L.woff, n->p + L.boff, nullptr, f32out, L.relu, rows, n->stream, n->tcgen05);
+        conv_gemm<false>(g, in, n->pb + L.woff, n->p + L.boff, nullptr, f32out, L.relu, rows, n->stream, n->path);
     else
         conv_gemm<true>(g, in, n->pb + L.woff, n->p + L.boff, nullptr, n->act[i], L.relu, rows, n->stream,
-                        n->tcgen05);
+                        n->path);
 }
 
 // backward of layer i: gout is the FP32 gradient w.r.t. the layer's output
@@ -1056,7 +1329,7 @@ void layer_backward(qmin_warmnet_ctx *n, int i, const float *gout, const bf16 *a
     const int flip = (L.stride == 1 && L.taps == 27) ? 1 : 0;
     k_dgrad_weights<<<grid1((long long)L.cout * L.cin * L.taps), 256, 0, s>>>(n->pb + L.woff, n->wd, L.cout, L.cin,
                                                                               L.taps, flip);
-    conv_gemm<false>(d, n->gbf, n->wd, nullptr, addend, gin, 0, (int)rows_in, s, n->tcgen05);
+    conv_gemm<false>(d, n->gbf, n->wd, nullptr, addend, gin, 0, (int)rows_in, s, n->path);
     n->launches += 2;
 }
 
@@ -1352,10 +1625,11 @@ int qmin_warmnet_sync(qmin_warmnet n)
     return QMIN_OK;
 }
 
-int qmin_warmnet_set_tensor_path(qmin_warmnet n, int tcgen05)
+int qmin_warmnet_set_tensor_path(qmin_warmnet n, int path)
 {
     if (!n) return nfail(QMIN_EINVAL, "qmin_warmnet_set_tensor_path: null handle");
-    n->tcgen05 = tcgen05 != 0;
+    if (path < 0 || path > 2) return nfail(QMIN_EINVAL, "qmin_warmnet_set_tensor_path: path must be 0, 1 or 2");
+    n->path = path;
     return QMIN_OK;
 }
 

@@ -132,6 +132,42 @@ def test_tcgen05_matches_mma_sync(qmin, L):
     assert np.linalg.norm(g1 - g0) <= 2e-2 * np.linalg.norm(g0)
 
 
+@pytest.mark.parametrize("L", [(40, 48, 24), (56, 40, 16)])
+def test_tma_staging_matches_thread_staging(qmin, L):
+    """The direct 3^3 kernel with its halo planes staged by TMA (tensor path
+    1, the default) against the same kernel staged by the threads (path 2):
+    the MMAs read the same operands in the same order, so the outputs, the loss
+    and the gradients are identical bit for bit.  Two samples (the tensor
+    map's sample coordinate), tiles that overhang the grid in x and y (56 x 40:
+    16-row tiles over 40 rows, 8-wide tiles over 28 columns at level 1), and
+    the zero padding read past every face."""
+    sols = []
+    for seed in (81, 82):
+        s = _lattice(qmin, seed, max(L))
+        side = max(L)
+        idx = np.arange(side ** 3).reshape(side, side, side)[:L[2], :L[1], :L[0]].ravel()
+        sols.append(dict(s, L=L, Q=np.ascontiguousarray(s["Q"][idx]), types=np.ascontiguousarray(s["types"][idx])))
+    rng = np.random.default_rng(11)
+    n = L[0] * L[1] * L[2]
+    tgt = torch.as_tensor((0.3 * rng.standard_normal((2, n, 5))).astype(np.float32)).cuda()
+    outs = []
+    for path in (2, 1):
+        net, _keep = _net_with_inputs(qmin, sols, train=True)
+        net.set_tensor_path(path)
+        net.forward()
+        torch.cuda.synchronize()
+        loss = net.backward(tgt.data_ptr())
+        net.sync()
+        _x, y, _m = net.torch_views()
+        outs.append((y.float().cpu().numpy(), loss, net.get_params(grads=True)[1]))
+        net.close()
+    (y0, l0, g0), (y1, l1, g1) = outs
+    assert np.isfinite(y1).all()
+    assert np.array_equal(y0, y1)
+    assert l0 == l1
+    assert np.array_equal(g0, g1)
+
+
 def test_backward_matches_torch_fp64(qmin):
     L = (16, 16, 16)
     sols = [_lattice(qmin, s, 16) for s in (31, 32)]
