@@ -136,8 +136,9 @@ def test_tcgen05_matches_mma_sync(qmin, L):
 def test_tma_staging_matches_thread_staging(qmin, L):
     """The direct 3^3 kernel with its halo planes staged by TMA (tensor path
     1, the default) against the same kernel staged by the threads (path 2):
-    the MMAs read the same operands in the same order, so the outputs, the loss
-    and the gradients are identical bit for bit.  Two samples (the tensor
+    the MMAs read the same operands in the same order, so the outputs are
+    identical bit for bit (the loss and the gradients to their atomic
+    summation order).  Two samples (the tensor
     map's sample coordinate), tiles that overhang the grid in x and y (56 x 40:
     16-row tiles over 40 rows, 8-wide tiles over 28 columns at level 1), and
     the zero padding read past every face."""
@@ -164,8 +165,9 @@ def test_tma_staging_matches_thread_staging(qmin, L):
     (y0, l0, g0), (y1, l1, g1) = outs
     assert np.isfinite(y1).all()
     assert np.array_equal(y0, y1)
-    assert l0 == l1
-    assert np.array_equal(g0, g1)
+    # the loss and the weight gradients are summed with atomics (their order varies run to run)
+    assert abs(l1 - l0) <= 1e-12 * abs(l0)
+    assert np.linalg.norm(g1 - g0) <= 1e-5 * np.linalg.norm(g0)
 
 
 def test_backward_matches_torch_fp64(qmin):
