@@ -691,6 +691,17 @@ def run_kernels(args):
         bt.fire_init()
         timed("batch fire_run 10", lambda: bt.fire_run(10))
         bt.close()
+    if "batchmc" in fams:
+        # batched multi-constant solves: 16 c4 solves (64^3, walls + sphere, L1-L3), FP32
+        c4s = [wl.c4_solve(100000 + k) for k in range(16)]
+        bt = q.Batch([d["L"] for d in c4s], q.FP32)
+        a4, b4, cc4 = c4s[0]["consts"]
+        bt.set_params(a4, b4, cc4, *c4s[0]["Ls"])
+        for k, d in enumerate(c4s):
+            bt.set_solve(k, d["Q"], d["types"], d["objects"])
+        bt.fire_init()
+        timed("batch multi-constant fire_run 10", lambda: bt.fire_run(10))
+        bt.close()
     if "net" not in fams:
         return out
     # warm-start net: forward, backward, Adam at 64^3
@@ -927,8 +938,8 @@ def main():
                     help="c3: the batched uneven solves alone; c5: the 400^3 multi-sphere E-field case; "
                          "warmnet: the warm-start net's forward pass; kernels: one small call of every kernel family "
                          "(for profilers)")
-    ap.add_argument("--families", default="fp64,fp32,onec,batch,net",
-                    help="kernels workload: comma-separated families (fp64, fp32, onec, batch, net)")
+    ap.add_argument("--families", default="fp64,fp32,onec,batch,batchmc,net",
+                    help="kernels workload: comma-separated families (fp64, fp32, onec, batch, batchmc, net)")
     ap.add_argument("--c3-solves", type=int, default=512, help="c3: number of solves (profiling of smaller cases)")
     ap.add_argument("--c3-max-iterations", type=int, default=30000)
     ap.add_argument("--c5-max-iterations", type=int, default=20000)

@@ -192,6 +192,27 @@ def test_batch_chunk_shapes_match_each_solve(qmin, oracle, shape):
         b.close()
 
 
+@pytest.mark.parametrize("shape", [0, 1, 2, 3, 4])
+def test_batch_fp32_fused_every_chunk_shape(qmin, oracle, shape):
+    """The FP32 one-constant batch (predictor, force and kick as one phase over
+    two state sets) over every chunk shape, including tiles cut where they
+    overhang a solve's box: 21 iterations (an odd count, so that every solve
+    ends in the second set and is copied back) follow each solve's FP64
+    oracle run within FP32 accuracy."""
+    systems = [oracle_system(oracle, parse_args(c)) for c in _cfgs()]
+    b = _batch(qmin, systems, qmin.FP32)
+    b.set_chunk_shape(shape)
+    b.fire_init()
+    r = b.fire_run(21)
+    assert b.tuning()["shape"] == shape
+    for k, s in enumerate(systems):
+        ro = s.fire(21)
+        assert r["iterations"][k] == 21
+        assert abs(r["forceMax"][k] - ro["forceMax"]) <= 1e-4 * ro["forceMax"], k
+        assert rel_err(b.get_solve(k), s.Q) <= 2e-5, k
+    b.close()
+
+
 def test_batch_one_persistent_launch(qmin):
     """A run of many uneven solves is a handful of launches (the entry forces,
     the tuner's timings on the first run, one persistent launch, the final
