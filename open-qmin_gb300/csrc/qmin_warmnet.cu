@@ -585,19 +585,20 @@ __device__ __forceinline__ void tma_box_5d(unsigned dst, const CUtensorMap *map,
 }
 }  // namespace
 
-template <int N>
+template <int N, int CIN>
 __global__ void __launch_bounds__(128) k_conv3_direct_z_tma(Geo g, const __grid_constant__ CUtensorMap tmap,
                                                             const bf16 *__restrict__ w,
                                                             const float *__restrict__ bias, bf16 *__restrict__ out,
                                                             int relu, int zt)
 {
     static_assert(N % 16 == 0 && N >= 16 && 2 * N <= 256, "two M=128 accumulators of N columns");
+    static_assert(CIN % 16 == 0 && CIN >= 16, "input channels a multiple of 16");
     constexpr int COLS = 2 * N <= 32 ? 32 : (2 * N <= 64 ? 64 : (2 * N <= 128 ? 128 : 256));
     extern __shared__ __align__(128) unsigned char smem_raw[];
-    const int cin = g.cin, kc8 = cin >> 3, K = 27 * cin;
+    constexpr int cin = CIN, kc8 = CIN / 8, K = 27 * CIN;
     const int W = g.Wo, H = g.Ho, D = g.Do;
-    const size_t w_bytes = (size_t)27 * N * cin * 2;  // a multiple of 128 (27 * 2 * 16 * 16 divides it)
-    const unsigned slot_bytes = (unsigned)kc8 * kTmaSlab;
+    constexpr size_t w_bytes = (size_t)27 * N * cin * 2;  // a multiple of 128 (27 * 2 * 16 * 16 divides it)
+    constexpr unsigned slot_bytes = (unsigned)kc8 * kTmaSlab;
     // the boxes start on 128-byte boundaries: the dynamic area rounded up (128 bytes spare are allocated)
     unsigned char *base = smem_raw + ((128u - (s_addr(smem_raw) & 127u)) & 127u);
     unsigned char *wts = base;
@@ -651,17 +652,25 @@ __global__ void __launch_bounds__(128) k_conv3_direct_z_tma(Geo g, const __grid_
         *reinterpret_cast<uint4 *>(wts + (size_t)tap * N * cin * 2 + ((size_t)(co >> 3) * kc8 + k8) * 128 +
                                    (co & 7) * 16) = v;
     }
+    // descriptors of the ring's and the weights' first core matrices; a
+    // descriptor's address field is the byte address / 16 in its low 14 bits,
+    // so an offset (a multiple of 16 bytes, the sum below 256 KB) is added to
+    // the descriptor itself: the issuing thread does one add per operand per MMA
+    const uint64_t da0 = umma_desc(s_addr(ring), kTmaSlab, 160);
+    const uint64_t db0 = umma_desc(s_addr(wts), 128, (unsigned)kc8 * 128u);
     auto issue = [&](int z, int acc_idx) {
         asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
-        const unsigned sw = s_addr(wts), sbo_b = (unsigned)kc8 * 128u;
         const uint32_t dst = *tmem_slot + (uint32_t)(acc_idx * N);
+        const uint64_t das[3] = {da0 + ((uint64_t)slot_of(z - 1) * slot_bytes >> 4),
+                                 da0 + ((uint64_t)slot_of(z) * slot_bytes >> 4),
+                                 da0 + ((uint64_t)slot_of(z + 1) * slot_bytes >> 4)};
+#pragma unroll
         for (int tap = 0; tap < 27; ++tap) {
             const int dz = tap / 9, dy = (tap / 3) % 3, dx = tap % 3;
-            const unsigned sa = s_addr(ring) + (unsigned)slot_of(z - 1 + dz) * slot_bytes;
-            for (int kk = 0; kk < (cin >> 4); ++kk) {
-                const unsigned a0 = sa + (unsigned)(2 * kk) * kTmaSlab + (unsigned)(dy * 10 + dx) * 16u;
-                const unsigned b0 = sw + (unsigned)tap * (unsigned)(N * cin * 2) + (unsigned)kk * 256u;
-                const uint64_t da = umma_desc(a0, kTmaSlab, 160), db = umma_desc(b0, 128, sbo_b);
+#pragma unroll
+            for (int kk = 0; kk < CIN / 16; ++kk) {
+                const uint64_t da = das[dz] + (uint64_t)((2 * kk * kTmaSlab + (dy * 10 + dx) * 16) >> 4);
+                const uint64_t db = db0 + (uint64_t)((tap * N * CIN * 2 + kk * 256) >> 4);
                 const unsigned acc = (tap > 0 || kk > 0) ? 1u : 0u;
                 asm volatile(
                     "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
@@ -1086,12 +1095,12 @@ static PFN_cuTensorMapEncodeTiled_v12000 tmap_encoder()
 // the TMA-staged direct kernel; false (nothing launched) where its tensor map
 // cannot describe the input: no encoder, an input not 16-byte aligned, or a
 // grid smaller than one halo box (10 x 18)
-template <int N>
+template <int N, int CIN>
 static bool conv3_direct_z_tma(const Geo &g, const bf16 *in, const bf16 *w, const float *bias, bf16 *out, int relu,
                                cudaStream_t s)
 {
     auto enc = tmap_encoder();
-    if (!enc || (reinterpret_cast<uintptr_t>(in) & 15) || g.Wi < 10 || g.Hi < 18 || g.cin % 16 != 0) return false;
+    if (!enc || (reinterpret_cast<uintptr_t>(in) & 15) || g.Wi < 10 || g.Hi < 18 || g.cin != CIN) return false;
     CUtensorMap map;
     const cuuint64_t es = 2;  // BF16
     const cuuint64_t dims[5] = {(cuuint64_t)g.cin, (cuuint64_t)g.Wi, (cuuint64_t)g.Hi, (cuuint64_t)g.Di,
@@ -1105,16 +1114,17 @@ static bool conv3_direct_z_tma(const Geo &g, const bf16 *in, const bf16 *w, cons
             CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
         return false;
     static int attr_bytes = 0;
-    const size_t sm = direct_z_tma_smem(g.cin, N);
+    const size_t sm = direct_z_tma_smem(CIN, N);
+    if (sm > 232448 - 1024) return false;
     if ((int)sm > attr_bytes) {
         // a failure here surfaces as the launch's error
-        if (cudaFuncSetAttribute(k_conv3_direct_z_tma<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm) ==
-            cudaSuccess)
+        if (cudaFuncSetAttribute(k_conv3_direct_z_tma<N, CIN>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)sm) == cudaSuccess)
             attr_bytes = (int)sm;
     }
     const int zt = std::min(g.Do, 16);
     const long long tiles = (long long)((g.Wo + 7) / 8) * ((g.Ho + 15) / 16) * ((g.Do + zt - 1) / zt) * g.nb;
-    k_conv3_direct_z_tma<N><<<(unsigned)tiles, 128, sm, s>>>(g, map, w, bias, out, relu, zt);
+    k_conv3_direct_z_tma<N, CIN><<<(unsigned)tiles, 128, sm, s>>>(g, map, w, bias, out, relu, zt);
     return true;
 }
 
@@ -1133,15 +1143,19 @@ static void conv_gemm(const Geo &g, const bf16 *in, const bf16 *w, const float *
     if (tcgen05 && OB && g.mode == 0 && g.taps == 27 && g.stride == 1 && !addend && bias &&
         direct_z_smem(g.cin, g.cout) <= 232448 - 1024) {
         if (g.cout == 32) {
-            if (path == 1 && direct_z_tma_smem(g.cin, 32) <= 232448 - 1024 &&
-                conv3_direct_z_tma<32>(g, in, w, bias, reinterpret_cast<bf16 *>(out), relu, s))
+            // the network's direct layers: 16 -> 32 and 32 -> 32 (TMA kernel per input width)
+            if (path == 1 && g.cin == 16 &&
+                conv3_direct_z_tma<32, 16>(g, in, w, bias, reinterpret_cast<bf16 *>(out), relu, s))
+                return;
+            if (path == 1 && g.cin == 32 &&
+                conv3_direct_z_tma<32, 32>(g, in, w, bias, reinterpret_cast<bf16 *>(out), relu, s))
                 return;
             conv3_direct_z<32>(g, in, w, bias, reinterpret_cast<bf16 *>(out), relu, s);
             return;
         }
         if (g.cout == 48) {
-            if (path == 1 && direct_z_tma_smem(g.cin, 48) <= 232448 - 1024 &&
-                conv3_direct_z_tma<48>(g, in, w, bias, reinterpret_cast<bf16 *>(out), relu, s))
+            if (path == 1 && g.cin == 48 &&
+                conv3_direct_z_tma<48, 48>(g, in, w, bias, reinterpret_cast<bf16 *>(out), relu, s))
                 return;
             conv3_direct_z<48>(g, in, w, bias, reinterpret_cast<bf16 *>(out), relu, s);
             return;
