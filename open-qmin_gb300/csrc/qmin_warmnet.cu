@@ -6,7 +6,11 @@
 // Layout: activations channels-last, [sample][z][y][x][channel]; every
 // tensor-core operand BF16, every accumulator and gradient FP32.  Each
 // convolution (3x3x3 or 1x1x1, stride 1 or 2, zero padding) is an implicit
-// GEMM on the BF16 tensor cores (mma.sync m16n8k16, FP32 accumulate):
+// GEMM on the BF16 tensor cores: by default tcgen05.mma with tensor-memory
+// accumulators (a direct kernel with TMA-staged halo planes for the 3^3
+// stride-1 layers of 32 and 48 output channels, a gathering kernel
+// otherwise), or mma.sync m16n8k16 (tensor path 0; the weight gradient
+// always), FP32 accumulate:
 //   forward:      out[v][co]      = sum_{tap,ci} in[src(v,tap)][ci] * W[co][tap][ci]
 //   data grad:    din[u][ci]      = sum_{tap,co} dout[src'(u,tap)][co] * W'[ci][tap][co]
 //   weight grad:  dW[co][tap][ci] = sum_v dout[v][co] * in[src(v,tap)][ci]
