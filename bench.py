@@ -524,7 +524,8 @@ def time_to_converge(q, consts, g, precision, max_iterations=20000, fcut=1e-6, n
     return out
 
 
-WARMNET_WEIGHTS = os.path.join(ROOT, "open-qmin_gb300", "weights", "warmnet_c4.npz")
+# trained on 4096 c4 solves, then fine-tuned on 64^3 crops of c2 and c5 lattices (train_warmstart.py)
+WARMNET_WEIGHTS = os.path.join(ROOT, "open-qmin_gb300", "weights", "warmnet_c4_crops.npz")
 
 
 def warm_start_c2(q, consts, g, t64, t32):
@@ -549,7 +550,7 @@ def warm_start_c2(q, consts, g, t64, t32):
               "protocol_time_s": charged, "protocol_speedup_vs_plain_fp64": t64["time_s"] / charged,
               "protocol_speedup_vs_plain_fp32": t32["time_s"] / charged,
               "raw_speedup_vs_plain_fp64": t64["time_s"] / w["time_s"], "net_kernel_launches": l_net,
-              "weights": "open-qmin_gb300/weights/warmnet_c4.npz (trained on 4096 c4 solves at 64^3)"})
+              "weights": os.path.relpath(WARMNET_WEIGHTS, ROOT)})
     return w
 
 
@@ -889,8 +890,8 @@ def run_c5(args):
                                   "forceMax_fp64": fm64, "E_per_site_fp64": e64, "E_rel_vs_plain_fp64": rel,
                                   "E_lower_than_plain": bool(e64 < ep), "protocol_pass": ok,
                                   "protocol_time_s": dt + (0.0 if ok else out["fire_fp32"]["time_s"]),
-                                  "note": "net trained on c4 (64^3, walls + one sphere, no field); no retraining"}
-    for name, prec in (("adam", q.FP32), ("lbfgs", q.FP32), ("lbfgs", q.FP64)):
+                                  "weights": os.path.relpath(WARMNET_WEIGHTS, ROOT)}
+    for name, prec in (() if args.c5_fire_only else (("adam", q.FP32), ("lbfgs", q.FP32), ("lbfgs", q.FP64))):
         tag = name + ("_fp32" if prec == q.FP32 else "_fp64")
         lat = lattice(prec)
         torch.cuda.synchronize()
@@ -934,15 +935,17 @@ def main():
     ap.add_argument("--no-configs", action="store_true", help="skip the c1 and c3 runs")
     ap.add_argument("--lattice", type=int, default=200, help="cube side (profiling of smaller cases)")
     ap.add_argument("--forms", default="both", choices=["both", "fp64", "fp32"])
-    ap.add_argument("--workload", default="c2", choices=["c2", "c3", "c5", "warmnet", "kernels"],
+    ap.add_argument("--workload", default="c2", choices=["c2", "c2-converge", "c3", "c5", "warmnet", "kernels"],
                     help="c3: the batched uneven solves alone; c5: the 400^3 multi-sphere E-field case; "
                          "warmnet: the warm-start net's forward pass; kernels: one small call of every kernel family "
                          "(for profilers)")
     ap.add_argument("--families", default="fp64,fp32,onec,batch,batchmc,net",
                     help="kernels workload: comma-separated families (fp64, fp32, onec, batch, batchmc, net)")
+    ap.add_argument("--warmnet-weights", default=None, help="warm-start weights file (default: the committed c4 weights)")
     ap.add_argument("--c3-solves", type=int, default=512, help="c3: number of solves (profiling of smaller cases)")
     ap.add_argument("--c3-max-iterations", type=int, default=30000)
     ap.add_argument("--c5-max-iterations", type=int, default=20000)
+    ap.add_argument("--c5-fire-only", action="store_true", help="c5: FIRE and the warm start only (no Adam, L-BFGS)")
     ap.add_argument("--c4-test", type=int, default=64, help="c4 test solves for the warm-start protocol (0: skip)")
     # a fixed FIRE strategy instead of the autotuner's choice (for profiling runs, where the
     # profiler's serialised launches would bias the autotuner's timings)
@@ -951,6 +954,9 @@ def main():
     ap.add_argument("--fire-variant-fp64", type=int, default=-1, help="variant index of the pinned FP64 strategy")
     ap.add_argument("--fire-variant-fp32", type=int, default=-1, help="variant index of the pinned FP32 strategy")
     args = ap.parse_args()
+    if args.warmnet_weights:
+        global WARMNET_WEIGHTS
+        WARMNET_WEIGHTS = os.path.abspath(args.warmnet_weights)
     rank = int(os.environ.get("RANK", 0))
     world = int(os.environ.get("WORLD_SIZE", 1))
     if args.workload == "c5":
@@ -966,6 +972,20 @@ def main():
     if args.workload == "kernels":
         if rank == 0:
             print(json.dumps(run_kernels(args)))
+        return 0
+    if args.workload == "c2-converge":
+        # time to forceMax < 1e-6 on the 200^3 workload only: plain FP64, plain
+        # FP32 and the learned warm start under the protocol
+        if rank == 0:
+            import __graft_entry__ as ge
+            q = ge.load_package()
+            consts, g = build_workload_host(q)
+            t64 = time_to_converge(q, consts, g, q.FP64)
+            t32 = time_to_converge(q, consts, g, q.FP32)
+            out = {"workload": "200^3 c2, FIRE to forceMax < 1e-6", "fp64": t64, "fp32_form": t32}
+            if os.path.exists(WARMNET_WEIGHTS):
+                out["warm_start_fp32"] = warm_start_c2(q, consts, g, t64, t32)
+            print(json.dumps(out))
         return 0
     if args.workload == "c3":
         if rank == 0:

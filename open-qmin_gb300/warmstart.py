@@ -108,6 +108,74 @@ def make_dataset(make_solve, seeds, group=256, log=print):
     return dict(x=X, target=T, mask=M, iterations=np.array(its), L=L)
 
 
+def fire_lattice(sol, precision=FP32, force_cutoff=1e-6, max_iterations=30000):
+    """Plain FIRE (CLI parameters, dt 5e-4) on one lattice through the
+    single-lattice path; returns (final Q host AoS, iterations, seconds)."""
+    lat = set_up_lattice(sol, precision)
+    lat.fire_init(dt=5e-4, force_cutoff=force_cutoff)
+    t0 = time.perf_counter()
+    r = lat.fire_run(max_iterations)
+    sec = time.perf_counter() - t0
+    Q = lat.get_state()[0]
+    lat.close()
+    return Q, int(r["iterations"]), sec
+
+
+def make_crop_dataset(lattices, side=64, border=8, log=print):
+    """Patch-tiled samples of large lattices: each lattice is minimised whole
+    (FP32 FIRE to forceMax < 1e-6), its features are computed whole, and
+    side^3 crops at origins spaced by `side` (the last one flush with the far
+    face) become samples: features, final Q and the moved-site mask with a
+    `border`-site band at every crop face taken out (the net sees zeros past a
+    crop's faces, where the lattice had context).  Same layout as make_dataset."""
+    torch = _torch()
+    crops = []
+    for sol in lattices:
+        L = sol["L"]
+        Q, its, sec = fire_lattice(sol)
+        fn = FeatureNet(L)
+        x, m = fn.features(sol)
+        fn.net.close()
+        x3 = x.view(L[2], L[1], L[0], 16)
+        m3 = m.view(L[2], L[1], L[0])
+        t3 = torch.as_tensor(Q.astype(np.float32)).cuda().view(L[2], L[1], L[0], 5)
+
+        def origins(n):
+            o = list(range(0, n - side + 1, side))
+            if o[-1] != n - side:
+                o.append(n - side)
+            return o
+
+        for z0 in origins(L[2]):
+            for y0 in origins(L[1]):
+                for x0 in origins(L[0]):
+                    sl = (slice(z0, z0 + side), slice(y0, y0 + side), slice(x0, x0 + side))
+                    mm = m3[sl].clone()
+                    mm[:border], mm[-border:] = 0, 0
+                    mm[:, :border], mm[:, -border:] = 0, 0
+                    mm[:, :, :border], mm[:, :, -border:] = 0, 0
+                    crops.append((x3[sl].reshape(-1, 16).clone(), t3[sl].reshape(-1, 5).clone(), mm.reshape(-1)))
+        log(f"crops: lattice {L} FIRE {its} iterations in {sec:.2f} s, {len(crops)} crops so far")
+        del x3, m3, t3, x, m
+    n = len(crops)
+    sites = side ** 3
+    X = torch.empty((n, sites, 16), dtype=torch.bfloat16, device="cuda")
+    T = torch.empty((n, sites, 5), dtype=torch.float32, device="cuda")
+    M = torch.empty((n, sites), dtype=torch.uint8, device="cuda")
+    for k, (x, t, m) in enumerate(crops):
+        X[k], T[k], M[k] = x, t, m
+    return dict(x=X, target=T, mask=M, iterations=np.zeros(0), L=(side, side, side))
+
+
+def concat_datasets(parts):
+    """One dataset from several with the same sample shape."""
+    torch = _torch()
+    assert len({tuple(p["L"]) for p in parts}) == 1
+    return dict(x=torch.cat([p["x"] for p in parts]), target=torch.cat([p["target"] for p in parts]),
+                mask=torch.cat([p["mask"] for p in parts]),
+                iterations=np.concatenate([np.asarray(p["iterations"]) for p in parts]), L=parts[0]["L"])
+
+
 # Lattice symmetries used for augmentation.  Q = (Qxx, Qxy, Qxz, Qyy, Qyz):
 # the mirror x -> -x negates Qxy and Qxz, y -> -y negates Qxy and Qyz,
 # z -> -z negates Qxz and Qyz; swapping x and y exchanges Qxx<->Qyy and Qxz<->Qyz.

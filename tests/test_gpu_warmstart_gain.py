@@ -1,5 +1,6 @@
 """What the trained warm-start net gains over plain FIRE, on solves it never
-saw.  The committed weights (trained on c4 seeds 0..4095) on 8 unseen c4
+saw.  The shipped weights (trained on c4 seeds 0..4095, fine-tuned on c4 seeds
+0..255 and 64^3 crops of c2 and c5 lattices, seeds 1..12 and 1..2) on 8 unseen c4
 solves (64^3, homeotropic z-walls, one homeotropic sphere; seeds 300000..
 300007) through the protocol: the net's prediction, FP32 FIRE to forceMax <
 1e-6, judged in FP64 (forceMax < 1e-6 and energy within 1e-4 of plain FP64
@@ -19,7 +20,7 @@ import pytest
 pytestmark = pytest.mark.gpu
 
 WEIGHTS = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "open-qmin_gb300", "weights",
-                       "warmnet_c4.npz")
+                       "warmnet_c4_crops.npz")
 
 
 def test_trained_weights_gain_on_unseen_c4(qmin):
