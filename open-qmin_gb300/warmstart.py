@@ -121,6 +121,18 @@ def fire_lattice(sol, precision=FP32, force_cutoff=1e-6, max_iterations=30000):
     return Q, int(r["iterations"]), sec
 
 
+def crop_origins(n, side):
+    """Origins of side-long crops along an axis of n sites: a pitch of `side`,
+    the last crop flush with the far face (it overlaps its neighbour when
+    side does not divide n)."""
+    if n < side:
+        raise ValueError(f"an axis of {n} sites holds no crop of {side}")
+    o = list(range(0, n - side + 1, side))
+    if o[-1] != n - side:
+        o.append(n - side)
+    return o
+
+
 def make_crop_dataset(lattices, side=64, border=8, log=print):
     """Patch-tiled samples of large lattices: each lattice is minimised whole
     (FP32 FIRE to forceMax < 1e-6), its features are computed whole, and
@@ -140,15 +152,9 @@ def make_crop_dataset(lattices, side=64, border=8, log=print):
         m3 = m.view(L[2], L[1], L[0])
         t3 = torch.as_tensor(Q.astype(np.float32)).cuda().view(L[2], L[1], L[0], 5)
 
-        def origins(n):
-            o = list(range(0, n - side + 1, side))
-            if o[-1] != n - side:
-                o.append(n - side)
-            return o
-
-        for z0 in origins(L[2]):
-            for y0 in origins(L[1]):
-                for x0 in origins(L[0]):
+        for z0 in crop_origins(L[2], side):
+            for y0 in crop_origins(L[1], side):
+                for x0 in crop_origins(L[0], side):
                     sl = (slice(z0, z0 + side), slice(y0, y0 + side), slice(x0, x0 + side))
                     mm = m3[sl].clone()
                     mm[:border], mm[-border:] = 0, 0

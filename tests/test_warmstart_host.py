@@ -53,3 +53,22 @@ def test_c4_generator_ranges(qmin):
     a = w.c4_solve(3)
     b = w.c4_solve(3, qseed=99)
     assert np.array_equal(a["types"], b["types"]) and not np.array_equal(a["Q"], b["Q"])
+
+
+def test_crop_origins(qmin):
+    """Crops of the patch-tiled fine-tuning: a 64-site pitch with the last crop
+    flush with the far face, so that every site of the axis is covered."""
+    import importlib
+    ws = importlib.import_module("qmin_gb300.warmstart")
+    assert ws.crop_origins(200, 64) == [0, 64, 128, 136]
+    assert ws.crop_origins(400, 64) == [0, 64, 128, 192, 256, 320, 336]
+    assert ws.crop_origins(128, 64) == [0, 64]
+    assert ws.crop_origins(64, 64) == [0]
+    for n in (64, 100, 200, 333, 400):
+        o = ws.crop_origins(n, 64)
+        covered = set()
+        for a in o:
+            covered.update(range(a, a + 64))
+        assert covered == set(range(n))
+    with pytest.raises(ValueError):
+        ws.crop_origins(48, 64)
