@@ -414,6 +414,14 @@ int qmin_warmnet_sync(qmin_warmnet n);
  * 0 the mma.sync kernels.  All compute BF16 x BF16 -> FP32; paths 1 and 2 give
  * identical bits.  QMIN_EINVAL for another value.  No reference counterpart. */
 int qmin_warmnet_set_tensor_path(qmin_warmnet n, int path);
+/* Polls of the TMA direct convolution's waits (for its copies and its MMAs)
+ * before a pass gives up, leaving its outputs void and qmin_warmnet_sync
+ * returning QMIN_ETIMEOUT; 0 makes every such wait give up at once (a pass
+ * then fails at its first wait: the reporting path, for tests), a negative
+ * value restores the default (about a second).  Process-wide: it applies to
+ * every net.  The waits that let the copies and MMAs in flight land before a
+ * CTA that gave up exits always use the default.  No reference counterpart. */
+int qmin_warmnet_set_wait_limit(long long polls);
 int qmin_warmnet_kernel_launches(qmin_warmnet n, long long *count);
 /* Warm-start a lattice in place: features from its current Q, types and
  * objects, one forward pass, the prediction written into its Q on the sites

@@ -188,6 +188,11 @@ __global__ void __launch_bounds__(128) k_conv_gemm(Geo g, const bf16 *__restrict
 // Every wait is bounded; a wait that gives up sets g_conv_err, and the CTA
 // still frees its tensor memory.
 __device__ int g_conv_err;
+// polls of the TMA direct kernel's waits for its copies and MMAs before it
+// gives up (qmin_warmnet_set_wait_limit); the waits that let copies and MMAs in
+// flight land before a CTA that gave up exits always poll kWaitPolls times
+constexpr int kWaitPolls = 1 << 22;
+__device__ int g_conv_wait_limit = kWaitPolls;
 
 namespace {
 __device__ __forceinline__ unsigned s_addr(const void *p) { return (unsigned)__cvta_generic_to_shared(p); }
@@ -203,9 +208,9 @@ __host__ __device__ constexpr uint32_t umma_idesc(int n)
 {
     return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(n >> 3) << 17) | ((uint32_t)(128 >> 4) << 24);
 }
-__device__ __forceinline__ bool mbar_wait_bounded(unsigned bar, unsigned parity)
+__device__ __forceinline__ bool mbar_wait_bounded(unsigned bar, unsigned parity, int polls = kWaitPolls)
 {
-    for (int it = 0; it < (1 << 22); ++it) {
+    for (int it = 0; it < polls; ++it) {
         unsigned ok;
         asm volatile(
             "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
@@ -642,7 +647,10 @@ __global__ void __launch_bounds__(128) k_conv3_direct_z_tma(Geo g, const __grid_
         const unsigned dst = s_addr(ring) + (unsigned)sl * slot_bytes;
         for (int k8 = 0; k8 < kc8; ++k8) tma_box_5d(dst + (unsigned)k8 * kTmaSlab, &tmap, k8 * 8, x0 - 1, y0 - 1, iz, b, bs);
     };
-    auto wait_plane = [&](int iz) { return mbar_wait_bounded(s_addr(&bar[2 + slot_of(iz)]), use_of(iz) & 1u); };
+    const int polls = *(volatile int *)&g_conv_wait_limit;
+    auto wait_plane = [&](int iz, int lim) {
+        return mbar_wait_bounded(s_addr(&bar[2 + slot_of(iz)]), use_of(iz) & 1u, lim);
+    };
     int issued_hi = z0 - 2;  // the last plane whose boxes were issued
     __syncthreads();         // the barriers are initialised
     if (tid == 0) {
@@ -730,8 +738,8 @@ __global__ void __launch_bounds__(128) k_conv3_direct_z_tma(Geo g, const __grid_
         bool good = true;
         if (tid == 0) {
             // planes z - 1 and z were waited for by earlier steps (all three at the first)
-            if (p == 0) good = wait_plane(z - 1) && wait_plane(z);
-            good = good && wait_plane(z + 1);
+            if (p == 0) good = wait_plane(z - 1, polls) && wait_plane(z, polls);
+            good = good && wait_plane(z + 1, polls);
             if (good) issue(z, p & 1);
         }
         if (__syncthreads_or(!good)) {
@@ -741,7 +749,7 @@ __global__ void __launch_bounds__(128) k_conv3_direct_z_tma(Geo g, const __grid_
         committed = p + 1;
         if (p >= 1) {
             // the MMAs of plane p - 1: done with their accumulator and with slot z - 2
-            const bool w_ok = mbar_wait_bounded(s_addr(&bar[(p - 1) & 1]), (unsigned)((p - 1) >> 1) & 1u);
+            const bool w_ok = mbar_wait_bounded(s_addr(&bar[(p - 1) & 1]), (unsigned)((p - 1) >> 1) & 1u, polls);
             if (__syncthreads_or(!w_ok)) {
                 ok = false;
                 break;
@@ -757,13 +765,14 @@ __global__ void __launch_bounds__(128) k_conv3_direct_z_tma(Geo g, const __grid_
     }
     if (ok) {
         const int last = nz - 1;
-        const bool w_ok = mbar_wait_bounded(s_addr(&bar[last & 1]), (unsigned)(last >> 1) & 1u);
+        const bool w_ok = mbar_wait_bounded(s_addr(&bar[last & 1]), (unsigned)(last >> 1) & 1u, polls);
         ok = !__syncthreads_or(!w_ok);
         if (ok) epilogue(z0 + last, last & 1, tmem);
     }
     if (!ok && tid == 0) {
-        // a wait gave up: let the boxes and the MMAs in flight land (bounded) before the buffers go away
-        for (int iz = max(z0 - 1, issued_hi - 3); iz <= issued_hi; ++iz) wait_plane(iz);
+        // a wait gave up: let the boxes and the MMAs in flight land (bounded,
+        // at the full poll count) before the buffers go away
+        for (int iz = max(z0 - 1, issued_hi - 3); iz <= issued_hi; ++iz) wait_plane(iz, kWaitPolls);
         for (int q = max(0, committed - 2); q < committed; ++q)
             mbar_wait_bounded(s_addr(&bar[q & 1]), (unsigned)(q >> 1) & 1u);
         atomicExch(&g_conv_err, 1);
@@ -1638,8 +1647,17 @@ int qmin_warmnet_sync(qmin_warmnet n)
     if (err) {
         const int zero = 0;
         cudaMemcpyToSymbol(g_conv_err, &zero, sizeof(int));
-        return nfail(QMIN_ECUDA, "qmin_warmnet_sync: a tensor-core wait in a convolution gave up");
+        return nfail(QMIN_ETIMEOUT, "qmin_warmnet_sync: a tensor-core or TMA wait in a convolution gave up "
+                                    "(the pass's outputs are void)");
     }
+    return QMIN_OK;
+}
+
+int qmin_warmnet_set_wait_limit(long long polls)
+{
+    const int v = polls < 0 ? kWaitPolls : (int)std::min<long long>(polls, 1LL << 30);
+    const cudaError_t e = cudaMemcpyToSymbol(g_conv_wait_limit, &v, sizeof(int));
+    if (e != cudaSuccess) return nfail(QMIN_ECUDA, std::string("qmin_warmnet_set_wait_limit: ") + cudaGetErrorString(e));
     return QMIN_OK;
 }
 

@@ -170,6 +170,38 @@ def test_tma_staging_matches_thread_staging(qmin, L):
     assert np.linalg.norm(g1 - g0) <= 1e-5 * np.linalg.norm(g0)
 
 
+def test_tma_wait_limit_reports_and_recovers(qmin):
+    """The TMA direct convolution's bounded waits made to run out: with a poll
+    limit of zero every CTA gives up at its first wait, lets the copies it
+    issued land, frees its tensor memory and raises the device error word;
+    the pass then reports QMIN_ETIMEOUT through sync.  With the default limit
+    restored the same net's next pass is identical to a clean one."""
+    L = (40, 48, 24)
+    side = max(L)
+    s = _lattice(qmin, 91, side)
+    idx = np.arange(side ** 3).reshape(side, side, side)[:L[2], :L[1], :L[0]].ravel()
+    sols = [dict(s, L=L, Q=np.ascontiguousarray(s["Q"][idx]), types=np.ascontiguousarray(s["types"][idx]))]
+    net, _keep = _net_with_inputs(qmin, sols, train=False)
+    net.set_tensor_path(1)
+    _x, y, _m = net.torch_views()
+    net.forward()
+    net.sync()
+    y_ref = y.float().cpu().numpy().copy()
+    try:
+        qmin.WarmNet.set_wait_limit(0)
+        net.forward()
+        with pytest.raises(qmin.QminError) as err:
+            net.sync()
+        assert err.value.code == qmin.QMIN_ETIMEOUT
+        assert "gave up" in str(err.value)
+    finally:
+        qmin.WarmNet.set_wait_limit(-1)
+    net.forward()
+    net.sync()
+    assert np.array_equal(y.float().cpu().numpy(), y_ref)
+    net.close()
+
+
 def test_backward_matches_torch_fp64(qmin):
     L = (16, 16, 16)
     sols = [_lattice(qmin, s, 16) for s in (31, 32)]
