@@ -490,6 +490,10 @@ static int build_split_lists(qmin_ctx *h)
     }
     if (n < 0) return fail(QMIN_ECUDA, std::string("split site lists: ") + cudaGetErrorString(cudaGetLastError()));
     h->launches += n;
+    // the derivative planes of object sites are read as zero and no longer
+    // written (object sites are not in the derivative list): clear planes a
+    // previous geometry left behind
+    if (h->D) CK(cudaMemsetAsync(h->D, 0, 15 * (size_t)h->P * h->esz, h->stream));
     return QMIN_OK;
 }
 

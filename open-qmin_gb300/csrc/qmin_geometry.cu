@@ -135,7 +135,8 @@ __global__ void __launch_bounds__(kScanBlock)
     }
 }
 
-// key 0 at every site one of whose six neighbours is a listed site
+// key 0 at every LC site one of whose six neighbours is a listed site (an
+// object site's derivative planes are zero, and stay so: they are never listed)
 __global__ void __launch_bounds__(kScanBlock)
     k_split_need(const uint8_t *__restrict__ cls, int Lx, int Ly, int Lz, uint8_t *key)
 {
@@ -143,12 +144,12 @@ __global__ void __launch_bounds__(kScanBlock)
     for (int i = blockIdx.x * kScanBlock + threadIdx.x; i < N; i += gridDim.x * kScanBlock) {
         int x, y, z;
         site_xyz(i, Lx, Ly, x, y, z);
-        const bool need = cls[(x == 0 ? Lx - 1 : x - 1) + Lx * (y + Ly * z)] == 1 ||
+        const bool need = cls[i] != 2 && (cls[(x == 0 ? Lx - 1 : x - 1) + Lx * (y + Ly * z)] == 1 ||
                           cls[(x == Lx - 1 ? 0 : x + 1) + Lx * (y + Ly * z)] == 1 ||
                           cls[x + Lx * ((y == 0 ? Ly - 1 : y - 1) + Ly * z)] == 1 ||
                           cls[x + Lx * ((y == Ly - 1 ? 0 : y + 1) + Ly * z)] == 1 ||
                           cls[x + Lx * (y + Ly * (z == 0 ? Lz - 1 : z - 1))] == 1 ||
-                          cls[x + Lx * (y + Ly * (z == Lz - 1 ? 0 : z + 1))] == 1;
+                          cls[x + Lx * (y + Ly * (z == Lz - 1 ? 0 : z + 1))] == 1);
         key[i] = need ? 0 : kNoBucket;
     }
 }
