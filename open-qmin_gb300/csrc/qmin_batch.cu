@@ -298,7 +298,7 @@ __device__ __forceinline__ void b_fused_chunk(const BatchArgs<T> &B, const Batch
 {
     const ChunkDesc ch = B.chunks[c];
     // coefficients formed in FP64 by one lane per warp
-    double cf[4] = {0.0, 0.0, 0.0, 0.0};
+    double cf[3] = {0.0, 0.0, 0.0};
     if ((threadIdx.x & 31) == 0) {
         const FireDev &fd = fds[ch.solve];
         const double dt = fd.dt, hdt = 0.5 * dt;
@@ -310,12 +310,11 @@ __device__ __forceinline__ void b_fused_chunk(const BatchArgs<T> &B, const Batch
         cf[0] = mv;
         cf[1] = mf + hdt;
         cf[2] = dt;
-        cf[3] = dt;
     }
 #pragma unroll
-    for (int k = 0; k < 4; ++k) cf[k] = __shfl_sync(0xffffffffu, cf[k], 0);
+    for (int k = 0; k < 3; ++k) cf[k] = __shfl_sync(0xffffffffu, cf[k], 0);
     const PredCoef<T> pc{T(cf[0]), T(cf[1]), T(cf[2])};
-    const T hdt = T(0.5) * T(cf[3]);
+    const T hdt = T(0.5) * T(cf[2]);  // the kick's half step, as b_force_chunk forms it
     const SolveDesc sd = B.solves[ch.solve];
     int li, x, y, z;
     const bool inb = chunk_site(B, sd, ch, threadIdx.x, li, x, y, z);
