@@ -151,6 +151,14 @@ def scale_workload(side):
     WORKLOAD["sphere"] = ((side / 2.0, side / 2.0, side / 2.0), 0.15 * side)
 
 
+def workload_name():
+    """The FIRE workload's description, from its current side (200 unless --lattice)."""
+    w = WORKLOAD
+    n = w["L"][0]
+    return (f"{n}^3 lattice, homeotropic z-walls (planes {w['walls'][0]} and {w['walls'][1]}) + centred homeotropic "
+            f"sphere r={w['sphere'][1]:g}, W={w['W']:g}, L1-L3 = 2.32/1.0/0.5, FIRE dt=5e-4")
+
+
 def build_workload_host(q, precision=None):
     """Host set-up of the workload through the package's own host helpers."""
     a, b, c, S0 = q.cli_phase_constants()
@@ -409,8 +417,7 @@ def finish(q, args, rank, world, consts, g, N, K, W, timed_fire, value, ms, laun
         out = {"metric": METRIC, "value": value, "unit": "site-steps/s", "n_gpus": world, "steps": K, "warmup": W,
                "ms_per_step": ms / K, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
                "dtype": "f64", "data": "synthetic (seeded random-director Q0, reference geometry builders)",
-               "config": {"workload": "200^3 lattice, homeotropic z-walls (planes 0 and 199) + centred homeotropic "
-                                      "sphere r=30, W=5.3, L1-L3 = 2.32/1.0/0.5, FIRE dt=5e-4, CLI FIRE params",
+               "config": {"workload": workload_name() + ", CLI FIRE params",
                           "sites": N, "fire_steps_per_run": K, "precision": "fp64",
                           "l2": "inputs larger than L2 (Q,V,F state = 960 MB)",
                           "parallelism": "replicas" if world > 1 else "single GPU"},
@@ -812,13 +819,12 @@ def run_reference(args):
     el = time.perf_counter() - t0
     value = s.N * done / el
     cpu = {"value": value, "unit": "site-steps/s", "cores": used, "kind": "port",
-           "sample": f"{done} FIRE iterations of the 200^3 workload (each with the minimize() entry force "
+           "sample": f"{done} FIRE iterations of the {w['L'][0]}^3 workload (each with the minimize() entry force "
                      f"evaluation), {used} OpenMP threads, wall-clock bounded to {budget:.0f} s"}
     return {"metric": METRIC, "value": value, "unit": "site-steps/s", "n_gpus": 0, "steps": done,
             "warmup": max(args.warmup, 1), "ms_per_step": el / max(done, 1) * 1e3, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": "200^3 lattice, homeotropic z-walls (planes 0 and 199) + centred homeotropic "
-                                   "sphere r=30, W=5.3, L1-L3 = 2.32/1.0/0.5, FIRE dt=5e-4", "sites": s.N},
+            "config": {"workload": workload_name() + ", CLI FIRE params", "sites": s.N},
             "impl": "reference", "cpu_baseline": cpu,
             "e2e": {"value": value, "unit": "site-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
 
