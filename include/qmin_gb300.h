@@ -186,7 +186,9 @@ int qmin_energy(qmin_handle h, double *e_per_active, double comps[5]);
 int qmin_fire_init(qmin_handle h, const qmin_fire_params *p);
 /* energyMinimizerFIRE::minimize (energyMinimizerFIRE.cpp:151-170) with
  * setMaximumIterations(max_iterations); velocity Verlet + FIRE on the GPU,
- * graph-captured, no host synchronisation inside a chunk of iterations. */
+ * graph-captured, no host synchronisation inside a chunk of iterations.
+ * QMIN_ETIMEOUT when a wait of the TMA-staged deep-site kernel (split variant
+ * 6) gave up (qmin_set_wait_limit): the lattice's state is then void. */
 int qmin_fire_run(qmin_handle h, int max_iterations, qmin_fire_result *res);
 /* The FIRE updater's state that persists between minimize() calls in the
  * reference: updater::iterations and energyMinimizerFIRE's forceMax, alpha,
@@ -414,14 +416,17 @@ int qmin_warmnet_sync(qmin_warmnet n);
  * 0 the mma.sync kernels.  All compute BF16 x BF16 -> FP32; paths 1 and 2 give
  * identical bits.  QMIN_EINVAL for another value.  No reference counterpart. */
 int qmin_warmnet_set_tensor_path(qmin_warmnet n, int path);
-/* Polls of the TMA direct convolution's waits (for its copies and its MMAs)
- * before a pass gives up, leaving its outputs void and qmin_warmnet_sync
- * returning QMIN_ETIMEOUT; 0 makes every such wait give up at once (a pass
- * then fails at its first wait: the reporting path, for tests), a negative
- * value restores the default (about a second).  Process-wide: it applies to
- * every net.  The waits that let the copies and MMAs in flight land before a
- * CTA that gave up exits always use the default.  No reference counterpart. */
-int qmin_warmnet_set_wait_limit(long long polls);
+/* Polls of the library's TMA waits before a kernel gives up: the TMA direct
+ * convolution's waits for its copies and MMAs (the pass's outputs are then
+ * void and qmin_warmnet_sync returns QMIN_ETIMEOUT) and the TMA-staged
+ * deep-site FIRE kernel's waits for its next planes (qmin_fire_run returns
+ * QMIN_ETIMEOUT and the lattice's state is void).  0 makes every such wait
+ * give up at once (a pass then fails at its first wait: the reporting path,
+ * for tests), a negative value restores the defaults (about a second).
+ * Process-wide: it applies to every net and handle.  The waits that let the
+ * copies and MMAs in flight land before a CTA that gave up exits always use
+ * the default.  No reference counterpart. */
+int qmin_set_wait_limit(long long polls);
 int qmin_warmnet_kernel_launches(qmin_warmnet n, long long *count);
 /* Warm-start a lattice in place: features from its current Q, types and
  * objects, one forward pass, the prediction written into its Q on the sites

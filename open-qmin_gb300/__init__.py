@@ -41,7 +41,7 @@ EXPORTED_SYMBOLS = [
     "qmin_warmnet_set_stream", "qmin_warmnet_param_count", "qmin_warmnet_shape", "qmin_warmnet_buffers",
     "qmin_warmnet_set_params", "qmin_warmnet_get_params", "qmin_warmnet_features", "qmin_warmnet_forward",
     "qmin_warmnet_backward", "qmin_warmnet_adam_step", "qmin_warmnet_write_state", "qmin_warmnet_sync",
-    "qmin_warmnet_set_tensor_path", "qmin_warmnet_set_wait_limit",
+    "qmin_warmnet_set_tensor_path", "qmin_set_wait_limit",
     "qmin_warmnet_kernel_launches", "qmin_warm_start",
 ]
 FIRE_SEPARATE, FIRE_FUSED, FIRE_AUTO, FIRE_TILED, FIRE_SPLIT = 0, 1, 2, 3, 4
@@ -148,7 +148,7 @@ def lib():
             "qmin_warmnet_write_state": [h, C.c_int, vp, C.c_int, C.c_longlong, vp],
             "qmin_warmnet_sync": [h], "qmin_warmnet_kernel_launches": [h, C.POINTER(C.c_longlong)],
             "qmin_warmnet_set_tensor_path": [h, C.c_int],
-            "qmin_warmnet_set_wait_limit": [C.c_longlong],
+            "qmin_set_wait_limit": [C.c_longlong],
             "qmin_warm_start": [h, h],
             "qmin_host_add_wall": [C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_double, C.c_double, dp,
                                    ip, C.POINTER(Object), ip],
@@ -176,6 +176,15 @@ def _check(code, iterations=None, force_max=None):
         err.iterations = iterations.value if iterations is not None else None
         err.forceMax = force_max.value if force_max is not None else None
         raise err
+
+
+def set_wait_limit(polls=-1):
+    """Polls of the library's TMA waits before a kernel gives up: the net's
+    direct convolution (WarmNet.sync then raises QMIN_ETIMEOUT) and the
+    TMA-staged deep-site FIRE kernel (fire_run raises QMIN_ETIMEOUT, the
+    lattice's state is void).  0 gives up at once, a negative value restores
+    the defaults.  Process-wide."""
+    _check(lib().qmin_set_wait_limit(int(polls)))
 
 
 def _dp(a):
@@ -600,13 +609,6 @@ class WarmNet:
 
     def set_stream(self, stream_ptr):
         _check(lib().qmin_warmnet_set_stream(self._h, C.c_void_p(stream_ptr)))
-
-    @staticmethod
-    def set_wait_limit(polls=-1):
-        """Polls of the TMA direct convolution's waits before a pass gives up
-        (sync then raises QMIN_ETIMEOUT); 0 gives up at once, a negative value
-        restores the default.  Process-wide."""
-        _check(lib().qmin_warmnet_set_wait_limit(int(polls)))
 
     def set_params(self, p):
         p = np.ascontiguousarray(p, dtype=np.float32)

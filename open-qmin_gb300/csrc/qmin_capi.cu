@@ -1239,7 +1239,8 @@ template <class T> static int fire_impl(qmin_ctx *h, int max_iterations)
         CK(cudaStreamSynchronize(h->stream));
         if (e) {
             cudaMemsetAsync(h->dev_err, 0, sizeof(int), h->stream);
-            return fail(QMIN_ECUDA, "qmin_fire_run: a TMA wait in the deep-site kernel gave up");
+            return fail(QMIN_ETIMEOUT, "qmin_fire_run: a TMA wait in the deep-site kernel gave up "
+                                       "(the lattice's state is void)");
         }
     }
     h->launches += launch_fire_finish<T>(L, h->fire, h->stream);

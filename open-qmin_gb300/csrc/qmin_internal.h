@@ -180,5 +180,9 @@ int launch_split_fused_list(const Lat<T> &Lin, T *Vo, T *Fo, const SplitLists &s
                             cudaStream_t s, int *nblocks);
 template <class T>
 int launch_split_list(const Lat<T> &L, const SplitLists &sl, FireDev *fd, double *partials, cudaStream_t s);
+// polls of the TMA deep-site kernel's waits for its next planes before a block
+// gives up (the waits that let boxes in flight land always use the default)
+constexpr int kSplitWaitPolls = 1 << 22;
+cudaError_t split_set_wait_limit(int polls);
 
 }  // namespace qmin

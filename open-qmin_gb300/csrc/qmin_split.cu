@@ -559,10 +559,12 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t *b, unsigned parity)
         : "memory");
     return ok != 0;
 }
-// bounded wait (about a second at most)
-__device__ __forceinline__ bool mbar_wait(uint64_t *b, unsigned parity)
+// bounded wait (about a second at most at the default poll count); the ring's
+// waits for the next planes poll g_split_wait_limit times (split_set_wait_limit)
+__device__ int g_split_wait_limit = kSplitWaitPolls;
+__device__ __forceinline__ bool mbar_wait(uint64_t *b, unsigned parity, int polls = kSplitWaitPolls)
 {
-    for (int it = 0; it < (1 << 22); ++it)
+    for (int it = 0; it < polls; ++it)
         if (mbar_try_wait(b, parity)) return true;
     return false;
 }
@@ -597,6 +599,7 @@ __global__ void __launch_bounds__(TX / 2 * TY, MINB)
     uint64_t *bar = reinterpret_cast<uint64_t *>(smem_al + NS * kSlotBytes);
     if (KICK && !fd->active) return;
     const float hdt = KICK ? 0.5f * float(fd->dt) : 0.f;
+    const int polls = *(volatile int *)&g_split_wait_limit;
     const int ntx = (L.Lx + TX - 1) / TX;
     const int gx0 = (blockIdx.x % ntx) * TX, gy0 = (blockIdx.x / ntx) * TY;
     const int zs = blockIdx.y * zc, ze = min(L.Lz, zs + zc);
@@ -686,7 +689,7 @@ __global__ void __launch_bounds__(TX / 2 * TY, MINB)
         fetch(z + 1);
         bool ok = true;
         if (use_tma) {
-            for (int w = waited + 1; w <= z + 2 && ok; ++w) ok = mbar_wait(&bar[slot_of(w)], parity_of(w));
+            for (int w = waited + 1; w <= z + 2 && ok; ++w) ok = mbar_wait(&bar[slot_of(w)], parity_of(w), polls);
             if (ok) waited = z + 2;
         } else {
             asm volatile("cp.async.wait_group 1;\n" ::: "memory");
@@ -743,7 +746,8 @@ __global__ void __launch_bounds__(TX / 2 * TY, MINB)
         __syncthreads();
     }
     if (aborted) {
-        // let the boxes still in flight land before the block's shared memory goes away
+        // let the boxes still in flight land before the block's shared memory
+        // goes away (at the default poll count, whatever the limit)
         if (use_tma && threadIdx.x == 0) {
             for (int w = waited + 1; w <= issued; ++w) mbar_wait(&bar[slot_of(w)], parity_of(w));
             atomicExch(err, 1);
@@ -1475,6 +1479,11 @@ template <class T> int launch_split_force(const Lat<T> &L, int grid, cudaStream_
         ++n;
     }
     return n;
+}
+
+cudaError_t split_set_wait_limit(int polls)
+{
+    return cudaMemcpyToSymbol(g_split_wait_limit, &polls, sizeof(int));
 }
 
 template int launch_split_derivs<double>(const Lat<double> &, const SplitLists &, FireDev *, cudaStream_t);

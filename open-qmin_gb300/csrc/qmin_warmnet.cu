@@ -189,7 +189,7 @@ __global__ void __launch_bounds__(128) k_conv_gemm(Geo g, const bf16 *__restrict
 // still frees its tensor memory.
 __device__ int g_conv_err;
 // polls of the TMA direct kernel's waits for its copies and MMAs before it
-// gives up (qmin_warmnet_set_wait_limit); the waits that let copies and MMAs in
+// gives up (qmin_set_wait_limit); the waits that let copies and MMAs in
 // flight land before a CTA that gave up exits always poll kWaitPolls times
 constexpr int kWaitPolls = 1 << 22;
 __device__ int g_conv_wait_limit = kWaitPolls;
@@ -1653,11 +1653,13 @@ int qmin_warmnet_sync(qmin_warmnet n)
     return QMIN_OK;
 }
 
-int qmin_warmnet_set_wait_limit(long long polls)
+int qmin_set_wait_limit(long long polls)
 {
-    const int v = polls < 0 ? kWaitPolls : (int)std::min<long long>(polls, 1LL << 30);
-    const cudaError_t e = cudaMemcpyToSymbol(g_conv_wait_limit, &v, sizeof(int));
-    if (e != cudaSuccess) return nfail(QMIN_ECUDA, std::string("qmin_warmnet_set_wait_limit: ") + cudaGetErrorString(e));
+    const int conv = polls < 0 ? kWaitPolls : (int)std::min<long long>(polls, 1LL << 30);
+    const int split = polls < 0 ? qmin::kSplitWaitPolls : conv;
+    cudaError_t e = cudaMemcpyToSymbol(g_conv_wait_limit, &conv, sizeof(int));
+    if (e == cudaSuccess) e = qmin::split_set_wait_limit(split);
+    if (e != cudaSuccess) return nfail(QMIN_ECUDA, std::string("qmin_set_wait_limit: ") + cudaGetErrorString(e));
     return QMIN_OK;
 }
 

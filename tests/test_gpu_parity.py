@@ -301,6 +301,43 @@ def test_split_variants_match_separate(qmin, oracle, L, prec, variant):
         assert rel_err(b, a) <= tol
 
 
+def test_split_tma_wait_limit_reports_and_recovers(qmin, oracle):
+    """The TMA-staged deep-site kernel's bounded waits made to run out: with a
+    poll limit of zero every block gives up at its first wait for a plane,
+    lets the boxes it issued land and raises the handle's device error word,
+    and fire_run raises QMIN_ETIMEOUT.  With the default limit restored and
+    the state set again, the same handle's run tracks a clean one."""
+    L = (104, 30, 20)
+    cfg = parse_args([f"L={L[0]},{L[1]},{L[2]}", "seed=13", "Ls=2.32,1.0,0.5,0.3,0", "wall=2,0,h,5.3",
+                      f"sphere={L[0] / 2},{L[1] / 2},{L[2] / 2},{min(L) / 4},p,2.0", "H=0.1,0.2,0.3,0.5,1.0,0.2"])
+    s = oracle_system(oracle, cfg)
+    lats = []
+    for _ in range(2):
+        lat = gpu_lattice(qmin, s, qmin.FP32)
+        lat.set_fire_kernel(4)
+        lat.set_fire_variant(6)
+        lat.fire_init()
+        lats.append(lat)
+    clean, lat = lats
+    r0 = clean.fire_run(7)
+    try:
+        qmin.set_wait_limit(0)
+        with pytest.raises(qmin.QminError) as err:
+            lat.fire_run(7)
+        assert err.value.code == qmin.QMIN_ETIMEOUT
+        assert "gave up" in str(err.value)
+    finally:
+        qmin.set_wait_limit(-1)
+    lat.set_state(s.Q, s.types)
+    lat.fire_init()
+    r1 = lat.fire_run(7)
+    assert lat.fire_tuning()["variant"] == 6
+    assert r1["iterations"] == r0["iterations"] == 7
+    assert abs(r1["forceMax"] - r0["forceMax"]) <= 1e-6 * r0["forceMax"]
+    for a, b in zip(clean.get_state(Q=True, V=True, F=True), lat.get_state(Q=True, V=True, F=True)):
+        assert rel_err(b, a) <= 1e-6
+
+
 def test_fire_variant_pin_errors(qmin, oracle):
     """A variant needs a pinned strategy and an index that strategy has; -1
     hands the choice back to the autotuner."""

@@ -188,14 +188,14 @@ def test_tma_wait_limit_reports_and_recovers(qmin):
     net.sync()
     y_ref = y.float().cpu().numpy().copy()
     try:
-        qmin.WarmNet.set_wait_limit(0)
+        qmin.set_wait_limit(0)
         net.forward()
         with pytest.raises(qmin.QminError) as err:
             net.sync()
         assert err.value.code == qmin.QMIN_ETIMEOUT
         assert "gave up" in str(err.value)
     finally:
-        qmin.WarmNet.set_wait_limit(-1)
+        qmin.set_wait_limit(-1)
     net.forward()
     net.sync()
     assert np.array_equal(y.float().cpu().numpy(), y_ref)
