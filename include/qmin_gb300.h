@@ -5,7 +5,10 @@
  * exceptions across the boundary.  A handle owns all device memory for one
  * lattice; callers own every host buffer they pass.  A handle is used from one
  * host thread at a time.  All work is issued on the handle's CUDA stream
- * (qmin_set_stream; default: a stream the handle creates).
+ * (qmin_set_stream; default: a stream the handle creates).  A process drives
+ * one GPU: handles and nets use the current CUDA device, which stays the same
+ * for the life of the process (the kernels' shared-memory limits are set
+ * once per process).
  *
  * Host arrays use the reference's layout unless a layout argument says
  * otherwise: Q/V/F as AoS double[N][5] with components (Qxx, Qxy, Qxz, Qyy,
