@@ -8,7 +8,7 @@ import re
 import numpy as np
 import pytest
 
-from cases import GOLDEN_CASES, load, oracle_system, parse_args
+from cases import GOLDEN_CASES, load, parse_args
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
